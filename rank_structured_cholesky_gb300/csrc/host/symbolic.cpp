@@ -1,0 +1,259 @@
+#include "symbolic.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <functional>
+#include <sstream>
+#include <stdexcept>
+
+namespace rschol {
+
+int block_rank(int nRows, int nCols, double c, int oversampling, int cap) {
+  // FactorManager::blockRank / diagonalBlockRank (FactorManager.cpp:7283-7338)
+  double nz = std::sqrt((double)std::min(nCols, nRows));
+  int bs = (int)(nz * std::log2(nz) * c);
+  bs += oversampling;
+  bs = std::max(bs, 16);
+  bs = std::min(bs, nRows);
+  bs = std::min(bs, nCols);
+  if (cap > 0) bs = std::min(bs, cap);
+  return bs;
+}
+
+namespace {
+
+// DiagonalBlock::init + buildTraversal + buildBlockList for one supernode.
+void build_hodlr(Node& nd, const std::vector<std::pair<int, int>>& leaves, int explicitThreshold) {
+  nd.H.clear();
+  nd.blocks.clear();
+  std::vector<std::pair<int, int>> L = leaves;
+  if (L.empty()) L.push_back({0, nd.n - 1});   // setDiagonalBlocks: one block for IN_PLACE
+  std::vector<int> level;
+  for (auto& r : L) {
+    HNode h;
+    h.r0 = r.first;
+    h.r1 = r.second;
+    nd.H.push_back(h);
+    level.push_back((int)nd.H.size() - 1);
+  }
+  while (level.size() > 1) {
+    if (level.size() % 2 != 0)
+      throw std::runtime_error("number of diagonal blocks must be a power of two");
+    std::vector<int> next;
+    for (size_t k = 0; k < level.size() / 2; ++k) {
+      HNode h;
+      h.left = level[2 * k];
+      h.right = level[2 * k + 1];
+      h.r0 = nd.H[h.left].r0;
+      h.r1 = nd.H[h.right].r1;
+      nd.H.push_back(h);
+      int id = (int)nd.H.size() - 1;
+      nd.H[h.left].parent = id;
+      nd.H[h.right].parent = id;
+      next.push_back(id);
+    }
+    level.swap(next);
+  }
+  nd.hroot = level[0];
+  nd.hasExplicit = false;
+  const int nLeaves = (int)L.size();
+  std::function<void(int, int)> traverse = [&](int h, int thr) {
+    HNode& x = nd.H[h];
+    int rows = x.r1 - x.r0 + 1;
+    if (!x.isLeaf() && rows > thr) traverse(x.left, thr);
+    if (rows <= thr) {
+      nd.hasExplicit = true;
+      nd.H[h].explicitBuild = true;
+    }
+    nd.blocks.push_back({h, nd.H[h].isLeaf(), nd.H[h].explicitBuild});
+    if (!nd.H[h].isLeaf() && rows > thr) traverse(nd.H[h].right, thr);
+  };
+  if (nLeaves > 1 && explicitThreshold > 0) {
+    traverse(nd.hroot, explicitThreshold);
+  } else {
+    traverse(nd.hroot, -1);   // plain in-order traversal of every block
+    nd.hasExplicit = false;
+  }
+}
+
+}  // namespace
+
+Symbolic build_symbolic(const CSC& A, const OrderingResult& ord, const Params& prm) {
+  Symbolic S;
+  S.n = A.n;
+  const int nn = (int)ord.nodes.size();
+  S.nodes.resize(nn);
+  S.colNode.assign(A.n, -1);
+  for (int s = 0; s < nn; ++s) {
+    Node& nd = S.nodes[s];
+    nd.c0 = ord.nodes[s].c0;
+    nd.c1 = ord.nodes[s].c1;
+    nd.n = nd.c1 - nd.c0 + 1;
+    nd.compressed = ord.nodes[s].compressed;
+    for (int c = nd.c0; c <= nd.c1; ++c) S.colNode[c] = s;
+  }
+  // Row structure: the system rows of each supernode's columns plus the
+  // rows propagated from every supernode below it (findSystemRows +
+  // propagateFillIn; propagating to the first ancestor only yields the same
+  // sets).  IN_PLACE keeps fill from compressed supernodes.
+  S.children.assign(nn, {});
+  std::vector<int> mark(A.n, -1);
+  for (int s = 0; s < nn; ++s) {
+    Node& nd = S.nodes[s];
+    std::vector<int> rows;
+    for (int c = nd.c0; c <= nd.c1; ++c)
+      for (int p = A.p[c]; p < A.p[c + 1]; ++p) {
+        int r = A.i[p];
+        if (r > nd.c1 && mark[r] != s) { mark[r] = s; rows.push_back(r); }
+      }
+    for (int ch : S.children[s])
+      for (int r : S.nodes[ch].rows)
+        if (r > nd.c1 && mark[r] != s) { mark[r] = s; rows.push_back(r); }
+    std::sort(rows.begin(), rows.end());
+    nd.rows.swap(rows);
+    nd.interNode.clear();
+    nd.interStart.clear();
+    for (int k = 0; k < (int)nd.rows.size(); ++k) {
+      int owner = S.colNode[nd.rows[k]];
+      if (nd.interNode.empty() || nd.interNode.back() != owner) {
+        nd.interNode.push_back(owner);
+        nd.interStart.push_back(k);
+      }
+    }
+    nd.interStart.push_back((int)nd.rows.size());
+    nd.parent = nd.interNode.empty() ? -1 : nd.interNode[0];
+    if (nd.parent >= 0) S.children[nd.parent].push_back(s);
+  }
+  // Diagonal blocks.
+  for (int s = 0; s < nn; ++s) build_hodlr(S.nodes[s], ord.diagBlocks[s], prm.explicit_threshold);
+  // Interior blocks: maximal runs of uncompressed supernodes.
+  int s = 0;
+  while (s < nn) {
+    int e = s;
+    while (e < nn && !S.nodes[e].compressed) ++e;
+    if (e > s) {
+      InteriorBlock ib;
+      ib.n0 = s;
+      ib.n1 = e - 1;
+      std::vector<int> anc;
+      for (int k = s; k < e; ++k) {
+        Node& nd = S.nodes[k];
+        nd.interior = (int)S.interiors.size();
+        nd.nStored = 0;
+        for (size_t q = 0; q < nd.interNode.size(); ++q) {
+          if (nd.interNode[q] <= ib.n1) nd.nStored = nd.interStart[q + 1];
+          else anc.push_back(nd.interNode[q]);
+        }
+        if (S.nodes[k].H.size() > 1)
+          throw std::runtime_error("uncompressed supernode with a hierarchical diagonal is not supported");
+      }
+      std::sort(anc.begin(), anc.end());
+      anc.erase(std::unique(anc.begin(), anc.end()), anc.end());
+      ib.ancestors = anc;
+      S.interiors.push_back(ib);
+      s = e;
+    } else {
+      S.nodes[s].nStored = 0;   // compressed: every interaction is compressed
+      ++s;
+    }
+  }
+  assign_ranks(S, prm, prm.rank_constant, prm.diag_rank_constant);
+  return S;
+}
+
+void assign_ranks(Symbolic& S, const Params& prm, double rankConstant, double diagRankConstant) {
+  // FactorManager constructor clamps both constants to >= RANK_CONSTANT.
+  const double rc = std::max(rankConstant, 0.4);
+  const double dc = std::max(diagRankConstant, 0.4);
+  const int nn = (int)S.nodes.size();
+  S.offRank.assign(nn, 0);
+  S.hRank.assign(nn, {});
+  S.draws.clear();
+  long long off = 0;
+  for (int s = 0; s < nn; ++s) {
+    Node& nd = S.nodes[s];
+    S.hRank[s].assign(nd.H.size(), 0);
+    for (size_t h = 0; h < nd.H.size(); ++h) {
+      const HNode& x = nd.H[h];
+      if (x.isLeaf()) continue;
+      const HNode& a = nd.H[x.left];
+      const HNode& b = nd.H[x.right];
+      S.hRank[s][h] = block_rank(b.r1 - b.r0 + 1, a.r1 - a.r0 + 1, dc, prm.oversampling, prm.rank_cap);
+    }
+    // Block list order: explicit subtrees draw in preorder
+    // (BlockNode::compressExplicitBlock), recursive off-diagonal blocks draw
+    // once (diagonalBlockRandomMultiply).
+    std::function<void(int)> pre = [&](int h) {
+      const HNode& x = nd.H[h];
+      if (x.isLeaf()) return;
+      SketchDraw d;
+      d.node = s;
+      d.kind = 0;
+      d.h = h;
+      d.rows = nd.H[x.right].r1 - nd.H[x.right].r0 + 1;
+      d.rank = S.hRank[s][h];
+      d.offset = off;
+      off += (long long)d.rows * d.rank;
+      S.draws.push_back(d);
+      pre(x.left);
+      pre(x.right);
+    };
+    for (const BlockEntry& be : nd.blocks) {
+      if (be.expl) {
+        pre(be.h);
+      } else if (!be.diag) {
+        const HNode& x = nd.H[be.h];
+        SketchDraw d;
+        d.node = s;
+        d.kind = 1;
+        d.h = be.h;
+        d.rows = nd.H[x.right].r1 - nd.H[x.right].r0 + 1;
+        d.rank = S.hRank[s][be.h];
+        d.offset = off;
+        off += (long long)d.rows * d.rank;
+        S.draws.push_back(d);
+      }
+    }
+    if (nd.compressed && nd.m() > 0) {
+      int r = block_rank(nd.m(), nd.n, rc, prm.oversampling, prm.rank_cap);
+      S.offRank[s] = r;
+      SketchDraw d;
+      d.node = s;
+      d.kind = 2;
+      d.rows = nd.m();
+      d.rank = r;
+      d.offset = off;
+      off += (long long)d.rows * d.rank;
+      S.draws.push_back(d);
+    }
+  }
+  S.totalDraws = off;
+}
+
+std::string describe(const Symbolic& S) {
+  std::ostringstream o;
+  long long storedL = 0, compressedVU = 0, denseDiag = 0;
+  int nComp = 0, maxN = 0, maxM = 0, nH = 0;
+  for (size_t s = 0; s < S.nodes.size(); ++s) {
+    const Node& nd = S.nodes[s];
+    if (nd.compressed) {
+      nComp++;
+      maxN = std::max(maxN, nd.n);
+      maxM = std::max(maxM, nd.m());
+      compressedVU += (long long)S.offRank[s] * (nd.m() + nd.n);
+      if (nd.H.size() > 1) nH++;
+      denseDiag += (long long)nd.n * nd.n;
+    } else {
+      storedL += (long long)nd.n * (nd.n + nd.nStored);
+    }
+  }
+  o << "{\"n\": " << S.n << ", \"supernodes\": " << S.nodes.size() << ", \"compressed\": " << nComp
+    << ", \"hodlr_nodes\": " << nH << ", \"interior_blocks\": " << S.interiors.size()
+    << ", \"max_compressed_cols\": " << maxN << ", \"max_compressed_rows\": " << maxM
+    << ", \"interior_factor_entries\": " << storedL << ", \"compressed_vu_entries\": " << compressedVU
+    << ", \"compressed_diag_entries\": " << denseDiag << ", \"gaussian_draws\": " << S.totalDraws << "}";
+  return o.str();
+}
+
+}  // namespace rschol
