@@ -1,0 +1,160 @@
+/*
+ * rschol_gpu.h -- C ABI of the GB300 rank-structured Cholesky preconditioner
+ * and its PCG solve.
+ *
+ * Plain pointers and sizes only.  Matrices are CSC with full symmetric
+ * storage (colptr[n] = nnz, 0-based int32 indices), as the reference's
+ * SparseColumnMatrix (src/rschol/linearalgebra/SPARSE_MATRIX.h:187-300).
+ * Host buffers unless a name ends in _device.  Every entry point returns a
+ * status code and never aborts the process; rschol_last_error() gives the
+ * message of the last failure on a context.
+ */
+#ifndef RSCHOL_GPU_H
+#define RSCHOL_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum rschol_status {
+  RSCHOL_OK = 0,
+  RSCHOL_E_BAD_INPUT = 1,
+  RSCHOL_E_NOT_PD_AFTER_RETRY = 2, /* IndefiniteDiagonalError after all retries */
+  RSCHOL_E_OOM = 3,
+  RSCHOL_E_CUDA = 4,
+  RSCHOL_E_BREAKDOWN = 5,          /* PCG breakdown: d' A d == 0 */
+  RSCHOL_E_TIMEOUT = 6,
+  RSCHOL_E_NO_DEVICE = 7,
+  RSCHOL_E_UNSUPPORTED = 8
+};
+
+enum rschol_precision {
+  RSCHOL_FP64 = 0,   /* plain FP64 factor and solve */
+  RSCHOL_MIXED = 1   /* FP32 factor storage and Schur/sketch products, FP64 PCG */
+};
+
+/* Factorisation parameters.  Defaults (rschol_default_params) are the
+ * values the reference's pcg_solver driver passes
+ * (src/pcg_solver.cpp:100-113, src/rschol/solver/FactorManager.cpp:58-71,
+ * src/rschol/solver/SparseSolver.cpp:76-77). */
+typedef struct rschol_params {
+  int max_dense_block;       /* maxDenseBlock: larger separators are compressed (200) */
+  int max_diag_block;        /* maxDiagonalBlock: HODLR leaf size bound (400) */
+  int explicit_threshold;    /* diagonal blocks up to this size are built explicitly (4000) */
+  int nd_leaf;               /* nested-dissection leaf size (64) */
+  int oversampling;          /* OVER_SAMPLING (5) */
+  int rank_cap;              /* 0 = reference rank heuristic; > 0 caps every rank */
+  int power_iters;           /* POWER_ITERATIONS (1) */
+  int reorder_separators;    /* sub-order separators by coordinates when given (1) */
+  double rank_constant;      /* RANK_CONSTANT (0.4) */
+  double diag_rank_constant; /* DIAGONAL_RANK_CONSTANT (0.5) */
+  int max_factor_attempts;   /* retries on an indefinite diagonal (10) */
+  double rank_alpha;         /* diagonal rank constant growth per retry (1.25) */
+  unsigned seed;             /* generator reseed at every numeric factorisation (152) */
+  int precision;             /* enum rschol_precision */
+  int device;                /* CUDA device ordinal (0) */
+} rschol_params;
+
+typedef struct rschol_ctx rschol_ctx;
+typedef struct rschol_factor rschol_factor;
+
+typedef struct rschol_pcg_info {
+  int iterations;          /* PCG_SOLVER::_totalIterations for this solve */
+  double residual;         /* final recurrence ||r|| / ||b|| */
+  double true_residual;    /* ||b - A x|| / ||b|| recomputed at the end */
+  double seconds;          /* wall time of the solve */
+} rschol_pcg_info;
+
+void rschol_default_params(rschol_params* p);
+
+/* Context: owns the CUDA device selection, streams and error state. */
+rschol_ctx* rschol_create(const rschol_params* p);
+void rschol_destroy(rschol_ctx* ctx);
+const char* rschol_last_error(const rschol_ctx* ctx);
+
+/* Symbolic + numeric factorisation.
+ * Replaces FactorPreconditioner::initialize
+ * (src/rschol/solver/FactorPreconditioner.h:92-103, .cpp:70-131), which runs
+ * SparseSolver::factorSymbolic (SparseSolver.cpp:95-154) and
+ * SparseSolver::factorNumeric with its retry loop (SparseSolver.cpp:174-214).
+ * xyz (3 doubles per unknown) may be NULL, as the reference's zero positions. */
+int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* rowind,
+                         const double* vals, const double* xyz, rschol_factor** out);
+
+/* New values, same pattern: FactorPreconditioner::initialize with only the
+ * numeric factor needed (FactorPreconditioner.cpp:115-129). */
+int rschol_refactor(rschol_factor* f, const double* vals);
+
+void rschol_factor_free(rschol_factor* f);
+
+/* x = M^{-1} b for nrhs column-major right-hand sides.
+ * Replaces FactorPreconditioner::solve (FactorPreconditioner.cpp:135-162),
+ * PRECONDITIONER::solve (src/rschol/linearalgebra/PRECONDITIONER.h:290-292). */
+int rschol_precond_apply(rschol_factor* f, const double* b, double* x, int nrhs);
+int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs);
+
+/* Preconditioned CG from x0 = 0 with the factor as M, stopping at
+ * ||r|| / ||b|| <= eps or maxit iterations; nrhs right-hand sides are solved
+ * together, sharing the factor.
+ * Replaces PCG_SOLVER(A, eps, iters) + solvePCG(x, b, M)
+ * (src/rschol/linearalgebra/PCG_SOLVER.h:344-417, PCG_SOLVER.cpp:226-363).
+ * info may be NULL; otherwise it receives nrhs entries. */
+int rschol_pcg(rschol_factor* f, const double* b, double* x, int nrhs, double eps, int maxit,
+               rschol_pcg_info* info);
+int rschol_pcg_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs, double eps, int maxit,
+                      rschol_pcg_info* info);
+
+/* Drop-in for the reference's Python entry point
+ * void pcg_pysolve(int nrow, const int* jc, const int* ir, const double* pr,
+ *                  const double* rhs, double* solution)
+ * (src/python/pcg_pysolver.h:35-36, .cpp:83-101): maxDenseBlock 200,
+ * maxDiagonalBlock 400, eps 1e-6, 10000 iterations, zero positions. */
+void rschol_pcg_pysolve(int nrow, const int* jc, const int* ir, const double* pr, const double* rhs,
+                        double* solution);
+
+/* ---- introspection (parity tests, benchmarks) ---------------------------- */
+int rschol_factor_n(const rschol_factor* f);
+int rschol_factor_num_nodes(const rschol_factor* f);
+/* info[0..7] = c0, c1, compressed, m (all rows), n_stored, rank, hodlr nodes, interior block */
+int rschol_factor_node_info(const rschol_factor* f, int node, int* info);
+/* dense expanded L11 (n x n row-major, lower) of a supernode */
+int rschol_factor_node_l11(rschol_factor* f, int node, double* out);
+/* interior node: stored rows (n_stored x n); compressed: V U^T (m x n) */
+int rschol_factor_node_l21(rschol_factor* f, int node, double* out);
+int rschol_factor_perm(const rschol_factor* f, int* perm);
+/* JSON summary of the symbolic structure and the last factorisation */
+const char* rschol_factor_describe(rschol_factor* f);
+/* stats[0..7]: symbolic s, numeric s, attempts, diag rank constant,
+ * kernel launches of the last factorisation, device bytes, gaussian draws, flops */
+int rschol_factor_stats(const rschol_factor* f, double* stats);
+
+/* ---- synthetic problems --------------------------------------------------- */
+void* rschol_problem_diffusion(int dim, int nx, int ny, int nz, double sigma, unsigned seed, int nrhs);
+void* rschol_problem_elasticity(int ne, double E, double nu, unsigned seed, int nrhs);
+int rschol_problem_n(const void* p);
+long long rschol_problem_nnz(const void* p);
+int rschol_problem_nrhs(const void* p);
+void rschol_problem_get(const void* p, int* colptr, int* rowind, double* vals, double* xyz, double* rhs);
+void rschol_problem_free(void* p);
+void rschol_mt_draws(unsigned seed, long long count, unsigned* out);
+void rschol_mt_gaussians(unsigned seed, long long count, double* out);
+
+/* ---- symbolic known-answer helpers ------------------------------------------
+ * FactorManager::blockRank / diagonalBlockRank (FactorManager.cpp:7283-7338) */
+int rschol_block_rank(int nRows, int nCols, double c, int oversampling, int cap);
+/* SeparatorTree order / leafRanges (src/rschol/datastructure/SeparatorTree.cpp);
+ * returns the number of leaves; leafFirst has nLeaves + 1 entries */
+int rschol_separator_tree(int npts, const double* xyz, int maxLeaf, int* order, int* leafFirst);
+/* cs_etree + cs_counts on an upper pattern with the identity postorder
+ * (NestedDissection.cpp:409-429) */
+void rschol_etree_counts(int n, const int* colptr, const int* rowind, int* parent, int* counts);
+/* BuildRelaxedSupernodes (NestedDissection.cpp:1266-1735); returns nsuper,
+ * superFirst has nsuper + 1 entries */
+int rschol_relaxed_supernodes(int n, const int* parent, const int* counts, int ncomp, const int* compSize,
+                              const int* compChildren, const int* compFirst, const int* compParent, int maxBlock,
+                              int* superFirst, int* compressed);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RSCHOL_GPU_H */

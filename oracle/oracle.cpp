@@ -930,6 +930,12 @@ void oracle_node_l21(void* h, int j, double* out) {
   oracle::gemm(nd.m(), nd.n, r, 1.0, F.V[j].data(), r, false, F.U[j].data(), r, true, 0.0, out, nd.n);
 }
 
+void oracle_node_rows(void* h, int j, int* out) {
+  Factor& F = *(Factor*)h;
+  const rschol::Node& nd = F.S.nodes[j];
+  std::memcpy(out, nd.rows.data(), sizeof(int) * nd.rows.size());
+}
+
 void oracle_perm(void* h, int* perm) {
   Factor& F = *(Factor*)h;
   std::memcpy(perm, F.ord.perm.data(), sizeof(int) * F.S.n);

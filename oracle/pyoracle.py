@@ -51,6 +51,7 @@ def load(use_blas=True):
     lib.oracle_node_l11.argtypes = [P, I, pD]
     lib.oracle_node_l21.argtypes = [P, I, pD]
     lib.oracle_perm.argtypes = [P, pI]
+    lib.oracle_node_rows.argtypes = [P, I, pI]
     lib.oracle_times.argtypes = [P, pD]
     lib.oracle_gaussians.argtypes = [P, ctypes.c_longlong, pD]
     lib.oracle_set_blas.argtypes = [P, P, P, P, P]
@@ -148,6 +149,12 @@ class OracleFactor:
         out = np.zeros((rows, n))
         if rows:
             load().oracle_node_l21(self.h, j, _dp(out))
+        return out
+
+    def node_rows(self, j):
+        out = np.zeros(self.node_info(j)["m"], dtype=np.int32)
+        if out.size:
+            load().oracle_node_rows(self.h, j, _ip(out))
         return out
 
     def perm(self):

@@ -1,0 +1,114 @@
+"""Build recipe for the native library (and the CPU oracle used by the tests).
+
+    python -m rank_structured_cholesky_gb300._build          # library + oracle
+
+Outputs stay in-tree:  rank_structured_cholesky_gb300/_build/librschol_gb300.so
+and oracle/_build/liboracle.so.  CUDA code is compiled for sm_103a only.
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+OUT = os.path.join(PKG, "_build")
+LIB = os.path.join(OUT, "librschol_gb300.so")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+ORACLE_OUT = os.path.join(ORACLE_DIR, "_build")
+ORACLE_LIB = os.path.join(ORACLE_OUT, "liboracle.so")
+
+HOST_SRC = ["host/ordering.cpp", "host/symbolic.cpp", "host/problems.cpp", "host/capi_host.cpp"]
+CUDA_SRC = ["cuda/dense.cu", "cuda/factor.cu", "cuda/solve.cu", "cuda/pcg.cu", "cuda/capi.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("build failed: %s\n%s" % (" ".join(cmd), p.stdout))
+    return p.stdout
+
+
+def _stale(target, sources):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def _headers():
+    hs = []
+    for d, _, files in os.walk(CSRC):
+        hs += [os.path.join(d, f) for f in files if f.endswith((".h", ".cuh"))]
+    hs.append(os.path.join(ROOT, "include", "rschol_gpu.h"))
+    return hs
+
+
+def build_library(verbose=False, jobs=None):
+    os.makedirs(os.path.join(OUT, "obj"), exist_ok=True)
+    nvcc = _nvcc()
+    heads = _headers()
+    cmds, objs = [], []
+    for src in HOST_SRC + CUDA_SRC:
+        path = os.path.join(CSRC, src)
+        obj = os.path.join(OUT, "obj", src.replace("/", "_") + ".o")
+        objs.append(obj)
+        if not _stale(obj, [path] + heads):
+            continue
+        if src.endswith(".cu"):
+            cmd = [nvcc] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-c", path, "-o", obj]
+        else:
+            cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-c", path, "-o", obj]
+        cmds.append(cmd)
+    with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
+        for out in ex.map(_run, cmds):
+            if verbose and out:
+                print(out)
+    if _stale(LIB, objs):
+        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    return LIB
+
+
+def build_oracle():
+    os.makedirs(ORACLE_OUT, exist_ok=True)
+    srcs = [os.path.join(ORACLE_DIR, "oracle.cpp")] + [os.path.join(CSRC, s) for s in HOST_SRC[:3]]
+    deps = srcs + [os.path.join(ORACLE_DIR, "dense.h")] + _headers()
+    if _stale(ORACLE_LIB, deps):
+        _run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-o", ORACLE_LIB] + srcs)
+    return ORACLE_LIB
+
+
+def build_reference_tools():
+    """Compile the reference's own MERSENNETWISTER header into a known-answer
+    tool under oracle/_ref/ (only where the reference sources are present)."""
+    ref_hdr_dir = "/root/reference/src/rschol/util"
+    if not os.path.exists(os.path.join(ref_hdr_dir, "MERSENNETWISTER.h")):
+        return None
+    out_dir = os.path.join(ORACLE_DIR, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "mt_ref_kat")
+    src = os.path.join(ORACLE_DIR, "ref_mt_kat.cpp")
+    if _stale(exe, [src]):
+        _run(["g++", "-O2", "-std=c++11", "-I", ref_hdr_dir, src, "-o", exe])
+    return exe
+
+
+def build_all(verbose=False):
+    lib = build_library(verbose=verbose)
+    orc = build_oracle()
+    ref = build_reference_tools()
+    return lib, orc, ref
+
+
+if __name__ == "__main__":
+    print(build_all(verbose="-v" in sys.argv))

@@ -1,0 +1,500 @@
+// C ABI (include/rschol_gpu.h): FactorPreconditioner / PCG_SOLVER /
+// pcg_pysolve replacements on one GB300.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../../include/rschol_gpu.h"
+#include "../host/ordering.h"
+#include "../host/symbolic.h"
+#include "factor.cuh"
+#include "pcg.cuh"
+#include "solve.cuh"
+
+using namespace rschol;
+
+struct rschol_ctx {
+  rschol_params prm;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int device = 0;
+};
+
+namespace {
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+Params to_params(const rschol_params& p) {
+  Params q;
+  q.max_dense_block = p.max_dense_block;
+  q.max_diag_block = p.max_diag_block;
+  q.explicit_threshold = p.explicit_threshold;
+  q.nd_leaf = p.nd_leaf;
+  q.oversampling = p.oversampling;
+  q.rank_cap = p.rank_cap;
+  q.power_iters = p.power_iters;
+  q.reorder_separators = p.reorder_separators;
+  q.rank_constant = p.rank_constant;
+  q.diag_rank_constant = p.diag_rank_constant;
+  q.max_factor_attempts = p.max_factor_attempts;
+  q.rank_alpha = p.rank_alpha;
+  q.seed = p.seed;
+  return q;
+}
+
+struct Impl {
+  virtual ~Impl() = default;
+  virtual void plan() = 0;
+  virtual int run() = 0;
+  virtual void apply(double* d_w, cudaStream_t s) = 0;
+  virtual void set_values(const double* lower) = 0;
+  virtual long long launches() const = 0;
+  virtual long long apply_launches() const = 0;
+  virtual double flops() const = 0;
+  virtual double apply_bytes() const = 0;
+  virtual size_t bytes() const = 0;
+  virtual void node_l11(int j, double* out) = 0;
+  virtual void node_l21(int j, double* out) = 0;
+};
+
+template <class T>
+struct ImplT : Impl {
+  FactorEngine<T> fe;
+  SolveEngine<T> se;
+  ImplT(const Symbolic& S, const CSC& A, const Params& p, cudaStream_t s) : fe(S, A, p, s), se(fe) {}
+  void plan() override {
+    fe.plan();
+    se.plan();
+  }
+  int run() override { return fe.run(); }
+  void apply(double* w, cudaStream_t s) override { se.apply_inplace(w, s); }
+  void set_values(const double* lower) override { fe.set_values(lower); }
+  long long launches() const override { return fe.launches; }
+  long long apply_launches() const override { return se.launches_per_apply(); }
+  double flops() const override { return fe.flops; }
+  double apply_bytes() const override { return se.bytes_per_apply(); }
+  size_t bytes() const override { return fe.deviceBytes; }
+  std::vector<T> fetch(const T* d, size_t count) {
+    std::vector<T> h(count);
+    if (count) RSCHOL_CUDA(cudaMemcpy(h.data(), d, sizeof(T) * count, cudaMemcpyDeviceToHost));
+    return h;
+  }
+  void node_l11(int j, double* out) override {
+    const Node& nd = fe.S.nodes[j];
+    const int n = nd.n, ld = fe.ld[j];
+    const T* base = nd.compressed ? fe.compressed() + fe.frontOff[j] : fe.interior() + fe.frontOff[j];
+    std::vector<T> h = fetch(base, (size_t)(n - 1) * ld + n);
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b) out[(size_t)a * n + b] = b <= a ? (double)h[(size_t)a * ld + b] : 0.0;
+  }
+  void node_l21(int j, double* out) override {
+    const Node& nd = fe.S.nodes[j];
+    const int n = nd.n, ld = fe.ld[j];
+    if (!nd.compressed) {
+      if (nd.nStored == 0) return;
+      std::vector<T> h = fetch(fe.interior() + fe.frontOff[j] + (size_t)n * ld, (size_t)(nd.nStored - 1) * ld + n);
+      for (int a = 0; a < nd.nStored; ++a)
+        for (int b = 0; b < n; ++b) out[(size_t)a * n + b] = (double)h[(size_t)a * ld + b];
+      return;
+    }
+    const int r = fe.rank[j], m = nd.m();
+    if (r == 0) return;
+    std::vector<T> V = fetch(fe.vu() + fe.vOff[j], (size_t)m * r);
+    std::vector<T> U = fetch(fe.vu() + fe.uOff[j], (size_t)n * r);
+    for (int a = 0; a < m; ++a)
+      for (int b = 0; b < n; ++b) {
+        double s = 0;
+        for (int k = 0; k < r; ++k) s += (double)V[(size_t)a * r + k] * (double)U[(size_t)b * r + k];
+        out[(size_t)a * n + b] = s;
+      }
+  }
+};
+
+}  // namespace
+
+struct rschol_factor {
+  rschol_ctx* ctx = nullptr;
+  Params prm;
+  int precision = RSCHOL_FP64;
+  CSC Afull;
+  OrderingResult ord;
+  CSC A;                      // tril(P A P^T)
+  std::vector<int> lowerSrc;  // A.x[k] = Afull.x[lowerSrc[k]]
+  Symbolic S;
+  std::unique_ptr<Impl> impl;
+  std::unique_ptr<PcgEngine> pcg;
+  std::vector<int> permCsrSrc;  // permuted CSR value k = Afull.x[permCsrSrc[k]]
+  DevBuf dPerm, dB, dX, dBp, dXp;
+  int nrhsCap = 0;
+  double tSymbolic = 0, tNumeric = 0;
+  int attempts = 0;
+  double diagRankConstant = 0.5;
+  std::string desc;
+};
+
+static int fail(rschol_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+extern "C" {
+
+void rschol_default_params(rschol_params* p) {
+  p->max_dense_block = 200;
+  p->max_diag_block = 400;
+  p->explicit_threshold = 4000;
+  p->nd_leaf = 64;
+  p->oversampling = 5;
+  p->rank_cap = 0;
+  p->power_iters = 1;
+  p->reorder_separators = 1;
+  p->rank_constant = 0.4;
+  p->diag_rank_constant = 0.5;
+  p->max_factor_attempts = 10;
+  p->rank_alpha = 1.25;
+  p->seed = 152;
+  p->precision = RSCHOL_FP64;
+  p->device = 0;
+}
+
+rschol_ctx* rschol_create(const rschol_params* p) {
+  rschol_ctx* c = new rschol_ctx();
+  if (p) c->prm = *p;
+  else rschol_default_params(&c->prm);
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    c->err = "no CUDA device available";
+    cudaGetLastError();
+    return c;
+  }
+  c->device = c->prm.device;
+  if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    c->err = "CUDA device initialisation failed";
+    c->stream = nullptr;
+  }
+  return c;
+}
+
+void rschol_destroy(rschol_ctx* c) {
+  if (!c) return;
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* rschol_last_error(const rschol_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+static int numeric_with_retry(rschol_factor* f) {
+  rschol_ctx* ctx = f->ctx;
+  double t0 = now_s();
+  double dc = f->prm.diag_rank_constant;
+  int status = 0;
+  f->attempts = 0;
+  for (int attempt = 0; attempt < f->prm.max_factor_attempts; ++attempt) {
+    f->attempts++;
+    if (attempt > 0) {
+      // SparseSolver::factorNumeric: bump the diagonal rank constant, redo
+      // the symbolic ranks without reordering, refactor from a reseeded stream
+      assign_ranks(f->S, f->prm, f->prm.rank_constant, dc);
+      f->impl->plan();
+    }
+    status = f->impl->run();
+    if (status == 0) break;
+    dc *= f->prm.rank_alpha;
+  }
+  f->diagRankConstant = dc;
+  f->tNumeric = now_s() - t0;
+  if (status != 0)
+    return fail(ctx, RSCHOL_E_NOT_PD_AFTER_RETRY,
+                "indefinite diagonal block (code " + std::to_string(status) + ") after " +
+                    std::to_string(f->attempts) + " attempts");
+  return RSCHOL_OK;
+}
+
+int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* rowind, const double* vals,
+                         const double* xyz, rschol_factor** out) {
+  if (!ctx || !out) return RSCHOL_E_BAD_INPUT;
+  *out = nullptr;
+  if (!ctx->stream) return fail(ctx, RSCHOL_E_NO_DEVICE, ctx->err.empty() ? "no device" : ctx->err);
+  if (n <= 0 || !colptr || !rowind || !vals) return fail(ctx, RSCHOL_E_BAD_INPUT, "empty or null matrix");
+  if (colptr[0] != 0) return fail(ctx, RSCHOL_E_BAD_INPUT, "colptr[0] must be 0");
+  for (int j = 0; j < n; ++j)
+    if (colptr[j + 1] < colptr[j]) return fail(ctx, RSCHOL_E_BAD_INPUT, "colptr must be non-decreasing");
+  const int nnz = colptr[n];
+  for (int k = 0; k < nnz; ++k)
+    if (rowind[k] < 0 || rowind[k] >= n) return fail(ctx, RSCHOL_E_BAD_INPUT, "row index out of range");
+  std::unique_ptr<rschol_factor> f(new rschol_factor());
+  f->ctx = ctx;
+  f->prm = to_params(ctx->prm);
+  f->precision = ctx->prm.precision;
+  try {
+    RSCHOL_CUDA(cudaSetDevice(ctx->device));
+    double t0 = now_s();
+    f->Afull.n = n;
+    f->Afull.p.assign(colptr, colptr + n + 1);
+    f->Afull.i.assign(rowind, rowind + nnz);
+    f->Afull.x.assign(vals, vals + nnz);
+    f->ord = build_ordering(f->Afull, xyz, f->prm);
+    // permuted lower part, remembering where every value comes from
+    {
+      CSC idx = f->Afull;
+      for (int k = 0; k < nnz; ++k) idx.x[k] = (double)k;
+      CSC L = permute_lower(idx, f->ord.perm, f->ord.iperm);
+      f->lowerSrc.resize(L.x.size());
+      for (size_t k = 0; k < L.x.size(); ++k) f->lowerSrc[k] = (int)L.x[k];
+      for (size_t k = 0; k < L.x.size(); ++k) L.x[k] = vals[f->lowerSrc[k]];
+      f->A = std::move(L);
+    }
+    f->S = build_symbolic(f->A, f->ord, f->prm);
+    // permuted full CSR for the PCG SpMV (symmetric: CSC columns = CSR rows)
+    std::vector<int> rp(n + 1, 0), ci(nnz);
+    std::vector<double> cv(nnz);
+    f->permCsrSrc.resize(nnz);
+    for (int j = 0; j < n; ++j) rp[f->ord.iperm[j] + 1] = colptr[j + 1] - colptr[j];
+    for (int i = 0; i < n; ++i) rp[i + 1] += rp[i];
+    std::vector<std::pair<int, int>> tmp;
+    for (int i = 0; i < n; ++i) {
+      const int j = f->ord.perm[i];
+      tmp.clear();
+      for (int p = colptr[j]; p < colptr[j + 1]; ++p) tmp.push_back({f->ord.iperm[rowind[p]], p});
+      std::sort(tmp.begin(), tmp.end());
+      for (size_t k = 0; k < tmp.size(); ++k) {
+        ci[rp[i] + k] = tmp[k].first;
+        f->permCsrSrc[rp[i] + k] = tmp[k].second;
+        cv[rp[i] + k] = vals[tmp[k].second];
+      }
+    }
+    f->tSymbolic = now_s() - t0;
+    if (f->precision == RSCHOL_MIXED) f->impl.reset(new ImplT<float>(f->S, f->A, f->prm, ctx->stream));
+    else f->impl.reset(new ImplT<double>(f->S, f->A, f->prm, ctx->stream));
+    f->impl->plan();
+    f->pcg.reset(new PcgEngine(n, rp, ci, cv, ctx->stream));
+    f->dPerm.alloc(sizeof(int) * n);
+    RSCHOL_CUDA(cudaMemcpy(f->dPerm.p, f->ord.perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    int st = numeric_with_retry(f.get());
+    if (st != RSCHOL_OK) return st;
+  } catch (const CudaError& e) {
+    cudaGetLastError();
+    std::string m = e.what();
+    return fail(ctx, m.find("out of memory") != std::string::npos ? RSCHOL_E_OOM : RSCHOL_E_CUDA, m);
+  } catch (const std::exception& e) {
+    return fail(ctx, RSCHOL_E_UNSUPPORTED, e.what());
+  }
+  *out = f.release();
+  return RSCHOL_OK;
+}
+
+int rschol_refactor(rschol_factor* f, const double* vals) {
+  if (!f || !vals) return RSCHOL_E_BAD_INPUT;
+  try {
+    std::vector<double> lower(f->lowerSrc.size());
+    for (size_t k = 0; k < lower.size(); ++k) lower[k] = vals[f->lowerSrc[k]];
+    f->A.x = lower;
+    f->Afull.x.assign(vals, vals + f->Afull.p[f->Afull.n]);
+    std::vector<double> cv(f->permCsrSrc.size());
+    for (size_t k = 0; k < cv.size(); ++k) cv[k] = vals[f->permCsrSrc[k]];
+    f->impl->set_values(lower.data());
+    f->pcg->set_values(cv);
+    if (f->attempts > 1) {   // the ranks of a previous retry do not carry over
+      assign_ranks(f->S, f->prm, f->prm.rank_constant, f->prm.diag_rank_constant);
+      f->impl->plan();
+    }
+    return numeric_with_retry(f);
+  } catch (const std::exception& e) {
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+}
+
+void rschol_factor_free(rschol_factor* f) { delete f; }
+
+static void ensure_vecs(rschol_factor* f, int nrhs) {
+  if (nrhs <= f->nrhsCap) return;
+  const size_t bytes = sizeof(double) * (size_t)f->Afull.n * nrhs;
+  f->dB.alloc(bytes);
+  f->dX.alloc(bytes);
+  f->dBp.alloc(sizeof(double) * f->Afull.n);
+  f->dXp.alloc(sizeof(double) * f->Afull.n);
+  f->nrhsCap = nrhs;
+}
+
+int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs) {
+  if (!f || !d_b || !d_x || nrhs <= 0) return RSCHOL_E_BAD_INPUT;
+  try {
+    ensure_vecs(f, 1);
+    const int n = f->Afull.n;
+    cudaStream_t s = f->ctx->stream;
+    for (int k = 0; k < nrhs; ++k) {
+      launch_gather(d_b + (size_t)k * n, f->dPerm.as<int>(), f->dBp.as<double>(), n, s);
+      f->impl->apply(f->dBp.as<double>(), s);
+      launch_scatter_perm(f->dBp.as<double>(), f->dPerm.as<int>(), d_x + (size_t)k * n, n, s);
+    }
+    RSCHOL_CUDA(cudaStreamSynchronize(s));
+  } catch (const std::exception& e) {
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+  return RSCHOL_OK;
+}
+
+int rschol_precond_apply(rschol_factor* f, const double* b, double* x, int nrhs) {
+  if (!f || !b || !x || nrhs <= 0) return RSCHOL_E_BAD_INPUT;
+  try {
+    ensure_vecs(f, nrhs);
+    const size_t bytes = sizeof(double) * (size_t)f->Afull.n * nrhs;
+    RSCHOL_CUDA(cudaMemcpyAsync(f->dB.p, b, bytes, cudaMemcpyHostToDevice, f->ctx->stream));
+    int st = rschol_precond_apply_device(f, f->dB.as<double>(), f->dX.as<double>(), nrhs);
+    if (st != RSCHOL_OK) return st;
+    RSCHOL_CUDA(cudaMemcpyAsync(x, f->dX.p, bytes, cudaMemcpyDeviceToHost, f->ctx->stream));
+    RSCHOL_CUDA(cudaStreamSynchronize(f->ctx->stream));
+  } catch (const std::exception& e) {
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+  return RSCHOL_OK;
+}
+
+int rschol_pcg_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs, double eps, int maxit,
+                      rschol_pcg_info* info) {
+  if (!f || !d_b || !d_x || nrhs <= 0 || maxit < 0) return RSCHOL_E_BAD_INPUT;
+  int status = RSCHOL_OK;
+  try {
+    ensure_vecs(f, 1);
+    const int n = f->Afull.n;
+    cudaStream_t s = f->ctx->stream;
+    Impl* impl = f->impl.get();
+    auto apply = [impl, s](double* w) { impl->apply(w, s); };
+    for (int k = 0; k < nrhs; ++k) {
+      double t0 = now_s();
+      launch_gather(d_b + (size_t)k * n, f->dPerm.as<int>(), f->dBp.as<double>(), n, s);
+      PcgResult r = f->pcg->solve(f->dBp.as<double>(), f->dXp.as<double>(), eps, maxit, apply);
+      launch_scatter_perm(f->dXp.as<double>(), f->dPerm.as<int>(), d_x + (size_t)k * n, n, s);
+      RSCHOL_CUDA(cudaStreamSynchronize(s));
+      if (info) {
+        info[k].iterations = r.iterations;
+        info[k].residual = r.residual;
+        info[k].true_residual = r.trueResidual;
+        info[k].seconds = now_s() - t0;
+      }
+      if (r.breakdown) status = RSCHOL_E_BREAKDOWN;
+    }
+  } catch (const std::exception& e) {
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+  if (status == RSCHOL_E_BREAKDOWN) fail(f->ctx, status, "PCG breakdown: d' A d == 0");
+  return status;
+}
+
+int rschol_pcg(rschol_factor* f, const double* b, double* x, int nrhs, double eps, int maxit,
+               rschol_pcg_info* info) {
+  if (!f || !b || !x || nrhs <= 0) return RSCHOL_E_BAD_INPUT;
+  try {
+    ensure_vecs(f, nrhs);
+    const size_t bytes = sizeof(double) * (size_t)f->Afull.n * nrhs;
+    RSCHOL_CUDA(cudaMemcpyAsync(f->dB.p, b, bytes, cudaMemcpyHostToDevice, f->ctx->stream));
+    int st = rschol_pcg_device(f, f->dB.as<double>(), f->dX.as<double>(), nrhs, eps, maxit, info);
+    RSCHOL_CUDA(cudaMemcpyAsync(x, f->dX.p, bytes, cudaMemcpyDeviceToHost, f->ctx->stream));
+    RSCHOL_CUDA(cudaStreamSynchronize(f->ctx->stream));
+    return st;
+  } catch (const std::exception& e) {
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+}
+
+void rschol_pcg_pysolve(int nrow, const int* jc, const int* ir, const double* pr, const double* rhs,
+                        double* solution) {
+  rschol_params p;
+  rschol_default_params(&p);
+  p.reorder_separators = 0;
+  rschol_ctx* ctx = rschol_create(&p);
+  rschol_factor* f = nullptr;
+  int st = rschol_factor_create(ctx, nrow, jc, ir, pr, nullptr, &f);
+  if (st == RSCHOL_OK) {
+    rschol_pcg_info info;
+    st = rschol_pcg(f, rhs, solution, 1, 1e-6, 10000, &info);
+    std::printf(" total iterations: %d\n residual: %g\n", info.iterations, info.true_residual);
+  }
+  if (st != RSCHOL_OK) {
+    std::fprintf(stderr, "rschol_pcg_pysolve: %s\n", rschol_last_error(ctx));
+    for (int i = 0; i < nrow; ++i) solution[i] = 0.0;
+  }
+  rschol_factor_free(f);
+  rschol_destroy(ctx);
+}
+
+int rschol_factor_n(const rschol_factor* f) { return f ? f->Afull.n : 0; }
+int rschol_factor_num_nodes(const rschol_factor* f) { return f ? (int)f->S.nodes.size() : 0; }
+
+int rschol_factor_node_info(const rschol_factor* f, int j, int* info) {
+  if (!f || j < 0 || j >= (int)f->S.nodes.size()) return RSCHOL_E_BAD_INPUT;
+  const Node& nd = f->S.nodes[j];
+  info[0] = nd.c0;
+  info[1] = nd.c1;
+  info[2] = nd.compressed;
+  info[3] = nd.m();
+  info[4] = nd.nStored;
+  info[5] = nd.compressed && nd.m() > 0 ? f->S.offRank[j] : 0;
+  info[6] = (int)nd.H.size();
+  info[7] = nd.interior;
+  return RSCHOL_OK;
+}
+
+int rschol_factor_node_l11(rschol_factor* f, int j, double* out) {
+  if (!f || j < 0 || j >= (int)f->S.nodes.size() || !out) return RSCHOL_E_BAD_INPUT;
+  try {
+    f->impl->node_l11(j, out);
+  } catch (const std::exception& e) {
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+  return RSCHOL_OK;
+}
+
+int rschol_factor_node_l21(rschol_factor* f, int j, double* out) {
+  if (!f || j < 0 || j >= (int)f->S.nodes.size() || !out) return RSCHOL_E_BAD_INPUT;
+  try {
+    f->impl->node_l21(j, out);
+  } catch (const std::exception& e) {
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+  return RSCHOL_OK;
+}
+
+int rschol_factor_perm(const rschol_factor* f, int* perm) {
+  if (!f || !perm) return RSCHOL_E_BAD_INPUT;
+  std::memcpy(perm, f->ord.perm.data(), sizeof(int) * f->Afull.n);
+  return RSCHOL_OK;
+}
+
+const char* rschol_factor_describe(rschol_factor* f) {
+  if (!f) return "{}";
+  std::ostringstream o;
+  std::string s = describe(f->S);
+  s.pop_back();
+  o << s << ", \"precision\": \"" << (f->precision == RSCHOL_MIXED ? "mixed" : "fp64") << "\""
+    << ", \"factor_launches\": " << f->impl->launches() << ", \"apply_launches\": " << f->impl->apply_launches()
+    << ", \"factor_flops\": " << f->impl->flops() << ", \"apply_bytes\": " << f->impl->apply_bytes()
+    << ", \"spmv_bytes\": " << f->pcg->spmvBytes << ", \"device_bytes\": " << f->impl->bytes()
+    << ", \"symbolic_s\": " << f->tSymbolic << ", \"numeric_s\": " << f->tNumeric
+    << ", \"attempts\": " << f->attempts << "}";
+  f->desc = o.str();
+  return f->desc.c_str();
+}
+
+int rschol_factor_stats(const rschol_factor* f, double* st) {
+  if (!f || !st) return RSCHOL_E_BAD_INPUT;
+  st[0] = f->tSymbolic;
+  st[1] = f->tNumeric;
+  st[2] = f->attempts;
+  st[3] = f->diagRankConstant;
+  st[4] = (double)f->impl->launches();
+  st[5] = (double)f->impl->bytes();
+  st[6] = (double)f->S.totalDraws;
+  st[7] = f->impl->flops();
+  return RSCHOL_OK;
+}
+
+}  // extern "C"

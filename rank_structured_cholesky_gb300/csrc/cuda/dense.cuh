@@ -1,0 +1,98 @@
+// Batched dense building blocks of the numeric factorisation.
+//
+// Every launch carries an array of independent tasks (one per front, per
+// tile column, ...) so that all supernodes of one elimination-tree level,
+// whatever their sizes, are processed by a single launch.  The reference
+// issues one CBLAS/LAPACKE call per supernode instead
+// (src/rschol/linearalgebra/MATRIX_FAST.cpp:1758 gemm, 1885 syrk, 2086
+// cholesky, 3049 triangularSolve).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace rschol {
+
+// C (M x N) = alpha * op(A) * op(B) + beta * C, row-major, leading dims.
+// lower != 0: tiles strictly above the diagonal of C are skipped (the
+// caller only reads C's lower triangle).
+template <class T>
+struct GemmTask {
+  const T* A;
+  const T* B;
+  T* C;
+  int M, N, K;
+  int lda, ldb, ldc;
+  int tA, tB, lower;
+  T alpha, beta;
+  int tilesN;
+  int tileBase;   // first tile of this task in the launch
+};
+
+// In-place lower Cholesky of one diagonal tile (n <= 64).  On a
+// non-positive pivot *flag receives min(*flag, code).
+template <class T>
+struct PotrfTask {
+  T* A;
+  int ld, n;
+  int code;
+};
+
+// B (rows x w) := B * L^{-T}, L the w x w (w <= 64) lower tile.
+template <class T>
+struct TrsmTask {
+  const T* L;
+  T* B;
+  int ldl, ldb, w, rows;
+  int chunkBase;  // first 64-row chunk of this task in the launch
+};
+
+// Extend-add "pull": each target column sums the contributions of its
+// sources in a fixed order (deterministic, no atomics).
+template <class T>
+struct ExtAddSource {
+  const T* D;          // source block (row-major)
+  const int* rowRel;   // target row of each source row
+  const int* colInv;   // per target column: source column or -1
+  int ld, nrows;
+  int lowerOnly;       // source rows a < b are not valid
+  T sign;
+};
+
+template <class T>
+struct ExtAddTarget {
+  T* F;
+  int ld, ncols;
+  int srcBegin, srcEnd;
+  int colBase;         // first global column of this target in the launch
+};
+
+template <class T> void launch_gemm(const GemmTask<T>* dTasks, int nTasks, int totalTiles, cudaStream_t s);
+template <class T> void launch_potrf(const PotrfTask<T>* dTasks, int nTasks, int* dFlag, cudaStream_t s);
+template <class T> void launch_trsm(const TrsmTask<T>* dTasks, int nTasks, int totalChunks, cudaStream_t s);
+template <class T>
+void launch_extadd(const ExtAddTarget<T>* dTargets, int nTargets, const ExtAddSource<T>* dSources,
+                   int totalCols, cudaStream_t s);
+template <class T>
+void launch_scatter(const double* Avals, const long long* srcIdx, const long long* dstIdx, long long count,
+                    T* dst, cudaStream_t s);
+// Shifted CholeskyQR: G += 11 (rows*r + r(r+1)) u trace(G) I on each Gram
+// matrix (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa, SIAM J. Sci.
+// Comput. 42 (2020) A477-A503).
+template <class T>
+struct ShiftTask {
+  T* G;
+  int r, ld, rows;
+};
+template <class T> void launch_shift_diag(const ShiftTask<T>* dTasks, int nTasks, cudaStream_t s);
+template <class T>
+struct IdentTask {
+  T* U;
+  int n, ld;
+};
+template <class T> void launch_set_identity(const IdentTask<T>* dTasks, int nTasks, cudaStream_t s);
+// Box-Muller on pairs of raw 32-bit Mersenne Twister draws.
+template <class T>
+void launch_box_muller(const uint32_t* raw, long long count, T* out, cudaStream_t s);
+
+}  // namespace rschol

@@ -1,0 +1,747 @@
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <functional>
+
+#include "../host/rng.h"
+#include "factor.cuh"
+
+namespace rschol {
+
+namespace {
+constexpr int NB = 64;           // tile width of the blocked factorisations
+constexpr int QR_CODE = 1 << 29; // POTRF code for a Gram matrix of the QR
+int tiles_of(int M, int N) { return ((M + 63) / 64) * ((N + 63) / 64); }
+}  // namespace
+
+template <class T>
+FactorEngine<T>::FactorEngine(const Symbolic& S_, const CSC& A_, const Params& p, cudaStream_t s)
+    : S(S_), A(A_), prm(p), stream(s) {
+  dAvals.alloc(sizeof(double) * std::max<size_t>(1, A.x.size()));
+  RSCHOL_CUDA(cudaMemcpyAsync(dAvals.p, A.x.data(), sizeof(double) * A.x.size(), cudaMemcpyHostToDevice, stream));
+  dFlag.alloc(sizeof(int));
+  RSCHOL_CUDA(cudaStreamSynchronize(stream));
+}
+
+template <class T>
+void FactorEngine<T>::set_values(const double* lowerVals) {
+  RSCHOL_CUDA(cudaMemcpyAsync(dAvals.p, lowerVals, sizeof(double) * A.x.size(), cudaMemcpyHostToDevice, stream));
+}
+
+template <class T>
+void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int tiles) {
+  if (batch.empty()) return;
+  Step st{ST_GEMM, (long long)gemm_.size(), (int)batch.size(), tiles};
+  gemm_.insert(gemm_.end(), batch.begin(), batch.end());
+  steps_.push_back(st);
+  batch.clear();
+}
+
+template <class T>
+void FactorEngine<T>::push_gemm(const GemmTask<T>& t0, int& tiles, std::vector<GemmTask<T>>& batch) {
+  if (t0.M <= 0 || t0.N <= 0) return;
+  GemmTask<T> t = t0;
+  t.tilesN = (t.N + 63) / 64;
+  t.tileBase = tiles;
+  tiles += tiles_of(t.M, t.N);
+  batch.push_back(t);
+  double f = 2.0 * t.M * t.N * std::max(t.K, 0);
+  if (t.lower && t.M == t.N) f *= 0.5;
+  flops += f;
+}
+
+template <class T>
+void FactorEngine<T>::gemm1(const GemmTask<T>& t) {
+  std::vector<GemmTask<T>> b;
+  int tiles = 0;
+  push_gemm(t, tiles, b);
+  flush_gemm(b, tiles);
+}
+
+static inline GemmTask<double> gemm_zero_d() { return GemmTask<double>{}; }
+
+template <class T>
+static GemmTask<T> mk_gemm(const T* A, int lda, bool tA, const T* B, int ldb, bool tB, T* C, int ldc, int M, int N,
+                           int K, T alpha, T beta, bool lower = false) {
+  GemmTask<T> t{};
+  t.A = A;
+  t.B = B;
+  t.C = C;
+  t.M = M;
+  t.N = N;
+  t.K = K;
+  t.lda = lda;
+  t.ldb = ldb;
+  t.ldc = ldc;
+  t.tA = tA;
+  t.tB = tB;
+  t.lower = lower;
+  t.alpha = alpha;
+  t.beta = beta;
+  return t;
+}
+
+template <class T>
+void FactorEngine<T>::emit_chol(const std::vector<CholJob<T>>& jobs) {
+  int maxN = 0;
+  for (auto& j : jobs) maxN = std::max(maxN, j.nDiag);
+  for (int kb = 0; kb < maxN; kb += NB) {
+    std::vector<PotrfTask<T>> pt;
+    for (auto& j : jobs) {
+      if (j.nDiag <= kb) continue;
+      int w = std::min(NB, j.nDiag - kb);
+      pt.push_back(PotrfTask<T>{j.F + (size_t)kb * j.ld + kb, j.ld, w, j.code});
+      flops += (double)w * w * w / 3.0;
+    }
+    if (!pt.empty()) {
+      steps_.push_back(Step{ST_POTRF, (long long)potrf_.size(), (int)pt.size(), (int)pt.size()});
+      potrf_.insert(potrf_.end(), pt.begin(), pt.end());
+    }
+    std::vector<TrsmTask<T>> tt;
+    int chunks = 0;
+    for (auto& j : jobs) {
+      if (j.nDiag <= kb) continue;
+      int w = std::min(NB, j.nDiag - kb);
+      int rows = j.nRows - kb - w;
+      if (rows <= 0) continue;
+      TrsmTask<T> t{j.F + (size_t)kb * j.ld + kb, j.F + (size_t)(kb + w) * j.ld + kb, j.ld, j.ld, w, rows, chunks};
+      chunks += (rows + 63) / 64;
+      tt.push_back(t);
+      flops += (double)rows * w * w;
+    }
+    if (!tt.empty()) {
+      steps_.push_back(Step{ST_TRSM, (long long)trsm_.size(), (int)tt.size(), chunks});
+      trsm_.insert(trsm_.end(), tt.begin(), tt.end());
+    }
+    std::vector<GemmTask<T>> gb;
+    int tiles = 0;
+    for (auto& j : jobs) {
+      if (j.nDiag <= kb) continue;
+      int w = std::min(NB, j.nDiag - kb);
+      int M = j.nRows - kb - w, N = j.nUpd - kb - w;
+      if (M <= 0 || N <= 0) continue;
+      const T* P = j.F + (size_t)(kb + w) * j.ld + kb;
+      push_gemm(mk_gemm<T>(P, j.ld, false, P, j.ld, true, j.F + (size_t)(kb + w) * j.ld + kb + w, j.ld, M, N, w,
+                           T(-1), T(1), true),
+                tiles, gb);
+    }
+    flush_gemm(gb, tiles);
+  }
+}
+
+template <class T>
+void FactorEngine<T>::emit_trsm(const std::vector<TrsmJob<T>>& jobs) {
+  int maxW = 0;
+  for (auto& j : jobs) maxW = std::max(maxW, j.rows > 0 ? j.w : 0);
+  for (int kb = 0; kb < maxW; kb += NB) {
+    std::vector<TrsmTask<T>> tt;
+    int chunks = 0;
+    for (auto& j : jobs) {
+      if (j.w <= kb || j.rows <= 0) continue;
+      int bw = std::min(NB, j.w - kb);
+      tt.push_back(TrsmTask<T>{j.L + (size_t)kb * j.ldl + kb, j.B + kb, j.ldl, j.ldb, bw, j.rows, chunks});
+      chunks += (j.rows + 63) / 64;
+      flops += (double)j.rows * bw * bw;
+    }
+    if (!tt.empty()) {
+      steps_.push_back(Step{ST_TRSM, (long long)trsm_.size(), (int)tt.size(), chunks});
+      trsm_.insert(trsm_.end(), tt.begin(), tt.end());
+    }
+    std::vector<GemmTask<T>> gb;
+    int tiles = 0;
+    for (auto& j : jobs) {
+      if (j.w <= kb || j.rows <= 0) continue;
+      int bw = std::min(NB, j.w - kb);
+      int N = j.w - kb - bw;
+      if (N <= 0) continue;
+      push_gemm(mk_gemm<T>(j.B + kb, j.ldb, false, j.L + (size_t)(kb + bw) * j.ldl + kb, j.ldl, true, j.B + kb + bw,
+                           j.ldb, j.rows, N, bw, T(-1), T(1)),
+                tiles, gb);
+    }
+    flush_gemm(gb, tiles);
+  }
+}
+
+template <class T>
+void FactorEngine<T>::emit_rf(const std::vector<RFJob<T>>& jobs) {
+  if (jobs.empty()) return;
+  std::vector<GemmTask<T>> gb;
+  int tiles = 0;
+  // Y = F^T G
+  for (auto& j : jobs)
+    push_gemm(mk_gemm<T>(j.F, j.ld, true, j.G, j.r, false, j.Y, j.r, j.cols, j.r, j.rows, T(1), T(0)), tiles, gb);
+  flush_gemm(gb, tiles);
+  for (int it = 0; it < prm.power_iters; ++it) {
+    tiles = 0;
+    for (auto& j : jobs)
+      push_gemm(mk_gemm<T>(j.F, j.ld, false, j.Y, j.r, false, j.X, j.r, j.rows, j.r, j.cols, T(1), T(0)), tiles, gb);
+    flush_gemm(gb, tiles);
+    tiles = 0;
+    for (auto& j : jobs)
+      push_gemm(mk_gemm<T>(j.F, j.ld, true, j.X, j.r, false, j.Y, j.r, j.cols, j.r, j.rows, T(1), T(0)), tiles, gb);
+    flush_gemm(gb, tiles);
+  }
+  // Thin QR of Y by shifted CholeskyQR3.
+  std::vector<const RFJob<T>*> qr;
+  std::vector<IdentTask<T>> id;
+  for (auto& j : jobs) {
+    if (j.identity) id.push_back(IdentTask<T>{j.Y, j.cols, j.r});
+    else qr.push_back(&j);
+  }
+  if (!id.empty()) {
+    steps_.push_back(Step{ST_IDENT, (long long)ident_.size(), (int)id.size(), (int)id.size()});
+    ident_.insert(ident_.end(), id.begin(), id.end());
+  }
+  for (int round = 0; round < 3 && !qr.empty(); ++round) {
+    tiles = 0;
+    for (auto* j : qr)
+      push_gemm(mk_gemm<T>(j->Y, j->r, true, j->Y, j->r, false, j->Gm, j->r, j->r, j->r, j->cols, T(1), T(0)), tiles,
+                gb);
+    flush_gemm(gb, tiles);
+    if (round == 0) {
+      std::vector<ShiftTask<T>> sh;
+      for (auto* j : qr) sh.push_back(ShiftTask<T>{j->Gm, j->r, j->r, j->cols});
+      steps_.push_back(Step{ST_SHIFT, (long long)shift_.size(), (int)sh.size(), (int)sh.size()});
+      shift_.insert(shift_.end(), sh.begin(), sh.end());
+    }
+    std::vector<CholJob<T>> cj;
+    std::vector<TrsmJob<T>> tj;
+    for (auto* j : qr) {
+      cj.push_back(CholJob<T>{j->Gm, j->r, j->r, j->r, j->r, QR_CODE});
+      tj.push_back(TrsmJob<T>{j->Gm, j->Y, j->r, j->r, j->cols, j->r});
+    }
+    emit_chol(cj);
+    emit_trsm(tj);
+  }
+  // V = F U
+  tiles = 0;
+  for (auto& j : jobs)
+    push_gemm(mk_gemm<T>(j.F, j.ld, false, j.Y, j.r, false, j.V, j.r, j.rows, j.r, j.cols, T(1), T(0)), tiles, gb);
+  flush_gemm(gb, tiles);
+  // Q = U^T U and / or F := V U^T
+  tiles = 0;
+  for (auto& j : jobs) {
+    if (j.Q)
+      push_gemm(mk_gemm<T>(j.Y, j.r, true, j.Y, j.r, false, j.Q, j.r, j.r, j.r, j.cols, T(1), T(0)), tiles, gb);
+    if (j.expand)
+      push_gemm(mk_gemm<T>(j.V, j.r, false, j.Y, j.r, true, j.F, j.ld, j.rows, j.cols, j.r, T(1), T(0)), tiles, gb);
+  }
+  flush_gemm(gb, tiles);
+}
+
+template <class T>
+void FactorEngine<T>::plan() {
+  const int nn = (int)S.nodes.size();
+  const int N = S.n;
+  steps_.clear();
+  gemm_.clear();
+  potrf_.clear();
+  trsm_.clear();
+  eaT_.clear();
+  eaS_.clear();
+  shift_.clear();
+  ident_.clear();
+  ints_.clear();
+  flops = 0;
+
+  // ---- levels
+  std::vector<int> h(nn, 0);
+  interiorLevels.clear();
+  compressedLevels.clear();
+  for (int s = 0; s < nn; ++s) {
+    const Node& nd = S.nodes[s];
+    int hh = 0;
+    for (int ch : S.children[s])
+      if (S.nodes[ch].compressed == nd.compressed) hh = std::max(hh, h[ch] + 1);
+    h[s] = hh;
+    auto& L = nd.compressed ? compressedLevels : interiorLevels;
+    if ((int)L.size() <= hh) L.resize(hh + 1);
+    L[hh].push_back(s);
+  }
+
+  // ---- arenas
+  frontOff.assign(nn, 0);
+  ld.assign(nn, 0);
+  long long curI = 0, curC = 0;
+  for (auto& lv : interiorLevels)
+    for (int d : lv) {
+      const Node& nd = S.nodes[d];
+      ld[d] = nd.n + nd.m();
+      frontOff[d] = curI;
+      curI += (long long)ld[d] * ld[d];
+    }
+  for (auto& lv : compressedLevels)
+    for (int j : lv) {
+      const Node& nd = S.nodes[j];
+      ld[j] = nd.n;
+      frontOff[j] = curC;
+      curC += (long long)(nd.n + nd.m()) * nd.n;
+    }
+  rank.assign(nn, 0);
+  vOff.assign(nn, -1);
+  uOff.assign(nn, -1);
+  qOff.assign(nn, -1);
+  std::vector<long long> xOff(nn, -1), gmOff(nn, -1);
+  long long curV = 0;
+  for (int j = 0; j < nn; ++j) {
+    const Node& nd = S.nodes[j];
+    if (!nd.compressed || nd.m() == 0) continue;
+    const int r = S.offRank[j], m = nd.m(), n = nd.n;
+    rank[j] = r;
+    vOff[j] = curV; curV += (long long)m * r;
+    uOff[j] = curV; curV += (long long)n * r;
+    qOff[j] = curV; curV += (long long)r * r;
+    xOff[j] = curV; curV += (long long)m * r;
+    gmOff[j] = curV; curV += (long long)r * r;
+  }
+  // HODLR internal-node buffers: V, Y/U, X, Gm
+  std::vector<std::vector<long long>> hOff(nn);
+  long long curH = 0;
+  for (int j = 0; j < nn; ++j) {
+    const Node& nd = S.nodes[j];
+    hOff[j].assign(nd.H.size(), -1);
+    if (!nd.compressed) continue;
+    for (size_t q = 0; q < nd.H.size(); ++q) {
+      const HNode& x = nd.H[q];
+      if (x.isLeaf()) continue;
+      const int rows = nd.H[x.right].r1 - nd.H[x.right].r0 + 1, cols = nd.H[x.left].r1 - nd.H[x.left].r0 + 1;
+      const int r = S.hRank[j][q];
+      hOff[j][q] = curH;
+      curH += (long long)rows * r * 2 + (long long)cols * r + (long long)r * r + (long long)r * r +
+              (long long)r * cols + (long long)rows * cols;  // + coupling scratch
+    }
+  }
+  // compressed descendants and interior roots of each compressed supernode
+  struct Pair { int src, q; };
+  std::vector<std::vector<Pair>> compDesc(nn), rootsOf(nn);
+  for (int c = 0; c < nn; ++c) {
+    const Node& cn = S.nodes[c];
+    bool isRoot = !cn.compressed && (cn.parent < 0 || S.nodes[cn.parent].compressed);
+    if (!cn.compressed && !isRoot) continue;
+    for (size_t q = 0; q < cn.interNode.size(); ++q) {
+      if (cn.compressed) compDesc[cn.interNode[q]].push_back(Pair{c, (int)q});
+      else rootsOf[cn.interNode[q]].push_back(Pair{c, (int)q});
+    }
+  }
+  std::vector<std::vector<long long>> contribOff(nn);
+  long long curT = 0;
+  for (int j = 0; j < nn; ++j) {
+    for (const Pair& p : compDesc[j]) {
+      const Node& cn = S.nodes[p.src];
+      const int s0 = cn.interStart[p.q], k1 = cn.interStart[p.q + 1] - s0, r = S.offRank[p.src];
+      contribOff[j].push_back(curT);
+      curT += (long long)r * k1 + (long long)(cn.m() - s0) * k1;
+    }
+  }
+  dInterior.alloc(sizeof(T) * std::max(1LL, curI));
+  dCompressed.alloc(sizeof(T) * std::max(1LL, curC));
+  dVU.alloc(sizeof(T) * std::max(1LL, curV));
+  dHodlr.alloc(sizeof(T) * std::max(1LL, curH));
+  dContrib.alloc(sizeof(T) * std::max(1LL, curT));
+  dGauss.alloc(sizeof(T) * std::max(1LL, S.totalDraws));
+  deviceBytes = sizeof(T) * (curI + curC + curV + curH + curT + S.totalDraws) + sizeof(double) * A.x.size();
+  T* const I0 = interior();
+  T* const C0 = compressed();
+  T* const V0 = vu();
+  T* const H0 = dHodlr.as<T>();
+  T* const T0 = dContrib.as<T>();
+  T* const G0 = dGauss.as<T>();
+
+  // ---- Gaussian stream (reseeded generator; raw draws on the host, the
+  // Box-Muller transform on the device)
+  {
+    const long long total = S.totalDraws;
+    if (total > 0) {
+      std::vector<uint32_t> raw((size_t)total * 2);
+      MT19937 g(prm.seed);
+      g.rawDraws(total * 2, raw.data());
+      DevBuf dRaw;
+      dRaw.alloc(raw.size() * sizeof(uint32_t));
+      RSCHOL_CUDA(cudaMemcpyAsync(dRaw.p, raw.data(), raw.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+      launch_box_muller<T>(dRaw.as<uint32_t>(), total, G0, stream);
+      RSCHOL_CUDA(cudaStreamSynchronize(stream));
+    }
+  }
+  auto draw_of = [&](int node, int kind, int hnode) -> const T* {
+    for (const SketchDraw& d : S.draws)
+      if (d.node == node && d.kind == kind && (kind == 2 || d.h == hnode)) return G0 + d.offset;
+    throw std::runtime_error("missing sketch draw");
+  };
+
+  // ---- scatter maps of A's lower entries into the fronts
+  std::vector<int> pos(N, -1);
+  scatSrc_.clear();
+  scatDst_.clear();
+  std::vector<long long> csrc, cdst;
+  for (int s = 0; s < nn; ++s) {
+    const Node& nd = S.nodes[s];
+    for (int a = 0; a < nd.m(); ++a) pos[nd.rows[a]] = a;
+    for (int c = nd.c0; c <= nd.c1; ++c)
+      for (int p = A.p[c]; p < A.p[c + 1]; ++p) {
+        int r = A.i[p];
+        long long row = (r <= nd.c1) ? (r - nd.c0) : (nd.n + pos[r]);
+        long long dst = frontOff[s] + row * ld[s] + (c - nd.c0);
+        if (nd.compressed) { csrc.push_back(p); cdst.push_back(dst); }
+        else { scatSrc_.push_back(p); scatDst_.push_back(dst); }
+      }
+    for (int a = 0; a < nd.m(); ++a) pos[nd.rows[a]] = -1;
+  }
+  nScatI_ = (long long)scatSrc_.size();
+  nScatC_ = (long long)csrc.size();
+  scatSrc_.insert(scatSrc_.end(), csrc.begin(), csrc.end());
+  scatDst_.insert(scatDst_.end(), cdst.begin(), cdst.end());
+
+  // ---- interior levels: extend-add of the children's update blocks, then
+  // the blocked partial Cholesky of every front (L panel + update block).
+  for (auto& lv : interiorLevels) {
+    std::vector<ExtAddTarget<T>> tgs;
+    int cols = 0;
+    for (int p : lv) {
+      const Node& pn = S.nodes[p];
+      if (S.children[p].empty()) continue;
+      ExtAddTarget<T> t{};
+      t.F = I0 + frontOff[p];
+      t.ld = ld[p];
+      t.ncols = ld[p];
+      t.srcBegin = (int)eaS_.size();
+      t.colBase = cols;
+      for (int a = 0; a < pn.m(); ++a) pos[pn.rows[a]] = a;
+      for (int c : S.children[p]) {
+        const Node& cn = S.nodes[c];
+        if (cn.m() == 0) continue;
+        ExtAddSource<T> src{};
+        src.D = I0 + frontOff[c] + (long long)cn.n * ld[c] + cn.n;
+        src.ld = ld[c];
+        src.nrows = cn.m();
+        src.lowerOnly = 1;
+        src.sign = T(1);
+        size_t ro = ints_.size();
+        for (int a = 0; a < cn.m(); ++a) {
+          int g = cn.rows[a];
+          ints_.push_back(g <= pn.c1 ? g - pn.c0 : pn.n + pos[g]);
+        }
+        size_t co = ints_.size();
+        ints_.resize(co + ld[p], -1);
+        for (int b = 0; b < cn.m(); ++b) ints_[co + ints_[ro + b]] = b;
+        src.rowRel = reinterpret_cast<const int*>(ro);
+        src.colInv = reinterpret_cast<const int*>(co);
+        eaS_.push_back(src);
+      }
+      for (int a = 0; a < pn.m(); ++a) pos[pn.rows[a]] = -1;
+      t.srcEnd = (int)eaS_.size();
+      if (t.srcEnd > t.srcBegin) {
+        tgs.push_back(t);
+        cols += t.ncols;
+      }
+    }
+    if (!tgs.empty()) {
+      steps_.push_back(Step{ST_EXTADD, (long long)eaT_.size(), (int)tgs.size(), cols});
+      eaT_.insert(eaT_.end(), tgs.begin(), tgs.end());
+    }
+    std::vector<CholJob<T>> jobs;
+    for (int d : lv) {
+      const Node& nd = S.nodes[d];
+      jobs.push_back(CholJob<T>{I0 + frontOff[d], ld[d], nd.n, ld[d], ld[d], d + 1});
+    }
+    emit_chol(jobs);
+  }
+
+  // ---- compressed levels
+  for (auto& lv : compressedLevels) {
+    // (a) compressed-descendant contributions V_c[s0:] (Q_c V_c[s0:s1]^T)
+    std::vector<GemmTask<T>> gb;
+    int tiles = 0;
+    for (int j : lv)
+      for (size_t k = 0; k < compDesc[j].size(); ++k) {
+        const Pair& p = compDesc[j][k];
+        const Node& cn = S.nodes[p.src];
+        const int s0 = cn.interStart[p.q], k1 = cn.interStart[p.q + 1] - s0, r = rank[p.src];
+        T* W = T0 + contribOff[j][k];
+        push_gemm(mk_gemm<T>(V0 + qOff[p.src], r, false, V0 + vOff[p.src] + (size_t)s0 * r, r, true, W, k1, r, k1, r,
+                             T(1), T(0)),
+                  tiles, gb);
+      }
+    flush_gemm(gb, tiles);
+    tiles = 0;
+    for (int j : lv)
+      for (size_t k = 0; k < compDesc[j].size(); ++k) {
+        const Pair& p = compDesc[j][k];
+        const Node& cn = S.nodes[p.src];
+        const int s0 = cn.interStart[p.q], k1 = cn.interStart[p.q + 1] - s0, r = rank[p.src];
+        T* W = T0 + contribOff[j][k];
+        T* Tm = W + (size_t)r * k1;
+        push_gemm(mk_gemm<T>(V0 + vOff[p.src] + (size_t)s0 * r, r, false, W, k1, false, Tm, k1, cn.m() - s0, k1, r,
+                             T(1), T(0)),
+                  tiles, gb);
+      }
+    flush_gemm(gb, tiles);
+    // (b) extend-add into the dense fronts [S11; S21]
+    std::vector<ExtAddTarget<T>> tgs;
+    int cols = 0;
+    for (int j : lv) {
+      const Node& nd = S.nodes[j];
+      ExtAddTarget<T> t{};
+      t.F = C0 + frontOff[j];
+      t.ld = ld[j];
+      t.ncols = nd.n;
+      t.srcBegin = (int)eaS_.size();
+      t.colBase = cols;
+      for (int a = 0; a < nd.m(); ++a) pos[nd.rows[a]] = a;
+      auto rel = [&](int g) { return g <= nd.c1 ? g - nd.c0 : nd.n + pos[g]; };
+      for (const Pair& p : rootsOf[j]) {
+        const Node& dn = S.nodes[p.src];
+        const int sq = dn.interStart[p.q], sq1 = dn.interStart[p.q + 1];
+        ExtAddSource<T> src{};
+        src.D = I0 + frontOff[p.src] + (long long)dn.n * ld[p.src] + dn.n;
+        src.ld = ld[p.src];
+        src.nrows = dn.m();
+        src.lowerOnly = 1;
+        src.sign = T(1);
+        size_t ro = ints_.size();
+        for (int a = 0; a < dn.m(); ++a) ints_.push_back(a >= sq ? rel(dn.rows[a]) : 0);
+        size_t co = ints_.size();
+        ints_.resize(co + nd.n, -1);
+        for (int b = sq; b < sq1; ++b) ints_[co + dn.rows[b] - nd.c0] = b;
+        src.rowRel = reinterpret_cast<const int*>(ro);
+        src.colInv = reinterpret_cast<const int*>(co);
+        eaS_.push_back(src);
+      }
+      for (size_t k = 0; k < compDesc[j].size(); ++k) {
+        const Pair& p = compDesc[j][k];
+        const Node& cn = S.nodes[p.src];
+        const int s0 = cn.interStart[p.q], k1 = cn.interStart[p.q + 1] - s0, r = rank[p.src];
+        ExtAddSource<T> src{};
+        src.D = T0 + contribOff[j][k] + (size_t)r * k1;
+        src.ld = k1;
+        src.nrows = cn.m() - s0;
+        src.lowerOnly = 0;
+        src.sign = T(-1);
+        size_t ro = ints_.size();
+        for (int a = s0; a < cn.m(); ++a) ints_.push_back(rel(cn.rows[a]));
+        size_t co = ints_.size();
+        ints_.resize(co + nd.n, -1);
+        for (int b = 0; b < k1; ++b) ints_[co + cn.rows[s0 + b] - nd.c0] = b;
+        src.rowRel = reinterpret_cast<const int*>(ro);
+        src.colInv = reinterpret_cast<const int*>(co);
+        eaS_.push_back(src);
+      }
+      for (int a = 0; a < nd.m(); ++a) pos[nd.rows[a]] = -1;
+      t.srcEnd = (int)eaS_.size();
+      if (t.srcEnd > t.srcBegin) {
+        tgs.push_back(t);
+        cols += t.ncols;
+      }
+    }
+    if (!tgs.empty()) {
+      steps_.push_back(Step{ST_EXTADD, (long long)eaT_.size(), (int)tgs.size(), cols});
+      eaT_.insert(eaT_.end(), tgs.begin(), tgs.end());
+    }
+
+    // (c) diagonal factor (+ L21 for single-block diagonals)
+    auto hjob = [&](int j, int q, bool identityAllowed) {
+      const Node& nd = S.nodes[j];
+      const HNode& x = nd.H[q];
+      const HNode& lc = nd.H[x.left];
+      const HNode& rc = nd.H[x.right];
+      const int rows = rc.r1 - rc.r0 + 1, cols = lc.r1 - lc.r0 + 1, r = S.hRank[j][q];
+      T* base = H0 + hOff[j][q];
+      RFJob<T> rj{};
+      rj.F = C0 + frontOff[j] + (size_t)rc.r0 * ld[j] + lc.r0;
+      rj.ld = ld[j];
+      rj.rows = rows;
+      rj.cols = cols;
+      rj.r = r;
+      rj.V = base;
+      rj.Y = base + (size_t)rows * r;
+      rj.X = rj.Y + (size_t)cols * r;
+      rj.Gm = rj.X + (size_t)rows * r;
+      rj.Q = nullptr;
+      rj.identity = identityAllowed && r >= cols;
+      rj.expand = true;
+      return rj;
+    };
+    std::vector<CholJob<T>> cj;
+    std::vector<RFJob<T>> hj;
+    std::vector<TrsmJob<T>> tj;
+    std::vector<int> rec;
+    for (int j : lv) {
+      const Node& nd = S.nodes[j];
+      T* F = C0 + frontOff[j];
+      if (nd.H.size() == 1) {
+        cj.push_back(CholJob<T>{F, ld[j], nd.n, nd.n + nd.m(), nd.n, j + 1});
+      } else if (nd.blocks.size() == 1 && nd.blocks[0].expl) {
+        cj.push_back(CholJob<T>{F, ld[j], nd.n, nd.n, nd.n, j + 1});
+        for (size_t q = 0; q < nd.H.size(); ++q)
+          if (!nd.H[q].isLeaf()) {
+            RFJob<T> rj = hjob(j, (int)q, false);
+            rj.G = draw_of(j, 0, (int)q);
+            hj.push_back(rj);
+          }
+        if (nd.m() > 0) tj.push_back(TrsmJob<T>{F, F + (size_t)nd.n * ld[j], ld[j], ld[j], nd.m(), nd.n});
+      } else {
+        rec.push_back(j);
+      }
+    }
+    emit_chol(cj);
+    emit_rf(hj);
+    emit_trsm(tj);
+    for (int j : rec) {   // HODLR diagonals with recursive blocks, in block-list order
+      const Node& nd = S.nodes[j];
+      T* F = C0 + frontOff[j];
+      const int L = ld[j];
+      for (const BlockEntry& be : nd.blocks) {
+        const HNode& x = nd.H[be.h];
+        if (be.expl) {
+          const int size = x.r1 - x.r0 + 1;
+          emit_chol({CholJob<T>{F + (size_t)x.r0 * L + x.r0, L, size, size, size, j + 1}});
+          std::vector<RFJob<T>> sub;
+          std::function<void(int)> pre = [&](int q) {
+            if (nd.H[q].isLeaf()) return;
+            RFJob<T> rj = hjob(j, q, false);
+            rj.G = draw_of(j, 0, q);
+            sub.push_back(rj);
+            pre(nd.H[q].left);
+            pre(nd.H[q].right);
+          };
+          pre(be.h);
+          emit_rf(sub);
+          continue;
+        }
+        if (!be.diag) {
+          const HNode& lc = nd.H[x.left];
+          const HNode& rc = nd.H[x.right];
+          const int rows = rc.r1 - rc.r0 + 1, cols = lc.r1 - lc.r0 + 1;
+          T* Fba = F + (size_t)rc.r0 * L + lc.r0;
+          // couplings from HODLR ancestors whose right subtree holds this block
+          for (int cur = be.h, anc = x.parent; anc >= 0; cur = anc, anc = nd.H[anc].parent) {
+            if (nd.H[anc].right != cur) continue;
+            const HNode& ax = nd.H[anc];
+            const HNode& ar = nd.H[ax.right];
+            const int aRows = ar.r1 - ar.r0 + 1, aCols = nd.H[ax.left].r1 - nd.H[ax.left].r0 + 1;
+            const int ra = S.hRank[j][anc];
+            T* abase = H0 + hOff[j][anc];
+            T* aV = abase;
+            T* aU = abase + (size_t)aRows * ra;
+            T* scratch = H0 + hOff[j][be.h] + (size_t)rows * S.hRank[j][be.h] * 2 +
+                         (size_t)cols * S.hRank[j][be.h] + (size_t)S.hRank[j][be.h] * S.hRank[j][be.h];
+            T* W1 = scratch;                       // ra x ra = U^T U
+            T* W2 = W1 + (size_t)ra * ra;          // ra x cols = W1 V2^T
+            gemm1(mk_gemm<T>(aU, ra, true, aU, ra, false, W1, ra, ra, ra, aCols, T(1), T(0)));
+            gemm1(mk_gemm<T>(W1, ra, false, aV + (size_t)(lc.r0 - ar.r0) * ra, ra, true, W2, cols, ra, cols, ra, T(1),
+                             T(0)));
+            gemm1(mk_gemm<T>(aV + (size_t)(rc.r0 - ar.r0) * ra, ra, false, W2, cols, false, Fba, L, rows, cols, ra,
+                             T(-1), T(1)));
+            (void)aRows;
+          }
+          emit_trsm({TrsmJob<T>{F + (size_t)lc.r0 * L + lc.r0, Fba, L, L, rows, cols}});
+          RFJob<T> rj = hjob(j, be.h, true);
+          rj.G = draw_of(j, 1, be.h);
+          emit_rf({rj});
+          continue;
+        }
+        // a diagonal leaf outside any explicit subtree: updateDiagonal + factor
+        const int sz = x.r1 - x.r0 + 1;
+        T* Lb = F + (size_t)x.r0 * L + x.r0;
+        for (int cur = be.h, anc = x.parent; anc >= 0; cur = anc, anc = nd.H[anc].parent) {
+          if (nd.H[anc].right != cur) continue;
+          const HNode& ax = nd.H[anc];
+          const HNode& ar = nd.H[ax.right];
+          const int aRows = ar.r1 - ar.r0 + 1, aCols = nd.H[ax.left].r1 - nd.H[ax.left].r0 + 1;
+          const int ra = S.hRank[j][anc];
+          T* aV = H0 + hOff[j][anc];
+          T* aU = aV + (size_t)aRows * ra;
+          T* Wv = aU + (size_t)aCols * ra + (size_t)aRows * ra + (size_t)ra * ra + (size_t)ra * ra;  // scratch
+          gemm1(mk_gemm<T>(aV + (size_t)(x.r0 - ar.r0) * ra, ra, false, aU, ra, true, Wv, aCols, sz, aCols, ra, T(1),
+                           T(0)));
+          gemm1(mk_gemm<T>(Wv, aCols, false, Wv, aCols, true, Lb, L, sz, sz, aCols, T(-1), T(1), true));
+        }
+        emit_chol({CholJob<T>{Lb, L, sz, sz, sz, j + 1}});
+      }
+      if (nd.m() > 0) emit_trsm({TrsmJob<T>{F, F + (size_t)nd.n * L, L, L, nd.m(), nd.n}});
+    }
+
+    // (d) off-diagonal range finder on L21 = F[n:n+m, 0:n]
+    std::vector<RFJob<T>> oj;
+    for (int j : lv) {
+      const Node& nd = S.nodes[j];
+      if (nd.m() == 0) continue;
+      RFJob<T> rj{};
+      rj.F = C0 + frontOff[j] + (size_t)nd.n * ld[j];
+      rj.ld = ld[j];
+      rj.rows = nd.m();
+      rj.cols = nd.n;
+      rj.r = rank[j];
+      rj.G = draw_of(j, 2, -1);
+      rj.Y = V0 + uOff[j];
+      rj.X = V0 + xOff[j];
+      rj.Gm = V0 + gmOff[j];
+      rj.V = V0 + vOff[j];
+      rj.Q = V0 + qOff[j];
+      rj.identity = rank[j] >= nd.n;
+      rj.expand = false;
+      oj.push_back(rj);
+    }
+    emit_rf(oj);
+  }
+
+  // ---- upload the schedule
+  auto up = [&](DevBuf& b, const void* src, size_t bytes) {
+    b.alloc(std::max<size_t>(bytes, 16));
+    if (bytes) RSCHOL_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, stream));
+  };
+  up(dInts_, ints_.data(), ints_.size() * sizeof(int));
+  for (auto& s : eaS_) {
+    s.rowRel = dInts_.as<int>() + reinterpret_cast<size_t>(s.rowRel);
+    s.colInv = dInts_.as<int>() + reinterpret_cast<size_t>(s.colInv);
+  }
+  up(dGemm_, gemm_.data(), gemm_.size() * sizeof(GemmTask<T>));
+  up(dPotrf_, potrf_.data(), potrf_.size() * sizeof(PotrfTask<T>));
+  up(dTrsm_, trsm_.data(), trsm_.size() * sizeof(TrsmTask<T>));
+  up(dEaT_, eaT_.data(), eaT_.size() * sizeof(ExtAddTarget<T>));
+  up(dEaS_, eaS_.data(), eaS_.size() * sizeof(ExtAddSource<T>));
+  up(dShift_, shift_.data(), shift_.size() * sizeof(ShiftTask<T>));
+  up(dIdent_, ident_.data(), ident_.size() * sizeof(IdentTask<T>));
+  up(dScatSrc_, scatSrc_.data(), scatSrc_.size() * sizeof(long long));
+  up(dScatDst_, scatDst_.data(), scatDst_.size() * sizeof(long long));
+  RSCHOL_CUDA(cudaStreamSynchronize(stream));
+  deviceBytes += ints_.size() * 4 + gemm_.size() * sizeof(GemmTask<T>) + scatSrc_.size() * 16;
+  planned_ = true;
+}
+
+template <class T>
+int FactorEngine<T>::run() {
+  if (!planned_) plan();
+  launches = 0;
+  RSCHOL_CUDA(cudaMemsetAsync(dInterior.p, 0, dInterior.bytes, stream));
+  RSCHOL_CUDA(cudaMemsetAsync(dCompressed.p, 0, dCompressed.bytes, stream));
+  static const int big = INT_MAX;
+  RSCHOL_CUDA(cudaMemcpyAsync(dFlag.p, &big, sizeof(int), cudaMemcpyHostToDevice, stream));
+  launch_scatter<T>(dAvals.as<double>(), dScatSrc_.as<long long>(), dScatDst_.as<long long>(), nScatI_, interior(),
+                    stream);
+  launch_scatter<T>(dAvals.as<double>(), dScatSrc_.as<long long>() + nScatI_, dScatDst_.as<long long>() + nScatI_,
+                    nScatC_, compressed(), stream);
+  launches += 2;
+  for (const Step& st : steps_) {
+    switch (st.kind) {
+      case ST_GEMM: launch_gemm<T>(dGemm_.as<GemmTask<T>>() + st.off, st.count, st.grid, stream); break;
+      case ST_POTRF: launch_potrf<T>(dPotrf_.as<PotrfTask<T>>() + st.off, st.count, dFlag.as<int>(), stream); break;
+      case ST_TRSM: launch_trsm<T>(dTrsm_.as<TrsmTask<T>>() + st.off, st.count, st.grid, stream); break;
+      case ST_EXTADD:
+        launch_extadd<T>(dEaT_.as<ExtAddTarget<T>>() + st.off, st.count, dEaS_.as<ExtAddSource<T>>(), st.grid,
+                         stream);
+        break;
+      case ST_SHIFT: launch_shift_diag<T>(dShift_.as<ShiftTask<T>>() + st.off, st.count, stream); break;
+      case ST_IDENT: launch_set_identity<T>(dIdent_.as<IdentTask<T>>() + st.off, st.count, stream); break;
+    }
+    ++launches;
+  }
+  int flag = 0;
+  RSCHOL_CUDA(cudaMemcpyAsync(&flag, dFlag.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  RSCHOL_CUDA(cudaStreamSynchronize(stream));
+  return flag == INT_MAX ? 0 : flag;
+}
+
+template class FactorEngine<double>;
+template class FactorEngine<float>;
+
+}  // namespace rschol

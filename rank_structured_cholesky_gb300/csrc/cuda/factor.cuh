@@ -1,0 +1,141 @@
+// Numeric factorisation on the GPU as a static, level-batched schedule.
+//
+// Mathematics (the same preconditioner as the reference's
+// FactorManager::factorNumeric, src/rschol/solver/FactorManager.cpp:357-804):
+//   * interior blocks (maximal runs of uncompressed supernodes) are exact
+//     sparse Cholesky factors.  They are computed multifrontally: each front
+//     carries all of its supernode's rows, so the root fronts of every
+//     interior subtree end with the exact Schur-complement contribution
+//     L_{R,I} L_{R,I}^T of that subtree to the compressed supernodes.  The
+//     reference applies the same contribution implicitly as
+//     A_{R,I} L_I^{-T} L_I^{-1} A_{I,C} (FactorManager.cpp:10792-11088);
+//   * each compressed supernode j assembles the dense Schur complement
+//     [S11; S21] from A, those interior contributions and its compressed
+//     descendants' V (U^T U) V^T, factors S11 (dense or HODLR: explicit
+//     builds compress the blocks of the exact factor, recursive builds
+//     sketch S_ba L_aa^{-T}), forms L21 = S21 L11^{-T} and runs the
+//     reference's randomized range finder on it (Gaussian G from the
+//     reseeded Mersenne Twister stream, one power iteration, thin QR,
+//     V = L21 U), as blockRandomMultiply_allRows + fixedOffDiagonalDecomposition
+//     + fullBasisProject_transpose_allRows (FactorManager.cpp:8193-8297,
+//     8717-8780, 5691-5751).
+// All supernodes of one level (interior: height in the elimination tree,
+// compressed: height among compressed supernodes) are processed by one
+// batched launch per phase.  The schedule is built once on the host and
+// replayed for every (re)factorisation.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../host/ordering.h"
+#include "../host/symbolic.h"
+#include "common.cuh"
+#include "dense.cuh"
+
+namespace rschol {
+
+enum StepKind : int {
+  ST_GEMM = 0,
+  ST_POTRF,
+  ST_TRSM,
+  ST_EXTADD,
+  ST_SHIFT,
+  ST_IDENT,
+};
+
+struct Step {
+  int kind;
+  long long off;    // first task in the kind's task array
+  int count;        // number of tasks
+  int grid;         // tiles / chunks / columns for the launch
+};
+
+template <class T>
+struct CholJob {   // blocked partial Cholesky of F's first nDiag columns
+  T* F;
+  int ld, nDiag, nRows, nUpd, code;
+};
+
+template <class T>
+struct TrsmJob {   // B (rows x w) := B L^{-T}
+  const T* L;
+  T* B;
+  int ldl, ldb, rows, w;
+};
+
+template <class T>
+struct RFJob {     // randomized range finder on the dense block F (rows x cols)
+  T* F;
+  int ld, rows, cols, r;
+  const T* G;      // rows x r Gaussian sketch
+  T* Y;            // cols x r: sketch, then the orthonormal basis U
+  T* X;            // rows x r scratch
+  T* Gm;           // r x r Gram scratch
+  T* V;            // rows x r
+  T* Q;            // r x r: U^T U (may be null)
+  bool identity;   // r >= cols: U = I (FactorManager.cpp:9598-9606)
+  bool expand;     // overwrite F with V U^T (HODLR block of L11)
+};
+
+template <class T>
+class FactorEngine {
+ public:
+  FactorEngine(const Symbolic& S, const CSC& Alower, const Params& prm, cudaStream_t stream);
+  ~FactorEngine() = default;
+
+  // (Re)build buffers and schedule for the ranks currently in S.
+  void plan();
+  // Upload new lower-triangle values (same pattern as Alower).
+  void set_values(const double* lowerVals);
+  // Run the numeric factorisation; returns 0 or the failing POTRF code.
+  int run();
+
+  // --- factor data for the solve and for introspection
+  const Symbolic& S;
+  const CSC& A;
+  Params prm;
+  cudaStream_t stream;
+
+  std::vector<long long> frontOff;    // element offset (interior / compressed arena)
+  std::vector<int> ld;                // front leading dimension
+  std::vector<int> rank;              // off-diagonal rank of compressed supernodes
+  std::vector<long long> vOff, uOff, qOff;
+  DevBuf dInterior, dCompressed, dVU, dHodlr, dContrib, dGauss, dAvals, dFlag;
+  T* interior() const { return dInterior.as<T>(); }
+  T* compressed() const { return dCompressed.as<T>(); }
+  T* vu() const { return dVU.as<T>(); }
+
+  std::vector<std::vector<int>> interiorLevels, compressedLevels;
+  long long launches = 0;            // kernel launches of the last run
+  double flops = 0;                  // algorithmic flops of one factorisation
+  size_t deviceBytes = 0;
+
+ private:
+  void emit_chol(const std::vector<CholJob<T>>& jobs);
+  void emit_trsm(const std::vector<TrsmJob<T>>& jobs);
+  void emit_rf(const std::vector<RFJob<T>>& jobs);
+  void push_gemm(const GemmTask<T>& t, int& tiles, std::vector<GemmTask<T>>& batch);
+  void flush_gemm(std::vector<GemmTask<T>>& batch, int tiles);
+  void gemm1(const GemmTask<T>& t);   // a single-task GEMM step
+
+  std::vector<Step> steps_;
+  std::vector<GemmTask<T>> gemm_;
+  std::vector<PotrfTask<T>> potrf_;
+  std::vector<TrsmTask<T>> trsm_;
+  std::vector<ExtAddTarget<T>> eaT_;
+  std::vector<ExtAddSource<T>> eaS_;
+  std::vector<ShiftTask<T>> shift_;
+  std::vector<IdentTask<T>> ident_;
+  std::vector<int> ints_;
+  std::vector<long long> scatSrc_, scatDst_;
+  std::vector<int> scatIsInterior_;
+  DevBuf dGemm_, dPotrf_, dTrsm_, dEaT_, dEaS_, dShift_, dIdent_, dInts_, dScatSrc_, dScatDst_;
+  DevBuf dScatSrcC_, dScatDstC_;
+  long long nScatI_ = 0, nScatC_ = 0;
+  bool planned_ = false;
+};
+
+}  // namespace rschol

@@ -1,0 +1,236 @@
+#include <algorithm>
+#include <cmath>
+
+#include "pcg.cuh"
+
+namespace rschol {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int VEC_THREADS = 256;
+constexpr int VEC_BLOCKS = 152 * 8;   // fixed grid: 8 CTAs per SM on 152 SMs
+
+enum { S_DELTA = 0, S_ALPHA, S_BETA, S_RREL, S_BNORM, S_DQ, S_DELTA_NEW, S_BREAK, S_COUNT };
+enum { F_ALPHA = 0, F_RNORM, F_BETA, F_DELTA0, F_BNORM, F_TRUE };
+
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double ws[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) ws[warp] = v;
+  __syncthreads();
+  double t = 0;
+  if (warp == 0) {
+    t = (lane < (int)(blockDim.x >> 5)) ? ws[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(FULL, t, o);
+  }
+  return t;   // valid in thread 0
+}
+
+template <int TPR>
+__global__ void spmv_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                            const double* __restrict__ v, const double* __restrict__ x, double* __restrict__ y,
+                            double* __restrict__ part, int withDot) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = (int)(g / TPR), lane = (int)(g % TPR);
+  double s = 0.0;
+  if (row < n)
+    for (int p = rp[row] + lane; p < rp[row + 1]; p += TPR) s += v[p] * x[ci[p]];
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(FULL, s, o, TPR);
+  double dq = 0.0;
+  if (lane == 0 && row < n) {
+    y[row] = s;
+    dq = x[row] * s;
+  }
+  if (withDot) {
+    double t = block_sum(dq);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+  }
+}
+
+__global__ void dot_kernel(const double* __restrict__ a, const double* __restrict__ b, int n,
+                           double* __restrict__ part) {
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += a[i] * b[i];
+  double t = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void finish_kernel(const double* __restrict__ part, int count, double* __restrict__ sc, int mode) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) s += part[i];
+  double t = block_sum(s);
+  if (threadIdx.x != 0) return;
+  switch (mode) {
+    case F_ALPHA: {
+      sc[S_DQ] = t;
+      if (fabs(t) > 0.0) sc[S_ALPHA] = sc[S_DELTA] / t;
+      else { sc[S_ALPHA] = 0.0; sc[S_BREAK] = 1.0; }
+      break;
+    }
+    case F_RNORM: sc[S_RREL] = sqrt(t) / sc[S_BNORM]; break;
+    case F_BETA: {
+      sc[S_DELTA_NEW] = t;
+      sc[S_BETA] = t / sc[S_DELTA];
+      sc[S_DELTA] = t;
+      break;
+    }
+    case F_DELTA0: sc[S_DELTA] = t; break;
+    case F_BNORM: sc[S_BNORM] = sqrt(t); break;
+    case F_TRUE: sc[S_RREL] = sqrt(t) / sc[S_BNORM]; break;
+  }
+}
+
+__global__ void update_xr_kernel(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ d,
+                                 const double* __restrict__ q, const double* __restrict__ sc, int n,
+                                 double* __restrict__ part) {
+  const double a = sc[S_ALPHA];
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] += a * d[i];
+    const double ri = r[i] - a * q[i];
+    r[i] = ri;
+    s += ri * ri;
+  }
+  double t = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void update_d_kernel(double* __restrict__ d, const double* __restrict__ s,
+                                const double* __restrict__ sc, int n) {
+  const double b = sc[S_BETA];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) d[i] = s[i] + b * d[i];
+}
+
+__global__ void residual_kernel(const double* __restrict__ b, const double* __restrict__ q, int n,
+                                double* __restrict__ part) {
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double e = b[i] - q[i];
+    s += e * e;
+  }
+  double t = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void gather_kernel(const double* __restrict__ src, const int* __restrict__ perm, double* __restrict__ dst,
+                              int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[perm[i]];
+}
+
+__global__ void scatter_perm_kernel(const double* __restrict__ src, const int* __restrict__ perm,
+                                    double* __restrict__ dst, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[perm[i]] = src[i];
+}
+
+}  // namespace
+
+void launch_gather(const double* src, const int* perm, double* dst, int n, cudaStream_t s) {
+  gather_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(src, perm, dst, n);
+  RSCHOL_LAUNCH_CHECK();
+}
+void launch_scatter_perm(const double* src, const int* perm, double* dst, int n, cudaStream_t s) {
+  scatter_perm_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(src, perm, dst, n);
+  RSCHOL_LAUNCH_CHECK();
+}
+
+PcgEngine::PcgEngine(int n_, const std::vector<int>& rowptr, const std::vector<int>& colind,
+                     const std::vector<double>& vals, cudaStream_t s)
+    : n(n_), stream_(s) {
+  rowptr_.alloc(sizeof(int) * rowptr.size());
+  colind_.alloc(sizeof(int) * std::max<size_t>(1, colind.size()));
+  vals_.alloc(sizeof(double) * std::max<size_t>(1, vals.size()));
+  RSCHOL_CUDA(cudaMemcpyAsync(rowptr_.p, rowptr.data(), sizeof(int) * rowptr.size(), cudaMemcpyHostToDevice, s));
+  RSCHOL_CUDA(cudaMemcpyAsync(colind_.p, colind.data(), sizeof(int) * colind.size(), cudaMemcpyHostToDevice, s));
+  RSCHOL_CUDA(cudaMemcpyAsync(vals_.p, vals.data(), sizeof(double) * vals.size(), cudaMemcpyHostToDevice, s));
+  const double avg = n > 0 ? (double)colind.size() / n : 1.0;
+  tpr_ = avg <= 6 ? 4 : avg <= 12 ? 8 : avg <= 40 ? 16 : 32;
+  nblk_ = (int)(((long long)n * tpr_ + VEC_THREADS - 1) / VEC_THREADS);
+  for (auto* b : {&r_, &d_, &q_, &s_}) b->alloc(sizeof(double) * std::max(1, n));
+  part_.alloc(sizeof(double) * std::max(nblk_, VEC_BLOCKS));
+  scal_.alloc(sizeof(double) * S_COUNT);
+  RSCHOL_CUDA(cudaMallocHost((void**)&hScal_, sizeof(double) * S_COUNT));
+  spmvBytes = 12.0 * colind.size() + 4.0 * (n + 1) + 16.0 * n;
+  RSCHOL_CUDA(cudaStreamSynchronize(s));
+}
+
+PcgEngine::~PcgEngine() {
+  if (hScal_) cudaFreeHost(hScal_);
+}
+
+void PcgEngine::set_values(const std::vector<double>& vals) {
+  RSCHOL_CUDA(cudaMemcpyAsync(vals_.p, vals.data(), sizeof(double) * vals.size(), cudaMemcpyHostToDevice, stream_));
+}
+
+void PcgEngine::spmv(const double* x, double* y) {
+  switch (tpr_) {
+    case 4: spmv_kernel<4><<<nblk_, VEC_THREADS, 0, stream_>>>(n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
+    case 8: spmv_kernel<8><<<nblk_, VEC_THREADS, 0, stream_>>>(n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
+    case 16: spmv_kernel<16><<<nblk_, VEC_THREADS, 0, stream_>>>(n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
+    default: spmv_kernel<32><<<nblk_, VEC_THREADS, 0, stream_>>>(n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
+  }
+  RSCHOL_LAUNCH_CHECK();
+  ++launches;
+}
+
+PcgResult PcgEngine::solve(const double* b, double* x, double eps, int maxit,
+                           const std::function<void(double*)>& apply) {
+  PcgResult res;
+  double* r = r_.as<double>();
+  double* d = d_.as<double>();
+  double* q = q_.as<double>();
+  double* s = s_.as<double>();
+  double* part = part_.as<double>();
+  double* sc = scal_.as<double>();
+  cudaStream_t st = stream_;
+  launches = 0;
+  RSCHOL_CUDA(cudaMemsetAsync(sc, 0, sizeof(double) * S_COUNT, st));
+  RSCHOL_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+  RSCHOL_CUDA(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  dot_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(b, b, n, part);
+  finish_kernel<<<1, 1024, 0, st>>>(part, VEC_BLOCKS, sc, F_BNORM);
+  RSCHOL_CUDA(cudaMemcpyAsync(s, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  apply(s);
+  dot_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(r, s, n, part);
+  finish_kernel<<<1, 1024, 0, st>>>(part, VEC_BLOCKS, sc, F_DELTA0);
+  RSCHOL_CUDA(cudaMemcpyAsync(d, s, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  launches += 4;
+  RSCHOL_LAUNCH_CHECK();
+  double maxR = 2.0 * eps;
+  int i = 0;
+  while (i < maxit && maxR > eps) {
+    spmv(d, q);
+    finish_kernel<<<1, 1024, 0, st>>>(part, nblk_, sc, F_ALPHA);
+    update_xr_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(x, r, d, q, sc, n, part);
+    finish_kernel<<<1, 1024, 0, st>>>(part, VEC_BLOCKS, sc, F_RNORM);
+    RSCHOL_CUDA(cudaMemcpyAsync(s, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    apply(s);
+    dot_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(r, s, n, part);
+    finish_kernel<<<1, 1024, 0, st>>>(part, VEC_BLOCKS, sc, F_BETA);
+    update_d_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(d, s, sc, n);
+    RSCHOL_LAUNCH_CHECK();
+    launches += 6;
+    RSCHOL_CUDA(cudaMemcpyAsync(hScal_, sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
+    RSCHOL_CUDA(cudaStreamSynchronize(st));
+    maxR = hScal_[S_RREL];
+    if (hScal_[S_BREAK] != 0.0) res.breakdown = true;
+    ++i;
+    if (!(maxR == maxR)) break;   // NaN: stop
+  }
+  res.iterations = i;
+  res.residual = maxR;
+  // true residual ||b - A x|| / ||b||
+  spmv(x, q);
+  residual_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(b, q, n, part);
+  finish_kernel<<<1, 1024, 0, st>>>(part, VEC_BLOCKS, sc, F_TRUE);
+  RSCHOL_LAUNCH_CHECK();
+  launches += 2;
+  RSCHOL_CUDA(cudaMemcpyAsync(hScal_, sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
+  RSCHOL_CUDA(cudaStreamSynchronize(st));
+  res.trueResidual = hScal_[S_RREL];
+  return res;
+}
+
+}  // namespace rschol

@@ -1,0 +1,59 @@
+// Preconditioned conjugate gradients on the device (FP64 recurrences).
+//
+// PCG_SOLVER::solvePCG (src/rschol/linearalgebra/PCG_SOLVER.cpp:226-363):
+// x0 = 0, r = b, s = M^{-1} r, d = s, delta = r.s; per iteration
+// q = A d (CSR SpMV with the caller's full A), alpha = delta / (d.q) (0 when
+// d.q == 0, the reference's breakdown branch), x += alpha d, r -= alpha q,
+// s = M^{-1} r, beta = (r.s) / delta, d = s + beta d, stop when
+// ||r|| / ||b|| <= eps or after maxit iterations; the true residual
+// ||b - A x|| / ||b|| is recomputed at the end.
+//
+// The whole solve runs in the factor's permuted ordering (A is permuted
+// once), so the preconditioner needs no gather/scatter; dot products use a
+// two-pass fixed-order reduction, so results are reproducible bit for bit.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <functional>
+#include <vector>
+
+#include "common.cuh"
+
+namespace rschol {
+
+struct PcgResult {
+  int iterations = 0;
+  double residual = 0;
+  double trueResidual = 0;
+  bool breakdown = false;
+};
+
+class PcgEngine {
+ public:
+  // rowptr/colind/vals: CSR of the permuted full matrix (host).
+  PcgEngine(int n, const std::vector<int>& rowptr, const std::vector<int>& colind, const std::vector<double>& vals,
+            cudaStream_t s);
+  ~PcgEngine();
+  void set_values(const std::vector<double>& vals);
+  // d_b, d_x: permuted vectors on the device.  apply: in-place M^{-1}.
+  PcgResult solve(const double* d_b, double* d_x, double eps, int maxit,
+                  const std::function<void(double*)>& apply);
+  // y = A x on permuted device vectors
+  void spmv(const double* x, double* y);
+  long long launches = 0;
+  double spmvBytes = 0;    // algorithmic bytes of one SpMV
+  int n;
+
+ private:
+  cudaStream_t stream_;
+  DevBuf rowptr_, colind_, vals_, r_, d_, q_, s_, part_, scal_;
+  double* hScal_ = nullptr;   // pinned
+  int nblk_ = 0;
+  int tpr_ = 8;
+};
+
+// permuted <-> original order, nrhs = 1
+void launch_gather(const double* src, const int* perm, double* dst, int n, cudaStream_t s);
+void launch_scatter_perm(const double* src, const int* perm, double* dst, int n, cudaStream_t s);
+
+}  // namespace rschol
