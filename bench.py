@@ -1,0 +1,356 @@
+"""Benchmark: factor + PCG to a 1e-8 relative residual on one GB300.
+
+A step is one numeric factorisation of the workload's matrix (same pattern,
+values resident on the device) followed by one PCG solve to ||r||/||b|| <=
+1e-8.  `value` is solves per second over the K timed steps (whole job: N
+independent replicas under torchrun, max time over ranks).  `e2e` is the same
+step through the C ABI with host buffers (values and right-hand side copied
+in, solution copied out inside the timed region).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2]
+                    [--precision fp64|mixed] [--impl ours|reference]
+
+The CPU baseline (and the reference arm) is the CPU oracle -- the FP64
+restatement of the reference's factor + PCG path (the reference itself
+cannot be built: CHOLMOD, CSparse, Boost and LAPACKE are absent) -- timed on
+the host cores with threaded BLAS.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # name: (description, generator kwargs, nrhs)
+    "c1": ("2D 5-point Poisson 128x128, Dirichlet, seed 0", ("diffusion", 2, 128, 0.0, 0), 1),
+    "c2": ("3D 7-point variable-coefficient diffusion 64^3, log-normal sigma=1 seed 1, harmonic faces",
+           ("diffusion", 3, 64, 1.0, 1), 1),
+    "c3": ("3D Q1 hex linear elasticity 48^3 elements, E=1 nu=0.3, x=0 face clamped, seed 2",
+           ("elasticity", 48, 0, 0, 2), 1),
+    "c4": ("2D 5-point variable-coefficient 1024^2, log-normal sigma=2 seed 3, 64 RHS",
+           ("diffusion", 2, 1024, 2.0, 3), 64),
+}
+
+
+def make_problem(cfg):
+    import rank_structured_cholesky_gb300 as rs
+    _, spec, nrhs = CONFIGS[cfg]
+    if spec[0] == "diffusion":
+        _, dim, nx, sigma, seed = spec
+        return rs.diffusion(dim, nx, sigma=sigma, seed=seed, nrhs=nrhs)
+    _, ne, _, _, seed = spec
+    return rs.elasticity(ne, seed=seed, nrhs=nrhs)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup(gpus):
+    if gpus <= 1 and "RANK" not in os.environ:
+        return 0, 1, None
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", gpus))
+    backend = "nccl" if os.environ.get("RSCHOL_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+    dist.init_process_group(backend=backend)
+    return rank, world, dist
+
+
+def reduce_max(dist, value, device):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_oracle_solve(prob, params):
+    from oracle import pyoracle as po
+    t0 = time.perf_counter()
+    F = po.OracleFactor(prob.colptr, prob.rowind, prob.vals, prob.xyz, params)
+    t1 = time.perf_counter()
+    assert F.factor() == 0
+    t2 = time.perf_counter()
+    x, it, rec, true = F.pcg(prob.rhs[0], 1e-8, 10000)
+    t3 = time.perf_counter()
+    return dict(symbolic_s=t1 - t0, factor_s=t2 - t1, pcg_s=t3 - t2, iterations=it, true_residual=true)
+
+
+def run_reference(args):
+    rank, world, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return 0
+    prob = make_problem(args.config)
+    params = dict()
+    cores = os.cpu_count()
+    for _ in range(args.warmup):
+        cpu_oracle_solve(prob, params)
+    times = []
+    last = None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        last = cpu_oracle_solve(prob, params)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = args.steps / total
+    line = {
+        "impl": "reference", "metric": "factor+PCG solves/s to 1e-8 relative residual", "value": value,
+        "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.config, "description": CONFIGS[args.config][0], "n": prob.n,
+                   "parallelism": "single process, threaded BLAS"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": "full %s solve per step (symbolic + factor + PCG to 1e-8)" % args.config},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "iterations": last["iterations"], "true_residual": last["true_residual"],
+        "factor_s": last["factor_s"], "pcg_s": last["pcg_s"], "symbolic_s": last["symbolic_s"],
+        "p50_ms": 1e3 * statistics.median(times),
+        "p99_ms": 1e3 * float(np.percentile(times, 99)),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import rank_structured_cholesky_gb300 as rs
+
+    rank, world, dist = dist_setup(args.gpus)
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    lib = rs.load_library()
+    prob = make_problem(args.config)
+    params = dict(precision=args.precision, device=local)
+    ctx = rs.Context(**params)
+    t0 = time.perf_counter()
+    F = rs.GpuFactor(ctx, prob.colptr, prob.rowind, prob.vals, prob.xyz)
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(lib.rschol_stream(ctx.h), device=device)
+    n, nrhs = prob.n, prob.nrhs
+    d_vals = torch.from_numpy(prob.vals).to(device)
+    d_b = torch.from_numpy(np.ascontiguousarray(prob.rhs[:nrhs])).to(device)
+    d_x = torch.zeros_like(d_b)
+    infos = (rs.PcgInfo * nrhs)()
+
+    def step_device():
+        st = lib.rschol_refactor_device(F.h, d_vals.data_ptr())
+        if st != 0:
+            raise rs.RscholError(st, ctx.last_error())
+        st = lib.rschol_pcg_device(F.h, d_b.data_ptr(), d_x.data_ptr(), nrhs, 1e-8, 10000, infos)
+        if st not in (0, 5):
+            raise rs.RscholError(st, ctx.last_error())
+
+    h_vals = prob.vals
+    h_b = np.ascontiguousarray(prob.rhs[:nrhs])
+    h_x = np.zeros_like(h_b)
+
+    def step_e2e():
+        st = lib.rschol_refactor(F.h, rs._dp(h_vals))
+        if st != 0:
+            raise rs.RscholError(st, ctx.last_error())
+        st = lib.rschol_pcg(F.h, rs._dp(h_b), rs._dp(h_x), nrhs, 1e-8, 10000, infos)
+        if st not in (0, 5):
+            raise rs.RscholError(st, ctx.last_error())
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    if args.profile:
+        # ncu --profile-from-start off: capture exactly the K steps
+        torch.cuda.profiler.start()
+        for _ in range(args.steps):
+            step_device()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        if rank == 0:
+            print(json.dumps({"profiled_steps": args.steps, "config": args.config, "precision": args.precision,
+                              "iterations": [infos[k].iterations for k in range(nrhs)]}), flush=True)
+        return 0
+    barrier(dist)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for k in range(args.steps):
+            step_device()
+            ev[k + 1].record(stream)
+        torch.cuda.synchronize()
+    barrier(dist)
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_s = ev[0].elapsed_time(ev[args.steps]) / 1e3
+    total_s = reduce_max(dist, total_s, device)
+    iters = [infos[k].iterations for k in range(nrhs)]
+    resid = max(infos[k].true_residual for k in range(nrhs))
+    stats = F.stats()
+    desc = F.describe()
+
+    # end to end through the C ABI with host buffers
+    for _ in range(max(1, args.warmup // 2)):
+        step_e2e()
+    torch.cuda.synchronize()
+    barrier(dist)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_e2e()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = reduce_max(dist, e0.elapsed_time(e1) / 1e3, device)
+
+    # phase breakdown and the roofline of the dominant kernel family
+    phase = profile_phases(lib, F, ctx, stream, d_b, nrhs, torch)
+    hbm, bf16, src = peaks()
+    line = None
+    if rank == 0:
+        value = world * args.steps / total_s
+        cpu = None
+        if not args.no_cpu_baseline and world == 1:
+            cores = os.cpu_count()
+            res = cpu_oracle_solve(prob, dict())
+            t = res["symbolic_s"] + res["factor_s"] + res["pcg_s"]
+            cpu = {"value": 1.0 / t, "unit": "solves/s", "cores": cores, "kind": "port",
+                   "sample": "one full %s solve (symbolic + FP64 factor + PCG to 1e-8, %d iterations) with the "
+                             "CPU oracle, threaded BLAS" % (args.config, res["iterations"]),
+                   "factor_s": res["factor_s"], "pcg_s": res["pcg_s"], "iterations": res["iterations"]}
+        roof = phase["roofline"]
+        roof["peak"] = hbm if roof["bound"] == "hbm" else bf16
+        roof["frac"] = roof["achieved"] / roof["peak"]
+        roof["peak_source"] = src
+        line = {
+            "metric": "factor+PCG solves/s to 1e-8 relative residual", "value": value, "unit": "solves/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32 factor / f64 pcg",
+            "data": "synthetic",
+            "config": {"workload": args.config, "description": CONFIGS[args.config][0], "n": n, "nrhs": nrhs,
+                       "precision": args.precision, "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (factor arena %.0f MB)" % (stats["device_bytes"] / 1e6)},
+            "e2e": {"value": world * args.steps / e2e_s, "unit": "solves/s",
+                    "h2d_bytes_per_step": int(prob.vals.nbytes + h_b.nbytes),
+                    "d2h_bytes_per_step": int(h_x.nbytes)},
+            "gpu_launches": int(args.steps * (phase["factor_launches"] + phase["pcg_launches"])),
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "iterations": iters if nrhs > 1 else iters[0], "true_residual": resid,
+            "factor_ms": phase["factor_ms"], "pcg_ms": phase["pcg_ms"], "apply_ms": phase["apply_ms"],
+            "spmv_ms": phase["spmv_ms"], "setup_s": setup_s, "symbolic_s": stats["symbolic_s"],
+            "p50_ms": statistics.median(step_ms), "p99_ms": float(np.percentile(step_ms, 99)),
+            "factor_gflop": stats["factor_flops"] / 1e9, "structure": desc,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def profile_phases(lib, F, ctx, stream, d_b, nrhs, torch):
+    """CUDA-event timings of the factor, one preconditioner apply, one SpMV."""
+    import ctypes
+    out = np.zeros(16)
+    st = lib.rschol_profile(F.h, d_b.data_ptr(), out.ctypes.data)
+    if st != 0:
+        raise RuntimeError("rschol_profile failed: %s" % ctx.last_error())
+    factor_ms, apply_ms, spmv_ms, pcg_ms = out[0], out[1], out[2], out[3]
+    apply_bytes, spmv_bytes = out[4], out[5]
+    factor_launches, pcg_launches = out[6], out[7]
+    dom_ms, dom_bytes, name = out[8], out[9], "compressed/interior solve kernels (one preconditioner apply)"
+    return {"factor_ms": factor_ms, "apply_ms": apply_ms, "spmv_ms": spmv_ms, "pcg_ms": pcg_ms,
+            "factor_launches": factor_launches, "pcg_launches": pcg_launches,
+            "roofline": {"bound": "hbm", "kernel": name, "achieved": apply_bytes / (apply_ms * 1e-3) / 1e9,
+                         "unit": "GB/s", "traffic": None,
+                         "algorithmic_bytes_per_launch": apply_bytes, "launch_ms": apply_ms,
+                         "spmv_GBs": spmv_bytes / (spmv_ms * 1e-3) / 1e9}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="warm up, then run the steps between cudaProfilerStart/Stop (for ncu), no timing line")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

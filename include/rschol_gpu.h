@@ -85,7 +85,21 @@ int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* r
  * numeric factor needed (FactorPreconditioner.cpp:115-129). */
 int rschol_refactor(rschol_factor* f, const double* vals);
 
+/* Same, with the new values (full CSC order) already resident on the device. */
+int rschol_refactor_device(rschol_factor* f, const double* d_vals);
+
 void rschol_factor_free(rschol_factor* f);
+
+/* The context's CUDA stream (cudaStream_t): every call of the context runs
+ * on it and synchronises it before returning. */
+void* rschol_stream(rschol_ctx* ctx);
+
+/* CUDA-event timings on the context stream, for benchmarks: out[0] numeric
+ * factorisation ms, [1] one preconditioner apply ms, [2] one SpMV ms, [3] one
+ * PCG solve of d_b (device, original order) ms, [4] algorithmic bytes of an
+ * apply, [5] of an SpMV, [6] factorisation launches, [7] launches of the PCG
+ * solve, [10] its iterations, [11] its true residual. */
+int rschol_profile(rschol_factor* f, const double* d_b, double* out);
 
 /* x = M^{-1} b for nrhs column-major right-hand sides.
  * Replaces FactorPreconditioner::solve (FactorPreconditioner.cpp:135-162),

@@ -30,7 +30,7 @@ FP64, MIXED = 0, 1
 # Every entry point declared in include/rschol_gpu.h.
 EXPORTED = [
     "rschol_default_params", "rschol_create", "rschol_destroy", "rschol_last_error", "rschol_factor_create",
-    "rschol_refactor", "rschol_factor_free", "rschol_precond_apply", "rschol_precond_apply_device", "rschol_pcg",
+    "rschol_refactor", "rschol_refactor_device", "rschol_stream", "rschol_profile", "rschol_factor_free", "rschol_precond_apply", "rschol_precond_apply_device", "rschol_pcg",
     "rschol_pcg_device", "rschol_pcg_pysolve", "rschol_factor_n", "rschol_factor_num_nodes",
     "rschol_factor_node_info", "rschol_factor_node_l11", "rschol_factor_node_l21", "rschol_factor_perm",
     "rschol_factor_describe", "rschol_factor_stats", "rschol_problem_diffusion", "rschol_problem_elasticity",
@@ -82,6 +82,9 @@ def load_library():
         "rschol_last_error": (ctypes.c_char_p, [P]),
         "rschol_factor_create": (I, [P, I, pI, pI, pD, pD, ctypes.POINTER(P)]),
         "rschol_refactor": (I, [P, pD]),
+        "rschol_refactor_device": (I, [P, P]),
+        "rschol_stream": (P, [P]),
+        "rschol_profile": (I, [P, P, P]),
         "rschol_factor_free": (None, [P]),
         "rschol_precond_apply": (I, [P, pD, pD, I]),
         "rschol_precond_apply_device": (I, [P, P, P, I]),

@@ -56,6 +56,7 @@ struct Impl {
   virtual int run() = 0;
   virtual void apply(double* d_w, cudaStream_t s) = 0;
   virtual void set_values(const double* lower) = 0;
+  virtual double* device_values() = 0;
   virtual long long launches() const = 0;
   virtual long long apply_launches() const = 0;
   virtual double flops() const = 0;
@@ -77,6 +78,7 @@ struct ImplT : Impl {
   int run() override { return fe.run(); }
   void apply(double* w, cudaStream_t s) override { se.apply_inplace(w, s); }
   void set_values(const double* lower) override { fe.set_values(lower); }
+  double* device_values() override { return fe.dAvals.template as<double>(); }
   long long launches() const override { return fe.launches; }
   long long apply_launches() const override { return se.launches_per_apply(); }
   double flops() const override { return fe.flops; }
@@ -132,7 +134,7 @@ struct rschol_factor {
   std::unique_ptr<Impl> impl;
   std::unique_ptr<PcgEngine> pcg;
   std::vector<int> permCsrSrc;  // permuted CSR value k = Afull.x[permCsrSrc[k]]
-  DevBuf dPerm, dB, dX, dBp, dXp;
+  DevBuf dPerm, dB, dX, dBp, dXp, dLowerSrc, dCsrSrc;
   int nrhsCap = 0;
   double tSymbolic = 0, tNumeric = 0;
   int attempts = 0;
@@ -278,6 +280,12 @@ int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* r
     f->pcg.reset(new PcgEngine(n, rp, ci, cv, ctx->stream));
     f->dPerm.alloc(sizeof(int) * n);
     RSCHOL_CUDA(cudaMemcpy(f->dPerm.p, f->ord.perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    f->dLowerSrc.alloc(sizeof(int) * std::max<size_t>(1, f->lowerSrc.size()));
+    RSCHOL_CUDA(cudaMemcpy(f->dLowerSrc.p, f->lowerSrc.data(), sizeof(int) * f->lowerSrc.size(),
+                           cudaMemcpyHostToDevice));
+    f->dCsrSrc.alloc(sizeof(int) * std::max<size_t>(1, f->permCsrSrc.size()));
+    RSCHOL_CUDA(cudaMemcpy(f->dCsrSrc.p, f->permCsrSrc.data(), sizeof(int) * f->permCsrSrc.size(),
+                           cudaMemcpyHostToDevice));
     int st = numeric_with_retry(f.get());
     if (st != RSCHOL_OK) return st;
   } catch (const CudaError& e) {
@@ -310,6 +318,76 @@ int rschol_refactor(rschol_factor* f, const double* vals) {
   } catch (const std::exception& e) {
     return fail(f->ctx, RSCHOL_E_CUDA, e.what());
   }
+}
+
+static void ensure_vecs(rschol_factor* f, int nrhs);
+
+int rschol_refactor_device(rschol_factor* f, const double* d_vals) {
+  if (!f || !d_vals) return RSCHOL_E_BAD_INPUT;
+  try {
+    cudaStream_t s = f->ctx->stream;
+    launch_index_gather(d_vals, f->dLowerSrc.as<int>(), f->impl->device_values(), (long long)f->lowerSrc.size(), s);
+    launch_index_gather(d_vals, f->dCsrSrc.as<int>(), f->pcg->values(), (long long)f->permCsrSrc.size(), s);
+    if (f->attempts > 1) {
+      assign_ranks(f->S, f->prm, f->prm.rank_constant, f->prm.diag_rank_constant);
+      f->impl->plan();
+    }
+    return numeric_with_retry(f);
+  } catch (const std::exception& e) {
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+}
+
+void* rschol_stream(rschol_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int rschol_profile(rschol_factor* f, const double* d_b, double* out) {
+  if (!f || !d_b || !out) return RSCHOL_E_BAD_INPUT;
+  try {
+    cudaStream_t s = f->ctx->stream;
+    ensure_vecs(f, 1);
+    cudaEvent_t e[8];
+    for (auto& x : e) RSCHOL_CUDA(cudaEventCreate(&x));
+    const int n = f->Afull.n;
+    RSCHOL_CUDA(cudaEventRecord(e[0], s));
+    int st = f->impl->run();
+    RSCHOL_CUDA(cudaEventRecord(e[1], s));
+    launch_gather(d_b, f->dPerm.as<int>(), f->dBp.as<double>(), n, s);
+    RSCHOL_CUDA(cudaEventRecord(e[2], s));
+    f->impl->apply(f->dBp.as<double>(), s);
+    RSCHOL_CUDA(cudaEventRecord(e[3], s));
+    f->pcg->spmv(f->dBp.as<double>(), f->dXp.as<double>());
+    RSCHOL_CUDA(cudaEventRecord(e[4], s));
+    launch_gather(d_b, f->dPerm.as<int>(), f->dBp.as<double>(), n, s);
+    Impl* impl = f->impl.get();
+    RSCHOL_CUDA(cudaEventRecord(e[5], s));
+    PcgResult r = f->pcg->solve(f->dBp.as<double>(), f->dXp.as<double>(), 1e-8, 10000,
+                                [impl, s](double* w) { impl->apply(w, s); });
+    RSCHOL_CUDA(cudaEventRecord(e[6], s));
+    RSCHOL_CUDA(cudaEventSynchronize(e[6]));
+    float ms[6];
+    RSCHOL_CUDA(cudaEventElapsedTime(&ms[0], e[0], e[1]));
+    RSCHOL_CUDA(cudaEventElapsedTime(&ms[1], e[2], e[3]));
+    RSCHOL_CUDA(cudaEventElapsedTime(&ms[2], e[3], e[4]));
+    RSCHOL_CUDA(cudaEventElapsedTime(&ms[3], e[5], e[6]));
+    for (auto& x : e) cudaEventDestroy(x);
+    out[0] = ms[0];
+    out[1] = ms[1];
+    out[2] = ms[2];
+    out[3] = ms[3];
+    out[4] = f->impl->apply_bytes();
+    out[5] = f->pcg->spmvBytes;
+    out[6] = (double)f->impl->launches();
+    out[7] = (double)f->pcg->launches + (double)r.iterations * f->impl->apply_launches() +
+             f->impl->apply_launches() + 2;
+    out[8] = ms[1];
+    out[9] = f->impl->apply_bytes();
+    out[10] = r.iterations;
+    out[11] = r.trueResidual;
+    if (st != 0) return fail(f->ctx, RSCHOL_E_NOT_PD_AFTER_RETRY, "profile factorisation failed");
+  } catch (const std::exception& e) {
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+  return RSCHOL_OK;
 }
 
 void rschol_factor_free(rschol_factor* f) { delete f; }

@@ -149,8 +149,9 @@ __global__ void __launch_bounds__(256) trsm_kernel(const TrsmTask<T>* __restrict
   const int r0 = (b - t.chunkBase) * 64;
   const int nr = min(64, t.rows - r0);
   const int w = t.w, tid = threadIdx.x;
-  __shared__ T L[64][65];
-  __shared__ T X[64][65];
+  extern __shared__ __align__(16) unsigned char trsm_smem[];
+  T (*L)[65] = reinterpret_cast<T (*)[65]>(trsm_smem);
+  T (*X)[65] = reinterpret_cast<T (*)[65]>(trsm_smem + sizeof(T) * 64 * 65);
   for (int idx = tid; idx < w * w; idx += blockDim.x) {
     int i = idx / w, j = idx - i * w;
     L[i][j] = (j <= i) ? t.L[(size_t)i * t.ldl + j] : T(0);
@@ -210,26 +211,106 @@ __global__ void scatter_kernel(const double* __restrict__ Avals, const long long
     dst[dstIdx[k]] = (T)Avals[srcIdx[k]];
 }
 
-template <class T> struct Unit;
-template <> struct Unit<double> { static __device__ double v() { return 1.1102230246251565e-16; } };
-template <> struct Unit<float> { static __device__ float v() { return 5.9604645e-08f; } };
+constexpr int QR_THREADS = 512;
 
-template <class T>
-__global__ void shift_diag_kernel(const ShiftTask<T>* __restrict__ tasks) {
-  const ShiftTask<T> t = tasks[blockIdx.x];
-  T* G = t.G;
-  const int r = t.r, ld = t.ld, rows = t.rows;
-  __shared__ double part[256];
-  double s = 0;
-  for (int i = threadIdx.x; i < r; i += blockDim.x) s += (double)G[(size_t)i * ld + i];
-  part[threadIdx.x] = s;
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum, broadcast to every thread.
+__device__ double block_sum_bcast(double v, double* red) {
+  v = warp_sum_d(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    double t = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.0;
+    t = warp_sum_d(t);
+    if (lane == 0) red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+// Householder QR (LAPACK dgeqr2: dlarfg reflectors with v_0 = 1) followed by
+// the explicit thin Q (dorg2r), on a column-major copy of Y.
+template <class T>
+__global__ void __launch_bounds__(QR_THREADS) householder_qr_kernel(const QrTask<T>* __restrict__ tasks) {
+  const QrTask<T> t = tasks[blockIdx.x];
+  const int n = t.n, r = t.r;
+  T* W = t.W;
+  T* tau = W + (size_t)r * n;
+  __shared__ double red[33];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  for (long long idx = tid; idx < (long long)n * r; idx += blockDim.x) {
+    const int i = (int)(idx / r), j = (int)(idx - (long long)i * r);
+    W[(size_t)j * n + i] = t.Y[idx];
+  }
+  __syncthreads();
+  for (int k = 0; k < r; ++k) {
+    T* ck = W + (size_t)k * n;
+    double s = 0.0;
+    for (int i = k + 1 + tid; i < n; i += blockDim.x) s += (double)ck[i] * (double)ck[i];
+    const double xnorm2 = block_sum_bcast(s, red);
+    const double alpha = (double)ck[k];
+    double tk = 0.0, beta = alpha, scal = 0.0;
+    if (xnorm2 > 0.0) {
+      beta = -copysign(sqrt(alpha * alpha + xnorm2), alpha);
+      tk = (beta - alpha) / beta;
+      scal = 1.0 / (alpha - beta);
+    }
+    __syncthreads();
+    if (xnorm2 > 0.0)
+      for (int i = k + 1 + tid; i < n; i += blockDim.x) ck[i] = (T)((double)ck[i] * scal);
+    if (tid == 0) {
+      ck[k] = (T)beta;
+      tau[k] = (T)tk;
+    }
+    __syncthreads();
+    if (tk != 0.0) {
+      for (int j = k + 1 + warp; j < r; j += nw) {
+        T* cj = W + (size_t)j * n;
+        double w = 0.0;
+        for (int i = k + 1 + lane; i < n; i += 32) w += (double)ck[i] * (double)cj[i];
+        w = warp_sum_d(w);
+        const double cjk = (double)cj[k];
+        __syncwarp();
+        w = tk * (w + cjk);
+        if (lane == 0) cj[k] = (T)(cjk - w);
+        for (int i = k + 1 + lane; i < n; i += 32) cj[i] = (T)((double)cj[i] - w * (double)ck[i]);
+      }
+    }
     __syncthreads();
   }
-  const double shift = 11.0 * ((double)rows * r + (double)r * (r + 1)) * (double)Unit<T>::v() * part[0];
-  for (int i = threadIdx.x; i < r; i += blockDim.x) G[(size_t)i * ld + i] += (T)shift;
+  for (int k = r - 1; k >= 0; --k) {
+    T* ck = W + (size_t)k * n;
+    const double tk = (double)tau[k];
+    if (tk != 0.0) {
+      for (int j = k + 1 + warp; j < r; j += nw) {
+        T* cj = W + (size_t)j * n;
+        double w = 0.0;
+        for (int i = k + 1 + lane; i < n; i += 32) w += (double)ck[i] * (double)cj[i];
+        w = warp_sum_d(w);
+        const double cjk = (double)cj[k];
+        __syncwarp();
+        w = tk * (w + cjk);
+        if (lane == 0) cj[k] = (T)(cjk - w);
+        for (int i = k + 1 + lane; i < n; i += 32) cj[i] = (T)((double)cj[i] - w * (double)ck[i]);
+      }
+    }
+    __syncthreads();
+    for (int i = k + 1 + tid; i < n; i += blockDim.x) ck[i] = (T)(-tk * (double)ck[i]);
+    for (int i = tid; i < k; i += blockDim.x) ck[i] = T(0);
+    if (tid == 0) ck[k] = (T)(1.0 - tk);
+    __syncthreads();
+  }
+  for (long long idx = tid; idx < (long long)n * r; idx += blockDim.x) {
+    const int i = (int)(idx / r), j = (int)(idx - (long long)i * r);
+    t.Y[idx] = W[(size_t)j * n + i];
+  }
 }
 
 template <class T>
@@ -277,7 +358,13 @@ template <class T> void launch_potrf(const PotrfTask<T>* d, int n, int* flag, cu
 }
 template <class T> void launch_trsm(const TrsmTask<T>* d, int n, int chunks, cudaStream_t s) {
   if (n <= 0 || chunks <= 0) return;
-  trsm_kernel<T><<<chunks, 256, 0, s>>>(d, n);
+  const int smem = (int)(2 * sizeof(T) * 64 * 65);
+  static bool configured = false;   // per instantiation
+  if (!configured) {
+    RSCHOL_CUDA(cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    configured = true;
+  }
+  trsm_kernel<T><<<chunks, 256, smem, s>>>(d, n);
   RSCHOL_LAUNCH_CHECK();
 }
 template <class T>
@@ -293,9 +380,9 @@ void launch_scatter(const double* A, const long long* si, const long long* di, l
   scatter_kernel<T><<<grid_for(count, 256), 256, 0, s>>>(A, si, di, count, dst);
   RSCHOL_LAUNCH_CHECK();
 }
-template <class T> void launch_shift_diag(const ShiftTask<T>* d, int n, cudaStream_t s) {
+template <class T> void launch_householder_qr(const QrTask<T>* d, int n, cudaStream_t s) {
   if (n <= 0) return;
-  shift_diag_kernel<T><<<n, 256, 0, s>>>(d);
+  householder_qr_kernel<T><<<n, QR_THREADS, 0, s>>>(d);
   RSCHOL_LAUNCH_CHECK();
 }
 template <class T> void launch_set_identity(const IdentTask<T>* d, int n, cudaStream_t s) {
@@ -316,7 +403,7 @@ template <class T> void launch_box_muller(const uint32_t* raw, long long count, 
   template void launch_extadd<T>(const ExtAddTarget<T>*, int, const ExtAddSource<T>*, int, cudaStream_t); \
   template void launch_scatter<T>(const double*, const long long*, const long long*, long long, T*,      \
                                   cudaStream_t);                                                         \
-  template void launch_shift_diag<T>(const ShiftTask<T>*, int, cudaStream_t);                            \
+  template void launch_householder_qr<T>(const QrTask<T>*, int, cudaStream_t);                           \
   template void launch_set_identity<T>(const IdentTask<T>*, int, cudaStream_t);                          \
   template void launch_box_muller<T>(const uint32_t*, long long, T*, cudaStream_t);
 RSCHOL_INST(double)

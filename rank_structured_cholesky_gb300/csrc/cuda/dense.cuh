@@ -76,15 +76,17 @@ void launch_extadd(const ExtAddTarget<T>* dTargets, int nTargets, const ExtAddSo
 template <class T>
 void launch_scatter(const double* Avals, const long long* srcIdx, const long long* dstIdx, long long count,
                     T* dst, cudaStream_t s);
-// Shifted CholeskyQR: G += 11 (rows*r + r(r+1)) u trace(G) I on each Gram
-// matrix (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa, SIAM J. Sci.
-// Comput. 42 (2020) A477-A503).
+// Thin Householder QR, Y (n x r, row-major, r <= n) := Q: the LAPACK
+// geqrf + orgqr pair the reference calls (MATRIX::qr / extractQRfactor,
+// src/rschol/linearalgebra/MATRIX_FAST.cpp:1095-1180), one CTA per matrix.
+// W is an r x n column-major scratch, tau r scalars.
 template <class T>
-struct ShiftTask {
-  T* G;
-  int r, ld, rows;
+struct QrTask {
+  T* Y;
+  T* W;
+  int n, r;
 };
-template <class T> void launch_shift_diag(const ShiftTask<T>* dTasks, int nTasks, cudaStream_t s);
+template <class T> void launch_householder_qr(const QrTask<T>* dTasks, int nTasks, cudaStream_t s);
 template <class T>
 struct IdentTask {
   T* U;

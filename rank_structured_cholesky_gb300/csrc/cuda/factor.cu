@@ -10,7 +10,6 @@ namespace rschol {
 
 namespace {
 constexpr int NB = 64;           // tile width of the blocked factorisations
-constexpr int QR_CODE = 1 << 29; // POTRF code for a Gram matrix of the QR
 int tiles_of(int M, int N) { return ((M + 63) / 64) * ((N + 63) / 64); }
 }  // namespace
 
@@ -181,37 +180,26 @@ void FactorEngine<T>::emit_rf(const std::vector<RFJob<T>>& jobs) {
       push_gemm(mk_gemm<T>(j.F, j.ld, true, j.X, j.r, false, j.Y, j.r, j.cols, j.r, j.rows, T(1), T(0)), tiles, gb);
     flush_gemm(gb, tiles);
   }
-  // Thin QR of Y by shifted CholeskyQR3.
-  std::vector<const RFJob<T>*> qr;
+  // Thin Householder QR of Y (the sketch of a fast-decaying block is
+  // numerically rank deficient, so Gram-based QR variants break down), or
+  // the identity basis.
+  std::vector<QrTask<T>> qt;
   std::vector<IdentTask<T>> id;
   for (auto& j : jobs) {
-    if (j.identity) id.push_back(IdentTask<T>{j.Y, j.cols, j.r});
-    else qr.push_back(&j);
+    if (j.identity) {
+      id.push_back(IdentTask<T>{j.Y, j.cols, j.r});
+    } else {
+      qt.push_back(QrTask<T>{j.Y, j.W, j.cols, j.r});
+      flops += 4.0 * j.cols * (double)j.r * j.r;
+    }
   }
   if (!id.empty()) {
     steps_.push_back(Step{ST_IDENT, (long long)ident_.size(), (int)id.size(), (int)id.size()});
     ident_.insert(ident_.end(), id.begin(), id.end());
   }
-  for (int round = 0; round < 3 && !qr.empty(); ++round) {
-    tiles = 0;
-    for (auto* j : qr)
-      push_gemm(mk_gemm<T>(j->Y, j->r, true, j->Y, j->r, false, j->Gm, j->r, j->r, j->r, j->cols, T(1), T(0)), tiles,
-                gb);
-    flush_gemm(gb, tiles);
-    if (round == 0) {
-      std::vector<ShiftTask<T>> sh;
-      for (auto* j : qr) sh.push_back(ShiftTask<T>{j->Gm, j->r, j->r, j->cols});
-      steps_.push_back(Step{ST_SHIFT, (long long)shift_.size(), (int)sh.size(), (int)sh.size()});
-      shift_.insert(shift_.end(), sh.begin(), sh.end());
-    }
-    std::vector<CholJob<T>> cj;
-    std::vector<TrsmJob<T>> tj;
-    for (auto* j : qr) {
-      cj.push_back(CholJob<T>{j->Gm, j->r, j->r, j->r, j->r, QR_CODE});
-      tj.push_back(TrsmJob<T>{j->Gm, j->Y, j->r, j->r, j->cols, j->r});
-    }
-    emit_chol(cj);
-    emit_trsm(tj);
+  if (!qt.empty()) {
+    steps_.push_back(Step{ST_QR, (long long)qr_.size(), (int)qt.size(), (int)qt.size()});
+    qr_.insert(qr_.end(), qt.begin(), qt.end());
   }
   // V = F U
   tiles = 0;
@@ -239,7 +227,7 @@ void FactorEngine<T>::plan() {
   trsm_.clear();
   eaT_.clear();
   eaS_.clear();
-  shift_.clear();
+  qr_.clear();
   ident_.clear();
   ints_.clear();
   flops = 0;
@@ -292,23 +280,36 @@ void FactorEngine<T>::plan() {
     uOff[j] = curV; curV += (long long)n * r;
     qOff[j] = curV; curV += (long long)r * r;
     xOff[j] = curV; curV += (long long)m * r;
-    gmOff[j] = curV; curV += (long long)r * r;
+    gmOff[j] = curV; curV += (long long)n * r + r;   // Householder QR scratch
   }
-  // HODLR internal-node buffers: V, Y/U, X, Gm
+  // HODLR internal-node buffers, per internal node (rows x cols block, rank r):
+  // V (rows*r) | Y/U (cols*r) | X (rows*r) | QR scratch (cols*r + r) |
+  // coupling scratch (hmax*hmax + hmax*cols + rows*cols)
   std::vector<std::vector<long long>> hOff(nn);
   long long curH = 0;
+  auto hdims = [&](const Node& nd, int q, int& rows, int& cols) {
+    const HNode& x = nd.H[q];
+    rows = nd.H[x.right].r1 - nd.H[x.right].r0 + 1;
+    cols = nd.H[x.left].r1 - nd.H[x.left].r0 + 1;
+  };
+  auto hscratch = [&](int j, int q) -> long long {   // offset of the coupling scratch
+    int rows, cols;
+    hdims(S.nodes[j], q, rows, cols);
+    const long long r = S.hRank[j][q];
+    return 2 * rows * r + 2 * cols * r + r;
+  };
   for (int j = 0; j < nn; ++j) {
     const Node& nd = S.nodes[j];
     hOff[j].assign(nd.H.size(), -1);
     if (!nd.compressed) continue;
+    long long hmax = 0;
+    for (int v : S.hRank[j]) hmax = std::max<long long>(hmax, v);
     for (size_t q = 0; q < nd.H.size(); ++q) {
-      const HNode& x = nd.H[q];
-      if (x.isLeaf()) continue;
-      const int rows = nd.H[x.right].r1 - nd.H[x.right].r0 + 1, cols = nd.H[x.left].r1 - nd.H[x.left].r0 + 1;
-      const int r = S.hRank[j][q];
+      if (nd.H[q].isLeaf()) continue;
+      int rows, cols;
+      hdims(nd, (int)q, rows, cols);
       hOff[j][q] = curH;
-      curH += (long long)rows * r * 2 + (long long)cols * r + (long long)r * r + (long long)r * r +
-              (long long)r * cols + (long long)rows * cols;  // + coupling scratch
+      curH += hscratch(j, (int)q) + hmax * hmax + hmax * cols + (long long)rows * cols;
     }
   }
   // compressed descendants and interior roots of each compressed supernode
@@ -554,7 +555,7 @@ void FactorEngine<T>::plan() {
       rj.V = base;
       rj.Y = base + (size_t)rows * r;
       rj.X = rj.Y + (size_t)cols * r;
-      rj.Gm = rj.X + (size_t)rows * r;
+      rj.W = rj.X + (size_t)rows * r;
       rj.Q = nullptr;
       rj.identity = identityAllowed && r >= cols;
       rj.expand = true;
@@ -622,9 +623,8 @@ void FactorEngine<T>::plan() {
             T* abase = H0 + hOff[j][anc];
             T* aV = abase;
             T* aU = abase + (size_t)aRows * ra;
-            T* scratch = H0 + hOff[j][be.h] + (size_t)rows * S.hRank[j][be.h] * 2 +
-                         (size_t)cols * S.hRank[j][be.h] + (size_t)S.hRank[j][be.h] * S.hRank[j][be.h];
-            T* W1 = scratch;                       // ra x ra = U^T U
+            T* scratch = H0 + hOff[j][be.h] + hscratch(j, be.h);
+            T* W1 = scratch;                      // ra x ra = U^T U
             T* W2 = W1 + (size_t)ra * ra;          // ra x cols = W1 V2^T
             gemm1(mk_gemm<T>(aU, ra, true, aU, ra, false, W1, ra, ra, ra, aCols, T(1), T(0)));
             gemm1(mk_gemm<T>(W1, ra, false, aV + (size_t)(lc.r0 - ar.r0) * ra, ra, true, W2, cols, ra, cols, ra, T(1),
@@ -650,7 +650,7 @@ void FactorEngine<T>::plan() {
           const int ra = S.hRank[j][anc];
           T* aV = H0 + hOff[j][anc];
           T* aU = aV + (size_t)aRows * ra;
-          T* Wv = aU + (size_t)aCols * ra + (size_t)aRows * ra + (size_t)ra * ra + (size_t)ra * ra;  // scratch
+          T* Wv = H0 + hOff[j][anc] + hscratch(j, anc);   // sz x aCols <= aRows x aCols
           gemm1(mk_gemm<T>(aV + (size_t)(x.r0 - ar.r0) * ra, ra, false, aU, ra, true, Wv, aCols, sz, aCols, ra, T(1),
                            T(0)));
           gemm1(mk_gemm<T>(Wv, aCols, false, Wv, aCols, true, Lb, L, sz, sz, aCols, T(-1), T(1), true));
@@ -674,7 +674,7 @@ void FactorEngine<T>::plan() {
       rj.G = draw_of(j, 2, -1);
       rj.Y = V0 + uOff[j];
       rj.X = V0 + xOff[j];
-      rj.Gm = V0 + gmOff[j];
+      rj.W = V0 + gmOff[j];
       rj.V = V0 + vOff[j];
       rj.Q = V0 + qOff[j];
       rj.identity = rank[j] >= nd.n;
@@ -699,7 +699,7 @@ void FactorEngine<T>::plan() {
   up(dTrsm_, trsm_.data(), trsm_.size() * sizeof(TrsmTask<T>));
   up(dEaT_, eaT_.data(), eaT_.size() * sizeof(ExtAddTarget<T>));
   up(dEaS_, eaS_.data(), eaS_.size() * sizeof(ExtAddSource<T>));
-  up(dShift_, shift_.data(), shift_.size() * sizeof(ShiftTask<T>));
+  up(dQr_, qr_.data(), qr_.size() * sizeof(QrTask<T>));
   up(dIdent_, ident_.data(), ident_.size() * sizeof(IdentTask<T>));
   up(dScatSrc_, scatSrc_.data(), scatSrc_.size() * sizeof(long long));
   up(dScatDst_, scatDst_.data(), scatDst_.size() * sizeof(long long));
@@ -730,7 +730,7 @@ int FactorEngine<T>::run() {
         launch_extadd<T>(dEaT_.as<ExtAddTarget<T>>() + st.off, st.count, dEaS_.as<ExtAddSource<T>>(), st.grid,
                          stream);
         break;
-      case ST_SHIFT: launch_shift_diag<T>(dShift_.as<ShiftTask<T>>() + st.off, st.count, stream); break;
+      case ST_QR: launch_householder_qr<T>(dQr_.as<QrTask<T>>() + st.off, st.count, stream); break;
       case ST_IDENT: launch_set_identity<T>(dIdent_.as<IdentTask<T>>() + st.off, st.count, stream); break;
     }
     ++launches;

@@ -42,7 +42,7 @@ enum StepKind : int {
   ST_POTRF,
   ST_TRSM,
   ST_EXTADD,
-  ST_SHIFT,
+  ST_QR,
   ST_IDENT,
 };
 
@@ -73,7 +73,7 @@ struct RFJob {     // randomized range finder on the dense block F (rows x cols)
   const T* G;      // rows x r Gaussian sketch
   T* Y;            // cols x r: sketch, then the orthonormal basis U
   T* X;            // rows x r scratch
-  T* Gm;           // r x r Gram scratch
+  T* W;            // cols x r + r scratch of the Householder QR
   T* V;            // rows x r
   T* Q;            // r x r: U^T U (may be null)
   bool identity;   // r >= cols: U = I (FactorManager.cpp:9598-9606)
@@ -127,12 +127,12 @@ class FactorEngine {
   std::vector<TrsmTask<T>> trsm_;
   std::vector<ExtAddTarget<T>> eaT_;
   std::vector<ExtAddSource<T>> eaS_;
-  std::vector<ShiftTask<T>> shift_;
+  std::vector<QrTask<T>> qr_;
   std::vector<IdentTask<T>> ident_;
   std::vector<int> ints_;
   std::vector<long long> scatSrc_, scatDst_;
   std::vector<int> scatIsInterior_;
-  DevBuf dGemm_, dPotrf_, dTrsm_, dEaT_, dEaS_, dShift_, dIdent_, dInts_, dScatSrc_, dScatDst_;
+  DevBuf dGemm_, dPotrf_, dTrsm_, dEaT_, dEaS_, dQr_, dIdent_, dInts_, dScatSrc_, dScatDst_;
   DevBuf dScatSrcC_, dScatDstC_;
   long long nScatI_ = 0, nScatC_ = 0;
   bool planned_ = false;

@@ -125,7 +125,20 @@ __global__ void scatter_perm_kernel(const double* __restrict__ src, const int* _
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[perm[i]] = src[i];
 }
 
+__global__ void index_gather_kernel(const double* __restrict__ src, const int* __restrict__ idx,
+                                    double* __restrict__ dst, long long count) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count;
+       k += (long long)gridDim.x * blockDim.x)
+    dst[k] = src[idx[k]];
+}
+
 }  // namespace
+
+void launch_index_gather(const double* src, const int* idx, double* dst, long long count, cudaStream_t s) {
+  if (count <= 0) return;
+  index_gather_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(src, idx, dst, count);
+  RSCHOL_LAUNCH_CHECK();
+}
 
 void launch_gather(const double* src, const int* perm, double* dst, int n, cudaStream_t s) {
   gather_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(src, perm, dst, n);

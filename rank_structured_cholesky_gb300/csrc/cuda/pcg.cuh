@@ -35,6 +35,7 @@ class PcgEngine {
             cudaStream_t s);
   ~PcgEngine();
   void set_values(const std::vector<double>& vals);
+  double* values() { return vals_.as<double>(); }
   // d_b, d_x: permuted vectors on the device.  apply: in-place M^{-1}.
   PcgResult solve(const double* d_b, double* d_x, double eps, int maxit,
                   const std::function<void(double*)>& apply);
@@ -52,6 +53,8 @@ class PcgEngine {
   int tpr_ = 8;
 };
 
+// dst[k] = src[idx[k]], k < count (value re-mapping on the device)
+void launch_index_gather(const double* src, const int* idx, double* dst, long long count, cudaStream_t s);
 // permuted <-> original order, nrhs = 1
 void launch_gather(const double* src, const int* perm, double* dst, int n, cudaStream_t s);
 void launch_scatter_perm(const double* src, const int* perm, double* dst, int n, cudaStream_t s);

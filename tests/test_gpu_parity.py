@@ -1,0 +1,173 @@
+"""GPU parity: the CUDA factor / preconditioner / PCG against the CPU oracle.
+
+Tolerances (FP64 path), relative Frobenius / 2-norm error against the oracle:
+  * EXACT_TOL = 1e-11 for blocks no compression touches (interior factor
+    panels of supernodes whose interior block has no compressed ancestor
+    contribution, i.e. everything below the first compressed separator);
+  * COMPRESSED_TOL = 1e-6 for everything a randomized compression feeds
+    (L11 of HODLR diagonals, V U^T, and every block assembled from them).
+    The sketch Y = (L21^T L21) L21^T G has numerical rank below r; the basis
+    columns beyond that rank are fixed by rounding in any QR (LAPACK's
+    included), so V U^T = L21 U U^T agrees only up to the neglected singular
+    values of L21;
+  * APPLY_TOL = 1e-7 for one preconditioner application.
+PCG reaches ||r||/||b|| <= 1e-8 in the oracle's iteration count +-1.  Mixed
+precision (FP32 factor, FP64 PCG) must reach the same 1e-8 residual; its
+error against the FP64 oracle is asserted below 1e-3.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import rank_structured_cholesky_gb300 as rs
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+EXACT_TOL = 1e-11
+COMPRESSED_TOL = 1e-6
+APPLY_TOL = 1e-7
+
+
+def make(case):
+    from tests.golden import make_golden
+    return make_golden.make_problem(make_golden.CASES[case]["problem"]), make_golden.CASES[case]["params"]
+
+
+def gpu_factor(prob, params, **extra):
+    ctx = rs.Context(**params, **extra)
+    return rs.GpuFactor(ctx, prob.colptr, prob.rowind, prob.vals, prob.xyz)
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+@pytest.fixture(scope="module")
+def oracles():
+    cache = {}
+
+    def get(case):
+        if case not in cache:
+            prob, params = make(case)
+            F = po.OracleFactor(prob.colptr, prob.rowind, prob.vals, prob.xyz, params)
+            assert F.factor() == 0
+            cache[case] = (prob, params, F)
+        return cache[case]
+    return get
+
+
+@pytest.mark.parametrize("case", ["2d48", "3d16", "3d20h", "el5"])
+def test_factor_blocks_match_oracle(case, oracles):
+    prob, params, O = oracles(case)
+    G = gpu_factor(prob, params)
+    assert G.num_nodes() == O.num_nodes()
+    for j in range(G.num_nodes()):
+        gi, oi = G.node_info(j), O.node_info(j)
+        assert (gi["c0"], gi["c1"], gi["compressed"]) == (oi["c0"], oi["c1"], oi["compressed"])
+        if not gi["compressed"] and j % 5:
+            continue
+        tol = COMPRESSED_TOL if gi["compressed"] else EXACT_TOL
+        assert rel(G.node_l11(j), O.node_l11(j)) < tol, ("l11", j, gi)
+        l21o = O.node_l21(j)
+        if l21o.size:
+            assert rel(G.node_l21(j), l21o) < tol, ("l21", j, gi)
+
+
+@pytest.mark.parametrize("case", ["2d48", "3d16", "3d20h", "el5"])
+def test_pcg_matches_oracle(case, oracles):
+    prob, params, O = oracles(case)
+    G = gpu_factor(prob, params)
+    b = prob.rhs[0]
+    x, info = G.pcg(b, 1e-8, 2000)
+    _, it, _, true = O.pcg(b, 1e-8, 2000)
+    assert abs(info["iterations"] - it) <= 1, (info, it)
+    assert info["true_residual"] <= 1e-8
+    A = prob.scipy()
+    assert np.linalg.norm(b - A @ x) / np.linalg.norm(b) <= 1e-8
+    assert rel(G.apply(b), O.apply(b)) < APPLY_TOL
+
+
+@pytest.mark.parametrize("case", ["2d48", "3d16", "3d20h", "el5"])
+def test_matches_golden_fixture(case):
+    prob, params = make(case)
+    g = np.load(os.path.join(GOLDEN, "oracle_%s.npz" % case))
+    G = gpu_factor(prob, params)
+    assert np.array_equal(G.perm(), g["perm"])
+    assert rel(G.apply(prob.rhs[0]), g["apply"]) < APPLY_TOL
+    for j in g["compressed_nodes"]:
+        l11 = G.node_l11(int(j))
+        probe = np.random.default_rng(1000 + int(j)).standard_normal(l11.shape[1])
+        assert rel(l11 @ probe, g["l11p_%d" % j]) < COMPRESSED_TOL
+        if "l21p_%d" % j in g:
+            assert rel(G.node_l21(int(j)) @ probe, g["l21p_%d" % j]) < COMPRESSED_TOL
+    x, info = G.pcg(prob.rhs[0], 1e-8, 2000)
+    assert abs(info["iterations"] - int(g["iterations"])) <= 1
+
+
+@pytest.mark.parametrize("case", ["3d16", "el5"])
+def test_mixed_precision_reaches_fp64_accuracy(case, oracles):
+    prob, params, O = oracles(case)
+    G = gpu_factor(prob, params, precision=rs.MIXED)
+    x, info = G.pcg(prob.rhs[0], 1e-8, 2000)
+    assert info["true_residual"] <= 1e-8
+    _, it, _, _ = O.pcg(prob.rhs[0], 1e-8, 2000)
+    assert info["iterations"] <= it + 3
+    # error of the FP32 factor against the FP64 oracle, stated as a bound
+    assert rel(G.apply(prob.rhs[0]), O.apply(prob.rhs[0])) < 1e-3
+
+
+def test_results_are_bitwise_reproducible():
+    prob, params = make("3d20h")
+    a = gpu_factor(prob, params)
+    b = gpu_factor(prob, params)
+    ya, yb = a.apply(prob.rhs[0]), b.apply(prob.rhs[0])
+    assert np.array_equal(ya, yb)
+    xa, ia = a.pcg(prob.rhs[0], 1e-8, 500)
+    xb, ib = b.pcg(prob.rhs[0], 1e-8, 500)
+    assert np.array_equal(xa, xb) and ia["iterations"] == ib["iterations"]
+
+
+def test_refactor_same_pattern_matches_fresh_factor():
+    prob, params = make("3d16")
+    G = gpu_factor(prob, params)
+    scaled = prob.vals * 2.5
+    G.refactor(scaled)
+    ctx = rs.Context(**params)
+    F = rs.GpuFactor(ctx, prob.colptr, prob.rowind, scaled, prob.xyz)
+    assert rel(G.apply(prob.rhs[0]), F.apply(prob.rhs[0])) < 1e-12
+    x, info = G.pcg(prob.rhs[0], 1e-8, 500)
+    assert info["true_residual"] <= 1e-8
+
+
+def test_indefinite_matrix_reports_status():
+    prob = rs.diffusion(2, 12, sigma=0.0)
+    vals = prob.vals.copy()
+    for p in range(prob.colptr[70], prob.colptr[71]):
+        if prob.rowind[p] == 70:
+            vals[p] = -4.0
+    ctx = rs.Context(max_dense_block=8, max_diag_block=32)
+    with pytest.raises(rs.RscholError) as e:
+        rs.GpuFactor(ctx, prob.colptr, prob.rowind, vals, prob.xyz)
+    assert e.value.status == 2   # RSCHOL_E_NOT_PD_AFTER_RETRY
+
+
+def test_pcg_pysolve_drop_in():
+    prob = rs.diffusion(2, 40, sigma=1.0, seed=4)
+    A = prob.scipy()
+    x = rs.solve(A, prob.rhs[0])
+    assert np.linalg.norm(prob.rhs[0] - A @ x) / np.linalg.norm(prob.rhs[0]) <= 1e-6
+
+
+def test_multiple_rhs_share_the_factor():
+    prob = rs.diffusion(3, 12, sigma=1.0, seed=3, nrhs=3)
+    G = gpu_factor(prob, dict(max_dense_block=24, max_diag_block=48, nd_leaf=16))
+    X, infos = G.pcg(prob.rhs, 1e-8, 500)
+    A = prob.scipy()
+    for k in range(3):
+        assert np.linalg.norm(prob.rhs[k] - A @ X[k]) / np.linalg.norm(prob.rhs[k]) <= 1e-8
+        x1, _ = G.pcg(prob.rhs[k], 1e-8, 500)
+        assert np.array_equal(x1, X[k])
