@@ -213,21 +213,23 @@ __global__ void scatter_kernel(const double* __restrict__ Avals, const long long
 
 constexpr int QR_THREADS = 512;
 
-__device__ __forceinline__ double warp_sum_d(double v) {
+template <class R>
+__device__ __forceinline__ R warp_sum_d(R v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
 // Block-wide sum, broadcast to every thread.
-__device__ double block_sum_bcast(double v, double* red) {
+template <class R>
+__device__ R block_sum_bcast(R v, R* red) {
   v = warp_sum_d(v);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __syncthreads();
   if (lane == 0) red[warp] = v;
   __syncthreads();
   if (warp == 0) {
-    double t = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.0;
+    R t = (lane < (int)(blockDim.x >> 5)) ? red[lane] : R(0);
     t = warp_sum_d(t);
     if (lane == 0) red[32] = t;
   }
@@ -243,7 +245,7 @@ __global__ void __launch_bounds__(QR_THREADS) householder_qr_kernel(const QrTask
   const int n = t.n, r = t.r;
   T* W = t.W;
   T* tau = W + (size_t)r * n;
-  __shared__ double red[33];
+  __shared__ T red[33];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   for (long long idx = tid; idx < (long long)n * r; idx += blockDim.x) {
     const int i = (int)(idx / r), j = (int)(idx - (long long)i * r);
@@ -252,59 +254,59 @@ __global__ void __launch_bounds__(QR_THREADS) householder_qr_kernel(const QrTask
   __syncthreads();
   for (int k = 0; k < r; ++k) {
     T* ck = W + (size_t)k * n;
-    double s = 0.0;
-    for (int i = k + 1 + tid; i < n; i += blockDim.x) s += (double)ck[i] * (double)ck[i];
-    const double xnorm2 = block_sum_bcast(s, red);
-    const double alpha = (double)ck[k];
-    double tk = 0.0, beta = alpha, scal = 0.0;
-    if (xnorm2 > 0.0) {
+    T s = T(0);
+    for (int i = k + 1 + tid; i < n; i += blockDim.x) s += ck[i] * ck[i];
+    const T xnorm2 = block_sum_bcast<T>(s, red);
+    const T alpha = ck[k];
+    T tk = T(0), beta = alpha, scal = T(0);
+    if (xnorm2 > T(0)) {
       beta = -copysign(sqrt(alpha * alpha + xnorm2), alpha);
       tk = (beta - alpha) / beta;
-      scal = 1.0 / (alpha - beta);
+      scal = T(1) / (alpha - beta);
     }
     __syncthreads();
-    if (xnorm2 > 0.0)
-      for (int i = k + 1 + tid; i < n; i += blockDim.x) ck[i] = (T)((double)ck[i] * scal);
+    if (xnorm2 > T(0))
+      for (int i = k + 1 + tid; i < n; i += blockDim.x) ck[i] = ck[i] * scal;
     if (tid == 0) {
-      ck[k] = (T)beta;
-      tau[k] = (T)tk;
+      ck[k] = beta;
+      tau[k] = tk;
     }
     __syncthreads();
-    if (tk != 0.0) {
+    if (tk != T(0)) {
       for (int j = k + 1 + warp; j < r; j += nw) {
         T* cj = W + (size_t)j * n;
-        double w = 0.0;
-        for (int i = k + 1 + lane; i < n; i += 32) w += (double)ck[i] * (double)cj[i];
-        w = warp_sum_d(w);
-        const double cjk = (double)cj[k];
+        T w = T(0);
+        for (int i = k + 1 + lane; i < n; i += 32) w += ck[i] * cj[i];
+        w = warp_sum_d<T>(w);
+        const T cjk = cj[k];
         __syncwarp();
         w = tk * (w + cjk);
-        if (lane == 0) cj[k] = (T)(cjk - w);
-        for (int i = k + 1 + lane; i < n; i += 32) cj[i] = (T)((double)cj[i] - w * (double)ck[i]);
+        if (lane == 0) cj[k] = cjk - w;
+        for (int i = k + 1 + lane; i < n; i += 32) cj[i] = cj[i] - w * ck[i];
       }
     }
     __syncthreads();
   }
   for (int k = r - 1; k >= 0; --k) {
     T* ck = W + (size_t)k * n;
-    const double tk = (double)tau[k];
-    if (tk != 0.0) {
+    const T tk = tau[k];
+    if (tk != T(0)) {
       for (int j = k + 1 + warp; j < r; j += nw) {
         T* cj = W + (size_t)j * n;
-        double w = 0.0;
-        for (int i = k + 1 + lane; i < n; i += 32) w += (double)ck[i] * (double)cj[i];
-        w = warp_sum_d(w);
-        const double cjk = (double)cj[k];
+        T w = T(0);
+        for (int i = k + 1 + lane; i < n; i += 32) w += ck[i] * cj[i];
+        w = warp_sum_d<T>(w);
+        const T cjk = cj[k];
         __syncwarp();
         w = tk * (w + cjk);
-        if (lane == 0) cj[k] = (T)(cjk - w);
-        for (int i = k + 1 + lane; i < n; i += 32) cj[i] = (T)((double)cj[i] - w * (double)ck[i]);
+        if (lane == 0) cj[k] = cjk - w;
+        for (int i = k + 1 + lane; i < n; i += 32) cj[i] = cj[i] - w * ck[i];
       }
     }
     __syncthreads();
-    for (int i = k + 1 + tid; i < n; i += blockDim.x) ck[i] = (T)(-tk * (double)ck[i]);
+    for (int i = k + 1 + tid; i < n; i += blockDim.x) ck[i] = -tk * ck[i];
     for (int i = tid; i < k; i += blockDim.x) ck[i] = T(0);
-    if (tid == 0) ck[k] = (T)(1.0 - tk);
+    if (tid == 0) ck[k] = T(1) - tk;
     __syncthreads();
   }
   for (long long idx = tid; idx < (long long)n * r; idx += blockDim.x) {

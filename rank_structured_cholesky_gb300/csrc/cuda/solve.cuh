@@ -55,7 +55,7 @@ class SolveEngine {
  private:
   FactorEngine<T>& F_;
   std::vector<SNode<T>> nodes_;
-  DevBuf dNodes_, dRows_, dRel_, dChild_, dPull_, dWu_, dLevelNodes_;
+  DevBuf dNodes_, dRows_, dRel_, dChild_, dPull_, dWu_, dW_, dLevelNodes_;
   std::vector<std::pair<long long, int>> iLevels_, cLevels_;  // (offset, count) into level node list
   std::vector<size_t> smemIF_, smemIB_, smemCF_, smemCB_;
   int maxCompN_ = 0;

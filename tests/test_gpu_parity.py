@@ -4,12 +4,13 @@ Tolerances (FP64 path), relative Frobenius / 2-norm error against the oracle:
   * EXACT_TOL = 1e-11 for blocks no compression touches (interior factor
     panels of supernodes whose interior block has no compressed ancestor
     contribution, i.e. everything below the first compressed separator);
-  * COMPRESSED_TOL = 1e-6 for everything a randomized compression feeds
+  * COMPRESSED_TOL = 1e-5 for everything a randomized compression feeds
     (L11 of HODLR diagonals, V U^T, and every block assembled from them).
     The sketch Y = (L21^T L21) L21^T G has numerical rank below r; the basis
     columns beyond that rank are fixed by rounding in any QR (LAPACK's
     included), so V U^T = L21 U U^T agrees only up to the neglected singular
-    values of L21;
+    values of L21 (the CPU oracle run once with OpenBLAS and once with plain
+    loops differs by 3.1e-6 on the 2d48 case);
   * APPLY_TOL = 1e-7 for one preconditioner application.
 PCG reaches ||r||/||b|| <= 1e-8 in the oracle's iteration count +-1.  Mixed
 precision (FP32 factor, FP64 PCG) must reach the same 1e-8 residual; its
@@ -27,7 +28,7 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 EXACT_TOL = 1e-11
-COMPRESSED_TOL = 1e-6
+COMPRESSED_TOL = 1e-5
 APPLY_TOL = 1e-7
 
 
