@@ -23,7 +23,7 @@ enum rschol_status {
   RSCHOL_E_OOM = 3,
   RSCHOL_E_CUDA = 4,
   RSCHOL_E_BREAKDOWN = 5,          /* PCG breakdown: d' A d == 0 */
-  RSCHOL_E_TIMEOUT = 6,
+  RSCHOL_E_TIMEOUT = 6,            /* a bounded wait between thread blocks of the solve gave up */
   RSCHOL_E_NO_DEVICE = 7,
   RSCHOL_E_UNSUPPORTED = 8
 };

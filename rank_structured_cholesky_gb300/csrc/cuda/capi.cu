@@ -55,6 +55,7 @@ struct Impl {
   virtual void plan() = 0;
   virtual int run() = 0;
   virtual void apply(double* d_w, cudaStream_t s) = 0;
+  virtual int apply_error(cudaStream_t s) = 0;   // nonzero: a row-block wait of the solve gave up
   virtual void set_values(const double* lower) = 0;
   virtual double* device_values() = 0;
   virtual long long launches() const = 0;
@@ -70,13 +71,16 @@ template <class T>
 struct ImplT : Impl {
   FactorEngine<T> fe;
   SolveEngine<T> se;
-  ImplT(const Symbolic& S, const CSC& A, const Params& p, cudaStream_t s) : fe(S, A, p, s), se(fe) {}
+  ImplT(const Symbolic& S, const CSC& A, const Params& p, cudaStream_t s) : fe(S, A, p, s), se(fe) {
+    fe.post = [this]() { return se.prepare(fe.stream); };
+  }
   void plan() override {
     fe.plan();
     se.plan();
   }
   int run() override { return fe.run(); }
   void apply(double* w, cudaStream_t s) override { se.apply_inplace(w, s); }
+  int apply_error(cudaStream_t s) override { return se.take_error(s); }
   void set_values(const double* lower) override { fe.set_values(lower); }
   double* device_values() override { return fe.dAvals.template as<double>(); }
   long long launches() const override { return fe.launches; }
@@ -141,6 +145,9 @@ struct rschol_factor {
   double diagRankConstant = 0.5;
   std::string desc;
 };
+
+static const char* const kSolveWaitMsg =
+    "preconditioner solve: a wait between thread blocks exceeded its limit (result discarded)";
 
 static int fail(rschol_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
@@ -370,6 +377,7 @@ int rschol_profile(rschol_factor* f, const double* d_b, double* out) {
     RSCHOL_CUDA(cudaEventElapsedTime(&ms[2], e[3], e[4]));
     RSCHOL_CUDA(cudaEventElapsedTime(&ms[3], e[5], e[6]));
     for (auto& x : e) cudaEventDestroy(x);
+    if (f->impl->apply_error(s)) return fail(f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);
     out[0] = ms[0];
     out[1] = ms[1];
     out[2] = ms[2];
@@ -414,6 +422,7 @@ int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x
       launch_scatter_perm(f->dBp.as<double>(), f->dPerm.as<int>(), d_x + (size_t)k * n, n, s);
     }
     RSCHOL_CUDA(cudaStreamSynchronize(s));
+    if (f->impl->apply_error(s)) return fail(f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);
   } catch (const std::exception& e) {
     return fail(f->ctx, RSCHOL_E_CUDA, e.what());
   }
@@ -452,6 +461,7 @@ int rschol_pcg_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs
       PcgResult r = f->pcg->solve(f->dBp.as<double>(), f->dXp.as<double>(), eps, maxit, apply);
       launch_scatter_perm(f->dXp.as<double>(), f->dPerm.as<int>(), d_x + (size_t)k * n, n, s);
       RSCHOL_CUDA(cudaStreamSynchronize(s));
+      if (f->impl->apply_error(s)) return fail(f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);
       if (info) {
         info[k].iterations = r.iterations;
         info[k].residual = r.residual;

@@ -735,6 +735,7 @@ int FactorEngine<T>::run() {
     }
     ++launches;
   }
+  if (post) launches += post();
   int flag = 0;
   RSCHOL_CUDA(cudaMemcpyAsync(&flag, dFlag.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
   RSCHOL_CUDA(cudaStreamSynchronize(stream));

@@ -28,6 +28,7 @@
 
 #include <cstdint>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "../host/ordering.h"
@@ -109,6 +110,9 @@ class FactorEngine {
   T* vu() const { return dVU.as<T>(); }
 
   std::vector<std::vector<int>> interiorLevels, compressedLevels;
+  // Work queued on the stream after the last factor step and before the
+  // status read (solve-side preprocessing of the factor); returns its launches.
+  std::function<int()> post;
   long long launches = 0;            // kernel launches of the last run
   double flops = 0;                  // algorithmic flops of one factorisation
   size_t deviceBytes = 0;

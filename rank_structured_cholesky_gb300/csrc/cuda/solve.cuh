@@ -8,12 +8,20 @@
 // A_{rest,I} L_I^{-T} L_I^{-1} are stored explicitly), compressed nodes use
 // the (HODLR-expanded) dense L11 and the V U^T off-diagonal.
 //
-// Forward: interior levels bottom-up, each node assembling its children's
-// update vectors (extend-add, fixed order); compressed levels bottom-up,
-// each node pulling the interior roots' update vectors and the compressed
-// descendants' V z contributions.  Backward: compressed levels top-down,
-// then interior levels top-down, each node gathering its rows from the
-// already-solved vector.  No atomics: results are bitwise reproducible.
+// Forward: interior levels bottom-up, one block per supernode, each
+// assembling its children's update vectors (extend-add, fixed order).
+// Compressed levels bottom-up: every compressed supernode is cut into
+// 64-row blocks and each block gets its own thread block, which adds the
+// fixed-order contribution list of its rows (interior-root update vectors,
+// -V_c z_c of compressed descendants), accumulates L[b, k] y_k of the
+// earlier row blocks as their ready flags are raised, and multiplies by the
+// inverted 64 x 64 diagonal block.  z = U^T y is reduced in fixed order by
+// the last row block to finish.  Backward mirrors this (s = V^T x_R by a
+// chunked pass, then row blocks in reverse order), then interior levels
+// top-down.  Thread blocks take their row block from a ticket counter, so a
+// block only ever waits on blocks that started before it; every wait is
+// bounded and reports through an error word instead of hanging.  No atomics
+// touch the numbers: results are bitwise reproducible.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -24,22 +32,47 @@
 
 namespace rschol {
 
+constexpr int SOLVE_RB = 64;   // rows per compressed row block
+
 template <class T>
 struct SNode {
   const T* L;       // interior: [L11; L21] panel; compressed: L11 (HODLR expanded)
   const T* V;       // compressed: m x r
   const T* U;       // compressed: n x r
+  const T* Dinv;    // compressed: nb inverted 64 x 64 diagonal blocks of L11
   int ld, n, m, r, c0;
-  int childBegin, childEnd;   // interior: children; compressed: pull list range
+  int childBegin, childEnd;   // interior: children (range in the child list)
+  int nb, nch;                // compressed: row blocks of L11, 128-row chunks of V
+  int syncOff;                // compressed: nb ready flags, then 3 completion counters
   long long rowsOff;          // rows of this node in the row arena
-  long long wuOff;            // interior: update vector; compressed: z (r values)
+  long long wuOff;            // interior: update vector; compressed: z and s (r values each)
   long long relOff;           // interior: target index in the parent front of each row
+  long long cOff;             // compressed: first of its n+1 contribution-list offsets
+  long long zpOff, spOff;     // compressed: partials of z (nb x r) and s (nch x r)
 };
 
-struct SPull {       // compressed-node forward pull
+template <class T>
+struct CEntry {      // one contribution to a row of a compressed supernode's right-hand side
+  const T* v;        // r == 0: the value to add; r > 0: a row of V (r entries)
+  const T* z;        // r > 0: z = U^T y of the contributing supernode
+  int r;
+};
+
+struct SPull {       // contribution source of a compressed supernode (plan time)
   int src;           // source node
   int a0, a1;        // source rows mapping into this node's columns
   int kind;          // 0: interior root update vector, 1: compressed V z
+};
+
+struct RowBlock {    // one thread block's work in a compressed level
+  int node, b;
+};
+
+template <class T>
+struct DinvTask {    // invert one lower-triangular diagonal block (h x h, h <= 64)
+  const T* L;
+  int ld, h;
+  T* D;              // 64 x 64 row-major, zero outside the h x h lower triangle
 };
 
 template <class T>
@@ -47,18 +80,29 @@ class SolveEngine {
  public:
   explicit SolveEngine(FactorEngine<T>& F);
   void plan();                           // after the factor plan
-  // w (permuted, length n, device) := M^{-1} w, in place.  scratch-free.
+  // Queue the solve-side preprocessing of a fresh factor (inverted diagonal
+  // blocks); returns its launches.
+  int prepare(cudaStream_t s);
+  // w (permuted, length n, device) := M^{-1} w, in place.
   void apply_inplace(double* d_w, cudaStream_t s);
+  // Reads (synchronously) and clears the error word of the row-block waits:
+  // 0, or 1 if a wait gave up (the result of that apply is undefined).
+  int take_error(cudaStream_t s);
   long long launches_per_apply() const { return launchesPerApply_; }
   double bytes_per_apply() const { return bytesPerApply_; }
 
  private:
   FactorEngine<T>& F_;
   std::vector<SNode<T>> nodes_;
-  DevBuf dNodes_, dRows_, dRel_, dChild_, dPull_, dWu_, dW_, dLevelNodes_;
+  DevBuf dNodes_, dRows_, dRel_, dChild_, dWu_, dW_, dLevelNodes_, dCStart_, dCEnt_;
+  DevBuf dDinv_, dDinvTasks_, dZp_, dSp_, dSync_, dTickF_, dTickB_;
+  int nDinv_ = 0;
+  int syncInts_ = 0;
+  std::vector<long long> tickOff_;   // per compressed level: first ticket entry
+  std::vector<int> cBlocks_;         // per compressed level: row blocks
+  std::vector<int> cMaxCh_;          // per compressed level: most V chunks of a node
   std::vector<std::pair<long long, int>> iLevels_, cLevels_;  // (offset, count) into level node list
-  std::vector<size_t> smemIF_, smemIB_, smemCF_, smemCB_;
-  int maxCompN_ = 0;
+  std::vector<size_t> smemIF_, smemIB_;
   long long launchesPerApply_ = 0;
   double bytesPerApply_ = 0;
 };
