@@ -107,6 +107,25 @@ int rschol_profile(rschol_factor* f, const double* d_b, double* out);
 int rschol_precond_apply(rschol_factor* f, const double* b, double* x, int nrhs);
 int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs);
 
+/* Same result as rschol_precond_apply_device, but the call allocates no
+ * device memory: for callers that apply the preconditioner inside their own
+ * solver loop and cannot let a call allocate (cudaMalloc synchronises the
+ * device and stalls their other streams, or their memory budget is fixed).
+ * No counterpart in the reference (its solve allocates host work vectors).
+ *   - n (the matrix order) must be <= RSCHOL_NOALLOC_MAX_N, otherwise
+ *     RSCHOL_E_BAD_INPUT with a message naming the limit;
+ *   - the permuted work vector is one static device array of
+ *     RSCHOL_NOALLOC_MAX_N doubles (16 MiB) per device, shared by every
+ *     factor: calls that overlap in time (other host threads, other factors'
+ *     streams) race on it, so serialise them;
+ *   - nothing in it has to start at zero: each right-hand side is written
+ *     completely before it is read;
+ *   - the first call on a device looks up the array's address
+ *     (cudaGetSymbolAddress, with that device current); make that first call
+ *     before any stream capture that would include this function. */
+#define RSCHOL_NOALLOC_MAX_N 2097152
+int rschol_precond_apply_device_noalloc(rschol_factor* f, const double* d_b, double* d_x, int nrhs);
+
 /* Preconditioned CG from x0 = 0 with the factor as M, stopping at
  * ||r|| / ||b|| <= eps or maxit iterations; nrhs right-hand sides are solved
  * together, sharing the factor.

@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -586,3 +587,58 @@ int rschol_factor_stats(const rschol_factor* f, double* st) {
 }
 
 }  // extern "C"
+
+// ---- allocation-free preconditioner apply ----------------------------------
+// The permuted work vector lives in a file-scope device array instead of a
+// buffer allocated on first use, so the call itself never allocates.
+namespace {
+constexpr int kNoAllocMaxN = RSCHOL_NOALLOC_MAX_N;
+constexpr int kNoAllocMaxDevices = 64;
+__device__ __align__(256) double g_noalloc_work[kNoAllocMaxN];
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+extern "C" int rschol_precond_apply_device_noalloc(rschol_factor* f, const double* d_b, double* d_x, int nrhs) {
+  if (!f || !d_b || !d_x || nrhs <= 0) return RSCHOL_E_BAD_INPUT;
+  const int n = f->Afull.n;
+  if (n > kNoAllocMaxN)
+    return fail(f->ctx, RSCHOL_E_BAD_INPUT,
+                "rschol_precond_apply_device_noalloc: n = " + std::to_string(n) + " exceeds the static work vector (" +
+                    std::to_string(kNoAllocMaxN) + " unknowns); use rschol_precond_apply_device");
+  const int dev = f->ctx->device;
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return fail(f->ctx, RSCHOL_E_UNSUPPORTED, "rschol_precond_apply_device_noalloc: device ordinal out of range");
+  try {
+    double* work = nullptr;
+    {
+      std::lock_guard<std::mutex> lock(g_noalloc_mu);
+      if (!g_noalloc_addr[dev]) {
+        // once per device, with that device current
+        int prev = -1;
+        RSCHOL_CUDA(cudaGetDevice(&prev));
+        RSCHOL_CUDA(cudaSetDevice(dev));
+        void* addr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_work);
+        if (prev >= 0 && prev != dev) cudaSetDevice(prev);
+        if (e != cudaSuccess)
+          return fail(f->ctx, RSCHOL_E_CUDA,
+                      std::string("rschol_precond_apply_device_noalloc: cudaGetSymbolAddress: ") +
+                          cudaGetErrorString(e));
+        g_noalloc_addr[dev] = addr;
+      }
+      work = static_cast<double*>(g_noalloc_addr[dev]);
+    }
+    cudaStream_t s = f->ctx->stream;
+    for (int k = 0; k < nrhs; ++k) {
+      launch_gather(d_b + (size_t)k * n, f->dPerm.as<int>(), work, n, s);
+      f->impl->apply(work, s);
+      launch_scatter_perm(work, f->dPerm.as<int>(), d_x + (size_t)k * n, n, s);
+    }
+    RSCHOL_CUDA(cudaStreamSynchronize(s));
+    if (f->impl->apply_error(s)) return fail(f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);
+  } catch (const std::exception& e) {
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+  return RSCHOL_OK;
+}
