@@ -1,4 +1,5 @@
 // Batched dense kernels (FP64 and FP32 instantiations).
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 
@@ -211,7 +212,18 @@ __global__ void scatter_kernel(const double* __restrict__ Avals, const long long
     dst[dstIdx[k]] = (T)Avals[srcIdx[k]];
 }
 
-constexpr int QR_THREADS = 512;
+// ---------------------------------------------------------------------------
+// Blocked Householder QR of the sketches (LAPACK dgeqrf + dorgqr: dlarfg
+// reflectors with v_0 = 1, compact-WY panels of QR_PB columns, dlarft's
+// forward column-wise T).  Per panel: one block per matrix factors the panel
+// (in shared memory when it fits), then many blocks apply the panel's block
+// reflector to the trailing columns.  Q = H_0 ... H_{r-1} [I; 0] is formed by
+// applying the block reflectors to [I; 0] in reverse order.
+constexpr int QR_PB = 16;          // panel width
+constexpr int QRP_THREADS = 512;   // panel kernel
+constexpr int QA_ROWS = 64;        // apply kernel: row chunk
+constexpr int QA_CW = 16;          // apply kernel: columns per block
+constexpr int QR_SMEM_MAX = 200 * 1024;
 
 template <class R>
 __device__ __forceinline__ R warp_sum_d(R v) {
@@ -220,98 +232,245 @@ __device__ __forceinline__ R warp_sum_d(R v) {
   return v;
 }
 
-// Block-wide sum, broadcast to every thread.
+// Sum of v[0..15] over the 32 lanes of a warp; lane l (l < 16) returns the
+// total of v[l] (31 shuffles, fixed order).
 template <class R>
-__device__ R block_sum_bcast(R v, R* red) {
-  v = warp_sum_d(v);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  if (warp == 0) {
-    R t = (lane < (int)(blockDim.x >> 5)) ? red[lane] : R(0);
-    t = warp_sum_d(t);
-    if (lane == 0) red[32] = t;
+__device__ __forceinline__ R warp_transpose_sum16(R (&v)[QR_PB]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], 16);
+#pragma unroll
+  for (int w = 8; w >= 1; w >>= 1) {
+    const bool up = (lane & w) != 0;
+#pragma unroll
+    for (int i = 0; i < w; ++i) {
+      const R send = up ? v[i] : v[i + w];
+      const R keep = up ? v[i + w] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, w);
+    }
   }
-  __syncthreads();
-  return red[32];
+  return v[0];
 }
 
-// Householder QR (LAPACK dgeqr2: dlarfg reflectors with v_0 = 1) followed by
-// the explicit thin Q (dorg2r), on a column-major copy of Y.
+// Y (row-major n x r) -> W (column-major, ld n), 32 x 32 tiles.
 template <class T>
-__global__ void __launch_bounds__(QR_THREADS) householder_qr_kernel(const QrTask<T>* __restrict__ tasks) {
+__global__ void __launch_bounds__(256) qr_to_colmajor(const QrTask<T>* __restrict__ tasks) {
+  __shared__ T tile[32][33];
+  const QrTask<T> t = tasks[blockIdx.y];
+  const int n = t.n, r = t.r;
+  const int tr = (n + 31) / 32, tc = (r + 31) / 32;
+  const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+  for (int tl = blockIdx.x; tl < tr * tc; tl += gridDim.x) {
+    const int i0 = (tl / tc) * 32, j0 = (tl % tc) * 32;
+    for (int y = ly; y < 32; y += 8)
+      if (i0 + y < n && j0 + lx < r) tile[y][lx] = t.Y[(size_t)(i0 + y) * r + j0 + lx];
+    __syncthreads();
+    for (int y = ly; y < 32; y += 8)
+      if (j0 + y < r && i0 + lx < n) t.W[(size_t)(j0 + y) * n + i0 + lx] = tile[lx][y];
+    __syncthreads();
+  }
+}
+
+// Y (row-major n x r) := [I; 0]
+template <class T>
+__global__ void qr_set_e(const QrTask<T>* __restrict__ tasks) {
+  const QrTask<T> t = tasks[blockIdx.y];
+  const long long tot = (long long)t.n * t.r;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < tot; k += (long long)gridDim.x * blockDim.x) {
+    const long long i = k / t.r, j = k - i * t.r;
+    t.Y[k] = (i == j) ? T(1) : T(0);
+  }
+}
+
+// Factor columns j0 .. j0+pw-1 of W (rows j0 .. n-1).  On return the panel
+// holds V below its diagonal and T (pw x pw, upper) in place of the upper
+// triangle of its diagonal block (R is not needed: only Q is used).
+template <class T>
+__global__ void __launch_bounds__(QRP_THREADS) qr_panel_kernel(const QrTask<T>* __restrict__ tasks, int j0,
+                                                               long long smemElems) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int NW = QRP_THREADS / 32;
+  __shared__ T redA[NW];
+  __shared__ T redC[NW][QR_PB];
+  __shared__ T sred[QR_PB], sfin[QR_PB];
+  __shared__ T Ts[QR_PB][QR_PB + 1];
   const QrTask<T> t = tasks[blockIdx.x];
   const int n = t.n, r = t.r;
-  T* W = t.W;
-  T* tau = W + (size_t)r * n;
-  __shared__ T red[33];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-  for (long long idx = tid; idx < (long long)n * r; idx += blockDim.x) {
-    const int i = (int)(idx / r), j = (int)(idx - (long long)i * r);
-    W[(size_t)j * n + i] = t.Y[idx];
+  if (j0 >= r) return;
+  const int pw = min(QR_PB, r - j0), nr = n - j0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  T* Wg = t.W + (size_t)j0 * n + j0;   // panel element (i, c) at Wg[c * n + i]
+  T* P = Wg;
+  long long lp = n;
+  const bool inSmem = (long long)nr * pw <= smemElems;
+  if (inSmem) {
+    P = reinterpret_cast<T*>(smraw);
+    lp = nr;
+    for (int c = 0; c < pw; ++c)
+      for (int i = tid; i < nr; i += QRP_THREADS) P[c * lp + i] = Wg[(size_t)c * n + i];
+  }
+  for (int idx = tid; idx < QR_PB * (QR_PB + 1); idx += QRP_THREADS) (&Ts[0][0])[idx] = T(0);
+  __syncthreads();
+  for (int kk = 0; kk < pw; ++kk) {
+    T* pk = P + kk * lp;
+    // dlarfg on column kk
+    T x2 = T(0);
+    for (int i = kk + 1 + tid; i < nr; i += QRP_THREADS) x2 += pk[i] * pk[i];
+    x2 = warp_sum_d(x2);
+    if (lane == 0) redA[warp] = x2;
+    __syncthreads();
+    x2 = T(0);
+#pragma unroll
+    for (int q = 0; q < NW; ++q) x2 += redA[q];
+    const T alpha = pk[kk];
+    T tau = T(0), scal = T(1);
+    if (x2 > T(0)) {
+      const T beta = -copysign(sqrt(alpha * alpha + x2), alpha);
+      tau = (beta - alpha) / beta;
+      scal = T(1) / (alpha - beta);
+      for (int i = kk + 1 + tid; i < nr; i += QRP_THREADS) pk[i] *= scal;
+    }
+    // s_c = P[kk][c] + sum_{i>kk} v_i P[i][c] for every panel column c
+    T part[QR_PB];
+#pragma unroll
+    for (int c = 0; c < QR_PB; ++c) part[c] = T(0);
+    for (int i = kk + 1 + tid; i < nr; i += QRP_THREADS) {
+      const T vi = pk[i];
+#pragma unroll
+      for (int c = 0; c < QR_PB; ++c)
+        if (c < pw) part[c] += P[c * lp + i] * vi;
+    }
+    const T ws = warp_transpose_sum16(part);
+    if (lane < QR_PB) redC[warp][lane] = ws;
+    __syncthreads();
+    if (tid < pw) {
+      T s = T(0);
+#pragma unroll
+      for (int q = 0; q < NW; ++q) s += redC[q][tid];
+      sred[tid] = s + P[tid * lp + kk];
+    }
+    __syncthreads();
+    // T column kk (dlarft): T[p][kk] = -tau sum_{q=p}^{kk-1} T[p][q] y_q, T[kk][kk] = tau
+    if (tid < kk) {
+      T s = T(0);
+      for (int q = tid; q < kk; ++q) s += Ts[tid][q] * sred[q];
+      Ts[tid][kk] = -tau * s;
+    }
+    if (tid == kk) Ts[kk][kk] = tau;
+    if (tid < pw) sfin[tid] = tau * sred[tid];
+    __syncthreads();
+    // apply H_kk to the remaining panel columns
+    if (tau != T(0)) {
+      for (int c = kk + 1; c < pw; ++c) {
+        const T w = sfin[c];
+        T* pc = P + c * lp;
+        for (int i = kk + 1 + tid; i < nr; i += QRP_THREADS) pc[i] -= w * pk[i];
+        if (tid == 0) pc[kk] -= w;
+      }
+    }
+    __syncthreads();
+  }
+  if (inSmem)
+    for (int c = 0; c < pw; ++c)
+      for (int i = tid; i < nr; i += QRP_THREADS) Wg[(size_t)c * n + i] = P[c * lp + i];
+  __syncthreads();
+  // T over the upper triangle of the diagonal block
+  for (int idx = tid; idx < pw * pw; idx += QRP_THREADS) {
+    const int a = idx / pw, b = idx - a * pw;
+    if (a <= b) Wg[(size_t)b * n + a] = Ts[a][b];
+  }
+}
+
+// Apply the block reflector of panel j0 to a group of QA_CW columns.
+//   mode 0 (factor): W[j0:n, c] := (I - V T^T V^T) W[j0:n, c], c >= j0 + pw
+//   mode 1 (form Q): Y[j0:n, c] := (I - V T V^T) Y[j0:n, c],   c >= j0
+template <class T>
+__global__ void __launch_bounds__(256) qr_apply_kernel(const QrTask<T>* __restrict__ tasks, int j0, int mode) {
+  __shared__ T Vs[QA_ROWS][QR_PB + 1];
+  __shared__ T As[QA_ROWS][QA_CW + 1];
+  __shared__ T Z[QR_PB][QA_CW + 1];
+  __shared__ T M[QR_PB][QA_CW + 1];
+  __shared__ T Ts[QR_PB][QR_PB + 1];
+  const QrTask<T> t = tasks[blockIdx.y];
+  const int n = t.n, r = t.r;
+  if (j0 >= r) return;
+  const int pw = min(QR_PB, r - j0), nr = n - j0;
+  const int c0 = (mode == 0 ? j0 + pw : j0) + blockIdx.x * QA_CW;
+  if (c0 >= r) return;
+  const int cw = min(QA_CW, r - c0);
+  const int tid = threadIdx.x;
+  const T* Vg = t.W + (size_t)j0 * n + j0;
+  auto aidx = [&](int i, int c) -> size_t {
+    return mode == 0 ? (size_t)(c0 + c) * n + j0 + i : (size_t)(j0 + i) * r + c0 + c;
+  };
+  T* A = mode == 0 ? t.W : t.Y;
+  for (int idx = tid; idx < QR_PB * QR_PB; idx += blockDim.x) {
+    const int a = idx / QR_PB, b = idx - a * QR_PB;
+    Ts[a][b] = (a <= b && b < pw) ? Vg[(size_t)b * n + a] : T(0);
+  }
+  auto load_v = [&](int i0, int h) {
+    for (int idx = tid; idx < QA_ROWS * QR_PB; idx += blockDim.x) {
+      const int p = idx / QA_ROWS, i = idx - p * QA_ROWS;
+      const int gi = i0 + i;
+      T v = T(0);
+      if (i < h && p < pw) v = gi == p ? T(1) : (gi > p ? Vg[(size_t)p * n + gi] : T(0));
+      Vs[i][p] = v;
+    }
+  };
+  auto load_a = [&](int i0, int h) {
+    for (int idx = tid; idx < QA_ROWS * QA_CW; idx += blockDim.x) {
+      int i, c;
+      if (mode == 0) { c = idx / QA_ROWS; i = idx - c * QA_ROWS; }
+      else { i = idx / QA_CW; c = idx - i * QA_CW; }
+      As[i][c] = (i < h && c < cw) ? A[aidx(i0 + i, c)] : T(0);
+    }
+  };
+  // Z = V^T A (thread: p = tid % 16, c = tid / 16)
+  const int zp = tid % QR_PB, zc = tid / QR_PB;
+  T z = T(0);
+  for (int i0 = 0; i0 < nr; i0 += QA_ROWS) {
+    const int h = min(QA_ROWS, nr - i0);
+    load_v(i0, h);
+    load_a(i0, h);
+    __syncthreads();
+#pragma unroll 8
+    for (int i = 0; i < QA_ROWS; ++i) z += Vs[i][zp] * As[i][zc];
+    __syncthreads();
+  }
+  Z[zp][zc] = z;
+  __syncthreads();
+  {
+    T m = T(0);
+    if (mode == 0) {
+      for (int q = 0; q <= zp; ++q) m += Ts[q][zp] * Z[q][zc];   // T^T Z
+    } else {
+      for (int q = zp; q < QR_PB; ++q) m += Ts[zp][q] * Z[q][zc];   // T Z
+    }
+    M[zp][zc] = m;
   }
   __syncthreads();
-  for (int k = 0; k < r; ++k) {
-    T* ck = W + (size_t)k * n;
-    T s = T(0);
-    for (int i = k + 1 + tid; i < n; i += blockDim.x) s += ck[i] * ck[i];
-    const T xnorm2 = block_sum_bcast<T>(s, red);
-    const T alpha = ck[k];
-    T tk = T(0), beta = alpha, scal = T(0);
-    if (xnorm2 > T(0)) {
-      beta = -copysign(sqrt(alpha * alpha + xnorm2), alpha);
-      tk = (beta - alpha) / beta;
-      scal = T(1) / (alpha - beta);
+  // A -= V M (thread: row i = tid % 64, columns 4 (tid / 64) .. +3)
+  const int ai = tid % QA_ROWS, aq = (tid / QA_ROWS) * 4;
+  for (int i0 = 0; i0 < nr; i0 += QA_ROWS) {
+    const int h = min(QA_ROWS, nr - i0);
+    load_v(i0, h);
+    load_a(i0, h);
+    __syncthreads();
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {
+      T s = T(0);
+#pragma unroll
+      for (int p = 0; p < QR_PB; ++p) s += Vs[ai][p] * M[p][aq + cc];
+      As[ai][aq + cc] -= s;
     }
     __syncthreads();
-    if (xnorm2 > T(0))
-      for (int i = k + 1 + tid; i < n; i += blockDim.x) ck[i] = ck[i] * scal;
-    if (tid == 0) {
-      ck[k] = beta;
-      tau[k] = tk;
+    for (int idx = tid; idx < QA_ROWS * QA_CW; idx += blockDim.x) {
+      int i, c;
+      if (mode == 0) { c = idx / QA_ROWS; i = idx - c * QA_ROWS; }
+      else { i = idx / QA_CW; c = idx - i * QA_CW; }
+      if (i < h && c < cw) A[aidx(i0 + i, c)] = As[i][c];
     }
     __syncthreads();
-    if (tk != T(0)) {
-      for (int j = k + 1 + warp; j < r; j += nw) {
-        T* cj = W + (size_t)j * n;
-        T w = T(0);
-        for (int i = k + 1 + lane; i < n; i += 32) w += ck[i] * cj[i];
-        w = warp_sum_d<T>(w);
-        const T cjk = cj[k];
-        __syncwarp();
-        w = tk * (w + cjk);
-        if (lane == 0) cj[k] = cjk - w;
-        for (int i = k + 1 + lane; i < n; i += 32) cj[i] = cj[i] - w * ck[i];
-      }
-    }
-    __syncthreads();
-  }
-  for (int k = r - 1; k >= 0; --k) {
-    T* ck = W + (size_t)k * n;
-    const T tk = tau[k];
-    if (tk != T(0)) {
-      for (int j = k + 1 + warp; j < r; j += nw) {
-        T* cj = W + (size_t)j * n;
-        T w = T(0);
-        for (int i = k + 1 + lane; i < n; i += 32) w += ck[i] * cj[i];
-        w = warp_sum_d<T>(w);
-        const T cjk = cj[k];
-        __syncwarp();
-        w = tk * (w + cjk);
-        if (lane == 0) cj[k] = cjk - w;
-        for (int i = k + 1 + lane; i < n; i += 32) cj[i] = cj[i] - w * ck[i];
-      }
-    }
-    __syncthreads();
-    for (int i = k + 1 + tid; i < n; i += blockDim.x) ck[i] = -tk * ck[i];
-    for (int i = tid; i < k; i += blockDim.x) ck[i] = T(0);
-    if (tid == 0) ck[k] = T(1) - tk;
-    __syncthreads();
-  }
-  for (long long idx = tid; idx < (long long)n * r; idx += blockDim.x) {
-    const int i = (int)(idx / r), j = (int)(idx - (long long)i * r);
-    t.Y[idx] = W[(size_t)j * n + i];
   }
 }
 
@@ -382,10 +541,43 @@ void launch_scatter(const double* A, const long long* si, const long long* di, l
   scatter_kernel<T><<<grid_for(count, 256), 256, 0, s>>>(A, si, di, count, dst);
   RSCHOL_LAUNCH_CHECK();
 }
-template <class T> void launch_householder_qr(const QrTask<T>* d, int n, cudaStream_t s) {
-  if (n <= 0) return;
-  householder_qr_kernel<T><<<n, QR_THREADS, 0, s>>>(d);
+template <class T> int launch_householder_qr(const QrTask<T>* d, int n, int maxRows, int maxR, cudaStream_t s) {
+  if (n <= 0 || maxR <= 0) return 0;
+  static bool attr = false;
+  if (!attr) {
+    RSCHOL_CUDA(cudaFuncSetAttribute(qr_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, QR_SMEM_MAX));
+    attr = true;
+  }
+  const long long tiles = (long long)((maxRows + 31) / 32) * ((maxR + 31) / 32);
+  qr_to_colmajor<T><<<dim3((unsigned)std::min<long long>(tiles, 64), n), 256, 0, s>>>(d);
   RSCHOL_LAUNCH_CHECK();
+  int launches = 1;
+  const size_t smem = std::min<size_t>((size_t)QR_SMEM_MAX, sizeof(T) * (size_t)maxRows * QR_PB);
+  const long long smemElems = (long long)(smem / sizeof(T));
+  const int panels = (maxR + QR_PB - 1) / QR_PB;
+  for (int p = 0; p < panels; ++p) {
+    const int j0 = p * QR_PB;
+    qr_panel_kernel<T><<<n, QRP_THREADS, smem, s>>>(d, j0, smemElems);
+    RSCHOL_LAUNCH_CHECK();
+    ++launches;
+    const int trail = maxR - j0 - QR_PB;
+    if (trail > 0) {
+      qr_apply_kernel<T><<<dim3((trail + QA_CW - 1) / QA_CW, n), 256, 0, s>>>(d, j0, 0);
+      RSCHOL_LAUNCH_CHECK();
+      ++launches;
+    }
+  }
+  const long long ecount = (long long)maxRows * maxR;
+  qr_set_e<T><<<dim3((unsigned)std::max<long long>(1, std::min<long long>((ecount + 255) / 256, 256)), n), 256, 0, s>>>(d);
+  RSCHOL_LAUNCH_CHECK();
+  ++launches;
+  for (int p = panels - 1; p >= 0; --p) {
+    const int j0 = p * QR_PB;
+    qr_apply_kernel<T><<<dim3((maxR - j0 + QA_CW - 1) / QA_CW, n), 256, 0, s>>>(d, j0, 1);
+    RSCHOL_LAUNCH_CHECK();
+    ++launches;
+  }
+  return launches;
 }
 template <class T> void launch_set_identity(const IdentTask<T>* d, int n, cudaStream_t s) {
   if (n <= 0) return;
@@ -405,7 +597,7 @@ template <class T> void launch_box_muller(const uint32_t* raw, long long count, 
   template void launch_extadd<T>(const ExtAddTarget<T>*, int, const ExtAddSource<T>*, int, cudaStream_t); \
   template void launch_scatter<T>(const double*, const long long*, const long long*, long long, T*,      \
                                   cudaStream_t);                                                         \
-  template void launch_householder_qr<T>(const QrTask<T>*, int, cudaStream_t);                           \
+  template int launch_householder_qr<T>(const QrTask<T>*, int, int, int, cudaStream_t);                  \
   template void launch_set_identity<T>(const IdentTask<T>*, int, cudaStream_t);                          \
   template void launch_box_muller<T>(const uint32_t*, long long, T*, cudaStream_t);
 RSCHOL_INST(double)

@@ -76,17 +76,20 @@ void launch_extadd(const ExtAddTarget<T>* dTargets, int nTargets, const ExtAddSo
 template <class T>
 void launch_scatter(const double* Avals, const long long* srcIdx, const long long* dstIdx, long long count,
                     T* dst, cudaStream_t s);
-// Thin Householder QR, Y (n x r, row-major, r <= n) := Q: the LAPACK
+// Thin Householder QR, Y (n x r, row-major, r < n) := Q: the LAPACK
 // geqrf + orgqr pair the reference calls (MATRIX::qr / extractQRfactor,
-// src/rschol/linearalgebra/MATRIX_FAST.cpp:1095-1180), one CTA per matrix.
-// W is an r x n column-major scratch, tau r scalars.
+// src/rschol/linearalgebra/MATRIX_FAST.cpp:1095-1180), blocked in panels of
+// 16 columns (compact WY).  W is an n x r column-major scratch (the
+// reflectors and the panels' T factors).  maxRows / maxR bound n and r over
+// the batch.  Returns the number of launches.
 template <class T>
 struct QrTask {
   T* Y;
   T* W;
   int n, r;
 };
-template <class T> void launch_householder_qr(const QrTask<T>* dTasks, int nTasks, cudaStream_t s);
+template <class T>
+int launch_householder_qr(const QrTask<T>* dTasks, int nTasks, int maxRows, int maxR, cudaStream_t s);
 template <class T>
 struct IdentTask {
   T* U;

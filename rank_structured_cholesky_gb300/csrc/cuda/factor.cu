@@ -198,7 +198,12 @@ void FactorEngine<T>::emit_rf(const std::vector<RFJob<T>>& jobs) {
     ident_.insert(ident_.end(), id.begin(), id.end());
   }
   if (!qt.empty()) {
-    steps_.push_back(Step{ST_QR, (long long)qr_.size(), (int)qt.size(), (int)qt.size()});
+    int maxRows = 0, maxR = 0;
+    for (auto& q : qt) {
+      maxRows = std::max(maxRows, q.n);
+      maxR = std::max(maxR, q.r);
+    }
+    steps_.push_back(Step{ST_QR, (long long)qr_.size(), (int)qt.size(), maxR, maxRows});
     qr_.insert(qr_.end(), qt.begin(), qt.end());
   }
   // V = F U
@@ -730,7 +735,9 @@ int FactorEngine<T>::run() {
         launch_extadd<T>(dEaT_.as<ExtAddTarget<T>>() + st.off, st.count, dEaS_.as<ExtAddSource<T>>(), st.grid,
                          stream);
         break;
-      case ST_QR: launch_householder_qr<T>(dQr_.as<QrTask<T>>() + st.off, st.count, stream); break;
+      case ST_QR:
+        launches += launch_householder_qr<T>(dQr_.as<QrTask<T>>() + st.off, st.count, st.aux, st.grid, stream) - 1;
+        break;
       case ST_IDENT: launch_set_identity<T>(dIdent_.as<IdentTask<T>>() + st.off, st.count, stream); break;
     }
     ++launches;

@@ -52,6 +52,7 @@ struct Step {
   long long off;    // first task in the kind's task array
   int count;        // number of tasks
   int grid;         // tiles / chunks / columns for the launch
+  int aux = 0;      // ST_QR: largest row count of the batch (grid: largest rank)
 };
 
 template <class T>
