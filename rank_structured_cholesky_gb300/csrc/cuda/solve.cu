@@ -16,170 +16,188 @@ __device__ __forceinline__ V warp_sum(V v) {
   return v;
 }
 
-// f := L^{-1} f for a dense lower L (n x n, leading dimension ld); f in
-// shared memory.  32-wide tiles: warp 0 solves the diagonal tile, then every
-// thread updates its own rows below with a 32-term dot product whose 32
-// loads are independent (memory-level parallelism instead of one
-// latency-bound warp reduction per row).
+// f := L^{-1} f with the inverted 64 x 64 diagonal blocks of L (block b:
+// h_b x h_b row-major at D + 4096 b; only the last block can be smaller).
+// f (n) and t (64) in shared memory.  A warp per row: loads coalesced along
+// the row of L or D.
 template <class T>
-__device__ void trsv_lower(const T* __restrict__ L, int ld, int n, T* f, T (*tile)[33]) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int t0 = 0; t0 < n; t0 += 32) {
-    const int tw = min(32, n - t0);
-    for (int idx = threadIdx.x; idx < tw * tw; idx += blockDim.x) {
-      int i = idx / tw, j = idx - i * tw;
-      tile[i][j] = (j <= i) ? L[(size_t)(t0 + i) * ld + t0 + j] : T(0);
-    }
-    __syncthreads();
-    if (warp == 0) {
-      T v = (lane < tw) ? f[t0 + lane] : T(0);
-      for (int j = 0; j < tw; ++j) {
-        const T yj = __shfl_sync(FULL, v, j) / tile[j][j];
-        if (lane == j) v = yj;
-        else if (lane > j && lane < tw) v -= tile[lane][j] * yj;
-      }
-      if (lane < tw) f[t0 + lane] = v;
-    }
-    __syncthreads();
-    for (int i = t0 + tw + threadIdx.x; i < n; i += blockDim.x) {
-      const T* row = L + (size_t)i * ld + t0;
+__device__ void trsv_dinv(const T* __restrict__ L, int ld, int n, const T* __restrict__ D, T* f, T* t) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  for (int i0 = 0; i0 < n; i0 += 64) {
+    const int h = min(64, n - i0);
+    for (int i = warp; i < h; i += nwarp) {
+      const T* row = L + (size_t)(i0 + i) * ld;
       T s = T(0);
-      if (tw == 32) {
-#pragma unroll
-        for (int k = 0; k < 32; ++k) s += row[k] * f[t0 + k];
-      } else {
-        for (int k = 0; k < tw; ++k) s += row[k] * f[t0 + k];
-      }
-      f[i] -= s;
+      for (int j = lane; j < i0; j += 32) s += row[j] * f[j];
+      s = warp_sum(s);
+      if (lane == 0) t[i] = f[i0 + i] - s;
+    }
+    __syncthreads();
+    const T* Db = D + (size_t)i0 * 64;
+    for (int i = warp; i < h; i += nwarp) {
+      const T* row = Db + (size_t)i * h;
+      T s = T(0);
+      for (int j = lane; j <= i; j += 32) s += row[j] * t[j];
+      s = warp_sum(s);
+      if (lane == 0) f[i0 + i] = s;
     }
     __syncthreads();
   }
 }
 
-// out[k] = sum_{i < rows} M[i][k] * v(i) for k < cols (M row-major, ld),
-// computed by nGroups groups of threads that split the rows, then a
-// fixed-order reduction of the group partials in shared memory.
-// scratch: nGroups * cols doubles of shared memory.
-template <class T, class VecFn>
-__device__ void gemv_t_split(const T* __restrict__ M, int ld, int rows, int cols, VecFn v, T* out,
-                             T* scratch) {
-  const int groups = max(1, (int)blockDim.x / max(cols, 1));
-  const int g = threadIdx.x / max(cols, 1), k = threadIdx.x - g * max(cols, 1);
-  if (cols <= (int)blockDim.x) {
-    if (g < groups) {
-      T s = T(0);
-      for (int i = g; i < rows; i += groups) s += M[(size_t)i * ld + k] * v(i);
-      scratch[g * cols + k] = s;
-    }
-    __syncthreads();
-    for (int kk = threadIdx.x; kk < cols; kk += blockDim.x) {
-      T s = T(0);
-      for (int q = 0; q < groups; ++q) s += scratch[q * cols + kk];
-      out[kk] = s;
-    }
-  } else {
-    for (int kk = threadIdx.x; kk < cols; kk += blockDim.x) {
-      T s = T(0);
-      for (int i = 0; i < rows; ++i) s += M[(size_t)i * ld + kk] * v(i);
-      out[kk] = s;
-    }
-  }
-  __syncthreads();
-}
-
-// f := L^{-T} f.
+// f := L^{-T} f with the same inverted diagonal blocks.  red: 4 x 64 shared.
 template <class T>
-__device__ void trsv_lower_t(const T* __restrict__ L, int ld, int n, T* f, T (*tile)[33]) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ void trsv_dinv_t(const T* __restrict__ L, int ld, int n, const T* __restrict__ D, T* f, T* t,
+                            T (*red)[64]) {
+  const int c = threadIdx.x & 63, grp = threadIdx.x >> 6, ngrp = blockDim.x >> 6;
   if (n <= 0) return;
-  for (int t0 = ((n - 1) / 32) * 32; t0 >= 0; t0 -= 32) {
-    const int tw = min(32, n - t0);
-    for (int idx = threadIdx.x; idx < tw * tw; idx += blockDim.x) {
-      int i = idx / tw, j = idx - i * tw;
-      tile[i][j] = (j <= i) ? L[(size_t)(t0 + i) * ld + t0 + j] : T(0);
+  for (int i0 = ((n - 1) / 64) * 64; i0 >= 0; i0 -= 64) {
+    const int h = min(64, n - i0);
+    T s = T(0);
+    if (c < h)
+      for (int i = i0 + h + grp; i < n; i += ngrp) s += L[(size_t)i * ld + i0 + c] * f[i];
+    red[grp][c] = s;
+    __syncthreads();
+    if (threadIdx.x < h) {
+      T u = T(0);
+      for (int g = 0; g < ngrp; ++g) u += red[g][threadIdx.x];
+      t[threadIdx.x] = f[i0 + threadIdx.x] - u;
     }
     __syncthreads();
-    if (warp == 0) {
-      T v = (lane < tw) ? f[t0 + lane] : T(0);
-      for (int j = tw - 1; j >= 0; --j) {
-        const T xj = __shfl_sync(FULL, v, j) / tile[j][j];
-        if (lane == j) v = xj;
-        else if (lane < j) v -= tile[j][lane] * xj;
-      }
-      if (lane < tw) f[t0 + lane] = v;
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < t0; i += blockDim.x) {
-      T s = T(0);
-      for (int k = 0; k < tw; ++k) s += L[(size_t)(t0 + k) * ld + i] * f[t0 + k];
-      f[i] -= s;
+    if (threadIdx.x < h) {
+      const T* Db = D + (size_t)i0 * 64;
+      T x = T(0);
+      for (int i = threadIdx.x; i < h; ++i) x += Db[(size_t)i * h + threadIdx.x] * t[i];
+      f[i0 + threadIdx.x] = x;
     }
     __syncthreads();
   }
 }
 
+// Interior supernodes: one thread block per (supernode, 128-row chunk of its
+// off-diagonal rows).  Every chunk block assembles and solves the supernode's
+// own n columns (n is small); chunk 0 stores y.
+constexpr int ICH = 128;
+
 template <class T>
-__global__ void __launch_bounds__(256) interior_forward_kernel(const SNode<T>* __restrict__ nodes,
-                                                               const int* __restrict__ lvl,
-                                                               const int* __restrict__ rows,
+__global__ void __launch_bounds__(256) interior_forward_chunks(const SNode<T>* __restrict__ nodes,
+                                                               const RowBlock* __restrict__ work,
                                                                const int* __restrict__ rel,
                                                                const int* __restrict__ child,
-                                                               T* __restrict__ w, T* __restrict__ wu) {
+                                                               const T* __restrict__ w, T* __restrict__ yout,
+                                                               T* __restrict__ wu) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* f = reinterpret_cast<T*>(smraw);
-  __shared__ T tile[32][33];
-  const SNode<T> nd = nodes[lvl[blockIdx.x]];
+  __shared__ T tb[64];
+  const RowBlock wk = work[blockIdx.x];
+  const SNode<T>& nd = nodes[wk.node];
+  const int n = nd.n, a0 = wk.b * ICH, a1 = min(nd.m, a0 + ICH);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T* wud = wu + nd.wuOff;
-  for (int i = threadIdx.x; i < nd.n; i += blockDim.x) f[i] = w[nd.c0 + i];
-  for (int a = threadIdx.x; a < nd.m; a += blockDim.x) wud[a] = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) f[i] = w[nd.c0 + i];
+  for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) wud[a] = T(0);
   __syncthreads();
+  // children's update vectors, in child order
   for (int c = nd.childBegin; c < nd.childEnd; ++c) {
-    const SNode<T> cn = nodes[child[c]];
+    const SNode<T>& cn = nodes[child[c]];
     const T* wuc = wu + cn.wuOff;
     const int* rl = rel + cn.relOff;
     for (int a = threadIdx.x; a < cn.m; a += blockDim.x) {
       const int t = rl[a];
-      if (t < nd.n) f[t] += wuc[a];
-      else wud[t - nd.n] += wuc[a];
+      if (t < n) f[t] += wuc[a];
+      else if (t - n >= a0 && t - n < a1) wud[t - n] += wuc[a];
     }
     __syncthreads();
   }
-  trsv_lower<T>(nd.L, nd.ld, nd.n, f, tile);
-  // update vector: wud -= L21 y, one thread per row (independent loads)
-  for (int a = threadIdx.x; a < nd.m; a += blockDim.x) {
-    const T* row = nd.L + (size_t)(nd.n + a) * nd.ld;
-    T s = T(0);
-    for (int j = 0; j < nd.n; ++j) s += row[j] * f[j];
-    wud[a] -= s;
+  trsv_dinv<T>(nd.L, nd.ld, n, nd.Dinv, f, tb);
+  // y goes to a separate vector: the other chunk blocks still read w
+  if (wk.b == 0)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) yout[nd.c0 + i] = f[i];
+  // wud[a] -= L21[a] . y: a warp per 4 rows (loads coalesced along the rows)
+  for (int a = a0 + warp * 4; a < a1; a += 32) {
+    T s[4] = {T(0), T(0), T(0), T(0)};
+    const T* row = nd.L + (size_t)(n + a) * nd.ld;
+    for (int j = lane; j < n; j += 32) {
+      const T fj = f[j];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (a + q < a1) s[q] += row[(size_t)q * nd.ld + j] * fj;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const T v = warp_sum(s[q]);
+      if (lane == 0 && a + q < a1) wud[a + q] -= v;
+    }
   }
-  for (int i = threadIdx.x; i < nd.n; i += blockDim.x) w[nd.c0 + i] = f[i];
 }
 
+// Backward: each chunk block forms its part of L21^T x_R; the last chunk
+// block of the supernode to finish sums the parts in fixed order and solves
+// with L11^T.
 template <class T>
-__global__ void __launch_bounds__(256) interior_backward_kernel(const SNode<T>* __restrict__ nodes,
-                                                                const int* __restrict__ lvl,
+__global__ void __launch_bounds__(256) interior_backward_chunks(const SNode<T>* __restrict__ nodes,
+                                                                const RowBlock* __restrict__ work,
                                                                 const int* __restrict__ rows,
-                                                                T* __restrict__ w) {
+                                                                int* __restrict__ sync, T* __restrict__ ipart,
+                                                                const T* __restrict__ yin, T* __restrict__ w) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* sm = reinterpret_cast<T*>(smraw);
-  __shared__ T tile[32][33];
-  __shared__ T scratch[256];
-  const SNode<T> nd = nodes[lvl[blockIdx.x]];
-  T* f = sm;
-  T* t = sm + nd.n;
-  T* xr = sm + 2 * nd.n;
-  const int* rw = rows + nd.rowsOff;
-  for (int i = threadIdx.x; i < nd.n; i += blockDim.x) f[i] = w[nd.c0 + i];
-  for (int a = threadIdx.x; a < nd.m; a += blockDim.x) xr[a] = w[rw[a]];
-  __syncthreads();
-  if (nd.m > 0) {
-    // t = L21^T x_R with the rows split over thread groups
-    gemv_t_split<T>(nd.L + (size_t)nd.n * nd.ld, nd.ld, nd.m, nd.n, [&](int a) { return xr[a]; }, t, scratch);
-    for (int i = threadIdx.x; i < nd.n; i += blockDim.x) f[i] -= t[i];
+  __shared__ T tb[64];
+  __shared__ T red[8][256];
+  __shared__ int sLast;
+  const RowBlock wk = work[blockIdx.x];
+  const SNode<T>& nd = nodes[wk.node];
+  const int n = nd.n, a0 = wk.b * ICH, a1 = min(nd.m, a0 + ICH);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* f = reinterpret_cast<T*>(smraw);   // n values
+  T* xr = f + ((n + 1) & ~1);           // ICH values
+  const int nch = (nd.m + ICH - 1) / ICH;
+  if (nch > 0) {
+    const int* rw = rows + nd.rowsOff;
+    for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) xr[a - a0] = w[rw[a]];
     __syncthreads();
+    // part[j] = sum_{a in chunk} L21[a][j] x_a: warp w takes rows w, w+8, ...
+    // (lanes along the row), then the 8 warp partials are summed in order
+    const T* L21 = nd.L + (size_t)(n + a0) * nd.ld;
+    for (int jt = 0; jt < n; jt += 256) {
+      T acc[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = T(0);
+      for (int a = warp; a < a1 - a0; a += 8) {
+        const T x = xr[a];
+        const T* row = L21 + (size_t)a * nd.ld + jt;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (jt + lane + 32 * q < n) acc[q] += row[lane + 32 * q] * x;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) red[warp][lane + 32 * q] = acc[q];
+      __syncthreads();
+      const int j = jt + threadIdx.x;
+      if (threadIdx.x < 256 && j < n) {
+        T s = T(0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s += red[q][threadIdx.x];
+        ipart[nd.zpOff + (size_t)wk.b * n + j] = s;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      __threadfence();
+      sLast = (atomicAdd(sync + nd.syncOff, 1) == nch - 1);
+      __threadfence();
+    }
+    __syncthreads();
+    if (!sLast) return;
   }
-  trsv_lower_t<T>(nd.L, nd.ld, nd.n, f, tile);
-  for (int i = threadIdx.x; i < nd.n; i += blockDim.x) w[nd.c0 + i] = f[i];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    T t = T(0);
+    for (int c = 0; c < nch; ++c) t += __ldcg(ipart + nd.zpOff + (size_t)c * n + i);
+    f[i] = yin[nd.c0 + i] - t;
+  }
+  __syncthreads();
+  trsv_dinv_t<T>(nd.L, nd.ld, n, nd.Dinv, f, tb, reinterpret_cast<T(*)[64]>(&red[0][0]));
+  for (int i = threadIdx.x; i < n; i += blockDim.x) w[nd.c0 + i] = f[i];
+  if (threadIdx.x == 0 && nch > 0) sync[nd.syncOff] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -219,8 +237,8 @@ __device__ __forceinline__ bool wait_ready(const int* flag, int* err) {
 __device__ __forceinline__ bool finish_row_block(int* flag, int* nodeDone, int nb, int* levelTick, int* levelDone, int* sLast) {
   __syncthreads();
   if (threadIdx.x == 0) {
+    if (flag) st_release(flag, 1);   // release: the block's stores, ordered by the barrier, become visible first
     __threadfence();
-    st_release(flag, 1);
     const int d = atomicAdd(nodeDone, 1);
     *sLast = (d == nb - 1);
     if (atomicAdd(levelDone, 1) == (int)gridDim.x - 1) {
@@ -233,17 +251,21 @@ __device__ __forceinline__ bool finish_row_block(int* flag, int* nodeDone, int n
   return *sLast != 0;
 }
 
-// acc[rr] (row 8w+rr of the block) += P[row][2l] v0 + P[row][2l+1] v1 for a
-// 64-column tile P (row-major, ld), rows limited to h.
+// t[rr][0..1] = P[row][2l], P[row][2l+1] of a 64-column tile (rows
+// 8w+rr < h, zero elsewhere).
 template <class T>
-__device__ __forceinline__ void tile_rows(const T* __restrict__ P, int ld, int h, T v0, T v1, T (&acc)[8]) {
+__device__ __forceinline__ void load_tile(const T* __restrict__ P, int ld, int h, T (&t)[8][2]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int rr = 0; rr < 8; ++rr) {
     const int i = warp * 8 + rr;
     if (i < h) {
       const T* p = P + (size_t)i * ld + 2 * lane;
-      acc[rr] += p[0] * v0 + p[1] * v1;
+      t[rr][0] = p[0];
+      t[rr][1] = p[1];
+    } else {
+      t[rr][0] = T(0);
+      t[rr][1] = T(0);
     }
   }
 }
@@ -293,15 +315,26 @@ __global__ void __launch_bounds__(256) compressed_forward_blocks(const SNode<T>*
     acc = warp_sum(acc);
     if (lane == 0) fb[i] = (i < h) ? wn[i0 + i] + acc : T(0);
   }
-  // 2. earlier row blocks, as they become ready
-  T acc[8];
+  // 2. earlier row blocks, as they become ready; the L tile of the next
+  // block is loaded before waiting on the current one
+  T acc[8], cur[8][2], dv[8][2];
 #pragma unroll
   for (int rr = 0; rr < 8; ++rr) acc[rr] = T(0);
+  load_tile<T>(nd.Dinv + (size_t)tk.b * SOLVE_RB * SOLVE_RB, SOLVE_RB, h, dv);
+  const T* Lrow = nd.L + (size_t)i0 * nd.ld;
+  if (tk.b > 0) load_tile<T>(Lrow, nd.ld, h, cur);
   bool ok = true;
   for (int kb = 0; kb < tk.b && ok; ++kb) {
+    T nxt[8][2] = {};
+    if (kb + 1 < tk.b) load_tile<T>(Lrow + (kb + 1) * SOLVE_RB, nd.ld, h, nxt);
     ok = wait_ready(flags + kb, err);
     const T y0 = __ldcg(wn + kb * SOLVE_RB + 2 * lane), y1 = __ldcg(wn + kb * SOLVE_RB + 2 * lane + 1);
-    tile_rows<T>(nd.L + (size_t)i0 * nd.ld + kb * SOLVE_RB, nd.ld, h, y0, y1, acc);
+#pragma unroll
+    for (int rr = 0; rr < 8; ++rr) {
+      acc[rr] += cur[rr][0] * y0 + cur[rr][1] * y1;
+      cur[rr][0] = nxt[rr][0];
+      cur[rr][1] = nxt[rr][1];
+    }
   }
   __syncwarp();
 #pragma unroll
@@ -313,9 +346,9 @@ __global__ void __launch_bounds__(256) compressed_forward_blocks(const SNode<T>*
   // 3. y_b = Dinv_b f_b
   {
     T d[8];
+    const T f0 = fb[2 * lane], f1 = fb[2 * lane + 1];
 #pragma unroll
-    for (int rr = 0; rr < 8; ++rr) d[rr] = T(0);
-    tile_rows<T>(nd.Dinv + (size_t)tk.b * SOLVE_RB * SOLVE_RB, SOLVE_RB, h, fb[2 * lane], fb[2 * lane + 1], d);
+    for (int rr = 0; rr < 8; ++rr) d[rr] = dv[rr][0] * f0 + dv[rr][1] * f1;
 #pragma unroll
     for (int rr = 0; rr < 8; ++rr) {
       const T s = warp_sum(d[rr]);
@@ -327,6 +360,8 @@ __global__ void __launch_bounds__(256) compressed_forward_blocks(const SNode<T>*
     }
   }
   __syncthreads();
+  // y_b is final: publish it before the (off the critical path) z partial
+  if (threadIdx.x == 0) st_release(flags + tk.b, 1);
   // 4. partial z_b = U_b^T y_b
   const int r = nd.r;
   for (int k = threadIdx.x; k < r; k += blockDim.x) {
@@ -335,7 +370,7 @@ __global__ void __launch_bounds__(256) compressed_forward_blocks(const SNode<T>*
     zpart[nd.zpOff + (size_t)tk.b * r + k] = s;
   }
   const int nb = nd.nb;
-  if (finish_row_block(flags + tk.b, flags + nb, nb, &sync[levelSync], &sync[levelSync + 1], &sLast)) {
+  if (finish_row_block(nullptr, flags + nb, nb, &sync[levelSync], &sync[levelSync + 1], &sLast)) {
     // last row block of this supernode: z in fixed order, then reset the flags
     for (int k = threadIdx.x; k < r; k += blockDim.x) {
       T s = T(0);
@@ -420,21 +455,29 @@ __global__ void __launch_bounds__(256) compressed_backward_blocks(const SNode<T>
     acc = warp_sum(acc);
     if (lane == 0) gb[i] = (i < h) ? wn[i0 + i] - acc : T(0);
   }
-  // 2. later row blocks: column block b of L below the diagonal, transposed
-  T p0 = T(0), p1 = T(0);
+  // 2. later row blocks: column block b of L below the diagonal, transposed;
+  // the tile of the next block is loaded before waiting on the current one
+  T p0 = T(0), p1 = T(0), cur[8][2], dv[8][2];
+  load_tile<T>(nd.Dinv + (size_t)tk.b * SOLVE_RB * SOLVE_RB, SOLVE_RB, SOLVE_RB, dv);
+  const T* Lcol = nd.L + i0;
+  if (nb - 1 > tk.b) {
+    const int k0 = (nb - 1) * SOLVE_RB;
+    load_tile<T>(Lcol + (size_t)k0 * nd.ld, nd.ld, min(SOLVE_RB, n - k0), cur);
+  }
   bool ok = true;
   for (int kb = nb - 1; kb > tk.b && ok; --kb) {
+    T nxt[8][2] = {};
+    if (kb - 1 > tk.b) load_tile<T>(Lcol + (size_t)(kb - 1) * SOLVE_RB * nd.ld, nd.ld, SOLVE_RB, nxt);
     ok = wait_ready(flags + kb, err);
     const int k0 = kb * SOLVE_RB, kh = min(SOLVE_RB, n - k0);
 #pragma unroll
     for (int rr = 0; rr < 8; ++rr) {
       const int i = warp * 8 + rr;
-      if (i < kh) {
-        const T xi = __ldcg(wn + k0 + i);
-        const T* p = nd.L + (size_t)(k0 + i) * nd.ld + i0 + 2 * lane;
-        p0 += p[0] * xi;
-        p1 += p[1] * xi;
-      }
+      const T xi = (i < kh) ? __ldcg(wn + k0 + i) : T(0);
+      p0 += cur[rr][0] * xi;
+      p1 += cur[rr][1] * xi;
+      cur[rr][0] = nxt[rr][0];
+      cur[rr][1] = nxt[rr][1];
     }
   }
   red[warp][2 * lane] = p0;
@@ -449,14 +492,12 @@ __global__ void __launch_bounds__(256) compressed_backward_blocks(const SNode<T>
   __syncthreads();
   // 3. x_b = Dinv_b^T v (rows of Dinv split over the warps)
   {
-    const T* D = nd.Dinv + (size_t)tk.b * SOLVE_RB * SOLVE_RB;
     T q0 = T(0), q1 = T(0);
 #pragma unroll
     for (int rr = 0; rr < 8; ++rr) {
-      const int i = warp * 8 + rr;
-      const T vi = vb[i];
-      q0 += D[(size_t)i * SOLVE_RB + 2 * lane] * vi;
-      q1 += D[(size_t)i * SOLVE_RB + 2 * lane + 1] * vi;
+      const T vi = vb[warp * 8 + rr];
+      q0 += dv[rr][0] * vi;
+      q1 += dv[rr][1] * vi;
     }
     __syncthreads();
     red[warp][2 * lane] = q0;
@@ -476,24 +517,26 @@ __global__ void __launch_bounds__(256) compressed_backward_blocks(const SNode<T>
 }
 
 // Inverse of each lower-triangular diagonal block (column c by thread c,
-// forward substitution), zero-padded to 64 x 64.
+// forward substitution), written as pad x pad (row-major, ld pad) with zeros
+// outside the h x h lower triangle.
 template <class T>
 __global__ void __launch_bounds__(64) invert_diag_blocks(const DinvTask<T>* __restrict__ tasks) {
   __shared__ T Ls[SOLVE_RB][SOLVE_RB + 1];
   const DinvTask<T> t = tasks[blockIdx.x];
-  const int h = t.h, c = threadIdx.x;
+  const int h = t.h, pad = t.pad, c = threadIdx.x;
   for (int idx = threadIdx.x; idx < h * h; idx += blockDim.x) {
     const int i = idx / h, j = idx - i * h;
     Ls[i][j] = (j <= i) ? t.L[(size_t)i * t.ld + j] : T(0);
   }
   T* D = t.D;
-  for (int i = 0; i < SOLVE_RB; ++i) D[i * SOLVE_RB + c] = T(0);
+  if (c < pad)
+    for (int i = 0; i < pad; ++i) D[i * pad + c] = T(0);
   __syncthreads();
   if (c < h) {
     for (int i = c; i < h; ++i) {
       T s = (i == c) ? T(1) : T(0);
-      for (int k = c; k < i; ++k) s -= Ls[i][k] * D[k * SOLVE_RB + c];
-      D[i * SOLVE_RB + c] = s / Ls[i][i];
+      for (int k = c; k < i; ++k) s -= Ls[i][k] * D[k * pad + c];
+      D[i * pad + c] = s / Ls[i][i];
     }
   }
 }
@@ -515,7 +558,7 @@ void SolveEngine<T>::plan() {
   const int nn = (int)S.nodes.size();
   nodes_.assign(nn, SNode<T>{});
   std::vector<int> rowsAll, rel, child, lvlNodes;
-  long long wuCur = 0, dinvCur = 0, zpCur = 0, spCur = 0;
+  long long wuCur = 0, dinvCur = 0, zpCur = 0, spCur = 0, ipCur = 0;
   int syncCur = 1 + 4 * (int)F_.compressedLevels.size();   // error word, per-level tickets
   bytesPerApply_ = 0;
   std::vector<int> pos(S.n, -1);
@@ -535,6 +578,27 @@ void SolveEngine<T>::plan() {
       sn.r = 0;
       sn.wuOff = wuCur;
       wuCur += nd.m();
+      sn.nch = (nd.m() + ICH - 1) / ICH;
+      sn.syncOff = syncCur;
+      syncCur += 1;
+      sn.zpOff = ipCur;
+      ipCur += (long long)sn.nch * nd.n;
+      // inverted 64 x 64 diagonal blocks, the last one stored h x h
+      const int nbI = (nd.n + SOLVE_RB - 1) / SOLVE_RB;
+      for (int b = 0; b < nbI; ++b) {
+        DinvTask<T> t{};
+        t.L = sn.L + (size_t)b * SOLVE_RB * sn.ld + (size_t)b * SOLVE_RB;
+        t.ld = sn.ld;
+        t.h = std::min(SOLVE_RB, nd.n - b * SOLVE_RB);
+        t.pad = t.h;
+        dinvTasks.push_back(t);
+        dinvTaskOff.push_back(dinvCur + (long long)b * SOLVE_RB * SOLVE_RB);
+      }
+      dinvNodeOff[s] = dinvCur;
+      {
+        const int hl = nd.n - (nbI - 1) * SOLVE_RB;
+        dinvCur += (long long)(nbI - 1) * SOLVE_RB * SOLVE_RB + (long long)hl * hl;
+      }
       bytesPerApply_ += 2.0 * sizeof(T) * (double)(nd.n * (nd.n + 1) / 2 + (double)nd.m() * nd.n);
     } else {
       sn.L = F_.compressed() + F_.frontOff[s];
@@ -556,6 +620,7 @@ void SolveEngine<T>::plan() {
         t.L = sn.L + (size_t)b * SOLVE_RB * sn.ld + (size_t)b * SOLVE_RB;
         t.ld = sn.ld;
         t.h = std::min(SOLVE_RB, nd.n - b * SOLVE_RB);
+        t.pad = SOLVE_RB;
         dinvTasks.push_back(t);
         dinvTaskOff.push_back(dinvCur + (long long)b * SOLVE_RB * SOLVE_RB);
       }
@@ -599,14 +664,16 @@ void SolveEngine<T>::plan() {
   cLevels_.clear();
   smemIF_.clear();
   smemIB_.clear();
+  std::vector<RowBlock> iwork;
   for (auto& lv : F_.interiorLevels) {
-    iLevels_.push_back({(long long)lvlNodes.size(), (int)lv.size()});
-    lvlNodes.insert(lvlNodes.end(), lv.begin(), lv.end());
+    iLevels_.push_back({(long long)iwork.size(), 0});
     size_t f = 8, b = 8;
     for (int d : lv) {
+      for (int c = 0; c < std::max(1, nodes_[d].nch); ++c) iwork.push_back(RowBlock{d, c});
       f = std::max(f, sizeof(T) * S.nodes[d].n);
-      b = std::max(b, sizeof(T) * (2 * S.nodes[d].n + S.nodes[d].m()));
+      b = std::max(b, sizeof(T) * (((S.nodes[d].n + 1) & ~1) + ICH));
     }
+    iLevels_.back().second = (int)(iwork.size() - iLevels_.back().first);
     smemIF_.push_back(f);
     smemIB_.push_back(b);
   }
@@ -647,9 +714,10 @@ void SolveEngine<T>::plan() {
   dDinv_.alloc(sizeof(T) * std::max(1LL, dinvCur));
   dZp_.alloc(sizeof(T) * std::max(1LL, zpCur));
   dSp_.alloc(sizeof(T) * std::max(1LL, spCur));
+  dIp_.alloc(sizeof(T) * std::max(1LL, ipCur));
+  dYi_.alloc(sizeof(T) * std::max(1, S.n));
   for (size_t q = 0; q < dinvTasks.size(); ++q) dinvTasks[q].D = dDinv_.as<T>() + dinvTaskOff[q];
-  for (int s = 0; s < nn; ++s)
-    if (S.nodes[s].compressed) nodes_[s].Dinv = dDinv_.as<T>() + dinvNodeOff[s];
+  for (int s = 0; s < nn; ++s) nodes_[s].Dinv = dDinv_.as<T>() + dinvNodeOff[s];
   nDinv_ = (int)dinvTasks.size();
   // per-row contribution lists of the compressed supernodes (in source order)
   {
@@ -692,6 +760,7 @@ void SolveEngine<T>::plan() {
   up(dRel_, rel.data(), rel.size() * sizeof(int));
   up(dChild_, child.data(), child.size() * sizeof(int));
   up(dLevelNodes_, lvlNodes.data(), lvlNodes.size() * sizeof(int));
+  up(dIWork_, iwork.data(), iwork.size() * sizeof(RowBlock));
   up(dTickF_, tickF.data(), tickF.size() * sizeof(RowBlock));
   up(dTickB_, tickB.data(), tickB.size() * sizeof(RowBlock));
   up(dDinvTasks_, dinvTasks.data(), dinvTasks.size() * sizeof(DinvTask<T>));
@@ -701,8 +770,8 @@ void SolveEngine<T>::plan() {
   if (!std::is_same<T, double>::value) dW_.alloc(sizeof(T) * std::max(1, S.n));
   RSCHOL_CUDA(cudaStreamSynchronize(st));
   const int maxSmem = 200 * 1024;
-  RSCHOL_CUDA(cudaFuncSetAttribute(interior_forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
-  RSCHOL_CUDA(cudaFuncSetAttribute(interior_backward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
+  RSCHOL_CUDA(cudaFuncSetAttribute(interior_forward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
+  RSCHOL_CUDA(cudaFuncSetAttribute(interior_backward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
   launchesPerApply_ = 2 * (long long)iLevels_.size() + 3 * (long long)cLevels_.size() +
                       (std::is_same<T, double>::value ? 0 : 2);
   bytesPerApply_ += 8.0 * 4 * S.n;
@@ -741,9 +810,10 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
   }
   const int* lvl = dLevelNodes_.as<int>();
   int* sync = dSync_.as<int>();
+  const RowBlock* iwork = dIWork_.as<RowBlock>();
   for (size_t l = 0; l < iLevels_.size(); ++l) {
-    interior_forward_kernel<T><<<iLevels_[l].second, 256, smemIF_[l], st>>>(
-        dNodes_.as<SNode<T>>(), lvl + iLevels_[l].first, dRows_.as<int>(), dRel_.as<int>(), dChild_.as<int>(), w,
+    interior_forward_chunks<T><<<iLevels_[l].second, 256, smemIF_[l], st>>>(
+        dNodes_.as<SNode<T>>(), iwork + iLevels_[l].first, dRel_.as<int>(), dChild_.as<int>(), w, dYi_.as<T>(),
         dWu_.as<T>());
     RSCHOL_LAUNCH_CHECK();
   }
@@ -762,8 +832,8 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
     RSCHOL_LAUNCH_CHECK();
   }
   for (int l = (int)iLevels_.size() - 1; l >= 0; --l) {
-    interior_backward_kernel<T><<<iLevels_[l].second, 256, smemIB_[l], st>>>(
-        dNodes_.as<SNode<T>>(), lvl + iLevels_[l].first, dRows_.as<int>(), w);
+    interior_backward_chunks<T><<<iLevels_[l].second, 256, smemIB_[l], st>>>(
+        dNodes_.as<SNode<T>>(), iwork + iLevels_[l].first, dRows_.as<int>(), sync, dIp_.as<T>(), dYi_.as<T>(), w);
     RSCHOL_LAUNCH_CHECK();
   }
   if (!std::is_same<T, double>::value) {

@@ -8,8 +8,10 @@
 // A_{rest,I} L_I^{-T} L_I^{-1} are stored explicitly), compressed nodes use
 // the (HODLR-expanded) dense L11 and the V U^T off-diagonal.
 //
-// Forward: interior levels bottom-up, one block per supernode, each
-// assembling its children's update vectors (extend-add, fixed order).
+// Forward: interior levels bottom-up, one thread block per (supernode,
+// 128-row chunk of L21): each assembles the children's update vectors
+// (extend-add, fixed order) for the supernode's columns and its chunk, solves
+// with L11 and forms its chunk of the update vector.
 // Compressed levels bottom-up: every compressed supernode is cut into
 // 64-row blocks and each block gets its own thread block, which adds the
 // fixed-order contribution list of its rows (interior-root update vectors,
@@ -18,7 +20,8 @@
 // inverted 64 x 64 diagonal block.  z = U^T y is reduced in fixed order by
 // the last row block to finish.  Backward mirrors this (s = V^T x_R by a
 // chunked pass, then row blocks in reverse order), then interior levels
-// top-down.  Thread blocks take their row block from a ticket counter, so a
+// top-down (chunk blocks form parts of L21^T x_R, the last one to finish
+// sums them in fixed order and solves with L11^T).  Thread blocks take their row block from a ticket counter, so a
 // block only ever waits on blocks that started before it; every wait is
 // bounded and reports through an error word instead of hanging.  No atomics
 // touch the numbers: results are bitwise reproducible.
@@ -39,16 +42,18 @@ struct SNode {
   const T* L;       // interior: [L11; L21] panel; compressed: L11 (HODLR expanded)
   const T* V;       // compressed: m x r
   const T* U;       // compressed: n x r
-  const T* Dinv;    // compressed: nb inverted 64 x 64 diagonal blocks of L11
+  const T* Dinv;    // inverted 64 x 64 diagonal blocks of L11 (interior: last one h x h)
   int ld, n, m, r, c0;
   int childBegin, childEnd;   // interior: children (range in the child list)
-  int nb, nch;                // compressed: row blocks of L11, 128-row chunks of V
-  int syncOff;                // compressed: nb ready flags, then 3 completion counters
+  int nb, nch;                // compressed: row blocks of L11; both: 128-row chunks of V / L21
+  int syncOff;                // compressed: nb ready flags, then 3 completion counters;
+                              // interior: 1 completion counter
   long long rowsOff;          // rows of this node in the row arena
   long long wuOff;            // interior: update vector; compressed: z and s (r values each)
   long long relOff;           // interior: target index in the parent front of each row
   long long cOff;             // compressed: first of its n+1 contribution-list offsets
-  long long zpOff, spOff;     // compressed: partials of z (nb x r) and s (nch x r)
+  long long zpOff, spOff;     // compressed: partials of z (nb x r) and s (nch x r);
+                              // interior (zpOff): partials of L21^T x_R (nch x n)
 };
 
 template <class T>
@@ -64,7 +69,7 @@ struct SPull {       // contribution source of a compressed supernode (plan time
   int kind;          // 0: interior root update vector, 1: compressed V z
 };
 
-struct RowBlock {    // one thread block's work in a compressed level
+struct RowBlock {    // one thread block's work: (supernode, row block or chunk)
   int node, b;
 };
 
@@ -72,7 +77,8 @@ template <class T>
 struct DinvTask {    // invert one lower-triangular diagonal block (h x h, h <= 64)
   const T* L;
   int ld, h;
-  T* D;              // 64 x 64 row-major, zero outside the h x h lower triangle
+  int pad;           // D is pad x pad (64 for compressed supernodes, h for interior ones)
+  T* D;              // row-major, ld pad, zero outside the h x h lower triangle
 };
 
 template <class T>
@@ -95,13 +101,14 @@ class SolveEngine {
   FactorEngine<T>& F_;
   std::vector<SNode<T>> nodes_;
   DevBuf dNodes_, dRows_, dRel_, dChild_, dWu_, dW_, dLevelNodes_, dCStart_, dCEnt_;
-  DevBuf dDinv_, dDinvTasks_, dZp_, dSp_, dSync_, dTickF_, dTickB_;
+  DevBuf dDinv_, dDinvTasks_, dZp_, dSp_, dIp_, dYi_, dSync_, dTickF_, dTickB_, dIWork_;
   int nDinv_ = 0;
   int syncInts_ = 0;
   std::vector<long long> tickOff_;   // per compressed level: first ticket entry
   std::vector<int> cBlocks_;         // per compressed level: row blocks
   std::vector<int> cMaxCh_;          // per compressed level: most V chunks of a node
-  std::vector<std::pair<long long, int>> iLevels_, cLevels_;  // (offset, count) into level node list
+  std::vector<std::pair<long long, int>> iLevels_;  // (offset, count) into the interior work list
+  std::vector<std::pair<long long, int>> cLevels_;  // (offset, count) into the level node list
   std::vector<size_t> smemIF_, smemIB_;
   long long launchesPerApply_ = 0;
   double bytesPerApply_ = 0;
