@@ -276,7 +276,7 @@ template <class T>
 __global__ void __launch_bounds__(256) compressed_forward_blocks(const SNode<T>* __restrict__ nodes,
                                                                  const RowBlock* __restrict__ tickets,
                                                                  const long long* __restrict__ cstart,
-                                                                 const CEntry<T>* __restrict__ ent,
+                                                                 const T* const* __restrict__ ent,
                                                                  int* __restrict__ sync, int levelSync,
                                                                  T* __restrict__ zpart, T* __restrict__ w,
                                                                  T* __restrict__ wu) {
@@ -295,23 +295,14 @@ __global__ void __launch_bounds__(256) compressed_forward_blocks(const SNode<T>*
   const int n = nd.n, i0 = tk.b * SOLVE_RB, h = min(SOLVE_RB, n - i0);
   T* wn = w + nd.c0;
   int* flags = sync + nd.syncOff;
-  // 1. right-hand side rows with their contribution lists (warp per row)
+  // 1. right-hand side rows with their contribution lists (warp per row,
+  // lanes over the row's contributions)
   const long long* cs = cstart + nd.cOff;
   for (int rr = 0; rr < 8; ++rr) {
     const int i = warp * 8 + rr;
     T acc = T(0);
-    if (i < h) {
-      for (long long e = cs[i0 + i]; e < cs[i0 + i + 1]; ++e) {
-        const CEntry<T> E = ent[e];
-        if (E.r == 0) {
-          if (lane == 0) acc += *E.v;
-        } else {
-          T s = T(0);
-          for (int k = lane; k < E.r; k += 32) s += E.v[k] * E.z[k];
-          acc -= s;
-        }
-      }
-    }
+    if (i < h)
+      for (long long e = cs[i0 + i] + lane; e < cs[i0 + i + 1]; e += 32) acc += *ent[e];
     acc = warp_sum(acc);
     if (lane == 0) fb[i] = (i < h) ? wn[i0 + i] + acc : T(0);
   }
@@ -379,6 +370,25 @@ __global__ void __launch_bounds__(256) compressed_forward_blocks(const SNode<T>*
     }
     for (int b = threadIdx.x; b < nb; b += blockDim.x) flags[b] = 0;
     if (threadIdx.x == 0) flags[nb] = 0;
+  }
+}
+
+// u = -V z of every compressed supernode of a level (its contribution to the
+// right-hand sides of its ancestors), a warp per row.
+template <class T>
+__global__ void __launch_bounds__(256) compressed_vz_kernel(const SNode<T>* __restrict__ nodes,
+                                                            const int* __restrict__ lvl, T* __restrict__ wu) {
+  const SNode<T>& nd = nodes[lvl[blockIdx.y]];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int r = nd.r;
+  const T* z = wu + nd.wuOff;
+  T* u = wu + nd.wuOff + 2 * r;
+  for (int a = blockIdx.x * 8 + warp; a < nd.m; a += gridDim.x * 8) {
+    const T* v = nd.V + (size_t)a * r;
+    T s = T(0);
+    for (int k = lane; k < r; k += 32) s += v[k] * z[k];
+    s = warp_sum(s);
+    if (lane == 0) u[a] = -s;
   }
 }
 
@@ -606,7 +616,7 @@ void SolveEngine<T>::plan() {
       sn.V = sn.r ? F_.vu() + F_.vOff[s] : nullptr;
       sn.U = sn.r ? F_.vu() + F_.uOff[s] : nullptr;
       sn.wuOff = wuCur;
-      wuCur += 2LL * sn.r;
+      wuCur += 2LL * sn.r + sn.m;   // z | s | u = -V z
       sn.nb = (nd.n + SOLVE_RB - 1) / SOLVE_RB;
       sn.nch = (sn.r > 0 && sn.m > 0) ? (sn.m + 127) / 128 : 0;
       sn.syncOff = syncCur;
@@ -686,6 +696,7 @@ void SolveEngine<T>::plan() {
   tickOff_.clear();
   cBlocks_.clear();
   cMaxCh_.clear();
+  cVzGrid_.clear();
   for (auto& lv : F_.compressedLevels) {
     cLevels_.push_back({(long long)lvlNodes.size(), (int)lv.size()});
     lvlNodes.insert(lvlNodes.end(), lv.begin(), lv.end());
@@ -704,6 +715,9 @@ void SolveEngine<T>::plan() {
         }
     cBlocks_.push_back(blocks);
     cMaxCh_.push_back(maxCh);
+    int maxM = 1;
+    for (int j : lv) maxM = std::max(maxM, nodes_[j].m);
+    cVzGrid_.push_back(std::min(64, (maxM + 7) / 8));
   }
   cudaStream_t st = F_.stream;
   auto up = [&](DevBuf& b, const void* src, size_t bytes) {
@@ -722,7 +736,7 @@ void SolveEngine<T>::plan() {
   // per-row contribution lists of the compressed supernodes (in source order)
   {
     std::vector<long long> cstart;
-    std::vector<CEntry<T>> ents;
+    std::vector<const T*> ents;
     const T* wuBase = dWu_.as<T>();
     for (int s = 0; s < nn; ++s) {
       const Node& nd = S.nodes[s];
@@ -739,21 +753,14 @@ void SolveEngine<T>::plan() {
       for (const SPull& P : pl[s]) {
         const SNode<T>& src = nodes_[P.src];
         for (int a = P.a0; a < P.a1; ++a) {
-          CEntry<T> e{};
-          if (P.kind == 0) {
-            e.v = wuBase + src.wuOff + a;
-            e.r = 0;
-          } else {
-            e.v = src.V + (size_t)a * src.r;
-            e.z = wuBase + src.wuOff;
-            e.r = src.r;
-          }
+          // interior root: its update vector; compressed: u = -V z
+          const T* e = (P.kind == 0) ? wuBase + src.wuOff + a : wuBase + src.wuOff + 2 * src.r + a;
           ents[base + fill[S.nodes[P.src].rows[a] - nd.c0]++] = e;
         }
       }
     }
     up(dCStart_, cstart.data(), cstart.size() * sizeof(long long));
-    up(dCEnt_, ents.data(), ents.size() * sizeof(CEntry<T>));
+    up(dCEnt_, ents.data(), ents.size() * sizeof(const T*));
   }
   up(dNodes_, nodes_.data(), nodes_.size() * sizeof(SNode<T>));
   up(dRows_, rowsAll.data(), rowsAll.size() * sizeof(int));
@@ -772,7 +779,7 @@ void SolveEngine<T>::plan() {
   const int maxSmem = 200 * 1024;
   RSCHOL_CUDA(cudaFuncSetAttribute(interior_forward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
   RSCHOL_CUDA(cudaFuncSetAttribute(interior_backward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
-  launchesPerApply_ = 2 * (long long)iLevels_.size() + 3 * (long long)cLevels_.size() +
+  launchesPerApply_ = 2 * (long long)iLevels_.size() + 4 * (long long)cLevels_.size() - (cLevels_.empty() ? 0 : 1) +
                       (std::is_same<T, double>::value ? 0 : 2);
   bytesPerApply_ += 8.0 * 4 * S.n;
 }
@@ -820,8 +827,13 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
   for (size_t l = 0; l < cLevels_.size(); ++l) {
     compressed_forward_blocks<T><<<cBlocks_[l], 256, 0, st>>>(
         dNodes_.as<SNode<T>>(), dTickF_.as<RowBlock>() + tickOff_[l], dCStart_.as<long long>(),
-        dCEnt_.as<CEntry<T>>(), sync, 1 + 4 * (int)l, dZp_.as<T>(), w, dWu_.as<T>());
+        dCEnt_.as<const T*>(), sync, 1 + 4 * (int)l, dZp_.as<T>(), w, dWu_.as<T>());
     RSCHOL_LAUNCH_CHECK();
+    if (l + 1 < cLevels_.size()) {   // the top level's u feeds no one
+      compressed_vz_kernel<T><<<dim3(cVzGrid_[l], cLevels_[l].second), 256, 0, st>>>(
+          dNodes_.as<SNode<T>>(), lvl + cLevels_[l].first, dWu_.as<T>());
+      RSCHOL_LAUNCH_CHECK();
+    }
   }
   for (int l = (int)cLevels_.size() - 1; l >= 0; --l) {
     compressed_vtx_kernel<T><<<dim3(cMaxCh_[l], cLevels_[l].second), 256, 0, st>>>(

@@ -15,7 +15,8 @@
 // Compressed levels bottom-up: every compressed supernode is cut into
 // 64-row blocks and each block gets its own thread block, which adds the
 // fixed-order contribution list of its rows (interior-root update vectors,
-// -V_c z_c of compressed descendants), accumulates L[b, k] y_k of the
+// u_c = -V_c z_c of compressed descendants, formed by a launch after each
+// level), accumulates L[b, k] y_k of the
 // earlier row blocks as their ready flags are raised, and multiplies by the
 // inverted 64 x 64 diagonal block.  z = U^T y is reduced in fixed order by
 // the last row block to finish.  Backward mirrors this (s = V^T x_R by a
@@ -49,18 +50,11 @@ struct SNode {
   int syncOff;                // compressed: nb ready flags, then 3 completion counters;
                               // interior: 1 completion counter
   long long rowsOff;          // rows of this node in the row arena
-  long long wuOff;            // interior: update vector; compressed: z and s (r values each)
+  long long wuOff;            // interior: update vector; compressed: z (r), s (r), u = -V z (m)
   long long relOff;           // interior: target index in the parent front of each row
   long long cOff;             // compressed: first of its n+1 contribution-list offsets
   long long zpOff, spOff;     // compressed: partials of z (nb x r) and s (nch x r);
                               // interior (zpOff): partials of L21^T x_R (nch x n)
-};
-
-template <class T>
-struct CEntry {      // one contribution to a row of a compressed supernode's right-hand side
-  const T* v;        // r == 0: the value to add; r > 0: a row of V (r entries)
-  const T* z;        // r > 0: z = U^T y of the contributing supernode
-  int r;
 };
 
 struct SPull {       // contribution source of a compressed supernode (plan time)
@@ -107,6 +101,7 @@ class SolveEngine {
   std::vector<long long> tickOff_;   // per compressed level: first ticket entry
   std::vector<int> cBlocks_;         // per compressed level: row blocks
   std::vector<int> cMaxCh_;          // per compressed level: most V chunks of a node
+  std::vector<int> cVzGrid_;         // per compressed level: row blocks of the u = -V z launch
   std::vector<std::pair<long long, int>> iLevels_;  // (offset, count) into the interior work list
   std::vector<std::pair<long long, int>> cLevels_;  // (offset, count) into the level node list
   std::vector<size_t> smemIF_, smemIB_;
