@@ -180,27 +180,23 @@ __global__ void __launch_bounds__(256) trsm_kernel(const TrsmTask<T>* __restrict
 }
 
 template <class T>
-__global__ void __launch_bounds__(256) extadd_kernel(const ExtAddTarget<T>* __restrict__ tg, int nT,
+__global__ void __launch_bounds__(256) extadd_kernel(const ExtAddRow<T>* __restrict__ rows, int nRows,
+                                                     const ExtAddSeg* __restrict__ segs,
                                                      const ExtAddSource<T>* __restrict__ src) {
-  int lo = 0, hi = nT - 1;
-  const int b = blockIdx.x;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (tg[mid].colBase <= b) lo = mid;
-    else hi = mid - 1;
-  }
-  const ExtAddTarget<T> t = tg[lo];
-  const int col = b - t.colBase;
-  for (int s = t.srcBegin; s < t.srcEnd; ++s) {
-    const ExtAddSource<T> S = src[s];
-    const int sb = S.colInv[col];
-    if (sb < 0) continue;   // uniform across the block
-    const int a0 = S.lowerOnly ? sb : 0;
-    for (int a = a0 + threadIdx.x; a < S.nrows; a += blockDim.x) {
-      T* dst = t.F + (size_t)S.rowRel[a] * t.ld + col;
-      *dst = fma(S.sign, S.D[(size_t)a * S.ld + sb], *dst);
+  const int lane = threadIdx.x & 31;
+  const int rw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (rw >= nRows) return;
+  const ExtAddRow<T> R = rows[rw];
+  for (int g = R.segBegin; g < R.segEnd; ++g) {
+    const ExtAddSeg sg = segs[g];
+    const ExtAddSource<T>& S = src[sg.src];
+    const T* drow = S.D + (size_t)sg.a * S.ld;
+    const int b1 = min(S.b1, sg.a + 1);
+    for (int b = S.b0 + lane; b < b1; b += 32) {
+      T* dst = R.Frow + S.rowRel[b];
+      *dst = fma(S.sign, drow[b], *dst);
     }
-    __syncthreads();   // the next source may hit the same target rows
+    __syncwarp();   // the next source may hit the same target entries
   }
 }
 
@@ -529,9 +525,10 @@ template <class T> void launch_trsm(const TrsmTask<T>* d, int n, int chunks, cud
   RSCHOL_LAUNCH_CHECK();
 }
 template <class T>
-void launch_extadd(const ExtAddTarget<T>* tg, int nT, const ExtAddSource<T>* src, int cols, cudaStream_t s) {
-  if (nT <= 0 || cols <= 0) return;
-  extadd_kernel<T><<<cols, 128, 0, s>>>(tg, nT, src);
+void launch_extadd(const ExtAddRow<T>* rows, int nRows, const ExtAddSeg* segs, const ExtAddSource<T>* src,
+                   cudaStream_t s) {
+  if (nRows <= 0) return;
+  extadd_kernel<T><<<(nRows + 7) / 8, 256, 0, s>>>(rows, nRows, segs, src);
   RSCHOL_LAUNCH_CHECK();
 }
 template <class T>
@@ -594,7 +591,8 @@ template <class T> void launch_box_muller(const uint32_t* raw, long long count, 
   template void launch_gemm<T>(const GemmTask<T>*, int, int, cudaStream_t);                              \
   template void launch_potrf<T>(const PotrfTask<T>*, int, int*, cudaStream_t);                           \
   template void launch_trsm<T>(const TrsmTask<T>*, int, int, cudaStream_t);                              \
-  template void launch_extadd<T>(const ExtAddTarget<T>*, int, const ExtAddSource<T>*, int, cudaStream_t); \
+  template void launch_extadd<T>(const ExtAddRow<T>*, int, const ExtAddSeg*, const ExtAddSource<T>*,      \
+                                 cudaStream_t);                                                          \
   template void launch_scatter<T>(const double*, const long long*, const long long*, long long, T*,      \
                                   cudaStream_t);                                                         \
   template int launch_householder_qr<T>(const QrTask<T>*, int, int, int, cudaStream_t);                  \

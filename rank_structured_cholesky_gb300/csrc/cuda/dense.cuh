@@ -47,32 +47,36 @@ struct TrsmTask {
   int chunkBase;  // first 64-row chunk of this task in the launch
 };
 
-// Extend-add "pull": each target column sums the contributions of its
-// sources in a fixed order (deterministic, no atomics).
+// Extend-add "pull" by target row: a warp owns one target row and adds the
+// rows of its sources in a fixed order (deterministic, no atomics).  Source
+// row a, columns b in [b0, min(b1, a + 1)) (the lower part of a symmetric
+// update block), lands on target row rowRel[a], columns rowRel[b]; reads of
+// the source row and writes of the target row are both contiguous.
 template <class T>
 struct ExtAddSource {
   const T* D;          // source block (row-major)
-  const int* rowRel;   // target row of each source row
-  const int* colInv;   // per target column: source column or -1
-  int ld, nrows;
-  int lowerOnly;       // source rows a < b are not valid
+  const int* rowRel;   // target index (row or column) of each source row / column
+  int ld;
+  int b0, b1;          // source columns that land in the target's columns
   T sign;
 };
 
+struct ExtAddSeg {     // one source row feeding a target row
+  int src, a;
+};
+
 template <class T>
-struct ExtAddTarget {
-  T* F;
-  int ld, ncols;
-  int srcBegin, srcEnd;
-  int colBase;         // first global column of this target in the launch
+struct ExtAddRow {
+  T* Frow;             // target row
+  int segBegin, segEnd;
 };
 
 template <class T> void launch_gemm(const GemmTask<T>* dTasks, int nTasks, int totalTiles, cudaStream_t s);
 template <class T> void launch_potrf(const PotrfTask<T>* dTasks, int nTasks, int* dFlag, cudaStream_t s);
 template <class T> void launch_trsm(const TrsmTask<T>* dTasks, int nTasks, int totalChunks, cudaStream_t s);
 template <class T>
-void launch_extadd(const ExtAddTarget<T>* dTargets, int nTargets, const ExtAddSource<T>* dSources,
-                   int totalCols, cudaStream_t s);
+void launch_extadd(const ExtAddRow<T>* dRows, int nRows, const ExtAddSeg* dSegs, const ExtAddSource<T>* dSources,
+                   cudaStream_t s);
 template <class T>
 void launch_scatter(const double* Avals, const long long* srcIdx, const long long* dstIdx, long long count,
                     T* dst, cudaStream_t s);

@@ -162,6 +162,33 @@ void FactorEngine<T>::emit_trsm(const std::vector<TrsmJob<T>>& jobs) {
 }
 
 template <class T>
+void FactorEngine<T>::emit_extadd(const std::vector<EaTarget>& tgs) {
+  // bucket every source row by its target row; sources keep their order
+  const long long first = (long long)eaR_.size();
+  for (const EaTarget& t : tgs) {
+    std::vector<std::vector<ExtAddSeg>> bucket(t.rows);
+    for (const EaSrc& es : t.src) {
+      const int sidx = (int)eaS_.size();
+      ExtAddSource<T> src = es.s;
+      src.rowRel = reinterpret_cast<const int*>(es.relOff);   // rebased at upload
+      eaS_.push_back(src);
+      for (int a = es.aLo; a < es.aHi; ++a) bucket[ints_[es.relOff + a]].push_back(ExtAddSeg{sidx, a});
+    }
+    for (int row = 0; row < t.rows; ++row) {
+      if (bucket[row].empty()) continue;
+      ExtAddRow<T> R{};
+      R.Frow = t.F + (size_t)row * t.ld;
+      R.segBegin = (int)eaSeg_.size();
+      eaSeg_.insert(eaSeg_.end(), bucket[row].begin(), bucket[row].end());
+      R.segEnd = (int)eaSeg_.size();
+      eaR_.push_back(R);
+    }
+  }
+  const int count = (int)((long long)eaR_.size() - first);
+  if (count > 0) steps_.push_back(Step{ST_EXTADD, first, count, (count + 7) / 8});
+}
+
+template <class T>
 void FactorEngine<T>::emit_rf(const std::vector<RFJob<T>>& jobs) {
   if (jobs.empty()) return;
   std::vector<GemmTask<T>> gb;
@@ -230,7 +257,8 @@ void FactorEngine<T>::plan() {
   gemm_.clear();
   potrf_.clear();
   trsm_.clear();
-  eaT_.clear();
+  eaR_.clear();
+  eaSeg_.clear();
   eaS_.clear();
   qr_.clear();
   ident_.clear();
@@ -400,50 +428,37 @@ void FactorEngine<T>::plan() {
   // ---- interior levels: extend-add of the children's update blocks, then
   // the blocked partial Cholesky of every front (L panel + update block).
   for (auto& lv : interiorLevels) {
-    std::vector<ExtAddTarget<T>> tgs;
-    int cols = 0;
+    std::vector<EaTarget> tgs;
     for (int p : lv) {
       const Node& pn = S.nodes[p];
       if (S.children[p].empty()) continue;
-      ExtAddTarget<T> t{};
+      EaTarget t;
       t.F = I0 + frontOff[p];
       t.ld = ld[p];
-      t.ncols = ld[p];
-      t.srcBegin = (int)eaS_.size();
-      t.colBase = cols;
+      t.rows = ld[p];
       for (int a = 0; a < pn.m(); ++a) pos[pn.rows[a]] = a;
       for (int c : S.children[p]) {
         const Node& cn = S.nodes[c];
         if (cn.m() == 0) continue;
-        ExtAddSource<T> src{};
-        src.D = I0 + frontOff[c] + (long long)cn.n * ld[c] + cn.n;
-        src.ld = ld[c];
-        src.nrows = cn.m();
-        src.lowerOnly = 1;
-        src.sign = T(1);
-        size_t ro = ints_.size();
+        EaSrc es{};
+        es.s.D = I0 + frontOff[c] + (long long)cn.n * ld[c] + cn.n;
+        es.s.ld = ld[c];
+        es.s.b0 = 0;
+        es.s.b1 = cn.m();
+        es.s.sign = T(1);
+        es.relOff = ints_.size();
         for (int a = 0; a < cn.m(); ++a) {
           int g = cn.rows[a];
           ints_.push_back(g <= pn.c1 ? g - pn.c0 : pn.n + pos[g]);
         }
-        size_t co = ints_.size();
-        ints_.resize(co + ld[p], -1);
-        for (int b = 0; b < cn.m(); ++b) ints_[co + ints_[ro + b]] = b;
-        src.rowRel = reinterpret_cast<const int*>(ro);
-        src.colInv = reinterpret_cast<const int*>(co);
-        eaS_.push_back(src);
+        es.aLo = 0;
+        es.aHi = cn.m();
+        t.src.push_back(es);
       }
       for (int a = 0; a < pn.m(); ++a) pos[pn.rows[a]] = -1;
-      t.srcEnd = (int)eaS_.size();
-      if (t.srcEnd > t.srcBegin) {
-        tgs.push_back(t);
-        cols += t.ncols;
-      }
+      if (!t.src.empty()) tgs.push_back(std::move(t));
     }
-    if (!tgs.empty()) {
-      steps_.push_back(Step{ST_EXTADD, (long long)eaT_.size(), (int)tgs.size(), cols});
-      eaT_.insert(eaT_.end(), tgs.begin(), tgs.end());
-    }
+    emit_extadd(tgs);
     std::vector<CholJob<T>> jobs;
     for (int d : lv) {
       const Node& nd = S.nodes[d];
@@ -482,66 +497,50 @@ void FactorEngine<T>::plan() {
       }
     flush_gemm(gb, tiles);
     // (b) extend-add into the dense fronts [S11; S21]
-    std::vector<ExtAddTarget<T>> tgs;
-    int cols = 0;
+    std::vector<EaTarget> tgs;
     for (int j : lv) {
       const Node& nd = S.nodes[j];
-      ExtAddTarget<T> t{};
+      EaTarget t;
       t.F = C0 + frontOff[j];
       t.ld = ld[j];
-      t.ncols = nd.n;
-      t.srcBegin = (int)eaS_.size();
-      t.colBase = cols;
+      t.rows = nd.n + nd.m();
       for (int a = 0; a < nd.m(); ++a) pos[nd.rows[a]] = a;
       auto rel = [&](int g) { return g <= nd.c1 ? g - nd.c0 : nd.n + pos[g]; };
       for (const Pair& p : rootsOf[j]) {
         const Node& dn = S.nodes[p.src];
         const int sq = dn.interStart[p.q], sq1 = dn.interStart[p.q + 1];
-        ExtAddSource<T> src{};
-        src.D = I0 + frontOff[p.src] + (long long)dn.n * ld[p.src] + dn.n;
-        src.ld = ld[p.src];
-        src.nrows = dn.m();
-        src.lowerOnly = 1;
-        src.sign = T(1);
-        size_t ro = ints_.size();
+        EaSrc es{};
+        es.s.D = I0 + frontOff[p.src] + (long long)dn.n * ld[p.src] + dn.n;
+        es.s.ld = ld[p.src];
+        es.s.b0 = sq;
+        es.s.b1 = sq1;
+        es.s.sign = T(1);
+        es.relOff = ints_.size();
         for (int a = 0; a < dn.m(); ++a) ints_.push_back(a >= sq ? rel(dn.rows[a]) : 0);
-        size_t co = ints_.size();
-        ints_.resize(co + nd.n, -1);
-        for (int b = sq; b < sq1; ++b) ints_[co + dn.rows[b] - nd.c0] = b;
-        src.rowRel = reinterpret_cast<const int*>(ro);
-        src.colInv = reinterpret_cast<const int*>(co);
-        eaS_.push_back(src);
+        es.aLo = sq;
+        es.aHi = dn.m();
+        t.src.push_back(es);
       }
       for (size_t k = 0; k < compDesc[j].size(); ++k) {
         const Pair& p = compDesc[j][k];
         const Node& cn = S.nodes[p.src];
         const int s0 = cn.interStart[p.q], k1 = cn.interStart[p.q + 1] - s0, r = rank[p.src];
-        ExtAddSource<T> src{};
-        src.D = T0 + contribOff[j][k] + (size_t)r * k1;
-        src.ld = k1;
-        src.nrows = cn.m() - s0;
-        src.lowerOnly = 0;
-        src.sign = T(-1);
-        size_t ro = ints_.size();
+        EaSrc es{};
+        es.s.D = T0 + contribOff[j][k] + (size_t)r * k1;
+        es.s.ld = k1;
+        es.s.b0 = 0;
+        es.s.b1 = k1;
+        es.s.sign = T(-1);
+        es.relOff = ints_.size();
         for (int a = s0; a < cn.m(); ++a) ints_.push_back(rel(cn.rows[a]));
-        size_t co = ints_.size();
-        ints_.resize(co + nd.n, -1);
-        for (int b = 0; b < k1; ++b) ints_[co + cn.rows[s0 + b] - nd.c0] = b;
-        src.rowRel = reinterpret_cast<const int*>(ro);
-        src.colInv = reinterpret_cast<const int*>(co);
-        eaS_.push_back(src);
+        es.aLo = 0;
+        es.aHi = cn.m() - s0;
+        t.src.push_back(es);
       }
       for (int a = 0; a < nd.m(); ++a) pos[nd.rows[a]] = -1;
-      t.srcEnd = (int)eaS_.size();
-      if (t.srcEnd > t.srcBegin) {
-        tgs.push_back(t);
-        cols += t.ncols;
-      }
+      if (!t.src.empty()) tgs.push_back(std::move(t));
     }
-    if (!tgs.empty()) {
-      steps_.push_back(Step{ST_EXTADD, (long long)eaT_.size(), (int)tgs.size(), cols});
-      eaT_.insert(eaT_.end(), tgs.begin(), tgs.end());
-    }
+    emit_extadd(tgs);
 
     // (c) diagonal factor (+ L21 for single-block diagonals)
     auto hjob = [&](int j, int q, bool identityAllowed) {
@@ -695,14 +694,12 @@ void FactorEngine<T>::plan() {
     if (bytes) RSCHOL_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, stream));
   };
   up(dInts_, ints_.data(), ints_.size() * sizeof(int));
-  for (auto& s : eaS_) {
-    s.rowRel = dInts_.as<int>() + reinterpret_cast<size_t>(s.rowRel);
-    s.colInv = dInts_.as<int>() + reinterpret_cast<size_t>(s.colInv);
-  }
+  for (auto& s : eaS_) s.rowRel = dInts_.as<int>() + reinterpret_cast<size_t>(s.rowRel);
   up(dGemm_, gemm_.data(), gemm_.size() * sizeof(GemmTask<T>));
   up(dPotrf_, potrf_.data(), potrf_.size() * sizeof(PotrfTask<T>));
   up(dTrsm_, trsm_.data(), trsm_.size() * sizeof(TrsmTask<T>));
-  up(dEaT_, eaT_.data(), eaT_.size() * sizeof(ExtAddTarget<T>));
+  up(dEaR_, eaR_.data(), eaR_.size() * sizeof(ExtAddRow<T>));
+  up(dEaSeg_, eaSeg_.data(), eaSeg_.size() * sizeof(ExtAddSeg));
   up(dEaS_, eaS_.data(), eaS_.size() * sizeof(ExtAddSource<T>));
   up(dQr_, qr_.data(), qr_.size() * sizeof(QrTask<T>));
   up(dIdent_, ident_.data(), ident_.size() * sizeof(IdentTask<T>));
@@ -732,8 +729,8 @@ int FactorEngine<T>::run() {
       case ST_POTRF: launch_potrf<T>(dPotrf_.as<PotrfTask<T>>() + st.off, st.count, dFlag.as<int>(), stream); break;
       case ST_TRSM: launch_trsm<T>(dTrsm_.as<TrsmTask<T>>() + st.off, st.count, st.grid, stream); break;
       case ST_EXTADD:
-        launch_extadd<T>(dEaT_.as<ExtAddTarget<T>>() + st.off, st.count, dEaS_.as<ExtAddSource<T>>(), st.grid,
-                         stream);
+        launch_extadd<T>(dEaR_.as<ExtAddRow<T>>() + st.off, st.count, dEaSeg_.as<ExtAddSeg>(),
+                         dEaS_.as<ExtAddSource<T>>(), stream);
         break;
       case ST_QR:
         launches += launch_householder_qr<T>(dQr_.as<QrTask<T>>() + st.off, st.count, st.aux, st.grid, stream) - 1;

@@ -122,6 +122,17 @@ class FactorEngine {
   void emit_chol(const std::vector<CholJob<T>>& jobs);
   void emit_trsm(const std::vector<TrsmJob<T>>& jobs);
   void emit_rf(const std::vector<RFJob<T>>& jobs);
+  struct EaSrc {            // plan-time source of an extend-add
+    ExtAddSource<T> s;      // rowRel filled from relOff
+    size_t relOff;          // target index of each source row, in ints_
+    int aLo, aHi;           // source rows that feed the target
+  };
+  struct EaTarget {
+    T* F;
+    int ld, rows;
+    std::vector<EaSrc> src;
+  };
+  void emit_extadd(const std::vector<EaTarget>& tgs);
   void push_gemm(const GemmTask<T>& t, int& tiles, std::vector<GemmTask<T>>& batch);
   void flush_gemm(std::vector<GemmTask<T>>& batch, int tiles);
   void gemm1(const GemmTask<T>& t);   // a single-task GEMM step
@@ -130,14 +141,15 @@ class FactorEngine {
   std::vector<GemmTask<T>> gemm_;
   std::vector<PotrfTask<T>> potrf_;
   std::vector<TrsmTask<T>> trsm_;
-  std::vector<ExtAddTarget<T>> eaT_;
+  std::vector<ExtAddRow<T>> eaR_;
+  std::vector<ExtAddSeg> eaSeg_;
   std::vector<ExtAddSource<T>> eaS_;
   std::vector<QrTask<T>> qr_;
   std::vector<IdentTask<T>> ident_;
   std::vector<int> ints_;
   std::vector<long long> scatSrc_, scatDst_;
   std::vector<int> scatIsInterior_;
-  DevBuf dGemm_, dPotrf_, dTrsm_, dEaT_, dEaS_, dQr_, dIdent_, dInts_, dScatSrc_, dScatDst_;
+  DevBuf dGemm_, dPotrf_, dTrsm_, dEaR_, dEaSeg_, dEaS_, dQr_, dIdent_, dInts_, dScatSrc_, dScatDst_;
   DevBuf dScatSrcC_, dScatDstC_;
   long long nScatI_ = 0, nScatC_ = 0;
   bool planned_ = false;
