@@ -100,45 +100,70 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_kernel(const GemmTask<T>* _
 
 template <class T>
 __global__ void __launch_bounds__(256) potrf_kernel(const PotrfTask<T>* __restrict__ tasks, int* flag) {
+  // Right-looking Cholesky of one <= 64 x 64 tile.  Thread (i = tid / 4,
+  // g = tid % 4) keeps row i, columns g, g + 4, ..., in registers; column j
+  // is broadcast through a double-buffered shared array.
   const PotrfTask<T> t = tasks[blockIdx.x];
-  __shared__ T a[64][65];
+  __shared__ T col[2][64];
   __shared__ int bad;
-  const int n = t.n, tid = threadIdx.x;
-  for (int idx = tid; idx < n * n; idx += blockDim.x) {
-    int i = idx / n, j = idx - i * n;
-    a[i][j] = (j <= i) ? t.A[(size_t)i * t.ld + j] : T(0);
+  const int n = t.n, tid = threadIdx.x, i = tid >> 2, g = tid & 3;
+  T v[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int k = g + 4 * q;
+    v[q] = (i < n && k <= i) ? t.A[(size_t)i * t.ld + k] : T(0);
   }
   if (tid == 0) bad = 0;
   __syncthreads();
-  for (int j = 0; j < n; ++j) {
-    if (tid == 0) {
-      T d = a[j][j];
-      if (!(d > T(0))) {   // not positive definite (or NaN): keep going, report
-        bad = 1;
-        d = T(1);
+  // column j = 4 q0 + jj lives in slot q0 of the threads with g == jj
+  // (both loops unrolled so that every register index is static)
+#pragma unroll
+  for (int q0 = 0; q0 < 16; ++q0) {
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const int j = 4 * q0 + jj;
+      if (j < n) {
+        T* cj = col[j & 1];
+        if (g == jj && i == j) {
+          T d = v[q0];
+          if (!(d > T(0))) {   // not positive definite (or NaN): keep going, report
+            bad = 1;
+            d = T(1);
+          }
+          d = sqrt(d);
+          v[q0] = d;
+          cj[j] = d;
+        }
+        __syncthreads();
+        if (g == jj && i > j && i < n) {
+          const T x = v[q0] / cj[j];
+          v[q0] = x;
+          cj[i] = x;
+        }
+        __syncthreads();
+        if (i > j && i < n) {
+          const T ci = cj[i];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int k = g + 4 * q;
+            if (k > j && k <= i) v[q] -= ci * cj[k];
+          }
+        }
       }
-      a[j][j] = sqrt(d);
     }
-    __syncthreads();
-    const T djj = a[j][j];
-    for (int i = j + 1 + tid; i < n; i += blockDim.x) a[i][j] /= djj;
-    __syncthreads();
-    const int m = n - j - 1;
-    for (int idx = tid; idx < m * m; idx += blockDim.x) {
-      int ii = idx / m, kk = idx - ii * m;
-      if (kk <= ii) a[j + 1 + ii][j + 1 + kk] -= a[j + 1 + ii][j] * a[j + 1 + kk][j];
-    }
-    __syncthreads();
   }
-  for (int idx = tid; idx < n * n; idx += blockDim.x) {
-    int i = idx / n, j = idx - i * n;
-    if (j <= i) t.A[(size_t)i * t.ld + j] = a[i][j];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int k = g + 4 * q;
+    if (i < n && k <= i) t.A[(size_t)i * t.ld + k] = v[q];
   }
   if (tid == 0 && bad) atomicMin(flag, t.code);
 }
 
 template <class T>
 __global__ void __launch_bounds__(256) trsm_kernel(const TrsmTask<T>* __restrict__ tasks, int nTasks) {
+  // B (64-row chunk x w) := B L^{-T}: the block inverts its w x w tile
+  // (column c by thread c, forward substitution) and multiplies.
   int lo = 0, hi = nTasks - 1;
   const int b = blockIdx.x;
   while (lo < hi) {
@@ -152,30 +177,51 @@ __global__ void __launch_bounds__(256) trsm_kernel(const TrsmTask<T>* __restrict
   const int w = t.w, tid = threadIdx.x;
   extern __shared__ __align__(16) unsigned char trsm_smem[];
   T (*L)[65] = reinterpret_cast<T (*)[65]>(trsm_smem);
-  T (*X)[65] = reinterpret_cast<T (*)[65]>(trsm_smem + sizeof(T) * 64 * 65);
-  for (int idx = tid; idx < w * w; idx += blockDim.x) {
-    int i = idx / w, j = idx - i * w;
-    L[i][j] = (j <= i) ? t.L[(size_t)i * t.ldl + j] : T(0);
-  }
-  for (int idx = tid; idx < nr * w; idx += blockDim.x) {
-    int i = idx / w, j = idx - i * w;
-    X[i][j] = t.B[(size_t)(r0 + i) * t.ldb + j];
+  T (*Li)[65] = reinterpret_cast<T (*)[65]>(trsm_smem + sizeof(T) * 64 * 65);
+  T (*X)[65] = reinterpret_cast<T (*)[65]>(trsm_smem + 2 * sizeof(T) * 64 * 65);
+  for (int idx = tid; idx < 64 * 64; idx += blockDim.x) {
+    const int i = idx >> 6, j = idx & 63;
+    L[i][j] = (i < w && j <= i) ? t.L[(size_t)i * t.ldl + j] : T(0);
+    Li[i][j] = T(0);
+    X[i][j] = (i < nr && j < w) ? t.B[(size_t)(r0 + i) * t.ldb + j] : T(0);
   }
   __syncthreads();
-  for (int j = 0; j < w; ++j) {
-    const T d = L[j][j];
-    for (int i = tid; i < nr; i += blockDim.x) X[i][j] /= d;
-    __syncthreads();
-    const int rem = w - j - 1;
-    for (int idx = tid; idx < nr * rem; idx += blockDim.x) {
-      int i = idx / rem, k = j + 1 + (idx - i * rem);
-      X[i][k] -= X[i][j] * L[k][j];
+  if (tid < w) {
+    const int c = tid;
+    for (int r = c; r < w; ++r) {
+      T s = (r == c) ? T(1) : T(0);
+      for (int k = c; k < r; ++k) s -= L[r][k] * Li[k][c];
+      Li[r][c] = s / L[r][r];
     }
-    __syncthreads();
   }
-  for (int idx = tid; idx < nr * w; idx += blockDim.x) {
-    int i = idx / w, j = idx - i * w;
-    t.B[(size_t)(r0 + i) * t.ldb + j] = X[i][j];
+  __syncthreads();
+  // out[i][j] = sum_{k <= j} X[i][k] Li[j][k]; thread: rows ty + 16 a, columns tx + 16 c
+  const int tx = tid & 15, ty = tid >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[a][c] = T(0);
+  for (int k = 0; k < w; ++k) {
+    T xa[4], lb[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) xa[a] = X[ty + 16 * a][k];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) lb[c] = Li[tx + 16 * c][k];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[a][c] = fma(xa[a], lb[c], acc[a][c]);
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int i = ty + 16 * a;
+    if (i >= nr) continue;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int j = tx + 16 * c;
+      if (j < w) t.B[(size_t)(r0 + i) * t.ldb + j] = acc[a][c];
+    }
   }
 }
 
@@ -515,7 +561,7 @@ template <class T> void launch_potrf(const PotrfTask<T>* d, int n, int* flag, cu
 }
 template <class T> void launch_trsm(const TrsmTask<T>* d, int n, int chunks, cudaStream_t s) {
   if (n <= 0 || chunks <= 0) return;
-  const int smem = (int)(2 * sizeof(T) * 64 * 65);
+  const int smem = (int)(3 * sizeof(T) * 64 * 65);
   static bool configured = false;   // per instantiation
   if (!configured) {
     RSCHOL_CUDA(cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
