@@ -123,6 +123,13 @@ int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x
  *   - the first call on a device looks up the array's address
  *     (cudaGetSymbolAddress, with that device current); make that first call
  *     before any stream capture that would include this function. */
+/* Diagnostics (no reference counterpart): one tensor-core GEMM
+ * C = -1.25 op(A) op(B) + 0.5 C on random M x N x K operands (tA / tB:
+ * transposed storage, split: split-precision TF32, lower: lower-triangle
+ * tiles only) against a host FP64 product.  out[0]: largest error relative to
+ * sum_k |a_ik b_kj| (+ |beta c_ij|), out[1]: largest absolute error. */
+int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int split, int lower, double* out);
+
 #define RSCHOL_NOALLOC_MAX_N 2097152
 int rschol_precond_apply_device_noalloc(rschol_factor* f, const double* d_b, double* d_x, int nrhs);
 

@@ -588,6 +588,104 @@ int rschol_factor_stats(const rschol_factor* f, double* st) {
 
 }  // extern "C"
 
+// ---- diagnostics: the tensor-core GEMM against a host FP64 product -----------
+extern "C" int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int split, int lower, double* out) {
+  if (M <= 0 || N <= 0 || K < 0 || !out) return RSCHOL_E_BAD_INPUT;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return RSCHOL_E_NO_DEVICE;
+  try {
+    const int lda = tA ? M : K, ldb = tB ? K : N, ldc = N;
+    const size_t na = (size_t)M * K, nb = (size_t)K * N, nc = (size_t)M * N;
+    std::vector<float> A(std::max<size_t>(na, 1)), B(std::max<size_t>(nb, 1)), C(nc), C0(nc);
+    uint64_t st = 0x9E3779B97F4A7C15ull;
+    auto rnd = [&]() {
+      st = st * 6364136223846793005ull + 1442695040888963407ull;
+      return (float)((double)(st >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0);
+    };
+    for (auto& x : A) x = rnd();
+    for (auto& x : B) x = rnd();
+    for (auto& x : C0) x = rnd();
+    const float alpha = -1.25f, beta = 0.5f;
+    DevBuf dA, dB, dC, dT, dE;
+    dA.alloc(sizeof(float) * A.size());
+    dB.alloc(sizeof(float) * B.size());
+    dC.alloc(sizeof(float) * nc);
+    dT.alloc(sizeof(GemmTask<float>));
+    dE.alloc(sizeof(int));
+    RSCHOL_CUDA(cudaMemcpy(dA.p, A.data(), sizeof(float) * A.size(), cudaMemcpyHostToDevice));
+    RSCHOL_CUDA(cudaMemcpy(dB.p, B.data(), sizeof(float) * B.size(), cudaMemcpyHostToDevice));
+    RSCHOL_CUDA(cudaMemcpy(dC.p, C0.data(), sizeof(float) * nc, cudaMemcpyHostToDevice));
+    RSCHOL_CUDA(cudaMemset(dE.p, 0, sizeof(int)));
+    GemmTask<float> t{};
+    t.A = dA.as<float>();
+    t.B = dB.as<float>();
+    t.C = dC.as<float>();
+    t.M = M;
+    t.N = N;
+    t.K = K;
+    t.lda = lda;
+    t.ldb = ldb;
+    t.ldc = ldc;
+    t.tA = tA;
+    t.tB = tB;
+    t.lower = lower;
+    t.alpha = alpha;
+    t.beta = beta;
+    t.tilesN = (N + 63) / 64;
+    t.tileBase = 0;
+    t.split = split;
+    // K >= 1024 (and not lower): four K slices through the partial workspace
+    const int tilesPer = ((M + 127) / 128) * t.tilesN;
+    t.kSplit = 1;
+    t.kLen = K;
+    DevBuf dW, dIds, dBase;
+    if (K >= 1024 && !lower) {
+      t.kLen = ((K + 3) / 4 + 31) / 32 * 32;
+      t.kSplit = (K + t.kLen - 1) / t.kLen;
+      dW.alloc(sizeof(float) * (size_t)t.kSplit * tilesPer * 128 * 64);
+      t.ws = dW.as<float>();
+    }
+    RSCHOL_CUDA(cudaMemcpy(dT.p, &t, sizeof(t), cudaMemcpyHostToDevice));
+    launch_gemm_tc(dT.as<GemmTask<float>>(), 1, tilesPer * t.kSplit, dE.as<int>(), 0);
+    if (t.kSplit > 1) {
+      const int id = 0;
+      const long long base[2] = {0, (long long)M * N};
+      dIds.alloc(sizeof(int));
+      dBase.alloc(sizeof(base));
+      RSCHOL_CUDA(cudaMemcpy(dIds.p, &id, sizeof(int), cudaMemcpyHostToDevice));
+      RSCHOL_CUDA(cudaMemcpy(dBase.p, base, sizeof(base), cudaMemcpyHostToDevice));
+      launch_gemm_splitk_reduce(dT.as<GemmTask<float>>(), dIds.as<int>(), 1, dBase.as<long long>(), base[1], 0);
+    }
+    RSCHOL_CUDA(cudaDeviceSynchronize());
+    int err = 0;
+    RSCHOL_CUDA(cudaMemcpy(&err, dE.p, sizeof(int), cudaMemcpyDeviceToHost));
+    RSCHOL_CUDA(cudaMemcpy(C.data(), dC.p, sizeof(float) * nc, cudaMemcpyDeviceToHost));
+    double worst = 0, worstAbs = 0;
+    for (int i = 0; i < M; ++i)
+      for (int j = 0; j < N; ++j) {
+        if (lower && j > i) continue;
+        double s = 0, mag = 0;
+        for (int k = 0; k < K; ++k) {
+          const double a = tA ? A[(size_t)k * lda + i] : A[(size_t)i * lda + k];
+          const double b = tB ? B[(size_t)j * ldb + k] : B[(size_t)k * ldb + j];
+          s += a * b;
+          mag += std::fabs(a * b);
+        }
+        const double ref = alpha * s + beta * (double)C0[(size_t)i * ldc + j];
+        const double scale = std::fabs(alpha) * mag + std::fabs(beta * (double)C0[(size_t)i * ldc + j]);
+        const double e = std::fabs((double)C[(size_t)i * ldc + j] - ref);
+        worstAbs = std::max(worstAbs, e);
+        worst = std::max(worst, scale > 0 ? e / scale : e);
+      }
+    out[0] = worst;
+    out[1] = worstAbs;
+    if (err) return RSCHOL_E_TIMEOUT;
+  } catch (const std::exception&) {
+    return RSCHOL_E_CUDA;
+  }
+  return RSCHOL_OK;
+}
+
 // ---- allocation-free preconditioner apply ----------------------------------
 // The permuted work vector lives in a file-scope device array instead of a
 // buffer allocated on first use, so the call itself never allocates.

@@ -27,6 +27,10 @@ struct GemmTask {
   T alpha, beta;
   int tilesN;
   int tileBase;   // first tile of this task in the launch
+  int split;      // tensor-core path: split-precision (3 x TF32) products
+  int kSplit;     // tensor-core path: K slices (1: none); slices write partials to ws
+  int kLen;       // K per slice (a multiple of 32)
+  float* ws;      // kSplit x tiles x 128 x 64 partials (kSplit > 1)
 };
 
 // In-place lower Cholesky of one diagonal tile (n <= 64).  On a
@@ -72,6 +76,14 @@ struct ExtAddRow {
 };
 
 template <class T> void launch_gemm(const GemmTask<T>* dTasks, int nTasks, int totalTiles, cudaStream_t s);
+// FP32 tasks on the tensor cores (tcgen05, TF32 or split TF32), 128 x 64
+// output tiles (tileBase / tilesN counted for that tile); *dErr is set if an
+// mbarrier wait gives up.
+void launch_gemm_tc(const GemmTask<float>* dTasks, int nTasks, int totalTiles, int* dErr, cudaStream_t s);
+// C = alpha * sum of the K-slice partials + beta * C for the split tasks
+// ids[0..nIds) (elemBase: prefix sums of their M x N, elemBase[nIds] = elems).
+void launch_gemm_splitk_reduce(const GemmTask<float>* dTasks, const int* ids, int nIds, const long long* elemBase,
+                               long long elems, cudaStream_t s);
 template <class T> void launch_potrf(const PotrfTask<T>* dTasks, int nTasks, int* dFlag, cudaStream_t s);
 template <class T> void launch_trsm(const TrsmTask<T>* dTasks, int nTasks, int totalChunks, cudaStream_t s);
 template <class T>

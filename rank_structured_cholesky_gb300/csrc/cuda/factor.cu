@@ -1,7 +1,10 @@
 #include <algorithm>
 #include <climits>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <type_traits>
 
 #include "../host/rng.h"
 #include "factor.cuh"
@@ -10,7 +13,14 @@ namespace rschol {
 
 namespace {
 constexpr int NB = 64;           // tile width of the blocked factorisations
-int tiles_of(int M, int N) { return ((M + 63) / 64) * ((N + 63) / 64); }
+int tiles_of(int M, int N, int rowsPerTile) { return ((M + rowsPerTile - 1) / rowsPerTile) * ((N + 63) / 64); }
+
+// FP32 factors run their GEMMs on the tensor cores unless
+// RSCHOL_TENSOR_CORES=0 (the SIMT kernel then serves both precisions).
+bool tensor_cores_enabled() {
+  const char* e = std::getenv("RSCHOL_TENSOR_CORES");
+  return !(e && e[0] == '0');
+}
 }  // namespace
 
 template <class T>
@@ -18,7 +28,8 @@ FactorEngine<T>::FactorEngine(const Symbolic& S_, const CSC& A_, const Params& p
     : S(S_), A(A_), prm(p), stream(s) {
   dAvals.alloc(sizeof(double) * std::max<size_t>(1, A.x.size()));
   RSCHOL_CUDA(cudaMemcpyAsync(dAvals.p, A.x.data(), sizeof(double) * A.x.size(), cudaMemcpyHostToDevice, stream));
-  dFlag.alloc(sizeof(int));
+  dFlag.alloc(2 * sizeof(int));
+  useTc_ = std::is_same<T, float>::value && tensor_cores_enabled();
   RSCHOL_CUDA(cudaStreamSynchronize(stream));
 }
 
@@ -27,12 +38,74 @@ void FactorEngine<T>::set_values(const double* lowerVals) {
   RSCHOL_CUDA(cudaMemcpyAsync(dAvals.p, lowerVals, sizeof(double) * A.x.size(), cudaMemcpyHostToDevice, stream));
 }
 
+template <>
+void FactorEngine<float>::gemm_launch(const Step& st) {
+  if (st.kind == ST_GEMM_REDUCE)
+    launch_gemm_splitk_reduce(dGemm_.as<GemmTask<float>>(), dSplitIds_.as<int>() + st.off, st.count,
+                              dSplitBase_.as<long long>() + st.aux, st.elems, stream);
+  else if (st.aux)
+    launch_gemm_tc(dGemm_.as<GemmTask<float>>() + st.off, st.count, st.grid, dFlag.as<int>() + 1, stream);
+  else
+    launch_gemm<float>(dGemm_.as<GemmTask<float>>() + st.off, st.count, st.grid, stream);
+}
+
+template <>
+void FactorEngine<double>::gemm_launch(const Step& st) {
+  launch_gemm<double>(dGemm_.as<GemmTask<double>>() + st.off, st.count, st.grid, stream);
+}
+
 template <class T>
-void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int tiles) {
+void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
   if (batch.empty()) return;
-  Step st{ST_GEMM, (long long)gemm_.size(), (int)batch.size(), tiles};
+  // Path: the tensor cores for FP32 steps with a real K (rank-64 updates are
+  // bound by C traffic, which the SIMT kernel already streams); large-K tasks
+  // of steps with few tiles are split along K to fill the SMs.
+  int maxK = 0;
+  for (auto& t : batch) maxK = std::max(maxK, t.K);
+  const bool tc = useTc_ && maxK >= 128;
+  const int rowsPerTile = tc ? 128 : 64;
+  long long baseTiles = 0;
+  for (auto& t : batch) baseTiles += (long long)((t.M + rowsPerTile - 1) / rowsPerTile) * ((t.N + 63) / 64);
+  const long long want = 2LL * 152;   // two blocks per SM
+  int tiles = 0;
+  std::vector<int> ids;
+  std::vector<long long> base{0};
+  const long long first = (long long)gemm_.size();
+  for (size_t q = 0; q < batch.size(); ++q) {
+    GemmTask<T>& t = batch[q];
+    t.tilesN = (t.N + 63) / 64;
+    const int tilesPer = ((t.M + rowsPerTile - 1) / rowsPerTile) * t.tilesN;
+    t.kSplit = 1;
+    t.kLen = t.K;
+    long long wsOff = -1;
+    if (tc && !t.lower && t.K >= 1024 && baseTiles < want) {
+      int ks = (int)std::min<long long>(16, std::min<long long>(t.K / 512, (want + baseTiles - 1) / baseTiles));
+      if (ks > 1) {
+        const int kl = ((t.K + ks - 1) / ks + 31) / 32 * 32;
+        t.kSplit = (t.K + kl - 1) / kl;
+        t.kLen = kl;
+        wsOff = wsCur_;
+        wsCur_ += (long long)t.kSplit * tilesPer * 128 * 64;
+        ids.push_back((int)(first + q));
+        base.push_back(base.back() + (long long)t.M * t.N);
+      }
+    }
+    t.tileBase = tiles;
+    tiles += tilesPer * t.kSplit;
+    gemmWsOff_.push_back(wsOff);
+  }
+  Step st{ST_GEMM, first, (int)batch.size(), tiles};
+  st.aux = tc ? 1 : 0;
   gemm_.insert(gemm_.end(), batch.begin(), batch.end());
   steps_.push_back(st);
+  if (!ids.empty()) {
+    Step r{ST_GEMM_REDUCE, (long long)splitIds_.size(), (int)ids.size(), 0};
+    r.aux = (int)splitBase_.size();
+    r.elems = base.back();
+    splitIds_.insert(splitIds_.end(), ids.begin(), ids.end());
+    splitBase_.insert(splitBase_.end(), base.begin(), base.end());
+    steps_.push_back(r);
+  }
   batch.clear();
 }
 
@@ -40,9 +113,7 @@ template <class T>
 void FactorEngine<T>::push_gemm(const GemmTask<T>& t0, int& tiles, std::vector<GemmTask<T>>& batch) {
   if (t0.M <= 0 || t0.N <= 0) return;
   GemmTask<T> t = t0;
-  t.tilesN = (t.N + 63) / 64;
-  t.tileBase = tiles;
-  tiles += tiles_of(t.M, t.N);
+  tiles += tiles_of(t.M, t.N, 64);   // tiles and bases are fixed when the batch is flushed
   batch.push_back(t);
   double f = 2.0 * t.M * t.N * std::max(t.K, 0);
   if (t.lower && t.M == t.N) f *= 0.5;
@@ -77,6 +148,7 @@ static GemmTask<T> mk_gemm(const T* A, int lda, bool tA, const T* B, int ldb, bo
   t.lower = lower;
   t.alpha = alpha;
   t.beta = beta;
+  t.split = 1;   // tensor-core path: FP32-accurate products unless a caller opts out
   return t;
 }
 
@@ -193,18 +265,26 @@ void FactorEngine<T>::emit_rf(const std::vector<RFJob<T>>& jobs) {
   if (jobs.empty()) return;
   std::vector<GemmTask<T>> gb;
   int tiles = 0;
-  // Y = F^T G
+  // Y = F^T G and the power iteration: only the range of Y matters, so on
+  // the tensor-core path these products use plain TF32
+  auto sketch = [](GemmTask<T> t) {
+    t.split = 0;
+    return t;
+  };
   for (auto& j : jobs)
-    push_gemm(mk_gemm<T>(j.F, j.ld, true, j.G, j.r, false, j.Y, j.r, j.cols, j.r, j.rows, T(1), T(0)), tiles, gb);
+    push_gemm(sketch(mk_gemm<T>(j.F, j.ld, true, j.G, j.r, false, j.Y, j.r, j.cols, j.r, j.rows, T(1), T(0))), tiles,
+              gb);
   flush_gemm(gb, tiles);
   for (int it = 0; it < prm.power_iters; ++it) {
     tiles = 0;
     for (auto& j : jobs)
-      push_gemm(mk_gemm<T>(j.F, j.ld, false, j.Y, j.r, false, j.X, j.r, j.rows, j.r, j.cols, T(1), T(0)), tiles, gb);
+      push_gemm(sketch(mk_gemm<T>(j.F, j.ld, false, j.Y, j.r, false, j.X, j.r, j.rows, j.r, j.cols, T(1), T(0))),
+                tiles, gb);
     flush_gemm(gb, tiles);
     tiles = 0;
     for (auto& j : jobs)
-      push_gemm(mk_gemm<T>(j.F, j.ld, true, j.X, j.r, false, j.Y, j.r, j.cols, j.r, j.rows, T(1), T(0)), tiles, gb);
+      push_gemm(sketch(mk_gemm<T>(j.F, j.ld, true, j.X, j.r, false, j.Y, j.r, j.cols, j.r, j.rows, T(1), T(0))),
+                tiles, gb);
     flush_gemm(gb, tiles);
   }
   // Thin Householder QR of Y (the sketch of a fast-decaying block is
@@ -260,6 +340,10 @@ void FactorEngine<T>::plan() {
   eaR_.clear();
   eaSeg_.clear();
   eaS_.clear();
+  gemmWsOff_.clear();
+  splitIds_.clear();
+  splitBase_.clear();
+  wsCur_ = 0;
   qr_.clear();
   ident_.clear();
   ints_.clear();
@@ -688,6 +772,28 @@ void FactorEngine<T>::plan() {
     emit_rf(oj);
   }
 
+  // RSCHOL_PLAN_LOG=1: one line per GEMM step on stderr (tasks, tiles, flops,
+  // largest M / N / K) for tuning the batched kernels
+  if (const char* e = std::getenv("RSCHOL_PLAN_LOG")) {
+    if (e[0] == '1') {
+      for (size_t q = 0; q < steps_.size(); ++q) {
+        const Step& st = steps_[q];
+        if (st.kind != ST_GEMM) continue;
+        double f = 0;
+        int mM = 0, mN = 0, mK = 0;
+        for (int k = 0; k < st.count; ++k) {
+          const GemmTask<T>& g = gemm_[st.off + k];
+          f += 2.0 * g.M * g.N * (double)g.K;
+          mM = std::max(mM, g.M);
+          mN = std::max(mN, g.N);
+          mK = std::max(mK, g.K);
+        }
+        std::fprintf(stderr, "plan gemm step %zu tasks %d tiles %d gflop %.3f maxM %d maxN %d maxK %d tc %d\n", q,
+                     st.count, st.grid, f * 1e-9, mM, mN, mK, st.aux);
+      }
+    }
+  }
+
   // ---- upload the schedule
   auto up = [&](DevBuf& b, const void* src, size_t bytes) {
     b.alloc(std::max<size_t>(bytes, 16));
@@ -695,6 +801,11 @@ void FactorEngine<T>::plan() {
   };
   up(dInts_, ints_.data(), ints_.size() * sizeof(int));
   for (auto& s : eaS_) s.rowRel = dInts_.as<int>() + reinterpret_cast<size_t>(s.rowRel);
+  dSplitWs_.alloc(sizeof(float) * std::max(1LL, wsCur_));
+  for (size_t q = 0; q < gemm_.size(); ++q)
+    if (gemmWsOff_[q] >= 0) gemm_[q].ws = dSplitWs_.as<float>() + gemmWsOff_[q];
+  up(dSplitIds_, splitIds_.data(), splitIds_.size() * sizeof(int));
+  up(dSplitBase_, splitBase_.data(), splitBase_.size() * sizeof(long long));
   up(dGemm_, gemm_.data(), gemm_.size() * sizeof(GemmTask<T>));
   up(dPotrf_, potrf_.data(), potrf_.size() * sizeof(PotrfTask<T>));
   up(dTrsm_, trsm_.data(), trsm_.size() * sizeof(TrsmTask<T>));
@@ -716,8 +827,8 @@ int FactorEngine<T>::run() {
   launches = 0;
   RSCHOL_CUDA(cudaMemsetAsync(dInterior.p, 0, dInterior.bytes, stream));
   RSCHOL_CUDA(cudaMemsetAsync(dCompressed.p, 0, dCompressed.bytes, stream));
-  static const int big = INT_MAX;
-  RSCHOL_CUDA(cudaMemcpyAsync(dFlag.p, &big, sizeof(int), cudaMemcpyHostToDevice, stream));
+  static const int init[2] = {INT_MAX, 0};   // POTRF code, tensor-core wait error
+  RSCHOL_CUDA(cudaMemcpyAsync(dFlag.p, init, sizeof(init), cudaMemcpyHostToDevice, stream));
   launch_scatter<T>(dAvals.as<double>(), dScatSrc_.as<long long>(), dScatDst_.as<long long>(), nScatI_, interior(),
                     stream);
   launch_scatter<T>(dAvals.as<double>(), dScatSrc_.as<long long>() + nScatI_, dScatDst_.as<long long>() + nScatI_,
@@ -725,7 +836,8 @@ int FactorEngine<T>::run() {
   launches += 2;
   for (const Step& st : steps_) {
     switch (st.kind) {
-      case ST_GEMM: launch_gemm<T>(dGemm_.as<GemmTask<T>>() + st.off, st.count, st.grid, stream); break;
+      case ST_GEMM:
+      case ST_GEMM_REDUCE: gemm_launch(st); break;
       case ST_POTRF: launch_potrf<T>(dPotrf_.as<PotrfTask<T>>() + st.off, st.count, dFlag.as<int>(), stream); break;
       case ST_TRSM: launch_trsm<T>(dTrsm_.as<TrsmTask<T>>() + st.off, st.count, st.grid, stream); break;
       case ST_EXTADD:
@@ -740,10 +852,11 @@ int FactorEngine<T>::run() {
     ++launches;
   }
   if (post) launches += post();
-  int flag = 0;
-  RSCHOL_CUDA(cudaMemcpyAsync(&flag, dFlag.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  int flag[2] = {0, 0};
+  RSCHOL_CUDA(cudaMemcpyAsync(flag, dFlag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
   RSCHOL_CUDA(cudaStreamSynchronize(stream));
-  return flag == INT_MAX ? 0 : flag;
+  if (flag[1]) throw CudaError("tensor-core GEMM: an mbarrier wait exceeded its limit");
+  return flag[0] == INT_MAX ? 0 : flag[0];
 }
 
 template class FactorEngine<double>;

@@ -45,6 +45,7 @@ enum StepKind : int {
   ST_EXTADD,
   ST_QR,
   ST_IDENT,
+  ST_GEMM_REDUCE,   // sum the K-slice partials of the split tensor-core GEMM tasks
 };
 
 struct Step {
@@ -52,7 +53,9 @@ struct Step {
   long long off;    // first task in the kind's task array
   int count;        // number of tasks
   int grid;         // tiles / chunks / columns for the launch
-  int aux = 0;      // ST_QR: largest row count of the batch (grid: largest rank)
+  int aux = 0;      // ST_QR: largest row count of the batch (grid: largest rank);
+                    // ST_GEMM: 1 on the tensor cores
+  long long elems = 0;   // ST_GEMM_REDUCE: elements of C summed
 };
 
 template <class T>
@@ -136,6 +139,8 @@ class FactorEngine {
   void push_gemm(const GemmTask<T>& t, int& tiles, std::vector<GemmTask<T>>& batch);
   void flush_gemm(std::vector<GemmTask<T>>& batch, int tiles);
   void gemm1(const GemmTask<T>& t);   // a single-task GEMM step
+  void gemm_launch(const Step& st);    // SIMT kernel, or the tensor cores for FP32
+  bool useTc_ = false;
 
   std::vector<Step> steps_;
   std::vector<GemmTask<T>> gemm_;
@@ -147,6 +152,11 @@ class FactorEngine {
   std::vector<QrTask<T>> qr_;
   std::vector<IdentTask<T>> ident_;
   std::vector<int> ints_;
+  std::vector<long long> gemmWsOff_;       // per GEMM task: offset of its K-slice partials, or -1
+  std::vector<int> splitIds_;              // ST_GEMM_REDUCE: GEMM task ids
+  std::vector<long long> splitBase_;       // ST_GEMM_REDUCE: element prefix sums (nIds + 1 per step)
+  long long wsCur_ = 0;
+  DevBuf dSplitWs_, dSplitIds_, dSplitBase_;
   std::vector<long long> scatSrc_, scatDst_;
   std::vector<int> scatIsInterior_;
   DevBuf dGemm_, dPotrf_, dTrsm_, dEaR_, dEaSeg_, dEaS_, dQr_, dIdent_, dInts_, dScatSrc_, dScatDst_;

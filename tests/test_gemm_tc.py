@@ -1,0 +1,39 @@
+"""Tensor-core (tcgen05, TF32) GEMM self-test against a host FP64 product.
+
+Shapes with K >= 1024 run split along K (partials + ordered reduction).
+Error is measured relative to sum_k |a_ik b_kj| (+ |beta c_ij|) per entry:
+plain TF32 rounds each operand to 11 significant bits (bound 2^-10 per
+product, so 2e-3 with margin); split TF32 keeps the A_lo B_lo term out only
+(FP32 accumulation dominates: 1e-5).
+"""
+import ctypes
+
+import pytest
+
+import rank_structured_cholesky_gb300 as rs
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [
+    (128, 64, 32, 0, 0), (100, 50, 7, 0, 1), (300, 130, 257, 1, 0), (257, 200, 96, 1, 1),
+    (64, 300, 1000, 0, 0), (1000, 64, 64, 0, 1), (5, 3, 1, 0, 0),
+    # K >= 1024: four K slices summed by the split-K reduction
+    (300, 104, 2048, 1, 0), (129, 65, 3001, 0, 1),
+]
+
+
+@pytest.mark.parametrize("split", [0, 1])
+@pytest.mark.parametrize("shape", SHAPES)
+def test_tensor_core_gemm(shape, split):
+    M, N, K, tA, tB = shape
+    out = (ctypes.c_double * 2)()
+    st = rs.load_library().rschol_selftest_gemm(M, N, K, tA, tB, split, 0, out)
+    assert st == 0, st
+    tol = 1e-5 if split else 2e-3
+    assert out[0] < tol, (shape, split, out[0], out[1])
+
+
+def test_tensor_core_gemm_lower_tiles():
+    out = (ctypes.c_double * 2)()
+    st = rs.load_library().rschol_selftest_gemm(400, 400, 64, 0, 1, 1, 1, out)
+    assert st == 0 and out[0] < 1e-5, (st, out[0])
