@@ -142,6 +142,9 @@ class FactorEngine {
   void gemm_launch(const Step& st);    // SIMT kernel, or the tensor cores for FP32
   bool useTc_ = false;
 
+ public:
+  bool tensor_cores() const { return useTc_; }   // FP32 GEMMs on tcgen05
+
   std::vector<Step> steps_;
   std::vector<GemmTask<T>> gemm_;
   std::vector<PotrfTask<T>> potrf_;

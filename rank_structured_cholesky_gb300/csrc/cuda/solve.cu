@@ -201,8 +201,9 @@ __global__ void __launch_bounds__(256) interior_backward_chunks(const SNode<T>* 
 }
 
 // ---------------------------------------------------------------------------
-// Compressed supernodes: 64-row blocks, one thread block (256 threads, warp w
-// owning rows 8w..8w+7 of the block) per row block.
+// Compressed supernodes.  X = L11^{-1} is formed once per factorisation, so
+// the triangular solves are GEMVs: every 64-row (or 64-column) block of a
+// supernode is an independent thread block.
 
 constexpr int SPIN_LIMIT = 1 << 22;   // polls (with a short sleep) before a wait gives up
 
@@ -216,161 +217,143 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 }
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
 
-// Warp-uniform bounded wait for *flag != 0.  Returns false when the wait gave
-// up (after SPIN_LIMIT polls, or as soon as another block reported an error);
-// the error word is then set.
-__device__ __forceinline__ bool wait_ready(const int* flag, int* err) {
-  if (__all_sync(FULL, ld_acquire(flag) != 0)) return true;
-  for (int it = 1; it <= SPIN_LIMIT; ++it) {
-    __nanosleep(64);
-    if (__all_sync(FULL, ld_acquire(flag) != 0)) return true;
-    if ((it & 63) == 0 && __any_sync(FULL, ld_volatile(err) != 0)) return false;
-  }
-  if ((threadIdx.x & 31) == 0) atomicExch(err, 1);
-  return false;
-}
-
-// After the block's own results are stored: publish them (ready flag), and
-// let the last block of the supernode and the last block of the launch reset
-// the counters for the next apply.  Returns true in the supernode's last block
-// (all of its blocks have stored their partials and left their waits).
-__device__ __forceinline__ bool finish_row_block(int* flag, int* nodeDone, int nb, int* levelTick, int* levelDone, int* sLast) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    if (flag) st_release(flag, 1);   // release: the block's stores, ordered by the barrier, become visible first
-    __threadfence();
-    const int d = atomicAdd(nodeDone, 1);
-    *sLast = (d == nb - 1);
-    if (atomicAdd(levelDone, 1) == (int)gridDim.x - 1) {
-      atomicExch(levelTick, 0);
-      atomicExch(levelDone, 0);
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return *sLast != 0;
-}
-
-// t[rr][0..1] = P[row][2l], P[row][2l+1] of a 64-column tile (rows
-// 8w+rr < h, zero elsewhere).
+// Right-hand side of every compressed supernode of a level: w[c0 + i] plus
+// the fixed-order contribution list of row i (a warp per row, lanes over the
+// contributions).
 template <class T>
-__device__ __forceinline__ void load_tile(const T* __restrict__ P, int ld, int h, T (&t)[8][2]) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int rr = 0; rr < 8; ++rr) {
-    const int i = warp * 8 + rr;
-    if (i < h) {
-      const T* p = P + (size_t)i * ld + 2 * lane;
-      t[rr][0] = p[0];
-      t[rr][1] = p[1];
-    } else {
-      t[rr][0] = T(0);
-      t[rr][1] = T(0);
-    }
-  }
-}
-
-// Forward row block: f_b = w_b + contributions - sum_{k<b} L[b,k] y_k,
-// y_b = Dinv_b f_b, partial z_b = U_b^T y_b.
-template <class T>
-__global__ void __launch_bounds__(256) compressed_forward_blocks(const SNode<T>* __restrict__ nodes,
-                                                                 const RowBlock* __restrict__ tickets,
-                                                                 const long long* __restrict__ cstart,
-                                                                 const T* const* __restrict__ ent,
-                                                                 int* __restrict__ sync, int levelSync,
-                                                                 T* __restrict__ zpart, T* __restrict__ w,
-                                                                 T* __restrict__ wu) {
-  __shared__ int sTicket, sLast;
-  __shared__ T fb[SOLVE_RB], yb[SOLVE_RB];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int* err = sync;
-  if (threadIdx.x == 0) sTicket = atomicAdd(&sync[levelSync], 1);
-  __syncthreads();
-  if (sTicket >= (int)gridDim.x) {   // counters not reset: report, touch nothing
-    if (threadIdx.x == 0) atomicExch(err, 2);
-    return;
-  }
-  const RowBlock tk = tickets[sTicket];
-  const SNode<T>& nd = nodes[tk.node];
-  const int n = nd.n, i0 = tk.b * SOLVE_RB, h = min(SOLVE_RB, n - i0);
-  T* wn = w + nd.c0;
-  int* flags = sync + nd.syncOff;
-  // 1. right-hand side rows with their contribution lists (warp per row,
-  // lanes over the row's contributions)
+__global__ void __launch_bounds__(256) compressed_gather_rows(const SNode<T>* __restrict__ nodes,
+                                                              const int* __restrict__ lvl,
+                                                              const long long* __restrict__ cstart,
+                                                              const T* const* __restrict__ ent, T* __restrict__ w) {
+  const SNode<T>& nd = nodes[lvl[blockIdx.y]];
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= nd.n) return;
   const long long* cs = cstart + nd.cOff;
-  for (int rr = 0; rr < 8; ++rr) {
-    const int i = warp * 8 + rr;
-    T acc = T(0);
-    if (i < h)
-      for (long long e = cs[i0 + i] + lane; e < cs[i0 + i + 1]; e += 32) acc += *ent[e];
-    acc = warp_sum(acc);
-    if (lane == 0) fb[i] = (i < h) ? wn[i0 + i] + acc : T(0);
+  T acc = T(0);
+  for (long long e = cs[i] + lane; e < cs[i + 1]; e += 32) acc += *ent[e];
+  acc = warp_sum(acc);
+  if (lane == 0) w[nd.c0 + i] += acc;
+}
+
+// Partial products of y = X f and x = X^T g over 64 x 256 tiles of X (tiles
+// entirely above the diagonal are not listed): a level's tiles are spread
+// over all SMs, each thread keeping 64 independent loads in flight.
+//   P[i][jb] = sum_{j in column block jb} X[i][j] f_j    (forward)
+//   Q[j][ib] = sum_{i in row block ib} X[i][j] g_i       (backward)
+template <class T>
+__global__ void __launch_bounds__(256) compressed_ytile_kernel(const SNode<T>* __restrict__ nodes,
+                                                               const XTile* __restrict__ tiles,
+                                                               const T* __restrict__ w, T* __restrict__ part) {
+  const XTile tl = tiles[blockIdx.x];
+  const SNode<T>& nd = nodes[tl.node];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n = nd.n;
+  const int i0 = tl.ib * SOLVE_RB + warp * 8, j0 = tl.jb * XT_COLS;
+  T fj[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int j = j0 + lane + 32 * c;
+    fj[c] = (j < n) ? w[nd.c0 + j] : T(0);
   }
-  // 2. earlier row blocks, as they become ready; the L tile of the next
-  // block is loaded before waiting on the current one
-  T acc[8], cur[8][2], dv[8][2];
+  T acc[8];
 #pragma unroll
-  for (int rr = 0; rr < 8; ++rr) acc[rr] = T(0);
-  load_tile<T>(nd.Dinv + (size_t)tk.b * SOLVE_RB * SOLVE_RB, SOLVE_RB, h, dv);
-  const T* Lrow = nd.L + (size_t)i0 * nd.ld;
-  if (tk.b > 0) load_tile<T>(Lrow, nd.ld, h, cur);
-  bool ok = true;
-  for (int kb = 0; kb < tk.b && ok; ++kb) {
-    T nxt[8][2] = {};
-    if (kb + 1 < tk.b) load_tile<T>(Lrow + (kb + 1) * SOLVE_RB, nd.ld, h, nxt);
-    ok = wait_ready(flags + kb, err);
-    const T y0 = __ldcg(wn + kb * SOLVE_RB + 2 * lane), y1 = __ldcg(wn + kb * SOLVE_RB + 2 * lane + 1);
+  for (int q = 0; q < 8; ++q) {
+    acc[q] = T(0);
+    const int i = i0 + q;
+    if (i < n) {
+      const T* xr = nd.X + (size_t)i * n;
 #pragma unroll
-    for (int rr = 0; rr < 8; ++rr) {
-      acc[rr] += cur[rr][0] * y0 + cur[rr][1] * y1;
-      cur[rr][0] = nxt[rr][0];
-      cur[rr][1] = nxt[rr][1];
-    }
-  }
-  __syncwarp();
-#pragma unroll
-  for (int rr = 0; rr < 8; ++rr) {
-    const T s = warp_sum(acc[rr]);
-    if (lane == 0) fb[warp * 8 + rr] -= s;
-  }
-  __syncthreads();
-  // 3. y_b = Dinv_b f_b
-  {
-    T d[8];
-    const T f0 = fb[2 * lane], f1 = fb[2 * lane + 1];
-#pragma unroll
-    for (int rr = 0; rr < 8; ++rr) d[rr] = dv[rr][0] * f0 + dv[rr][1] * f1;
-#pragma unroll
-    for (int rr = 0; rr < 8; ++rr) {
-      const T s = warp_sum(d[rr]);
-      const int i = warp * 8 + rr;
-      if (lane == 0) {
-        yb[i] = (i < h) ? s : T(0);
-        if (i < h) wn[i0 + i] = s;
+      for (int c = 0; c < 8; ++c) {
+        const int j = j0 + lane + 32 * c;
+        if (j < n) acc[q] += xr[j] * fj[c];
       }
     }
   }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const T v = warp_sum(acc[q]);
+    if (lane == 0 && i0 + q < n) part[nd.zpOff2 + (size_t)(i0 + q) * nd.ncb + tl.jb] = v;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) compressed_xtile_kernel(const SNode<T>* __restrict__ nodes,
+                                                               const XTile* __restrict__ tiles,
+                                                               const T* __restrict__ gv, T* __restrict__ part) {
+  __shared__ T gs[SOLVE_RB];
+  const XTile tl = tiles[blockIdx.x];
+  const SNode<T>& nd = nodes[tl.node];
+  const int n = nd.n, i0 = tl.ib * SOLVE_RB, h = min(SOLVE_RB, n - i0);
+  if (threadIdx.x < SOLVE_RB) gs[threadIdx.x] = (threadIdx.x < h) ? gv[nd.c0 + i0 + threadIdx.x] : T(0);
   __syncthreads();
-  // y_b is final: publish it before the (off the critical path) z partial
-  if (threadIdx.x == 0) st_release(flags + tk.b, 1);
-  // 4. partial z_b = U_b^T y_b
+  const int j = tl.jb * XT_COLS + threadIdx.x;
+  if (j >= n) return;
+  T s = T(0);
+#pragma unroll 16
+  for (int i = 0; i < h; ++i) s += nd.X[(size_t)(i0 + i) * n + j] * gs[i];
+  part[nd.zpOff2 + (size_t)j * nd.nb + tl.ib] = s;
+}
+
+// y_i = sum of its tile partials (fixed order) for one 64-row block, then the
+// block's part of z = U^T y; the last block of the supernode to finish sums
+// the parts in fixed order.
+template <class T>
+__global__ void __launch_bounds__(256) compressed_y_kernel(const SNode<T>* __restrict__ nodes,
+                                                           const RowBlock* __restrict__ work, int* __restrict__ sync,
+                                                           T* __restrict__ zpart, const T* __restrict__ ypart,
+                                                           T* __restrict__ yv, T* __restrict__ wu) {
+  __shared__ T yb[SOLVE_RB];
+  __shared__ int sLast;
+  const RowBlock wk = work[blockIdx.x];
+  const SNode<T>& nd = nodes[wk.node];
+  const int n = nd.n, i0 = wk.b * SOLVE_RB, h = min(SOLVE_RB, n - i0);
+  if (threadIdx.x < SOLVE_RB) {
+    const int i = threadIdx.x;
+    T s = T(0);
+    if (i < h) {
+      const int jbEnd = min(nd.ncb - 1, (i0 + SOLVE_RB - 1) / XT_COLS);
+      const T* p = ypart + nd.zpOff2 + (size_t)(i0 + i) * nd.ncb;
+      for (int jb = 0; jb <= jbEnd; ++jb) s += p[jb];
+      yv[nd.c0 + i0 + i] = s;
+    }
+    yb[i] = s;
+  }
+  __syncthreads();
   const int r = nd.r;
   for (int k = threadIdx.x; k < r; k += blockDim.x) {
     T s = T(0);
     for (int i = 0; i < h; ++i) s += nd.U[(size_t)(i0 + i) * r + k] * yb[i];
-    zpart[nd.zpOff + (size_t)tk.b * r + k] = s;
+    zpart[nd.zpOff + (size_t)wk.b * r + k] = s;
   }
-  const int nb = nd.nb;
-  if (finish_row_block(nullptr, flags + nb, nb, &sync[levelSync], &sync[levelSync + 1], &sLast)) {
-    // last row block of this supernode: z in fixed order, then reset the flags
-    for (int k = threadIdx.x; k < r; k += blockDim.x) {
-      T s = T(0);
-      for (int b = 0; b < nb; ++b) s += __ldcg(zpart + nd.zpOff + (size_t)b * r + k);
-      wu[nd.wuOff + k] = s;
-    }
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) flags[b] = 0;
-    if (threadIdx.x == 0) flags[nb] = 0;
+  __syncthreads();
+  int* done = sync + nd.syncOff;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    sLast = (atomicAdd(done, 1) == nd.nb - 1);
+    __threadfence();
   }
+  __syncthreads();
+  if (!sLast) return;
+  for (int k = threadIdx.x; k < r; k += blockDim.x) {
+    T s = T(0);
+    for (int b = 0; b < nd.nb; ++b) s += __ldcg(zpart + nd.zpOff + (size_t)b * r + k);
+    wu[nd.wuOff + k] = s;
+  }
+  if (threadIdx.x == 0) *done = 0;
+}
+
+// x_j = sum of its tile partials over the row blocks ib >= 4 jb (fixed order).
+template <class T>
+__global__ void __launch_bounds__(256) compressed_x_reduce(const SNode<T>* __restrict__ nodes,
+                                                           const int* __restrict__ lvl, const T* __restrict__ xpart,
+                                                           T* __restrict__ w) {
+  const SNode<T>& nd = nodes[lvl[blockIdx.y]];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nd.n) return;
+  const T* p = xpart + nd.zpOff2 + (size_t)j * nd.nb;
+  T s = T(0);
+  for (int ib = (j / XT_COLS) * (XT_COLS / SOLVE_RB); ib < nd.nb; ++ib) s += p[ib];
+  w[nd.c0 + j] = s;
 }
 
 // u = -V z of every compressed supernode of a level (its contribution to the
@@ -415,7 +398,7 @@ __global__ void __launch_bounds__(256) compressed_vtx_kernel(const SNode<T>* __r
     spart[nd.spOff + (size_t)ch * r + k] = s;
   }
   __syncthreads();
-  int* done = sync + nd.syncOff + nd.nb + 2;
+  int* done = sync + nd.syncOff + 1;
   if (threadIdx.x == 0) {
     __threadfence();
     sLast = (atomicAdd(done, 1) == nd.nch - 1);
@@ -431,122 +414,45 @@ __global__ void __launch_bounds__(256) compressed_vtx_kernel(const SNode<T>* __r
   if (threadIdx.x == 0) *done = 0;
 }
 
-// Backward row block (row blocks in reverse order): g_b = w_b - U_b s,
-// v = g_b - sum_{k>b} L[k,b]^T x_k, x_b = Dinv_b^T v.
+// g = y - U s in place (a warp per row).
 template <class T>
-__global__ void __launch_bounds__(256) compressed_backward_blocks(const SNode<T>* __restrict__ nodes,
-                                                                  const RowBlock* __restrict__ tickets,
-                                                                  int* __restrict__ sync, int levelSync,
-                                                                  const T* __restrict__ sv, T* __restrict__ w) {
-  __shared__ int sTicket, sLast;
-  __shared__ T gb[SOLVE_RB], vb[SOLVE_RB];
-  __shared__ T red[8][SOLVE_RB];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int* err = sync;
-  if (threadIdx.x == 0) sTicket = atomicAdd(&sync[levelSync], 1);
-  __syncthreads();
-  if (sTicket >= (int)gridDim.x) {   // counters not reset: report, touch nothing
-    if (threadIdx.x == 0) atomicExch(err, 2);
-    return;
-  }
-  const RowBlock tk = tickets[sTicket];
-  const SNode<T>& nd = nodes[tk.node];
-  const int n = nd.n, nb = nd.nb, i0 = tk.b * SOLVE_RB, h = min(SOLVE_RB, n - i0), r = nd.r;
-  T* wn = w + nd.c0;
-  int* flags = sync + nd.syncOff;
-  // 1. g_b = w_b - U_b s (warp per row)
-  const bool offd = r > 0 && nd.m > 0;
+__global__ void __launch_bounds__(256) compressed_g_kernel(const SNode<T>* __restrict__ nodes,
+                                                           const int* __restrict__ lvl, const T* __restrict__ sv,
+                                                           T* __restrict__ yv) {
+  const SNode<T>& nd = nodes[lvl[blockIdx.y]];
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= nd.n || nd.r == 0 || nd.m == 0) return;
+  const int r = nd.r;
   const T* s = sv + nd.wuOff + r;
-  for (int rr = 0; rr < 8; ++rr) {
-    const int i = warp * 8 + rr;
-    T acc = T(0);
-    if (offd && i < h)
-      for (int k = lane; k < r; k += 32) acc += nd.U[(size_t)(i0 + i) * r + k] * s[k];
-    acc = warp_sum(acc);
-    if (lane == 0) gb[i] = (i < h) ? wn[i0 + i] - acc : T(0);
-  }
-  // 2. later row blocks: column block b of L below the diagonal, transposed;
-  // the tile of the next block is loaded before waiting on the current one
-  T p0 = T(0), p1 = T(0), cur[8][2], dv[8][2];
-  load_tile<T>(nd.Dinv + (size_t)tk.b * SOLVE_RB * SOLVE_RB, SOLVE_RB, SOLVE_RB, dv);
-  const T* Lcol = nd.L + i0;
-  if (nb - 1 > tk.b) {
-    const int k0 = (nb - 1) * SOLVE_RB;
-    load_tile<T>(Lcol + (size_t)k0 * nd.ld, nd.ld, min(SOLVE_RB, n - k0), cur);
-  }
-  bool ok = true;
-  for (int kb = nb - 1; kb > tk.b && ok; --kb) {
-    T nxt[8][2] = {};
-    if (kb - 1 > tk.b) load_tile<T>(Lcol + (size_t)(kb - 1) * SOLVE_RB * nd.ld, nd.ld, SOLVE_RB, nxt);
-    ok = wait_ready(flags + kb, err);
-    const int k0 = kb * SOLVE_RB, kh = min(SOLVE_RB, n - k0);
-#pragma unroll
-    for (int rr = 0; rr < 8; ++rr) {
-      const int i = warp * 8 + rr;
-      const T xi = (i < kh) ? __ldcg(wn + k0 + i) : T(0);
-      p0 += cur[rr][0] * xi;
-      p1 += cur[rr][1] * xi;
-      cur[rr][0] = nxt[rr][0];
-      cur[rr][1] = nxt[rr][1];
-    }
-  }
-  red[warp][2 * lane] = p0;
-  red[warp][2 * lane + 1] = p1;
-  __syncthreads();
-  if (threadIdx.x < SOLVE_RB) {
-    T t = T(0);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) t += red[q][threadIdx.x];
-    vb[threadIdx.x] = gb[threadIdx.x] - t;
-  }
-  __syncthreads();
-  // 3. x_b = Dinv_b^T v (rows of Dinv split over the warps)
-  {
-    T q0 = T(0), q1 = T(0);
-#pragma unroll
-    for (int rr = 0; rr < 8; ++rr) {
-      const T vi = vb[warp * 8 + rr];
-      q0 += dv[rr][0] * vi;
-      q1 += dv[rr][1] * vi;
-    }
-    __syncthreads();
-    red[warp][2 * lane] = q0;
-    red[warp][2 * lane + 1] = q1;
-    __syncthreads();
-    if (threadIdx.x < h) {
-      T t = T(0);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) t += red[q][threadIdx.x];
-      wn[i0 + threadIdx.x] = t;
-    }
-  }
-  if (finish_row_block(flags + tk.b, flags + nb + 1, nb, &sync[levelSync], &sync[levelSync + 1], &sLast)) {
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) flags[b] = 0;
-    if (threadIdx.x == 0) flags[nb + 1] = 0;
-  }
+  const T* u = nd.U + (size_t)i * r;
+  T acc = T(0);
+  for (int k = lane; k < r; k += 32) acc += u[k] * s[k];
+  acc = warp_sum(acc);
+  if (lane == 0) yv[nd.c0 + i] -= acc;
 }
 
 // Inverse of each lower-triangular diagonal block (column c by thread c,
-// forward substitution), written as pad x pad (row-major, ld pad) with zeros
-// outside the h x h lower triangle.
+// forward substitution), written as pad x pad (row-major, row stride ldD)
+// with zeros outside the h x h lower triangle.
 template <class T>
 __global__ void __launch_bounds__(64) invert_diag_blocks(const DinvTask<T>* __restrict__ tasks) {
   __shared__ T Ls[SOLVE_RB][SOLVE_RB + 1];
   const DinvTask<T> t = tasks[blockIdx.x];
-  const int h = t.h, pad = t.pad, c = threadIdx.x;
+  const int h = t.h, pad = t.pad, ldD = t.ldD, c = threadIdx.x;
   for (int idx = threadIdx.x; idx < h * h; idx += blockDim.x) {
     const int i = idx / h, j = idx - i * h;
     Ls[i][j] = (j <= i) ? t.L[(size_t)i * t.ld + j] : T(0);
   }
   T* D = t.D;
   if (c < pad)
-    for (int i = 0; i < pad; ++i) D[i * pad + c] = T(0);
+    for (int i = 0; i < pad; ++i) D[(size_t)i * ldD + c] = T(0);
   __syncthreads();
   if (c < h) {
     for (int i = c; i < h; ++i) {
       T s = (i == c) ? T(1) : T(0);
-      for (int k = c; k < i; ++k) s -= Ls[i][k] * D[k * pad + c];
-      D[i * pad + c] = s / Ls[i][i];
+      for (int k = c; k < i; ++k) s -= Ls[i][k] * D[(size_t)k * ldD + c];
+      D[(size_t)i * ldD + c] = s / Ls[i][i];
     }
   }
 }
@@ -568,8 +474,10 @@ void SolveEngine<T>::plan() {
   const int nn = (int)S.nodes.size();
   nodes_.assign(nn, SNode<T>{});
   std::vector<int> rowsAll, rel, child, lvlNodes;
-  long long wuCur = 0, dinvCur = 0, zpCur = 0, spCur = 0, ipCur = 0;
-  int syncCur = 1 + 4 * (int)F_.compressedLevels.size();   // error word, per-level tickets
+  long long wuCur = 0, dinvCur = 0, zpCur = 0, spCur = 0, ipCur = 0, xCur = 0, xpCur = 0;
+  int syncCur = 1;   // error word
+  std::vector<long long> xOff(nn, -1);
+  std::vector<long long> xTaskOff;   // per compressed diagonal-block task: offset in the X arena
   bytesPerApply_ = 0;
   std::vector<int> pos(S.n, -1);
   std::vector<DinvTask<T>> dinvTasks;
@@ -601,8 +509,10 @@ void SolveEngine<T>::plan() {
         t.ld = sn.ld;
         t.h = std::min(SOLVE_RB, nd.n - b * SOLVE_RB);
         t.pad = t.h;
+        t.ldD = t.h;
         dinvTasks.push_back(t);
         dinvTaskOff.push_back(dinvCur + (long long)b * SOLVE_RB * SOLVE_RB);
+        xTaskOff.push_back(-1);
       }
       dinvNodeOff[s] = dinvCur;
       {
@@ -620,22 +530,28 @@ void SolveEngine<T>::plan() {
       sn.nb = (nd.n + SOLVE_RB - 1) / SOLVE_RB;
       sn.nch = (sn.r > 0 && sn.m > 0) ? (sn.m + 127) / 128 : 0;
       sn.syncOff = syncCur;
-      syncCur += sn.nb + 3;
+      syncCur += 2;   // row blocks of y done, V chunks of s done
+      sn.ncb = (nd.n + XT_COLS - 1) / XT_COLS;
+      sn.zpOff2 = xpCur;
+      xpCur += (long long)nd.n * sn.nb;
       sn.zpOff = zpCur;
       zpCur += (long long)sn.nb * sn.r;
       sn.spOff = spCur;
       spCur += (long long)sn.nch * sn.r;
+      // X = L11^{-1}: the inverted 64 x 64 diagonal blocks go in place
+      xOff[s] = xCur;
       for (int b = 0; b < sn.nb; ++b) {
         DinvTask<T> t{};
         t.L = sn.L + (size_t)b * SOLVE_RB * sn.ld + (size_t)b * SOLVE_RB;
         t.ld = sn.ld;
         t.h = std::min(SOLVE_RB, nd.n - b * SOLVE_RB);
-        t.pad = SOLVE_RB;
+        t.pad = t.h;
+        t.ldD = nd.n;
         dinvTasks.push_back(t);
-        dinvTaskOff.push_back(dinvCur + (long long)b * SOLVE_RB * SOLVE_RB);
+        dinvTaskOff.push_back(-1);
+        xTaskOff.push_back(xCur + (long long)b * SOLVE_RB * nd.n + (long long)b * SOLVE_RB);
       }
-      dinvNodeOff[s] = dinvCur;
-      dinvCur += (long long)sn.nb * SOLVE_RB * SOLVE_RB;
+      xCur += (long long)nd.n * nd.n;
       bytesPerApply_ += 2.0 * sizeof(T) * ((double)nd.n * (nd.n + 1) / 2 + (double)sn.r * (nd.m() + nd.n));
     }
   }
@@ -689,35 +605,39 @@ void SolveEngine<T>::plan() {
   }
   for (size_t v : smemIB_)
     if (v > 200 * 1024) throw std::runtime_error("interior front too large for the shared-memory solve");
-  // compressed levels: row-block tickets (forward: block 0 of every node, then
-  // block 1, ...; backward: last blocks first), so that a thread block only
-  // waits on blocks with smaller tickets
-  std::vector<RowBlock> tickF, tickB;
+  // compressed levels: (supernode, 64-row block) work lists
+  std::vector<RowBlock> tickF;
   tickOff_.clear();
   cBlocks_.clear();
   cMaxCh_.clear();
   cVzGrid_.clear();
+  cRowGrid_.clear();
+  cColGrid_.clear();
+  std::vector<XTile> xtiles;
+  cTiles_.clear();
   for (auto& lv : F_.compressedLevels) {
     cLevels_.push_back({(long long)lvlNodes.size(), (int)lv.size()});
     lvlNodes.insert(lvlNodes.end(), lv.begin(), lv.end());
     tickOff_.push_back((long long)tickF.size());
-    int maxNb = 0, maxCh = 1, blocks = 0;
+    const long long t0 = (long long)xtiles.size();
+    for (int j : lv)   // tiles with a part on or below the diagonal
+      for (int ib = 0; ib < nodes_[j].nb; ++ib)
+        for (int jb = 0; jb < nodes_[j].ncb && jb * XT_COLS <= ib * SOLVE_RB + SOLVE_RB - 1; ++jb)
+          xtiles.push_back(XTile{j, ib, jb});
+    cTiles_.push_back({t0, (int)((long long)xtiles.size() - t0)});
+    int maxCh = 1, blocks = 0, maxN = 1, maxM = 1;
     for (int j : lv) {
-      maxNb = std::max(maxNb, nodes_[j].nb);
       maxCh = std::max(maxCh, nodes_[j].nch);
       blocks += nodes_[j].nb;
+      maxN = std::max(maxN, nodes_[j].n);
+      maxM = std::max(maxM, nodes_[j].m);
+      for (int b = 0; b < nodes_[j].nb; ++b) tickF.push_back(RowBlock{j, b});
     }
-    for (int d = 0; d < maxNb; ++d)
-      for (int j : lv)
-        if (d < nodes_[j].nb) {
-          tickF.push_back(RowBlock{j, d});
-          tickB.push_back(RowBlock{j, nodes_[j].nb - 1 - d});
-        }
     cBlocks_.push_back(blocks);
     cMaxCh_.push_back(maxCh);
-    int maxM = 1;
-    for (int j : lv) maxM = std::max(maxM, nodes_[j].m);
     cVzGrid_.push_back(std::min(64, (maxM + 7) / 8));
+    cRowGrid_.push_back((maxN + 7) / 8);
+    cColGrid_.push_back((maxN + 255) / 256);
   }
   cudaStream_t st = F_.stream;
   auto up = [&](DevBuf& b, const void* src, size_t bytes) {
@@ -730,9 +650,17 @@ void SolveEngine<T>::plan() {
   dSp_.alloc(sizeof(T) * std::max(1LL, spCur));
   dIp_.alloc(sizeof(T) * std::max(1LL, ipCur));
   dYi_.alloc(sizeof(T) * std::max(1, S.n));
-  for (size_t q = 0; q < dinvTasks.size(); ++q) dinvTasks[q].D = dDinv_.as<T>() + dinvTaskOff[q];
-  for (int s = 0; s < nn; ++s) nodes_[s].Dinv = dDinv_.as<T>() + dinvNodeOff[s];
+  dXp_.alloc(sizeof(T) * std::max(1LL, xpCur));
+  dX_.alloc(sizeof(T) * std::max(1LL, xCur));
+  RSCHOL_CUDA(cudaMemsetAsync(dX_.p, 0, sizeof(T) * std::max(1LL, xCur), st));   // upper triangles stay zero
+  for (size_t q = 0; q < dinvTasks.size(); ++q)
+    dinvTasks[q].D = xTaskOff[q] >= 0 ? dX_.as<T>() + xTaskOff[q] : dDinv_.as<T>() + dinvTaskOff[q];
+  for (int s = 0; s < nn; ++s) {
+    if (S.nodes[s].compressed) nodes_[s].X = dX_.as<T>() + xOff[s];
+    else nodes_[s].Dinv = dDinv_.as<T>() + dinvNodeOff[s];
+  }
   nDinv_ = (int)dinvTasks.size();
+  plan_inverse(xOff);
   // per-row contribution lists of the compressed supernodes (in source order)
   {
     std::vector<long long> cstart;
@@ -769,7 +697,7 @@ void SolveEngine<T>::plan() {
   up(dLevelNodes_, lvlNodes.data(), lvlNodes.size() * sizeof(int));
   up(dIWork_, iwork.data(), iwork.size() * sizeof(RowBlock));
   up(dTickF_, tickF.data(), tickF.size() * sizeof(RowBlock));
-  up(dTickB_, tickB.data(), tickB.size() * sizeof(RowBlock));
+  up(dTiles_, xtiles.data(), xtiles.size() * sizeof(XTile));
   up(dDinvTasks_, dinvTasks.data(), dinvTasks.size() * sizeof(DinvTask<T>));
   syncInts_ = syncCur;
   dSync_.alloc(sizeof(int) * syncCur);
@@ -779,17 +707,119 @@ void SolveEngine<T>::plan() {
   const int maxSmem = 200 * 1024;
   RSCHOL_CUDA(cudaFuncSetAttribute(interior_forward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
   RSCHOL_CUDA(cudaFuncSetAttribute(interior_backward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
-  launchesPerApply_ = 2 * (long long)iLevels_.size() + 4 * (long long)cLevels_.size() - (cLevels_.empty() ? 0 : 1) +
+  launchesPerApply_ = 2 * (long long)iLevels_.size() + 8 * (long long)cLevels_.size() - (cLevels_.empty() ? 0 : 1) +
                       (std::is_same<T, double>::value ? 0 : 2);
   bytesPerApply_ += 8.0 * 4 * S.n;
 }
 
 template <class T>
+void SolveEngine<T>::plan_inverse(const std::vector<long long>& xOff) {
+  // X = L11^{-1} of every compressed supernode by recursive doubling: with
+  // the diagonal 64 x 64 inverses in place, for block sizes sz = 64, 128, ...
+  // every pair (A, B) of consecutive sz-blocks gets X_BA = -X_BB (L_BA X_AA).
+  // Both products run by 64-column (64-row) blocks whose K stops at the
+  // triangle, so the work is n^3 / 3 per supernode.
+  const Symbolic& S = F_.S;
+  const bool tc = std::is_same<T, float>::value && F_.tensor_cores();
+  const int rpt = tc ? 128 : 64;
+  const int nn = (int)S.nodes.size();
+  int maxN = 0;
+  for (int s = 0; s < nn; ++s)
+    if (S.nodes[s].compressed) maxN = std::max(maxN, S.nodes[s].n);
+  long long t1Max = 1;
+  for (int sz = SOLVE_RB; sz < maxN; sz *= 2) {
+    long long t1 = 0;
+    for (int s = 0; s < nn; ++s) {
+      const int n = S.nodes[s].n;
+      if (!S.nodes[s].compressed) continue;
+      for (int A0 = 0; A0 + sz < n; A0 += 2 * sz) t1 += (long long)std::min(sz, n - A0 - sz) * sz;
+    }
+    t1Max = std::max(t1Max, t1);
+  }
+  dT1_.alloc(sizeof(T) * t1Max);
+  std::vector<GemmTask<T>> tasks;
+  xSteps_.clear();
+  auto mk = [&](const T* A, int lda, const T* B, int ldb, T* C, int ldc, int M, int N, int K, T alpha) {
+    GemmTask<T> t{};
+    t.A = A;
+    t.B = B;
+    t.C = C;
+    t.M = M;
+    t.N = N;
+    t.K = K;
+    t.lda = lda;
+    t.ldb = ldb;
+    t.ldc = ldc;
+    t.alpha = alpha;
+    t.beta = T(0);
+    t.tilesN = (N + 63) / 64;
+    t.split = 1;
+    t.kSplit = 1;
+    t.kLen = K;
+    return t;
+  };
+  auto flush = [&](std::vector<GemmTask<T>>& batch) {
+    if (batch.empty()) return;
+    int tiles = 0;
+    for (auto& t : batch) {
+      t.tileBase = tiles;
+      tiles += ((t.M + rpt - 1) / rpt) * t.tilesN;
+    }
+    xSteps_.push_back(XStep{(long long)tasks.size(), (int)batch.size(), tiles});
+    tasks.insert(tasks.end(), batch.begin(), batch.end());
+    batch.clear();
+  };
+  for (int sz = SOLVE_RB; sz < maxN; sz *= 2) {
+    std::vector<GemmTask<T>> b1, b2;
+    long long t1cur = 0;
+    for (int s = 0; s < nn; ++s) {
+      if (!S.nodes[s].compressed) continue;
+      const int n = S.nodes[s].n, ld = nodes_[s].ld;
+      const T* L = nodes_[s].L;
+      T* X = dX_.as<T>() + xOff[s];
+      for (int A0 = 0; A0 + sz < n; A0 += 2 * sz) {
+        const int B0 = A0 + sz, bsz = std::min(sz, n - B0);
+        T* T1 = dT1_.as<T>() + t1cur;
+        t1cur += (long long)bsz * sz;
+        for (int a = 0; a * SOLVE_RB < sz; ++a)   // T1[:, a] = L_BA[:, a:] X_AA[a:, a]
+          b1.push_back(mk(L + (size_t)B0 * ld + A0 + a * SOLVE_RB, ld,
+                          X + (size_t)(A0 + a * SOLVE_RB) * n + A0 + a * SOLVE_RB, n, T1 + a * SOLVE_RB, sz, bsz,
+                          SOLVE_RB, sz - a * SOLVE_RB, T(1)));
+        for (int b = 0; b * SOLVE_RB < bsz; ++b) {   // X_BA[b, :] = -X_BB[b, :b] T1[:b, :]
+          const int hb = std::min(SOLVE_RB, bsz - b * SOLVE_RB), K = std::min(bsz, (b + 1) * SOLVE_RB);
+          b2.push_back(mk(X + (size_t)(B0 + b * SOLVE_RB) * n + B0, n, T1, sz,
+                          X + (size_t)(B0 + b * SOLVE_RB) * n + A0, n, hb, sz, K, T(-1)));
+        }
+      }
+    }
+    flush(b1);
+    flush(b2);
+  }
+  dXGemm_.alloc(std::max<size_t>(16, tasks.size() * sizeof(GemmTask<T>)));
+  if (!tasks.empty())
+    RSCHOL_CUDA(cudaMemcpyAsync(dXGemm_.p, tasks.data(), tasks.size() * sizeof(GemmTask<T>), cudaMemcpyHostToDevice,
+                                F_.stream));
+}
+
+template <class T>
 int SolveEngine<T>::prepare(cudaStream_t st) {
-  if (nDinv_ == 0) return 0;
-  invert_diag_blocks<T><<<nDinv_, SOLVE_RB, 0, st>>>(dDinvTasks_.as<DinvTask<T>>());
-  RSCHOL_LAUNCH_CHECK();
-  return 1;
+  int launches = 0;
+  if (nDinv_ > 0) {
+    invert_diag_blocks<T><<<nDinv_, SOLVE_RB, 0, st>>>(dDinvTasks_.as<DinvTask<T>>());
+    RSCHOL_LAUNCH_CHECK();
+    ++launches;
+  }
+  for (const XStep& x : xSteps_) {
+    const GemmTask<T>* d = dXGemm_.as<GemmTask<T>>() + x.off;
+    if constexpr (std::is_same<T, float>::value) {
+      if (F_.tensor_cores()) launch_gemm_tc(d, x.count, x.tiles, F_.dFlag.template as<int>() + 1, st);
+      else launch_gemm<T>(d, x.count, x.tiles, st);
+    } else {
+      launch_gemm<T>(d, x.count, x.tiles, st);
+    }
+    ++launches;
+  }
+  return launches;
 }
 
 template <class T>
@@ -824,23 +854,37 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
         dWu_.as<T>());
     RSCHOL_LAUNCH_CHECK();
   }
+  T* yv = dYi_.as<T>();
   for (size_t l = 0; l < cLevels_.size(); ++l) {
-    compressed_forward_blocks<T><<<cBlocks_[l], 256, 0, st>>>(
-        dNodes_.as<SNode<T>>(), dTickF_.as<RowBlock>() + tickOff_[l], dCStart_.as<long long>(),
-        dCEnt_.as<const T*>(), sync, 1 + 4 * (int)l, dZp_.as<T>(), w, dWu_.as<T>());
+    const int* lv = lvl + cLevels_[l].first;
+    compressed_gather_rows<T><<<dim3(cRowGrid_[l], cLevels_[l].second), 256, 0, st>>>(
+        dNodes_.as<SNode<T>>(), lv, dCStart_.as<long long>(), dCEnt_.as<const T*>(), w);
+    RSCHOL_LAUNCH_CHECK();
+    compressed_ytile_kernel<T><<<cTiles_[l].second, 256, 0, st>>>(
+        dNodes_.as<SNode<T>>(), dTiles_.as<XTile>() + cTiles_[l].first, w, dXp_.as<T>());
+    RSCHOL_LAUNCH_CHECK();
+    compressed_y_kernel<T><<<cBlocks_[l], 256, 0, st>>>(dNodes_.as<SNode<T>>(), dTickF_.as<RowBlock>() + tickOff_[l],
+                                                         sync, dZp_.as<T>(), dXp_.as<T>(), yv, dWu_.as<T>());
     RSCHOL_LAUNCH_CHECK();
     if (l + 1 < cLevels_.size()) {   // the top level's u feeds no one
-      compressed_vz_kernel<T><<<dim3(cVzGrid_[l], cLevels_[l].second), 256, 0, st>>>(
-          dNodes_.as<SNode<T>>(), lvl + cLevels_[l].first, dWu_.as<T>());
+      compressed_vz_kernel<T><<<dim3(cVzGrid_[l], cLevels_[l].second), 256, 0, st>>>(dNodes_.as<SNode<T>>(), lv,
+                                                                                      dWu_.as<T>());
       RSCHOL_LAUNCH_CHECK();
     }
   }
   for (int l = (int)cLevels_.size() - 1; l >= 0; --l) {
+    const int* lv = lvl + cLevels_[l].first;
     compressed_vtx_kernel<T><<<dim3(cMaxCh_[l], cLevels_[l].second), 256, 0, st>>>(
-        dNodes_.as<SNode<T>>(), lvl + cLevels_[l].first, dRows_.as<int>(), sync, dSp_.as<T>(), w, dWu_.as<T>());
+        dNodes_.as<SNode<T>>(), lv, dRows_.as<int>(), sync, dSp_.as<T>(), w, dWu_.as<T>());
     RSCHOL_LAUNCH_CHECK();
-    compressed_backward_blocks<T><<<cBlocks_[l], 256, 0, st>>>(
-        dNodes_.as<SNode<T>>(), dTickB_.as<RowBlock>() + tickOff_[l], sync, 1 + 4 * l + 2, dWu_.as<T>(), w);
+    compressed_g_kernel<T><<<dim3(cRowGrid_[l], cLevels_[l].second), 256, 0, st>>>(dNodes_.as<SNode<T>>(), lv,
+                                                                                     dWu_.as<T>(), yv);
+    RSCHOL_LAUNCH_CHECK();
+    compressed_xtile_kernel<T><<<cTiles_[l].second, 256, 0, st>>>(
+        dNodes_.as<SNode<T>>(), dTiles_.as<XTile>() + cTiles_[l].first, yv, dXp_.as<T>());
+    RSCHOL_LAUNCH_CHECK();
+    compressed_x_reduce<T><<<dim3(cColGrid_[l], cLevels_[l].second), 256, 0, st>>>(dNodes_.as<SNode<T>>(), lv,
+                                                                                     dXp_.as<T>(), w);
     RSCHOL_LAUNCH_CHECK();
   }
   for (int l = (int)iLevels_.size() - 1; l >= 0; --l) {

@@ -12,20 +12,17 @@
 // 128-row chunk of L21): each assembles the children's update vectors
 // (extend-add, fixed order) for the supernode's columns and its chunk, solves
 // with L11 and forms its chunk of the update vector.
-// Compressed levels bottom-up: every compressed supernode is cut into
-// 64-row blocks and each block gets its own thread block, which adds the
-// fixed-order contribution list of its rows (interior-root update vectors,
-// u_c = -V_c z_c of compressed descendants, formed by a launch after each
-// level), accumulates L[b, k] y_k of the
-// earlier row blocks as their ready flags are raised, and multiplies by the
-// inverted 64 x 64 diagonal block.  z = U^T y is reduced in fixed order by
-// the last row block to finish.  Backward mirrors this (s = V^T x_R by a
-// chunked pass, then row blocks in reverse order), then interior levels
-// top-down (chunk blocks form parts of L21^T x_R, the last one to finish
-// sums them in fixed order and solves with L11^T).  Thread blocks take their row block from a ticket counter, so a
-// block only ever waits on blocks that started before it; every wait is
-// bounded and reports through an error word instead of hanging.  No atomics
-// touch the numbers: results are bitwise reproducible.
+// Compressed levels bottom-up: a gather pass adds each row's fixed-order
+// contribution list (interior-root update vectors, u_c = -V_c z_c of
+// compressed descendants, formed by a launch after each level); y = X f with
+// X = L11^{-1}, formed once per factorisation (inverted 64 x 64 diagonal
+// blocks, then recursive doubling X_BA = -X_BB L_BA X_AA with batched GEMMs),
+// so the triangular solve becomes a GEMV with no chain of dependent blocks;
+// z = U^T y is reduced in fixed order by the last row block to finish.
+// Backward mirrors this (s = V^T x_R, g = y - U s, x = X^T g), then interior
+// levels top-down (chunk blocks form parts of L21^T x_R, the last one to
+// finish sums them in fixed order and solves with L11^T).  No atomics touch
+// the numbers: results are bitwise reproducible.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -37,13 +34,15 @@
 namespace rschol {
 
 constexpr int SOLVE_RB = 64;   // rows per compressed row block
+constexpr int XT_COLS = 256;   // columns per tile of X = L11^{-1} in the apply GEMVs
 
 template <class T>
 struct SNode {
   const T* L;       // interior: [L11; L21] panel; compressed: L11 (HODLR expanded)
   const T* V;       // compressed: m x r
   const T* U;       // compressed: n x r
-  const T* Dinv;    // inverted 64 x 64 diagonal blocks of L11 (interior: last one h x h)
+  const T* Dinv;    // interior: inverted 64 x 64 diagonal blocks of L11 (the last one h x h)
+  const T* X;       // compressed: L11^{-1} (n x n, row-major, upper triangle zero)
   int ld, n, m, r, c0;
   int childBegin, childEnd;   // interior: children (range in the child list)
   int nb, nch;                // compressed: row blocks of L11; both: 128-row chunks of V / L21
@@ -55,6 +54,8 @@ struct SNode {
   long long cOff;             // compressed: first of its n+1 contribution-list offsets
   long long zpOff, spOff;     // compressed: partials of z (nb x r) and s (nch x r);
                               // interior (zpOff): partials of L21^T x_R (nch x n)
+  long long zpOff2;           // compressed: tile partials of X f (n x ncb) and X^T g (n x nb)
+  int ncb;                    // compressed: 256-column blocks of X
 };
 
 struct SPull {       // contribution source of a compressed supernode (plan time)
@@ -67,12 +68,22 @@ struct RowBlock {    // one thread block's work: (supernode, row block or chunk)
   int node, b;
 };
 
+struct XTile {       // a 64 x 256 tile of X = L11^{-1} (row block ib, column block jb)
+  int node, ib, jb;
+};
+
 template <class T>
 struct DinvTask {    // invert one lower-triangular diagonal block (h x h, h <= 64)
   const T* L;
   int ld, h;
-  int pad;           // D is pad x pad (64 for compressed supernodes, h for interior ones)
-  T* D;              // row-major, ld pad, zero outside the h x h lower triangle
+  int pad;           // D is pad x pad, zero outside the h x h lower triangle
+  int ldD;           // row stride of D
+  T* D;
+};
+
+struct XStep {       // one batched GEMM launch of the compressed L11^{-1} computation
+  long long off;
+  int count, tiles;
 };
 
 template <class T>
@@ -95,13 +106,20 @@ class SolveEngine {
   FactorEngine<T>& F_;
   std::vector<SNode<T>> nodes_;
   DevBuf dNodes_, dRows_, dRel_, dChild_, dWu_, dW_, dLevelNodes_, dCStart_, dCEnt_;
-  DevBuf dDinv_, dDinvTasks_, dZp_, dSp_, dIp_, dYi_, dSync_, dTickF_, dTickB_, dIWork_;
+  DevBuf dDinv_, dDinvTasks_, dZp_, dSp_, dIp_, dYi_, dSync_, dTickF_, dIWork_;
+  DevBuf dX_, dT1_, dXGemm_;          // compressed L11^{-1}, its temporaries and GEMM tasks
+  DevBuf dXp_, dTiles_;               // tile partials of the X products, tile lists
+  std::vector<std::pair<long long, int>> cTiles_;   // per compressed level: (offset, count) of tiles
+  std::vector<XStep> xSteps_;
   int nDinv_ = 0;
   int syncInts_ = 0;
   std::vector<long long> tickOff_;   // per compressed level: first ticket entry
   std::vector<int> cBlocks_;         // per compressed level: row blocks
   std::vector<int> cMaxCh_;          // per compressed level: most V chunks of a node
   std::vector<int> cVzGrid_;         // per compressed level: row blocks of the u = -V z launch
+  std::vector<int> cRowGrid_;        // per compressed level: 8-row blocks of the largest supernode
+  std::vector<int> cColGrid_;        // per compressed level: 256-column blocks of the largest supernode
+  void plan_inverse(const std::vector<long long>& xOff);   // GEMM schedule of X = L11^{-1}
   std::vector<std::pair<long long, int>> iLevels_;  // (offset, count) into the interior work list
   std::vector<std::pair<long long, int>> cLevels_;  // (offset, count) into the level node list
   std::vector<size_t> smemIF_, smemIB_;
