@@ -16,6 +16,38 @@ __device__ __forceinline__ V warp_sum(V v) {
   return v;
 }
 
+// out[k] = sum_{i < rows} M[i][k] v[i] (v == nullptr: v[i] = 1, and M was
+// written by other blocks of this launch, so its loads bypass L1) for k < r,
+// M row-major with leading dimension ld.  Eight warps split the rows, lanes
+// run along k (coalesced), and the eight warp partials are added in a fixed
+// order.  blockDim.x == 256; red: 8 x 256 shared; every thread must call it.
+template <class T>
+__device__ void rows_t_gemv(const T* __restrict__ M, int ld, int rows, int r, const T* v, T* out, T (*red)[256]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k0 = 0; k0 < r; k0 += 256) {
+    T acc[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[c] = T(0);
+    for (int i = warp; i < rows; i += 8) {
+      const T vi = v ? v[i] : T(1);
+      const T* row = M + (size_t)i * ld + k0;
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (k0 + lane + 32 * c < r) acc[c] += (v ? row[lane + 32 * c] : __ldcg(row + lane + 32 * c)) * vi;
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) red[warp][lane + 32 * c] = acc[c];
+    __syncthreads();
+    if (k0 + (int)threadIdx.x < r) {
+      T s = T(0);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s += red[q][threadIdx.x];
+      out[k0 + threadIdx.x] = s;
+    }
+    __syncthreads();
+  }
+}
+
 // f := L^{-1} f with the inverted 64 x 64 diagonal blocks of L (block b:
 // h_b x h_b row-major at D + 4096 b; only the last block can be smaller).
 // f (n) and t (64) in shared memory.  A warp per row: loads coalesced along
@@ -303,6 +335,7 @@ __global__ void __launch_bounds__(256) compressed_y_kernel(const SNode<T>* __res
                                                            T* __restrict__ zpart, const T* __restrict__ ypart,
                                                            T* __restrict__ yv, T* __restrict__ wu) {
   __shared__ T yb[SOLVE_RB];
+  __shared__ T red[8][256];
   __shared__ int sLast;
   const RowBlock wk = work[blockIdx.x];
   const SNode<T>& nd = nodes[wk.node];
@@ -320,12 +353,7 @@ __global__ void __launch_bounds__(256) compressed_y_kernel(const SNode<T>* __res
   }
   __syncthreads();
   const int r = nd.r;
-  for (int k = threadIdx.x; k < r; k += blockDim.x) {
-    T s = T(0);
-    for (int i = 0; i < h; ++i) s += nd.U[(size_t)(i0 + i) * r + k] * yb[i];
-    zpart[nd.zpOff + (size_t)wk.b * r + k] = s;
-  }
-  __syncthreads();
+  rows_t_gemv<T>(nd.U + (size_t)i0 * r, r, h, r, yb, zpart + nd.zpOff + (size_t)wk.b * r, red);
   int* done = sync + nd.syncOff;
   if (threadIdx.x == 0) {
     __threadfence();
@@ -334,11 +362,7 @@ __global__ void __launch_bounds__(256) compressed_y_kernel(const SNode<T>* __res
   }
   __syncthreads();
   if (!sLast) return;
-  for (int k = threadIdx.x; k < r; k += blockDim.x) {
-    T s = T(0);
-    for (int b = 0; b < nd.nb; ++b) s += __ldcg(zpart + nd.zpOff + (size_t)b * r + k);
-    wu[nd.wuOff + k] = s;
-  }
+  rows_t_gemv<T>(zpart + nd.zpOff, r, nd.nb, r, nullptr, wu + nd.wuOff, red);
   if (threadIdx.x == 0) *done = 0;
 }
 
@@ -384,6 +408,7 @@ __global__ void __launch_bounds__(256) compressed_vtx_kernel(const SNode<T>* __r
                                                              int* __restrict__ sync, T* __restrict__ spart,
                                                              const T* __restrict__ w, T* __restrict__ sv) {
   __shared__ T xs[128];
+  __shared__ T red[8][256];
   __shared__ int sLast;
   const SNode<T>& nd = nodes[lvl[blockIdx.y]];
   const int ch = blockIdx.x;
@@ -392,12 +417,7 @@ __global__ void __launch_bounds__(256) compressed_vtx_kernel(const SNode<T>* __r
   const int* rw = rows + nd.rowsOff + a0;
   for (int a = threadIdx.x; a < ah; a += blockDim.x) xs[a] = w[rw[a]];
   __syncthreads();
-  for (int k = threadIdx.x; k < r; k += blockDim.x) {
-    T s = T(0);
-    for (int a = 0; a < ah; ++a) s += nd.V[(size_t)(a0 + a) * r + k] * xs[a];
-    spart[nd.spOff + (size_t)ch * r + k] = s;
-  }
-  __syncthreads();
+  rows_t_gemv<T>(nd.V + (size_t)a0 * r, r, ah, r, xs, spart + nd.spOff + (size_t)ch * r, red);
   int* done = sync + nd.syncOff + 1;
   if (threadIdx.x == 0) {
     __threadfence();
@@ -406,11 +426,7 @@ __global__ void __launch_bounds__(256) compressed_vtx_kernel(const SNode<T>* __r
   }
   __syncthreads();
   if (!sLast) return;
-  for (int k = threadIdx.x; k < r; k += blockDim.x) {
-    T s = T(0);
-    for (int c = 0; c < nd.nch; ++c) s += __ldcg(spart + nd.spOff + (size_t)c * r + k);
-    sv[nd.wuOff + r + k] = s;
-  }
+  rows_t_gemv<T>(spart + nd.spOff, r, nd.nch, r, nullptr, sv + nd.wuOff + r, red);
   if (threadIdx.x == 0) *done = 0;
 }
 
