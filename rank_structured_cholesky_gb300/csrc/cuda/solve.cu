@@ -106,26 +106,83 @@ __device__ void trsv_dinv_t(const T* __restrict__ L, int ld, int n, const T* __r
   }
 }
 
-// Interior supernodes: one thread block per (supernode, 128-row chunk of its
-// off-diagonal rows).  Every chunk block assembles and solves the supernode's
-// own n columns (n is small); chunk 0 stores y.
+constexpr int SPIN_LIMIT = 1 << 22;   // polls (with a short sleep) before a wait gives up
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
+
+// Warp-uniform bounded wait for *p >= target.  Returns false when the wait
+// gave up (after SPIN_LIMIT polls, or as soon as another block reported an
+// error); the error word is then set.
+__device__ __forceinline__ bool wait_geq(const int* p, int target, int* err) {
+  if (__all_sync(FULL, ld_acquire(p) >= target)) return true;
+  for (int it = 1; it <= SPIN_LIMIT; ++it) {
+    __nanosleep(64);
+    if (__all_sync(FULL, ld_acquire(p) >= target)) return true;
+    if ((it & 63) == 0 && __any_sync(FULL, ld_volatile(err) != 0)) return false;
+  }
+  if ((threadIdx.x & 31) == 0) atomicExch(err, 1);
+  return false;
+}
+
+// Every block of a ticketed launch calls this once when it is done; the last
+// one resets the ticket and completion counters for the next launch.
+__device__ __forceinline__ void launch_done(int* tick, int* done) {
+  __syncthreads();
+  if (threadIdx.x == 0 && atomicAdd(done, 1) == (int)gridDim.x - 1) {
+    atomicExch(tick, 0);
+    atomicExch(done, 0);
+  }
+}
+
+// Interior supernodes: all levels in one launch per direction.  A block takes
+// the next (supernode, 128-row chunk of its off-diagonal rows) from a ticket
+// counter, in level order, so it only waits on blocks that started before it:
+// forward, on the chunk blocks of the supernode's children (per-supernode
+// completion counters that grow by one per chunk and apply); backward, on
+// the solve of its interior parent (a flag set to the apply's epoch).  Every
+// chunk block assembles and solves the supernode's own n columns (n is small);
+// chunk 0 stores y.
 constexpr int ICH = 128;
+constexpr int SYNC_TICK_F = 1, SYNC_DONE_F = 2, SYNC_TICK_B = 3, SYNC_DONE_B = 4, SYNC_GLOBAL = 5;
 
 template <class T>
 __global__ void __launch_bounds__(256) interior_forward_chunks(const SNode<T>* __restrict__ nodes,
                                                                const RowBlock* __restrict__ work,
                                                                const int* __restrict__ rel,
                                                                const int* __restrict__ child,
+                                                               int* __restrict__ sync, int epoch,
                                                                const T* __restrict__ w, T* __restrict__ yout,
                                                                T* __restrict__ wu) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* f = reinterpret_cast<T*>(smraw);
   __shared__ T tb[64];
-  const RowBlock wk = work[blockIdx.x];
+  __shared__ int sTicket;
+  int* err = sync;
+  if (threadIdx.x == 0) sTicket = atomicAdd(&sync[SYNC_TICK_F], 1);
+  __syncthreads();
+  if (sTicket >= (int)gridDim.x) {   // counters not reset: report, touch nothing
+    if (threadIdx.x == 0) atomicExch(err, 2);
+    return;
+  }
+  const RowBlock wk = work[sTicket];
   const SNode<T>& nd = nodes[wk.node];
   const int n = nd.n, a0 = wk.b * ICH, a1 = min(nd.m, a0 + ICH);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T* wud = wu + nd.wuOff;
+  if (warp == 0)   // every chunk block of every child has stored its update rows
+    for (int c = nd.childBegin; c < nd.childEnd; ++c) {
+      const SNode<T>& cn = nodes[child[c]];
+      if (!wait_geq(sync + cn.syncOff + 1, epoch * max(1, cn.nch), err)) break;
+    }
+  __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x) f[i] = w[nd.c0 + i];
   for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) wud[a] = T(0);
   __syncthreads();
@@ -136,8 +193,8 @@ __global__ void __launch_bounds__(256) interior_forward_chunks(const SNode<T>* _
     const int* rl = rel + cn.relOff;
     for (int a = threadIdx.x; a < cn.m; a += blockDim.x) {
       const int t = rl[a];
-      if (t < n) f[t] += wuc[a];
-      else if (t - n >= a0 && t - n < a1) wud[t - n] += wuc[a];
+      if (t < n) f[t] += __ldcg(wuc + a);
+      else if (t - n >= a0 && t - n < a1) wud[t - n] += __ldcg(wuc + a);
     }
     __syncthreads();
   }
@@ -161,6 +218,12 @@ __global__ void __launch_bounds__(256) interior_forward_chunks(const SNode<T>* _
       if (lane == 0 && a + q < a1) wud[a + q] -= v;
     }
   }
+  __syncthreads();
+  if (threadIdx.x == 0) {   // this chunk's rows of the update vector are final
+    __threadfence();
+    atomicAdd(sync + nd.syncOff + 1, 1);
+  }
+  launch_done(&sync[SYNC_TICK_F], &sync[SYNC_DONE_F]);
 }
 
 // Backward: each chunk block forms its part of L21^T x_R; the last chunk
@@ -170,14 +233,25 @@ template <class T>
 __global__ void __launch_bounds__(256) interior_backward_chunks(const SNode<T>* __restrict__ nodes,
                                                                 const RowBlock* __restrict__ work,
                                                                 const int* __restrict__ rows,
-                                                                int* __restrict__ sync, T* __restrict__ ipart,
-                                                                const T* __restrict__ yin, T* __restrict__ w) {
+                                                                int* __restrict__ sync, int epoch,
+                                                                T* __restrict__ ipart, const T* __restrict__ yin,
+                                                                T* __restrict__ w) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ T tb[64];
   __shared__ T red[8][256];
-  __shared__ int sLast;
-  const RowBlock wk = work[blockIdx.x];
+  __shared__ int sLast, sTicket;
+  int* err = sync;
+  if (threadIdx.x == 0) sTicket = atomicAdd(&sync[SYNC_TICK_B], 1);
+  __syncthreads();
+  if (sTicket >= (int)gridDim.x) {   // counters not reset: report, touch nothing
+    if (threadIdx.x == 0) atomicExch(err, 2);
+    return;
+  }
+  const RowBlock wk = work[sTicket];
   const SNode<T>& nd = nodes[wk.node];
+  if (nd.parentI >= 0 && (threadIdx.x >> 5) == 0)   // the parent (and so every ancestor) is solved
+    wait_geq(sync + nodes[nd.parentI].syncOff + 2, epoch, err);
+  __syncthreads();
   const int n = nd.n, a0 = wk.b * ICH, a1 = min(nd.m, a0 + ICH);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T* f = reinterpret_cast<T*>(smraw);   // n values
@@ -185,7 +259,7 @@ __global__ void __launch_bounds__(256) interior_backward_chunks(const SNode<T>* 
   const int nch = (nd.m + ICH - 1) / ICH;
   if (nch > 0) {
     const int* rw = rows + nd.rowsOff;
-    for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) xr[a - a0] = w[rw[a]];
+    for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) xr[a - a0] = __ldcg(w + rw[a]);
     __syncthreads();
     // part[j] = sum_{a in chunk} L21[a][j] x_a: warp w takes rows w, w+8, ...
     // (lanes along the row), then the 8 warp partials are summed in order
@@ -219,7 +293,10 @@ __global__ void __launch_bounds__(256) interior_backward_chunks(const SNode<T>* 
       __threadfence();
     }
     __syncthreads();
-    if (!sLast) return;
+    if (!sLast) {
+      launch_done(&sync[SYNC_TICK_B], &sync[SYNC_DONE_B]);
+      return;
+    }
   }
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     T t = T(0);
@@ -229,25 +306,18 @@ __global__ void __launch_bounds__(256) interior_backward_chunks(const SNode<T>* 
   __syncthreads();
   trsv_dinv_t<T>(nd.L, nd.ld, n, nd.Dinv, f, tb, reinterpret_cast<T(*)[64]>(&red[0][0]));
   for (int i = threadIdx.x; i < n; i += blockDim.x) w[nd.c0 + i] = f[i];
-  if (threadIdx.x == 0 && nch > 0) sync[nd.syncOff] = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (nch > 0) sync[nd.syncOff] = 0;
+    st_release(sync + nd.syncOff + 2, epoch);   // x of this supernode is final
+  }
+  launch_done(&sync[SYNC_TICK_B], &sync[SYNC_DONE_B]);
 }
 
 // ---------------------------------------------------------------------------
 // Compressed supernodes.  X = L11^{-1} is formed once per factorisation, so
 // the triangular solves are GEMVs: every 64-row (or 64-column) block of a
 // supernode is an independent thread block.
-
-constexpr int SPIN_LIMIT = 1 << 22;   // polls (with a short sleep) before a wait gives up
-
-__device__ __forceinline__ int ld_acquire(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release(int* p, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
 
 // Right-hand side of every compressed supernode of a level: w[c0 + i] plus
 // the fixed-order contribution list of row i (a warp per row, lanes over the
@@ -491,7 +561,7 @@ void SolveEngine<T>::plan() {
   nodes_.assign(nn, SNode<T>{});
   std::vector<int> rowsAll, rel, child, lvlNodes;
   long long wuCur = 0, dinvCur = 0, zpCur = 0, spCur = 0, ipCur = 0, xCur = 0, xpCur = 0;
-  int syncCur = 1;   // error word
+  int syncCur = SYNC_GLOBAL;   // error word, ticket and completion counters of the interior launches
   std::vector<long long> xOff(nn, -1);
   std::vector<long long> xTaskOff;   // per compressed diagonal-block task: offset in the X arena
   bytesPerApply_ = 0;
@@ -514,7 +584,8 @@ void SolveEngine<T>::plan() {
       wuCur += nd.m();
       sn.nch = (nd.m() + ICH - 1) / ICH;
       sn.syncOff = syncCur;
-      syncCur += 1;
+      syncCur += 3;   // backward chunk counter, forward completion count, backward solved epoch
+      sn.parentI = (nd.parent >= 0 && !S.nodes[nd.parent].compressed) ? nd.parent : -1;
       sn.zpOff = ipCur;
       ipCur += (long long)sn.nch * nd.n;
       // inverted 64 x 64 diagonal blocks, the last one stored h x h
@@ -619,6 +690,11 @@ void SolveEngine<T>::plan() {
     smemIF_.push_back(f);
     smemIB_.push_back(b);
   }
+  // backward order: the levels top-down
+  std::vector<RowBlock> iworkB;
+  for (int l = (int)iLevels_.size() - 1; l >= 0; --l)
+    iworkB.insert(iworkB.end(), iwork.begin() + iLevels_[l].first,
+                  iwork.begin() + iLevels_[l].first + iLevels_[l].second);
   for (size_t v : smemIB_)
     if (v > 200 * 1024) throw std::runtime_error("interior front too large for the shared-memory solve");
   // compressed levels: (supernode, 64-row block) work lists
@@ -712,6 +788,13 @@ void SolveEngine<T>::plan() {
   up(dChild_, child.data(), child.size() * sizeof(int));
   up(dLevelNodes_, lvlNodes.data(), lvlNodes.size() * sizeof(int));
   up(dIWork_, iwork.data(), iwork.size() * sizeof(RowBlock));
+  up(dIWorkB_, iworkB.data(), iworkB.size() * sizeof(RowBlock));
+  nIWork_ = (int)iwork.size();
+  smemIFmax_ = 8;
+  smemIBmax_ = 8;
+  for (size_t v : smemIF_) smemIFmax_ = std::max(smemIFmax_, v);
+  for (size_t v : smemIB_) smemIBmax_ = std::max(smemIBmax_, v);
+  epoch_ = 0;
   up(dTickF_, tickF.data(), tickF.size() * sizeof(RowBlock));
   up(dTiles_, xtiles.data(), xtiles.size() * sizeof(XTile));
   up(dDinvTasks_, dinvTasks.data(), dinvTasks.size() * sizeof(DinvTask<T>));
@@ -723,7 +806,7 @@ void SolveEngine<T>::plan() {
   const int maxSmem = 200 * 1024;
   RSCHOL_CUDA(cudaFuncSetAttribute(interior_forward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
   RSCHOL_CUDA(cudaFuncSetAttribute(interior_backward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
-  launchesPerApply_ = 2 * (long long)iLevels_.size() + 8 * (long long)cLevels_.size() - (cLevels_.empty() ? 0 : 1) +
+  launchesPerApply_ = (iLevels_.empty() ? 0 : 2) + 8 * (long long)cLevels_.size() - (cLevels_.empty() ? 0 : 1) +
                       (std::is_same<T, double>::value ? 0 : 2);
   bytesPerApply_ += 8.0 * 4 * S.n;
 }
@@ -845,9 +928,10 @@ int SolveEngine<T>::take_error(cudaStream_t st) {
   RSCHOL_CUDA(cudaMemcpyAsync(&e, dSync_.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   RSCHOL_CUDA(cudaStreamSynchronize(st));
   if (e) {
-    // a wait gave up: counters and flags are in an unknown state
+    // a wait gave up: counters and flags are in an unknown state; start over
     RSCHOL_CUDA(cudaMemsetAsync(dSync_.p, 0, sizeof(int) * syncInts_, st));
     RSCHOL_CUDA(cudaStreamSynchronize(st));
+    epoch_ = 0;
   }
   return e;
 }
@@ -863,11 +947,14 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
   }
   const int* lvl = dLevelNodes_.as<int>();
   int* sync = dSync_.as<int>();
-  const RowBlock* iwork = dIWork_.as<RowBlock>();
-  for (size_t l = 0; l < iLevels_.size(); ++l) {
-    interior_forward_chunks<T><<<iLevels_[l].second, 256, smemIF_[l], st>>>(
-        dNodes_.as<SNode<T>>(), iwork + iLevels_[l].first, dRel_.as<int>(), dChild_.as<int>(), w, dYi_.as<T>(),
-        dWu_.as<T>());
+  if (++epoch_ >= (1 << 24)) {   // keep epoch x chunks far from overflow
+    RSCHOL_CUDA(cudaMemsetAsync(dSync_.p, 0, sizeof(int) * syncInts_, st));
+    epoch_ = 1;
+  }
+  if (nIWork_ > 0) {
+    interior_forward_chunks<T><<<nIWork_, 256, smemIFmax_, st>>>(dNodes_.as<SNode<T>>(), dIWork_.as<RowBlock>(),
+                                                                  dRel_.as<int>(), dChild_.as<int>(), sync, epoch_, w,
+                                                                  dYi_.as<T>(), dWu_.as<T>());
     RSCHOL_LAUNCH_CHECK();
   }
   T* yv = dYi_.as<T>();
@@ -903,9 +990,10 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
                                                                                      dXp_.as<T>(), w);
     RSCHOL_LAUNCH_CHECK();
   }
-  for (int l = (int)iLevels_.size() - 1; l >= 0; --l) {
-    interior_backward_chunks<T><<<iLevels_[l].second, 256, smemIB_[l], st>>>(
-        dNodes_.as<SNode<T>>(), iwork + iLevels_[l].first, dRows_.as<int>(), sync, dIp_.as<T>(), dYi_.as<T>(), w);
+  if (nIWork_ > 0) {
+    interior_backward_chunks<T><<<nIWork_, 256, smemIBmax_, st>>>(dNodes_.as<SNode<T>>(), dIWorkB_.as<RowBlock>(),
+                                                                   dRows_.as<int>(), sync, epoch_, dIp_.as<T>(),
+                                                                   dYi_.as<T>(), w);
     RSCHOL_LAUNCH_CHECK();
   }
   if (!std::is_same<T, double>::value) {

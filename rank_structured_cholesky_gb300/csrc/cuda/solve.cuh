@@ -8,10 +8,11 @@
 // A_{rest,I} L_I^{-T} L_I^{-1} are stored explicitly), compressed nodes use
 // the (HODLR-expanded) dense L11 and the V U^T off-diagonal.
 //
-// Forward: interior levels bottom-up, one thread block per (supernode,
-// 128-row chunk of L21): each assembles the children's update vectors
-// (extend-add, fixed order) for the supernode's columns and its chunk, solves
-// with L11 and forms its chunk of the update vector.
+// Forward: interior supernodes in one launch, one thread block per
+// (supernode, 128-row chunk of L21) taken in level order from a ticket
+// counter; each waits (bounded) for its children's chunk blocks, assembles
+// their update vectors (extend-add, fixed order) for the supernode's columns
+// and its chunk, solves with L11 and forms its chunk of the update vector.
 // Compressed levels bottom-up: a gather pass adds each row's fixed-order
 // contribution list (interior-root update vectors, u_c = -V_c z_c of
 // compressed descendants, formed by a launch after each level); y = X f with
@@ -19,9 +20,10 @@
 // blocks, then recursive doubling X_BA = -X_BB L_BA X_AA with batched GEMMs),
 // so the triangular solve becomes a GEMV with no chain of dependent blocks;
 // z = U^T y is reduced in fixed order by the last row block to finish.
-// Backward mirrors this (s = V^T x_R, g = y - U s, x = X^T g), then interior
-// levels top-down (chunk blocks form parts of L21^T x_R, the last one to
-// finish sums them in fixed order and solves with L11^T).  No atomics touch
+// Backward mirrors this (s = V^T x_R, g = y - U s, x = X^T g), then the
+// interior supernodes top-down in one launch (each waits for its parent's
+// solve; chunk blocks form parts of L21^T x_R, the last one to finish sums
+// them in fixed order and solves with L11^T).  No atomics touch
 // the numbers: results are bitwise reproducible.
 #pragma once
 #include <cuda_runtime.h>
@@ -46,8 +48,9 @@ struct SNode {
   int ld, n, m, r, c0;
   int childBegin, childEnd;   // interior: children (range in the child list)
   int nb, nch;                // compressed: row blocks of L11; both: 128-row chunks of V / L21
-  int syncOff;                // compressed: nb ready flags, then 3 completion counters;
-                              // interior: 1 completion counter
+  int syncOff;                // compressed: 2 completion counters; interior: backward chunk
+                              // counter, forward completion count, backward solved epoch
+  int parentI;                // interior: parent if it is interior, else -1
   long long rowsOff;          // rows of this node in the row arena
   long long wuOff;            // interior: update vector; compressed: z (r), s (r), u = -V z (m)
   long long relOff;           // interior: target index in the parent front of each row
@@ -106,7 +109,10 @@ class SolveEngine {
   FactorEngine<T>& F_;
   std::vector<SNode<T>> nodes_;
   DevBuf dNodes_, dRows_, dRel_, dChild_, dWu_, dW_, dLevelNodes_, dCStart_, dCEnt_;
-  DevBuf dDinv_, dDinvTasks_, dZp_, dSp_, dIp_, dYi_, dSync_, dTickF_, dIWork_;
+  DevBuf dDinv_, dDinvTasks_, dZp_, dSp_, dIp_, dYi_, dSync_, dTickF_, dIWork_, dIWorkB_;
+  int nIWork_ = 0;
+  size_t smemIFmax_ = 8, smemIBmax_ = 8;
+  int epoch_ = 0;                     // apply counter: the interior completion targets
   DevBuf dX_, dT1_, dXGemm_;          // compressed L11^{-1}, its temporaries and GEMM tasks
   DevBuf dXp_, dTiles_;               // tile partials of the X products, tile lists
   std::vector<std::pair<long long, int>> cTiles_;   // per compressed level: (offset, count) of tiles
