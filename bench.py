@@ -5,7 +5,9 @@ values resident on the device) followed by one PCG solve to ||r||/||b|| <=
 1e-8.  `value` is solves per second over the K timed steps (whole job: N
 independent replicas under torchrun, max time over ranks).  `e2e` is the same
 step through the C ABI with host buffers (values and right-hand side copied
-in, solution copied out inside the timed region).
+in, solution copied out inside the timed region).  The default precision is
+mixed (FP32 factor and apply, FP64 PCG); the plain FP64 GPU path is timed on
+the same workload in the same run (`plain_fp64`).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2]
                     [--precision fp64|mixed] [--impl ours|reference]
@@ -181,6 +183,73 @@ def run_reference(args):
     return 0
 
 
+def traffic_from_profiles(kernel):
+    """dram bytes per launch of `kernel` from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "%s_c2.md" % kernel)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def timed_solves(lib, rs, torch, prob, precision, device, local, steps, warmup, dist, step_timing):
+    """K timed factor + PCG steps (device-resident inputs) for one precision."""
+    ctx = rs.Context(precision=precision, device=local)
+    t0 = time.perf_counter()
+    F = rs.GpuFactor(ctx, prob.colptr, prob.rowind, prob.vals, prob.xyz)
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(lib.rschol_stream(ctx.h), device=device)
+    nrhs = prob.nrhs
+    d_vals = torch.from_numpy(prob.vals).to(device)
+    d_b = torch.from_numpy(np.ascontiguousarray(prob.rhs[:nrhs])).to(device)
+    d_x = torch.zeros_like(d_b)
+    infos = (rs.PcgInfo * nrhs)()
+    torch.cuda.synchronize()
+
+    def refactor():
+        st = lib.rschol_refactor_device(F.h, d_vals.data_ptr())
+        if st != 0:
+            raise rs.RscholError(st, ctx.last_error())
+
+    def pcg():
+        st = lib.rschol_pcg_device(F.h, d_b.data_ptr(), d_x.data_ptr(), nrhs, 1e-8, 10000, infos)
+        if st not in (0, 5):
+            raise rs.RscholError(st, ctx.last_error())
+
+    for _ in range(warmup):
+        refactor()
+        pcg()
+    torch.cuda.synchronize()
+    barrier(dist)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * steps + 1)]
+    counters = np.zeros(24)
+    if step_timing:
+        lib.rschol_step_timing(F.h, 1, None)
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for k in range(steps):
+            refactor()
+            ev[2 * k + 1].record(stream)
+            pcg()
+            ev[2 * k + 2].record(stream)
+        torch.cuda.synchronize()
+    if step_timing:
+        lib.rschol_step_timing(F.h, 0, counters.ctypes.data)
+    barrier(dist)
+    step_ms = [ev[2 * k].elapsed_time(ev[2 * k + 2]) for k in range(steps)]
+    factor_ms = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(steps)]
+    pcg_ms = [ev[2 * k + 1].elapsed_time(ev[2 * k + 2]) for k in range(steps)]
+    total_s = reduce_max(dist, ev[0].elapsed_time(ev[2 * steps]) / 1e3, device)
+    return dict(ctx=ctx, F=F, stream=stream, d_b=d_b, infos=infos, setup_s=setup_s, step_ms=step_ms,
+                factor_ms=factor_ms, pcg_ms=pcg_ms, total_s=total_s, clocks=clocks.summary(), counters=counters,
+                iterations=[infos[k].iterations for k in range(nrhs)],
+                true_residual=max(infos[k].true_residual for k in range(nrhs)))
+
+
 def run_ours(args):
     import torch
     import rank_structured_cholesky_gb300 as rs
@@ -191,43 +260,24 @@ def run_ours(args):
     device = torch.device("cuda", local)
     lib = rs.load_library()
     prob = make_problem(args.config)
-    params = dict(precision=args.precision, device=local)
-    ctx = rs.Context(**params)
-    t0 = time.perf_counter()
-    F = rs.GpuFactor(ctx, prob.colptr, prob.rowind, prob.vals, prob.xyz)
-    setup_s = time.perf_counter() - t0
-    stream = torch.cuda.ExternalStream(lib.rschol_stream(ctx.h), device=device)
     n, nrhs = prob.n, prob.nrhs
-    d_vals = torch.from_numpy(prob.vals).to(device)
-    d_b = torch.from_numpy(np.ascontiguousarray(prob.rhs[:nrhs])).to(device)
-    d_x = torch.zeros_like(d_b)
-    infos = (rs.PcgInfo * nrhs)()
 
-    def step_device():
-        st = lib.rschol_refactor_device(F.h, d_vals.data_ptr())
-        if st != 0:
-            raise rs.RscholError(st, ctx.last_error())
-        st = lib.rschol_pcg_device(F.h, d_b.data_ptr(), d_x.data_ptr(), nrhs, 1e-8, 10000, infos)
-        if st not in (0, 5):
-            raise rs.RscholError(st, ctx.last_error())
-
-    h_vals = prob.vals
-    h_b = np.ascontiguousarray(prob.rhs[:nrhs])
-    h_x = np.zeros_like(h_b)
-
-    def step_e2e():
-        st = lib.rschol_refactor(F.h, rs._dp(h_vals))
-        if st != 0:
-            raise rs.RscholError(st, ctx.last_error())
-        st = lib.rschol_pcg(F.h, rs._dp(h_b), rs._dp(h_x), nrhs, 1e-8, 10000, infos)
-        if st not in (0, 5):
-            raise rs.RscholError(st, ctx.last_error())
-
-    for _ in range(args.warmup):
-        step_device()
-    torch.cuda.synchronize()
     if args.profile:
         # ncu --profile-from-start off: capture exactly the K steps
+        ctx = rs.Context(precision=args.precision, device=local)
+        F = rs.GpuFactor(ctx, prob.colptr, prob.rowind, prob.vals, prob.xyz)
+        d_vals = torch.from_numpy(prob.vals).to(device)
+        d_b = torch.from_numpy(np.ascontiguousarray(prob.rhs[:nrhs])).to(device)
+        d_x = torch.zeros_like(d_b)
+        infos = (rs.PcgInfo * nrhs)()
+
+        def step_device():
+            lib.rschol_refactor_device(F.h, d_vals.data_ptr())
+            lib.rschol_pcg_device(F.h, d_b.data_ptr(), d_x.data_ptr(), nrhs, 1e-8, 10000, infos)
+
+        for _ in range(args.warmup):
+            step_device()
+        torch.cuda.synchronize()
         torch.cuda.profiler.start()
         for _ in range(args.steps):
             step_device()
@@ -237,25 +287,26 @@ def run_ours(args):
             print(json.dumps({"profiled_steps": args.steps, "config": args.config, "precision": args.precision,
                               "iterations": [infos[k].iterations for k in range(nrhs)]}), flush=True)
         return 0
-    barrier(dist)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    with ClockSampler(local) as clocks:
-        torch.cuda.synchronize()
-        ev[0].record(stream)
-        for k in range(args.steps):
-            step_device()
-            ev[k + 1].record(stream)
-        torch.cuda.synchronize()
-    barrier(dist)
-    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
-    total_s = ev[0].elapsed_time(ev[args.steps]) / 1e3
-    total_s = reduce_max(dist, total_s, device)
-    iters = [infos[k].iterations for k in range(nrhs)]
-    resid = max(infos[k].true_residual for k in range(nrhs))
+
+    main = timed_solves(lib, rs, torch, prob, args.precision, device, local, args.steps, args.warmup, dist, True)
+    F, ctx, stream = main["F"], main["ctx"], main["stream"]
     stats = F.stats()
     desc = F.describe()
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers (copies inside the timed region)
+    h_vals = prob.vals
+    h_b = np.ascontiguousarray(prob.rhs[:nrhs])
+    h_x = np.zeros_like(h_b)
+    infos = (rs.PcgInfo * nrhs)()
+
+    def step_e2e():
+        st = lib.rschol_refactor(F.h, rs._dp(h_vals))
+        if st != 0:
+            raise rs.RscholError(st, ctx.last_error())
+        st = lib.rschol_pcg(F.h, rs._dp(h_b), rs._dp(h_x), nrhs, 1e-8, 10000, infos)
+        if st not in (0, 5):
+            raise rs.RscholError(st, ctx.last_error())
+
     for _ in range(max(1, args.warmup // 2)):
         step_e2e()
     torch.cuda.synchronize()
@@ -268,11 +319,24 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_s = reduce_max(dist, e0.elapsed_time(e1) / 1e3, device)
 
-    # phase breakdown and the roofline of the dominant kernel family
-    phase = profile_phases(lib, F, ctx, stream, d_b, nrhs, torch)
+    # phase breakdown (apply, SpMV) and launch counts
+    phase = profile_phases(lib, F, ctx, stream, main["d_b"], nrhs, torch)
+
+    # the plain FP64 path on the same workload, for the mixed-precision speed-up
+    plain = None
+    if args.precision == "mixed" and not args.no_fp64_plain:
+        pf = timed_solves(lib, rs, torch, prob, "fp64", device, local, args.steps, args.warmup, dist, False)
+        plain = {"value": world * args.steps / pf["total_s"], "unit": "solves/s",
+                 "ms_per_step": 1e3 * pf["total_s"] / args.steps,
+                 "factor_ms": statistics.median(pf["factor_ms"]), "pcg_ms": statistics.median(pf["pcg_ms"]),
+                 "p50_ms": statistics.median(pf["step_ms"]), "p99_ms": float(np.percentile(pf["step_ms"], 99)),
+                 "iterations": pf["iterations"] if nrhs > 1 else pf["iterations"][0],
+                 "true_residual": pf["true_residual"], "clocks": pf["clocks"]}
+        del pf
+
     hbm, bf16, src = peaks()
-    line = None
     if rank == 0:
+        total_s = main["total_s"]
         value = world * args.steps / total_s
         cpu = None
         if not args.no_cpu_baseline and world == 1:
@@ -283,10 +347,27 @@ def run_ours(args):
                    "sample": "one full %s solve (symbolic + FP64 factor + PCG to 1e-8, %d iterations) with the "
                              "CPU oracle, threaded BLAS" % (args.config, res["iterations"]),
                    "factor_s": res["factor_s"], "pcg_s": res["pcg_s"], "iterations": res["iterations"]}
-        roof = phase["roofline"]
-        roof["peak"] = hbm if roof["bound"] == "hbm" else bf16
-        roof["frac"] = roof["achieved"] / roof["peak"]
-        roof["peak_source"] = src
+        # roofline of the dominant kernel family (the factor's GEMMs), timed
+        # with CUDA events around every GEMM launch of the timed steps
+        c = main["counters"]
+        gemm_ms, gemm_launch, gemm_flops = c[0], c[1], c[2]
+        step_total_ms = sum(main["step_ms"])
+        achieved = gemm_flops / (gemm_ms * 1e-3) / 1e12 if gemm_ms > 0 else 0.0
+        roof = {"bound": "tensor", "kernel": "factor GEMMs (gemm_kernel SIMT and gemm_tc_kernel tcgen05)",
+                "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
+                "traffic": traffic_from_profiles("gemm_kernel"), "peak_source": src,
+                "flops_per_launch": gemm_flops / max(gemm_launch, 1),
+                "launch_ms": gemm_ms / max(gemm_launch, 1), "launches_per_step": gemm_launch / args.steps,
+                "share_of_step_time": gemm_ms / step_total_ms if step_total_ms else None}
+        apply_bytes = phase["apply_bytes"]
+        its = main["iterations"][0]
+        pcg_bytes = its * (apply_bytes + phase["spmv_bytes"] + 8.0 * 10 * n)
+        pcg_med = statistics.median(main["pcg_ms"])
+        roof_pcg = {"bound": "hbm", "kernel": "PCG iteration (SpMV + preconditioner apply + vector updates)",
+                    "achieved": pcg_bytes / (pcg_med * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                    "frac": pcg_bytes / (pcg_med * 1e-3) / 1e9 / hbm, "peak_source": src,
+                    "bytes_per_iteration": pcg_bytes / its, "apply_bytes": apply_bytes,
+                    "apply_ms": phase["apply_ms"], "spmv_ms": phase["spmv_ms"]}
         line = {
             "metric": "factor+PCG solves/s to 1e-8 relative residual", "value": value, "unit": "solves/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -301,13 +382,20 @@ def run_ours(args):
                     "d2h_bytes_per_step": int(h_x.nbytes)},
             "gpu_launches": int(args.steps * (phase["factor_launches"] + phase["pcg_launches"])),
             "roofline": roof,
+            "roofline_pcg": roof_pcg,
             "cpu_baseline": cpu,
-            "clocks": clocks.summary(),
-            "iterations": iters if nrhs > 1 else iters[0], "true_residual": resid,
-            "factor_ms": phase["factor_ms"], "pcg_ms": phase["pcg_ms"], "apply_ms": phase["apply_ms"],
-            "spmv_ms": phase["spmv_ms"], "setup_s": setup_s, "symbolic_s": stats["symbolic_s"],
-            "p50_ms": statistics.median(step_ms), "p99_ms": float(np.percentile(step_ms, 99)),
+            "clocks": main["clocks"],
+            "plain_fp64": plain,
+            "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
+            "iterations": main["iterations"] if nrhs > 1 else main["iterations"][0],
+            "true_residual": main["true_residual"],
+            "factor_ms": statistics.median(main["factor_ms"]), "pcg_ms": statistics.median(main["pcg_ms"]),
+            "apply_ms": phase["apply_ms"], "spmv_ms": phase["spmv_ms"], "setup_s": main["setup_s"],
+            "symbolic_s": stats["symbolic_s"],
+            "p50_ms": statistics.median(main["step_ms"]), "p99_ms": float(np.percentile(main["step_ms"], 99)),
             "factor_gflop": stats["factor_flops"] / 1e9, "structure": desc,
+            "factor_step_ms": {name: c[3 * k] / args.steps for k, name in
+                               enumerate(["gemm", "potrf", "trsm", "extadd", "qr", "identity"])},
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -316,22 +404,13 @@ def run_ours(args):
 
 
 def profile_phases(lib, F, ctx, stream, d_b, nrhs, torch):
-    """CUDA-event timings of the factor, one preconditioner apply, one SpMV."""
-    import ctypes
+    """CUDA-event timings of one preconditioner apply and one SpMV, launch counts."""
     out = np.zeros(16)
     st = lib.rschol_profile(F.h, d_b.data_ptr(), out.ctypes.data)
     if st != 0:
         raise RuntimeError("rschol_profile failed: %s" % ctx.last_error())
-    factor_ms, apply_ms, spmv_ms, pcg_ms = out[0], out[1], out[2], out[3]
-    apply_bytes, spmv_bytes = out[4], out[5]
-    factor_launches, pcg_launches = out[6], out[7]
-    dom_ms, dom_bytes, name = out[8], out[9], "compressed/interior solve kernels (one preconditioner apply)"
-    return {"factor_ms": factor_ms, "apply_ms": apply_ms, "spmv_ms": spmv_ms, "pcg_ms": pcg_ms,
-            "factor_launches": factor_launches, "pcg_launches": pcg_launches,
-            "roofline": {"bound": "hbm", "kernel": name, "achieved": apply_bytes / (apply_ms * 1e-3) / 1e9,
-                         "unit": "GB/s", "traffic": None,
-                         "algorithmic_bytes_per_launch": apply_bytes, "launch_ms": apply_ms,
-                         "spmv_GBs": spmv_bytes / (spmv_ms * 1e-3) / 1e9}}
+    return {"factor_ms": out[0], "apply_ms": out[1], "spmv_ms": out[2], "pcg_ms": out[3],
+            "apply_bytes": out[4], "spmv_bytes": out[5], "factor_launches": out[6], "pcg_launches": out[7]}
 
 
 def main():
@@ -340,9 +419,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--profile", action="store_true",
                     help="warm up, then run the steps between cudaProfilerStart/Stop (for ncu), no timing line")
     args = ap.parse_args()

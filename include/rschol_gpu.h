@@ -123,6 +123,14 @@ int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x
  *   - the first call on a device looks up the array's address
  *     (cudaGetSymbolAddress, with that device current); make that first call
  *     before any stream capture that would include this function. */
+/* Diagnostics (no reference counterpart): CUDA-event timing of every step of
+ * the numeric factorisation while enabled.  out (may be null) receives, for
+ * step kinds 0..6 (GEMM, POTRF, TRSM, extend-add, QR, identity basis, -),
+ * 3 values each: device milliseconds, launches and GEMM flops accumulated
+ * since timing was last switched on; enable = 1 also resets them when timing
+ * was off. */
+int rschol_step_timing(rschol_factor* f, int enable, double* out);
+
 /* Diagnostics (no reference counterpart): one tensor-core GEMM
  * C = -1.25 op(A) op(B) + 0.5 C on random M x N x K operands (tA / tB:
  * transposed storage, split: split-precision TF32, lower: lower-triangle

@@ -57,6 +57,7 @@ struct Impl {
   virtual int run() = 0;
   virtual void apply(double* d_w, cudaStream_t s) = 0;
   virtual int apply_error(cudaStream_t s) = 0;   // nonzero: a row-block wait of the solve gave up
+  virtual void step_timing(bool on, double* out) = 0;
   virtual void set_values(const double* lower) = 0;
   virtual double* device_values() = 0;
   virtual long long launches() const = 0;
@@ -82,6 +83,17 @@ struct ImplT : Impl {
   int run() override { return fe.run(); }
   void apply(double* w, cudaStream_t s) override { se.apply_inplace(w, s); }
   int apply_error(cudaStream_t s) override { return se.take_error(s); }
+  void step_timing(bool on, double* out) override {
+    if (out)
+      for (int k = 0; k < 7; ++k) {
+        out[3 * k] = fe.stepMs[k];
+        out[3 * k + 1] = fe.stepCount[k];
+        out[3 * k + 2] = fe.stepFlops[k];
+      }
+    if (on && !fe.timeSteps)
+      for (int k = 0; k < 8; ++k) fe.stepMs[k] = fe.stepCount[k] = fe.stepFlops[k] = 0;
+    fe.timeSteps = on;
+  }
   void set_values(const double* lower) override { fe.set_values(lower); }
   double* device_values() override { return fe.dAvals.template as<double>(); }
   long long launches() const override { return fe.launches; }
@@ -587,6 +599,13 @@ int rschol_factor_stats(const rschol_factor* f, double* st) {
 }
 
 }  // extern "C"
+
+// ---- diagnostics: per-step-kind device time of the factorisation ------------
+extern "C" int rschol_step_timing(rschol_factor* f, int enable, double* out) {
+  if (!f) return RSCHOL_E_BAD_INPUT;
+  f->impl->step_timing(enable != 0, out);
+  return RSCHOL_OK;
+}
 
 // ---- diagnostics: the tensor-core GEMM against a host FP64 product -----------
 extern "C" int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int split, int lower, double* out) {

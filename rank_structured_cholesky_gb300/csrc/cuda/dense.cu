@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <climits>
+#include <type_traits>
 
 #include "common.cuh"
 #include "dense.cuh"
@@ -100,6 +101,126 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_kernel(const GemmTask<T>* _
 
 template <class T>
 __global__ void __launch_bounds__(256) potrf_kernel(const PotrfTask<T>* __restrict__ tasks, int* flag) {
+  // Right-looking Cholesky of one <= 64 x 64 tile in 16-column panels: one
+  // warp factors the panel's diagonal block, every thread solves a row of
+  // the panel below it, then all threads update the trailing triangle.
+  const PotrfTask<T> t = tasks[blockIdx.x];
+  __shared__ T a[64][65];
+  __shared__ int bad;
+  const int n = t.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int idx = tid; idx < n * n; idx += blockDim.x) {
+    const int i = idx / n, j = idx - i * n;
+    a[i][j] = (j <= i) ? t.A[(size_t)i * t.ld + j] : T(0);
+  }
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int p0 = 0; p0 < n; p0 += 16) {
+    const int pw = min(16, n - p0);
+    if (warp == 0) {
+      for (int j = 0; j < pw; ++j) {
+        const int jj = p0 + j;
+        if (lane == 0) {
+          T d = a[jj][jj];
+          if (!(d > T(0))) {   // not positive definite (or NaN): keep going, report
+            bad = 1;
+            d = T(1);
+          }
+          a[jj][jj] = sqrt(d);
+        }
+        __syncwarp();
+        if (lane > j && lane < pw) a[p0 + lane][jj] /= a[jj][jj];
+        __syncwarp();
+        if (lane > j && lane < pw) {
+          const T lij = a[p0 + lane][jj];
+          for (int k = j + 1; k <= lane; ++k) a[p0 + lane][p0 + k] -= lij * a[p0 + k][jj];
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    for (int i = p0 + pw + tid; i < n; i += blockDim.x)
+      for (int j = 0; j < pw; ++j) {
+        T s = a[i][p0 + j];
+        for (int k = 0; k < j; ++k) s -= a[i][p0 + k] * a[p0 + j][p0 + k];
+        a[i][p0 + j] = s / a[p0 + j][p0 + j];
+      }
+    __syncthreads();
+    const int q0 = p0 + pw, m = n - q0;
+    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+      const int ii = idx / m, kk = idx - ii * m;
+      if (kk <= ii) {
+        T s = T(0);
+        for (int c = 0; c < pw; ++c) s += a[q0 + ii][p0 + c] * a[q0 + kk][p0 + c];
+        a[q0 + ii][q0 + kk] -= s;
+      }
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < n * n; idx += blockDim.x) {
+    const int i = idx / n, j = idx - i * n;
+    if (j <= i) t.A[(size_t)i * t.ld + j] = a[i][j];
+  }
+  if (tid == 0 && bad) atomicMin(flag, t.code);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) trsm_kernel(const TrsmTask<T>* __restrict__ tasks, int nTasks) {
+  // B (64-row chunk x w) := B L^{-T} in 16-column panels: each row solves
+  // with the panel's diagonal block (16 steps), then all threads update the
+  // columns to the right.
+  int lo = 0, hi = nTasks - 1;
+  const int b = blockIdx.x;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (tasks[mid].chunkBase <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  const TrsmTask<T> t = tasks[lo];
+  const int r0 = (b - t.chunkBase) * 64;
+  const int nr = min(64, t.rows - r0);
+  const int w = t.w, tid = threadIdx.x;
+  extern __shared__ __align__(16) unsigned char trsm_smem[];
+  T (*L)[65] = reinterpret_cast<T (*)[65]>(trsm_smem);
+  T (*X)[65] = reinterpret_cast<T (*)[65]>(trsm_smem + sizeof(T) * 64 * 65);
+  for (int idx = tid; idx < w * w; idx += blockDim.x) {
+    const int i = idx / w, j = idx - i * w;
+    L[i][j] = (j <= i) ? t.L[(size_t)i * t.ldl + j] : T(0);
+  }
+  for (int idx = tid; idx < nr * w; idx += blockDim.x) {
+    const int i = idx / w, j = idx - i * w;
+    X[i][j] = t.B[(size_t)(r0 + i) * t.ldb + j];
+  }
+  __syncthreads();
+  for (int p0 = 0; p0 < w; p0 += 16) {
+    const int pw = min(16, w - p0);
+    if (tid < nr)
+      for (int j = 0; j < pw; ++j) {
+        T s = X[tid][p0 + j];
+        for (int k = 0; k < j; ++k) s -= X[tid][p0 + k] * L[p0 + j][p0 + k];
+        X[tid][p0 + j] = s / L[p0 + j][p0 + j];
+      }
+    __syncthreads();
+    const int q0 = p0 + pw, wq = w - q0;
+    for (int idx = tid; idx < nr * wq; idx += blockDim.x) {
+      const int i = idx / wq, q = q0 + (idx - i * wq);
+      T s = T(0);
+      for (int c = 0; c < pw; ++c) s += X[i][p0 + c] * L[q][p0 + c];
+      X[i][q] -= s;
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < nr * w; idx += blockDim.x) {
+    const int i = idx / w, j = idx - i * w;
+    t.B[(size_t)(r0 + i) * t.ldb + j] = X[i][j];
+  }
+}
+
+// FP32 variants: a register-resident POTRF (thread (i, g) keeps row i,
+// columns g, g + 4, ... of the tile) and a TRSM that inverts the tile in
+// every block and multiplies; they beat the panel-blocked kernels above in
+// FP32, while FP64 prefers the blocked ones.
+template <class T>
+__global__ void __launch_bounds__(256) potrf_reg_kernel(const PotrfTask<T>* __restrict__ tasks, int* flag) {
   // Right-looking Cholesky of one <= 64 x 64 tile.  Thread (i = tid / 4,
   // g = tid % 4) keeps row i, columns g, g + 4, ..., in registers; column j
   // is broadcast through a double-buffered shared array.
@@ -161,7 +282,7 @@ __global__ void __launch_bounds__(256) potrf_kernel(const PotrfTask<T>* __restri
 }
 
 template <class T>
-__global__ void __launch_bounds__(256) trsm_kernel(const TrsmTask<T>* __restrict__ tasks, int nTasks) {
+__global__ void __launch_bounds__(256) trsm_inv_kernel(const TrsmTask<T>* __restrict__ tasks, int nTasks) {
   // B (64-row chunk x w) := B L^{-T}: the block inverts its w x w tile
   // (column c by thread c, forward substitution) and multiplies.
   int lo = 0, hi = nTasks - 1;
@@ -556,18 +677,28 @@ template <class T> void launch_gemm(const GemmTask<T>* d, int n, int tiles, cuda
 }
 template <class T> void launch_potrf(const PotrfTask<T>* d, int n, int* flag, cudaStream_t s) {
   if (n <= 0) return;
-  potrf_kernel<T><<<n, 256, 0, s>>>(d, flag);
+  if constexpr (std::is_same<T, float>::value) potrf_reg_kernel<T><<<n, 256, 0, s>>>(d, flag);
+  else potrf_kernel<T><<<n, 256, 0, s>>>(d, flag);
   RSCHOL_LAUNCH_CHECK();
 }
 template <class T> void launch_trsm(const TrsmTask<T>* d, int n, int chunks, cudaStream_t s) {
   if (n <= 0 || chunks <= 0) return;
-  const int smem = (int)(3 * sizeof(T) * 64 * 65);
   static bool configured = false;   // per instantiation
-  if (!configured) {
-    RSCHOL_CUDA(cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    configured = true;
+  if constexpr (std::is_same<T, float>::value) {
+    const int smem = (int)(3 * sizeof(T) * 64 * 65);
+    if (!configured) {
+      RSCHOL_CUDA(cudaFuncSetAttribute(trsm_inv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      configured = true;
+    }
+    trsm_inv_kernel<T><<<chunks, 256, smem, s>>>(d, n);
+  } else {
+    const int smem = (int)(2 * sizeof(T) * 64 * 65);
+    if (!configured) {
+      RSCHOL_CUDA(cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      configured = true;
+    }
+    trsm_kernel<T><<<chunks, 256, smem, s>>>(d, n);
   }
-  trsm_kernel<T><<<chunks, 256, smem, s>>>(d, n);
   RSCHOL_LAUNCH_CHECK();
 }
 template <class T>

@@ -1,9 +1,11 @@
 #include <algorithm>
 #include <climits>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <stdexcept>
 #include <type_traits>
 
 #include "../host/rng.h"
@@ -806,6 +808,16 @@ void FactorEngine<T>::plan() {
     if (gemmWsOff_[q] >= 0) gemm_[q].ws = dSplitWs_.as<float>() + gemmWsOff_[q];
   up(dSplitIds_, splitIds_.data(), splitIds_.size() * sizeof(int));
   up(dSplitBase_, splitBase_.data(), splitBase_.size() * sizeof(long long));
+  // every task pointer must now be a device address, not a plan-time offset
+  auto device_ptr = [](const void* p) { return reinterpret_cast<uintptr_t>(p) >= (uintptr_t(1) << 32); };
+  for (const auto& g : gemm_)
+    if (!device_ptr(g.A) || !device_ptr(g.B) || !device_ptr(g.C))
+      throw std::runtime_error("factor plan: a GEMM operand was not rebased to a device address");
+  for (const auto& p : potrf_)
+    if (!device_ptr(p.A)) throw std::runtime_error("factor plan: a POTRF task without a device address");
+  for (const auto& t : trsm_)
+    if (!device_ptr(t.L) || !device_ptr(t.B))
+      throw std::runtime_error("factor plan: a TRSM task without a device address");
   up(dGemm_, gemm_.data(), gemm_.size() * sizeof(GemmTask<T>));
   up(dPotrf_, potrf_.data(), potrf_.size() * sizeof(PotrfTask<T>));
   up(dTrsm_, trsm_.data(), trsm_.size() * sizeof(TrsmTask<T>));
@@ -834,7 +846,15 @@ int FactorEngine<T>::run() {
   launch_scatter<T>(dAvals.as<double>(), dScatSrc_.as<long long>() + nScatI_, dScatDst_.as<long long>() + nScatI_,
                     nScatC_, compressed(), stream);
   launches += 2;
-  for (const Step& st : steps_) {
+  const bool timing = timeSteps && !steps_.empty();
+  if (timing && stepEv_.size() < 2 * steps_.size()) {
+    for (auto e : stepEv_) cudaEventDestroy(e);
+    stepEv_.assign(2 * steps_.size(), nullptr);
+    for (auto& e : stepEv_) RSCHOL_CUDA(cudaEventCreate(&e));
+  }
+  for (size_t q = 0; q < steps_.size(); ++q) {
+    const Step& st = steps_[q];
+    if (timing) RSCHOL_CUDA(cudaEventRecord(stepEv_[2 * q], stream));
     switch (st.kind) {
       case ST_GEMM:
       case ST_GEMM_REDUCE: gemm_launch(st); break;
@@ -849,12 +869,28 @@ int FactorEngine<T>::run() {
         break;
       case ST_IDENT: launch_set_identity<T>(dIdent_.as<IdentTask<T>>() + st.off, st.count, stream); break;
     }
+    if (timing) RSCHOL_CUDA(cudaEventRecord(stepEv_[2 * q + 1], stream));
     ++launches;
   }
   if (post) launches += post();
   int flag[2] = {0, 0};
   RSCHOL_CUDA(cudaMemcpyAsync(flag, dFlag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
   RSCHOL_CUDA(cudaStreamSynchronize(stream));
+  if (timing) {
+    for (size_t q = 0; q < steps_.size(); ++q) {
+      float ms = 0;
+      RSCHOL_CUDA(cudaEventElapsedTime(&ms, stepEv_[2 * q], stepEv_[2 * q + 1]));
+      const int k = steps_[q].kind == ST_GEMM_REDUCE ? (int)ST_GEMM : steps_[q].kind;
+      stepMs[k] += ms;
+      stepCount[k] += 1;
+    }
+    for (const Step& st : steps_)
+      if (st.kind == ST_GEMM)
+        for (int k = 0; k < st.count; ++k) {
+          const GemmTask<T>& g = gemm_[st.off + k];
+          stepFlops[ST_GEMM] += 2.0 * g.M * g.N * (double)g.K;
+        }
+  }
   if (flag[1]) throw CudaError("tensor-core GEMM: an mbarrier wait exceeded its limit");
   return flag[0] == INT_MAX ? 0 : flag[0];
 }

@@ -89,7 +89,9 @@ template <class T>
 class FactorEngine {
  public:
   FactorEngine(const Symbolic& S, const CSC& Alower, const Params& prm, cudaStream_t stream);
-  ~FactorEngine() = default;
+  ~FactorEngine() {
+    for (auto e : stepEv_) cudaEventDestroy(e);
+  }
 
   // (Re)build buffers and schedule for the ranks currently in S.
   void plan();
@@ -117,6 +119,10 @@ class FactorEngine {
   // Work queued on the stream after the last factor step and before the
   // status read (solve-side preprocessing of the factor); returns its launches.
   std::function<int()> post;
+  // Per-step CUDA-event timing (off by default): accumulated device time,
+  // launches and GEMM flops per step kind over the runs made while on.
+  bool timeSteps = false;
+  double stepMs[8] = {}, stepCount[8] = {}, stepFlops[8] = {};
   long long launches = 0;            // kernel launches of the last run
   double flops = 0;                  // algorithmic flops of one factorisation
   size_t deviceBytes = 0;
@@ -146,6 +152,7 @@ class FactorEngine {
   bool tensor_cores() const { return useTc_; }   // FP32 GEMMs on tcgen05
 
   std::vector<Step> steps_;
+  std::vector<cudaEvent_t> stepEv_;
   std::vector<GemmTask<T>> gemm_;
   std::vector<PotrfTask<T>> potrf_;
   std::vector<TrsmTask<T>> trsm_;
