@@ -40,6 +40,9 @@ CONFIGS = {
            ("elasticity", 48, 0, 0, 2), 1),
     "c4": ("2D 5-point variable-coefficient 1024^2, log-normal sigma=2 seed 3, 64 RHS",
            ("diffusion", 2, 1024, 2.0, 3), 64),
+    # a smaller case of c2 for multi-pass ncu captures (a few hundred MB on the device)
+    "c2s": ("3D 7-point variable-coefficient diffusion 40^3, log-normal sigma=1 seed 1, harmonic faces",
+            ("diffusion", 3, 40, 1.0, 1), 1),
 }
 
 
