@@ -21,7 +21,7 @@ ORACLE_OUT = os.path.join(ORACLE_DIR, "_build")
 ORACLE_LIB = os.path.join(ORACLE_OUT, "liboracle.so")
 
 HOST_SRC = ["host/ordering.cpp", "host/symbolic.cpp", "host/problems.cpp", "host/capi_host.cpp"]
-CUDA_SRC = ["cuda/dense.cu", "cuda/gemm_tc.cu", "cuda/factor.cu", "cuda/solve.cu", "cuda/pcg.cu", "cuda/capi.cu"]
+CUDA_SRC = ["cuda/dense.cu", "cuda/gemm_tc.cu", "cuda/factor.cu", "cuda/solve.cu", "cuda/solve_batch.cu", "cuda/pcg.cu", "cuda/pcg_batch.cu", "cuda/capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -58,6 +58,9 @@ struct Impl {
   virtual void apply(double* d_w, cudaStream_t s) = 0;
   virtual int apply_error(cudaStream_t s) = 0;   // nonzero: a row-block wait of the solve gave up
   virtual void step_timing(bool on, double* out) = 0;
+  virtual void apply_batch(double* W, int k, cudaStream_t s) = 0;   // W: n x k row-major, permuted
+  virtual int batch_capacity() const = 0;
+  virtual int apply_batch_error(cudaStream_t s) = 0;
   virtual void set_values(const double* lower) = 0;
   virtual double* device_values() = 0;
   virtual long long launches() const = 0;
@@ -83,6 +86,9 @@ struct ImplT : Impl {
   int run() override { return fe.run(); }
   void apply(double* w, cudaStream_t s) override { se.apply_inplace(w, s); }
   int apply_error(cudaStream_t s) override { return se.take_error(s); }
+  void apply_batch(double* W, int k, cudaStream_t s) override { se.apply_batch(W, k, s); }
+  int batch_capacity() const override { return se.batch_capacity(); }
+  int apply_batch_error(cudaStream_t s) override { return se.take_error_batch(s); }
   void step_timing(bool on, double* out) override {
     if (out)
       for (int k = 0; k < 7; ++k) {
@@ -152,6 +158,8 @@ struct rschol_factor {
   std::unique_ptr<PcgEngine> pcg;
   std::vector<int> permCsrSrc;  // permuted CSR value k = Afull.x[permCsrSrc[k]]
   DevBuf dPerm, dB, dX, dBp, dXp, dLowerSrc, dCsrSrc;
+  DevBuf dBk, dXk;   // batched right-hand sides / solutions, n x k row-major, permuted
+  int kCap = 0;
   int nrhsCap = 0;
   double tSymbolic = 0, tNumeric = 0;
   int attempts = 0;
@@ -341,6 +349,7 @@ int rschol_refactor(rschol_factor* f, const double* vals) {
 }
 
 static void ensure_vecs(rschol_factor* f, int nrhs);
+static void ensure_batch(rschol_factor* f, int k);
 
 int rschol_refactor_device(rschol_factor* f, const double* d_vals) {
   if (!f || !d_vals) return RSCHOL_E_BAD_INPUT;
@@ -413,6 +422,14 @@ int rschol_profile(rschol_factor* f, const double* d_b, double* out) {
 
 void rschol_factor_free(rschol_factor* f) { delete f; }
 
+static void ensure_batch(rschol_factor* f, int k) {
+  if (k <= f->kCap) return;
+  const size_t bytes = sizeof(double) * (size_t)f->Afull.n * k;
+  f->dBk.alloc(bytes);
+  f->dXk.alloc(bytes);
+  f->kCap = k;
+}
+
 static void ensure_vecs(rschol_factor* f, int nrhs) {
   if (nrhs <= f->nrhsCap) return;
   const size_t bytes = sizeof(double) * (size_t)f->Afull.n * nrhs;
@@ -429,13 +446,24 @@ int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x
     ensure_vecs(f, 1);
     const int n = f->Afull.n;
     cudaStream_t s = f->ctx->stream;
-    for (int k = 0; k < nrhs; ++k) {
-      launch_gather(d_b + (size_t)k * n, f->dPerm.as<int>(), f->dBp.as<double>(), n, s);
+    if (nrhs == 1) {
+      launch_gather(d_b, f->dPerm.as<int>(), f->dBp.as<double>(), n, s);
       f->impl->apply(f->dBp.as<double>(), s);
-      launch_scatter_perm(f->dBp.as<double>(), f->dPerm.as<int>(), d_x + (size_t)k * n, n, s);
+      launch_scatter_perm(f->dBp.as<double>(), f->dPerm.as<int>(), d_x, n, s);
+      RSCHOL_CUDA(cudaStreamSynchronize(s));
+      if (f->impl->apply_error(s)) return fail(f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);
+    } else {   // batches of right-hand sides share one pass over the factor
+      const int cap = std::max(1, std::min(64, f->impl->batch_capacity()));
+      for (int k0 = 0; k0 < nrhs; k0 += cap) {
+        const int k = std::min(cap, nrhs - k0);
+        ensure_batch(f, k);
+        launch_gather_k(d_b + (size_t)k0 * n, f->dPerm.as<int>(), f->dBk.as<double>(), n, k, s);
+        f->impl->apply_batch(f->dBk.as<double>(), k, s);
+        launch_scatter_k(f->dBk.as<double>(), f->dPerm.as<int>(), d_x + (size_t)k0 * n, n, k, s);
+      }
+      RSCHOL_CUDA(cudaStreamSynchronize(s));
+      if (f->impl->apply_batch_error(s)) return fail(f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);
     }
-    RSCHOL_CUDA(cudaStreamSynchronize(s));
-    if (f->impl->apply_error(s)) return fail(f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);
   } catch (const std::exception& e) {
     return fail(f->ctx, RSCHOL_E_CUDA, e.what());
   }
@@ -467,21 +495,44 @@ int rschol_pcg_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs
     const int n = f->Afull.n;
     cudaStream_t s = f->ctx->stream;
     Impl* impl = f->impl.get();
-    auto apply = [impl, s](double* w) { impl->apply(w, s); };
-    for (int k = 0; k < nrhs; ++k) {
+    if (nrhs == 1) {
+      auto apply = [impl, s](double* w) { impl->apply(w, s); };
       double t0 = now_s();
-      launch_gather(d_b + (size_t)k * n, f->dPerm.as<int>(), f->dBp.as<double>(), n, s);
+      launch_gather(d_b, f->dPerm.as<int>(), f->dBp.as<double>(), n, s);
       PcgResult r = f->pcg->solve(f->dBp.as<double>(), f->dXp.as<double>(), eps, maxit, apply);
-      launch_scatter_perm(f->dXp.as<double>(), f->dPerm.as<int>(), d_x + (size_t)k * n, n, s);
+      launch_scatter_perm(f->dXp.as<double>(), f->dPerm.as<int>(), d_x, n, s);
       RSCHOL_CUDA(cudaStreamSynchronize(s));
       if (f->impl->apply_error(s)) return fail(f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);
       if (info) {
-        info[k].iterations = r.iterations;
-        info[k].residual = r.residual;
-        info[k].true_residual = r.trueResidual;
-        info[k].seconds = now_s() - t0;
+        info[0].iterations = r.iterations;
+        info[0].residual = r.residual;
+        info[0].true_residual = r.trueResidual;
+        info[0].seconds = now_s() - t0;
       }
       if (r.breakdown) status = RSCHOL_E_BREAKDOWN;
+    } else {   // batched PCG: up to 64 right-hand sides in lockstep, one factor pass per apply
+      const int cap = std::max(1, std::min(64, impl->batch_capacity()));
+      for (int k0 = 0; k0 < nrhs; k0 += cap) {
+        const int k = std::min(cap, nrhs - k0);
+        ensure_batch(f, k);
+        double t0 = now_s();
+        auto apply = [impl, s, k](double* w) { impl->apply_batch(w, k, s); };
+        launch_gather_k(d_b + (size_t)k0 * n, f->dPerm.as<int>(), f->dBk.as<double>(), n, k, s);
+        std::vector<PcgResult> rs = f->pcg->solve_batch(f->dBk.as<double>(), f->dXk.as<double>(), k, eps, maxit, apply);
+        launch_scatter_k(f->dXk.as<double>(), f->dPerm.as<int>(), d_x + (size_t)k0 * n, n, k, s);
+        RSCHOL_CUDA(cudaStreamSynchronize(s));
+        if (impl->apply_batch_error(s)) return fail(f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);
+        const double dt = now_s() - t0;
+        for (int c = 0; c < k; ++c) {
+          if (info) {
+            info[k0 + c].iterations = rs[c].iterations;
+            info[k0 + c].residual = rs[c].residual;
+            info[k0 + c].true_residual = rs[c].trueResidual;
+            info[k0 + c].seconds = dt;
+          }
+          if (rs[c].breakdown) status = RSCHOL_E_BREAKDOWN;
+        }
+      }
     }
   } catch (const std::exception& e) {
     return fail(f->ctx, RSCHOL_E_CUDA, e.what());

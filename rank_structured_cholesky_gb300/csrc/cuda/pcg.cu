@@ -171,6 +171,7 @@ PcgEngine::PcgEngine(int n_, const std::vector<int>& rowptr, const std::vector<i
 
 PcgEngine::~PcgEngine() {
   if (hScal_) cudaFreeHost(hScal_);
+  if (hScalB_) cudaFreeHost(hScalB_);
 }
 
 void PcgEngine::set_values(const std::vector<double>& vals) {

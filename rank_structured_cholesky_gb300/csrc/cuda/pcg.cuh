@@ -39,6 +39,12 @@ class PcgEngine {
   // d_b, d_x: permuted vectors on the device.  apply: in-place M^{-1}.
   PcgResult solve(const double* d_b, double* d_x, double eps, int maxit,
                   const std::function<void(double*)>& apply);
+  // k right-hand sides at once: B, X are n x k row-major (the k values of a
+  // row contiguous), permuted; apply: in-place M^{-1} of such a block.
+  // Every column follows the single-vector recurrences and stops on its own
+  // (its alpha becomes 0 once ||r||/||b|| <= eps); results per column.
+  std::vector<PcgResult> solve_batch(const double* d_B, double* d_X, int k, double eps, int maxit,
+                                     const std::function<void(double*)>& apply);
   // y = A x on permuted device vectors
   void spmv(const double* x, double* y);
   long long launches = 0;
@@ -51,7 +57,16 @@ class PcgEngine {
   double* hScal_ = nullptr;   // pinned
   int nblk_ = 0;
   int tpr_ = 8;
+  // batched solves (allocated for kB_ right-hand sides on first use)
+  int kB_ = 0;
+  DevBuf rB_, dB_, qB_, sB_, partB_, scalB_;
+  double* hScalB_ = nullptr;   // pinned, k x S_COUNT
 };
+
+// permuted <-> original order for k right-hand sides: the stacked vectors
+// (column c at src + c n) <-> the n x k row-major block
+void launch_gather_k(const double* src, const int* perm, double* dst, int n, int k, cudaStream_t s);
+void launch_scatter_k(const double* src, const int* perm, double* dst, int n, int k, cudaStream_t s);
 
 // dst[k] = src[idx[k]], k < count (value re-mapping on the device)
 void launch_index_gather(const double* src, const int* idx, double* dst, long long count, cudaStream_t s);

@@ -2,19 +2,13 @@
 #include <type_traits>
 
 #include "solve.cuh"
+#include "solve_dev.cuh"
 
 namespace rschol {
 
 namespace {
 
-constexpr unsigned FULL = 0xffffffffu;
-
-template <class V>
-__device__ __forceinline__ V warp_sum(V v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
-  return v;
-}
+using namespace solvedev;
 
 // out[k] = sum_{i < rows} M[i][k] v[i] (v == nullptr: v[i] = 1, and M was
 // written by other blocks of this launch, so its loads bypass L1) for k < r,
@@ -106,42 +100,6 @@ __device__ void trsv_dinv_t(const T* __restrict__ L, int ld, int n, const T* __r
   }
 }
 
-constexpr int SPIN_LIMIT = 1 << 22;   // polls (with a short sleep) before a wait gives up
-
-__device__ __forceinline__ int ld_acquire(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release(int* p, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
-
-// Warp-uniform bounded wait for *p >= target.  Returns false when the wait
-// gave up (after SPIN_LIMIT polls, or as soon as another block reported an
-// error); the error word is then set.
-__device__ __forceinline__ bool wait_geq(const int* p, int target, int* err) {
-  if (__all_sync(FULL, ld_acquire(p) >= target)) return true;
-  for (int it = 1; it <= SPIN_LIMIT; ++it) {
-    __nanosleep(64);
-    if (__all_sync(FULL, ld_acquire(p) >= target)) return true;
-    if ((it & 63) == 0 && __any_sync(FULL, ld_volatile(err) != 0)) return false;
-  }
-  if ((threadIdx.x & 31) == 0) atomicExch(err, 1);
-  return false;
-}
-
-// Every block of a ticketed launch calls this once when it is done; the last
-// one resets the ticket and completion counters for the next launch.
-__device__ __forceinline__ void launch_done(int* tick, int* done) {
-  __syncthreads();
-  if (threadIdx.x == 0 && atomicAdd(done, 1) == (int)gridDim.x - 1) {
-    atomicExch(tick, 0);
-    atomicExch(done, 0);
-  }
-}
-
 // Interior supernodes: all levels in one launch per direction.  A block takes
 // the next (supernode, 128-row chunk of its off-diagonal rows) from a ticket
 // counter, in level order, so it only waits on blocks that started before it:
@@ -150,8 +108,6 @@ __device__ __forceinline__ void launch_done(int* tick, int* done) {
 // the solve of its interior parent (a flag set to the apply's epoch).  Every
 // chunk block assembles and solves the supernode's own n columns (n is small);
 // chunk 0 stores y.
-constexpr int ICH = 128;
-constexpr int SYNC_TICK_F = 1, SYNC_DONE_F = 2, SYNC_TICK_B = 3, SYNC_DONE_B = 4, SYNC_GLOBAL = 5;
 
 template <class T>
 __global__ void __launch_bounds__(256) interior_forward_chunks(const SNode<T>* __restrict__ nodes,
@@ -326,14 +282,15 @@ template <class T>
 __global__ void __launch_bounds__(256) compressed_gather_rows(const SNode<T>* __restrict__ nodes,
                                                               const int* __restrict__ lvl,
                                                               const long long* __restrict__ cstart,
-                                                              const T* const* __restrict__ ent, T* __restrict__ w) {
+                                                              const long long* __restrict__ ent,
+                                                              const T* __restrict__ wu, T* __restrict__ w) {
   const SNode<T>& nd = nodes[lvl[blockIdx.y]];
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (i >= nd.n) return;
   const long long* cs = cstart + nd.cOff;
   T acc = T(0);
-  for (long long e = cs[i] + lane; e < cs[i + 1]; e += 32) acc += *ent[e];
+  for (long long e = cs[i] + lane; e < cs[i + 1]; e += 32) acc += wu[ent[e]];
   acc = warp_sum(acc);
   if (lane == 0) w[nd.c0 + i] += acc;
 }
@@ -705,6 +662,7 @@ void SolveEngine<T>::plan() {
   cVzGrid_.clear();
   cRowGrid_.clear();
   cColGrid_.clear();
+  cMRowGrid_.clear();
   std::vector<XTile> xtiles;
   cTiles_.clear();
   for (auto& lv : F_.compressedLevels) {
@@ -729,6 +687,7 @@ void SolveEngine<T>::plan() {
     cMaxCh_.push_back(maxCh);
     cVzGrid_.push_back(std::min(64, (maxM + 7) / 8));
     cRowGrid_.push_back((maxN + 7) / 8);
+    cMRowGrid_.push_back((maxM + 7) / 8);
     cColGrid_.push_back((maxN + 255) / 256);
   }
   cudaStream_t st = F_.stream;
@@ -756,8 +715,7 @@ void SolveEngine<T>::plan() {
   // per-row contribution lists of the compressed supernodes (in source order)
   {
     std::vector<long long> cstart;
-    std::vector<const T*> ents;
-    const T* wuBase = dWu_.as<T>();
+    std::vector<long long> ents;   // offsets into the update-vector arena
     for (int s = 0; s < nn; ++s) {
       const Node& nd = S.nodes[s];
       if (!nd.compressed) continue;
@@ -774,13 +732,13 @@ void SolveEngine<T>::plan() {
         const SNode<T>& src = nodes_[P.src];
         for (int a = P.a0; a < P.a1; ++a) {
           // interior root: its update vector; compressed: u = -V z
-          const T* e = (P.kind == 0) ? wuBase + src.wuOff + a : wuBase + src.wuOff + 2 * src.r + a;
+          const long long e = (P.kind == 0) ? src.wuOff + a : src.wuOff + 2 * src.r + a;
           ents[base + fill[S.nodes[P.src].rows[a] - nd.c0]++] = e;
         }
       }
     }
     up(dCStart_, cstart.data(), cstart.size() * sizeof(long long));
-    up(dCEnt_, ents.data(), ents.size() * sizeof(const T*));
+    up(dCEnt_, ents.data(), ents.size() * sizeof(long long));
   }
   up(dNodes_, nodes_.data(), nodes_.size() * sizeof(SNode<T>));
   up(dRows_, rowsAll.data(), rowsAll.size() * sizeof(int));
@@ -790,6 +748,12 @@ void SolveEngine<T>::plan() {
   up(dIWork_, iwork.data(), iwork.size() * sizeof(RowBlock));
   up(dIWorkB_, iworkB.data(), iworkB.size() * sizeof(RowBlock));
   nIWork_ = (int)iwork.size();
+  wuTotal_ = wuCur;
+  ipTotal_ = ipCur;
+  maxNI_ = 0;
+  for (int s = 0; s < nn; ++s)
+    if (!S.nodes[s].compressed) maxNI_ = std::max(maxNI_, S.nodes[s].n);
+  kB_ = 0;   // the batched apply re-plans on its next use
   smemIFmax_ = 8;
   smemIBmax_ = 8;
   for (size_t v : smemIF_) smemIFmax_ = std::max(smemIFmax_, v);
@@ -864,7 +828,7 @@ void SolveEngine<T>::plan_inverse(const std::vector<long long>& xOff) {
       t.tileBase = tiles;
       tiles += ((t.M + rpt - 1) / rpt) * t.tilesN;
     }
-    xSteps_.push_back(XStep{(long long)tasks.size(), (int)batch.size(), tiles});
+    xSteps_.push_back(XStep{(long long)tasks.size(), (int)batch.size(), tiles, tc ? 1 : 0});
     tasks.insert(tasks.end(), batch.begin(), batch.end());
     batch.clear();
   };
@@ -961,7 +925,7 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
   for (size_t l = 0; l < cLevels_.size(); ++l) {
     const int* lv = lvl + cLevels_[l].first;
     compressed_gather_rows<T><<<dim3(cRowGrid_[l], cLevels_[l].second), 256, 0, st>>>(
-        dNodes_.as<SNode<T>>(), lv, dCStart_.as<long long>(), dCEnt_.as<const T*>(), w);
+        dNodes_.as<SNode<T>>(), lv, dCStart_.as<long long>(), dCEnt_.as<long long>(), dWu_.as<T>(), w);
     RSCHOL_LAUNCH_CHECK();
     compressed_ytile_kernel<T><<<cTiles_[l].second, 256, 0, st>>>(
         dNodes_.as<SNode<T>>(), dTiles_.as<XTile>() + cTiles_[l].first, w, dXp_.as<T>());

@@ -84,9 +84,10 @@ struct DinvTask {    // invert one lower-triangular diagonal block (h x h, h <= 
   T* D;
 };
 
-struct XStep {       // one batched GEMM launch of the compressed L11^{-1} computation
+struct XStep {       // one batched GEMM launch (X = L11^{-1} doubling, batched apply)
   long long off;
   int count, tiles;
+  int tc;            // on the tensor cores
 };
 
 template <class T>
@@ -102,6 +103,12 @@ class SolveEngine {
   // Reads (synchronously) and clears the error word of the row-block waits:
   // 0, or 1 if a wait gave up (the result of that apply is undefined).
   int take_error(cudaStream_t s);
+  // Batched apply: W (n x k, row-major: the k right-hand sides of a row are
+  // contiguous) := M^{-1} W with one pass over the factor; k <=
+  // batch_capacity().  take_error_batch: as take_error, for the batched path.
+  void apply_batch(double* d_W, int k, cudaStream_t s);
+  int batch_capacity() const;
+  int take_error_batch(cudaStream_t s);
   long long launches_per_apply() const { return launchesPerApply_; }
   double bytes_per_apply() const { return bytesPerApply_; }
 
@@ -131,6 +138,14 @@ class SolveEngine {
   std::vector<size_t> smemIF_, smemIB_;
   long long launchesPerApply_ = 0;
   double bytesPerApply_ = 0;
+  // batched apply (planned for k right-hand sides on first use)
+  void plan_batch(int k);
+  long long wuTotal_ = 0, ipTotal_ = 0;
+  int maxNI_ = 0;                      // largest interior supernode width
+  std::vector<int> cMRowGrid_;         // per compressed level: 8-row blocks of the largest m
+  int kB_ = 0, epochB_ = 0;
+  DevBuf dWuB_, dYB_, dIpB_, dSyncB_, dWB_, dBGemm_;
+  std::vector<std::vector<XStep>> bSteps_;   // [6 * level + phase]
 };
 
 }  // namespace rschol

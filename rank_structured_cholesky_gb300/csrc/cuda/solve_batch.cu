@@ -1,0 +1,453 @@
+// Batched preconditioner apply: W (n x k, row-major, the k right-hand sides
+// of a row contiguous) := M^{-1} W with one pass over the factor.
+//
+// Same operator and schedule as SolveEngine::apply_inplace, with every vector
+// widened to k columns: the interior supernodes run in one ticketed launch
+// per direction (a warp per row, lanes across the right-hand sides), and the
+// compressed levels become batched GEMMs on the factor's GEMM kernels:
+//   forward   Y = X F (row blocks of X stop at the diagonal), Z = U^T Y,
+//             U_c = -V Z;
+//   backward  S = V^T X_R, G = Y - U S, X = X^T G (column blocks of X start at
+//             the diagonal).
+// Factor bytes are read once per apply whatever k is; vector bytes scale
+// with k.
+#include <algorithm>
+#include <stdexcept>
+#include <type_traits>
+
+#include "solve.cuh"
+#include "solve_dev.cuh"
+
+namespace rschol {
+
+namespace {
+
+using namespace solvedev;
+
+// f := L^{-1} f for k right-hand sides (f: n x k in shared memory, row
+// stride k) with the inverted 64 x 64 diagonal blocks of L; t: 64 x k
+// shared.  A warp per row, lanes across the right-hand sides.
+template <class T>
+__device__ void trsv_dinv_k(const T* __restrict__ L, int ld, int n, const T* __restrict__ D, T* f, T* t, int k) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  for (int i0 = 0; i0 < n; i0 += 64) {
+    const int h = min(64, n - i0);
+    for (int i = warp; i < h; i += nwarp) {
+      const T* row = L + (size_t)(i0 + i) * ld;
+      for (int c = lane; c < k; c += 32) {
+        T s = f[(size_t)(i0 + i) * k + c];
+        for (int j = 0; j < i0; ++j) s -= row[j] * f[(size_t)j * k + c];
+        t[(size_t)i * k + c] = s;
+      }
+    }
+    __syncthreads();
+    const T* Db = D + (size_t)i0 * 64;
+    for (int i = warp; i < h; i += nwarp) {
+      const T* row = Db + (size_t)i * h;
+      for (int c = lane; c < k; c += 32) {
+        T s = T(0);
+        for (int j = 0; j <= i; ++j) s += row[j] * t[(size_t)j * k + c];
+        f[(size_t)(i0 + i) * k + c] = s;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// f := L^{-T} f for k right-hand sides, same blocks.
+template <class T>
+__device__ void trsv_dinv_t_k(const T* __restrict__ L, int ld, int n, const T* __restrict__ D, T* f, T* t, int k) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  if (n <= 0) return;
+  for (int i0 = ((n - 1) / 64) * 64; i0 >= 0; i0 -= 64) {
+    const int h = min(64, n - i0);
+    for (int j = warp; j < h; j += nwarp)
+      for (int c = lane; c < k; c += 32) {
+        T s = f[(size_t)(i0 + j) * k + c];
+        for (int i = i0 + h; i < n; ++i) s -= L[(size_t)i * ld + i0 + j] * f[(size_t)i * k + c];
+        t[(size_t)j * k + c] = s;
+      }
+    __syncthreads();
+    const T* Db = D + (size_t)i0 * 64;
+    for (int j = warp; j < h; j += nwarp)
+      for (int c = lane; c < k; c += 32) {
+        T s = T(0);
+        for (int i = j; i < h; ++i) s += Db[(size_t)i * h + j] * t[(size_t)i * k + c];
+        f[(size_t)(i0 + j) * k + c] = s;
+      }
+    __syncthreads();
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) interior_forward_k(const SNode<T>* __restrict__ nodes,
+                                                          const RowBlock* __restrict__ work,
+                                                          const int* __restrict__ rel, const int* __restrict__ child,
+                                                          int* __restrict__ sync, int epoch, int k,
+                                                          const T* __restrict__ w, T* __restrict__ yout,
+                                                          T* __restrict__ wu) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ int sTicket;
+  int* err = sync;
+  if (threadIdx.x == 0) sTicket = atomicAdd(&sync[SYNC_TICK_F], 1);
+  __syncthreads();
+  if (sTicket >= (int)gridDim.x) {   // counters not reset: report, touch nothing
+    if (threadIdx.x == 0) atomicExch(err, 2);
+    return;
+  }
+  const RowBlock wk = work[sTicket];
+  const SNode<T>& nd = nodes[wk.node];
+  const int n = nd.n, a0 = wk.b * ICH, a1 = min(nd.m, a0 + ICH);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* f = reinterpret_cast<T*>(smraw);   // n x k
+  T* t = f + (size_t)n * k;             // 64 x k
+  T* wud = wu + nd.wuOff * k;
+  if (warp == 0)
+    for (int c = nd.childBegin; c < nd.childEnd; ++c) {
+      const SNode<T>& cn = nodes[child[c]];
+      if (!wait_geq(sync + cn.syncOff + 1, epoch * max(1, cn.nch), err)) break;
+    }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < n * k; idx += blockDim.x) f[idx] = w[(size_t)nd.c0 * k + idx];
+  for (int idx = a0 * k + threadIdx.x; idx < a1 * k; idx += blockDim.x) wud[idx] = T(0);
+  __syncthreads();
+  for (int c = nd.childBegin; c < nd.childEnd; ++c) {
+    const SNode<T>& cn = nodes[child[c]];
+    const T* wuc = wu + cn.wuOff * k;
+    const int* rl = rel + cn.relOff;
+    for (int idx = threadIdx.x; idx < cn.m * k; idx += blockDim.x) {
+      const int a = idx / k, q = idx - a * k;
+      const int tr = rl[a];
+      const T v = __ldcg(wuc + idx);
+      if (tr < n) f[(size_t)tr * k + q] += v;
+      else if (tr - n >= a0 && tr - n < a1) wud[(size_t)(tr - n) * k + q] += v;
+    }
+    __syncthreads();
+  }
+  trsv_dinv_k<T>(nd.L, nd.ld, n, nd.Dinv, f, t, k);
+  if (wk.b == 0)
+    for (int idx = threadIdx.x; idx < n * k; idx += blockDim.x) yout[(size_t)nd.c0 * k + idx] = f[idx];
+  // wud[a][c] -= L21[a] . y[:, c]: a warp per row, lanes across the right-hand sides
+  for (int a = a0 + warp; a < a1; a += 8) {
+    const T* row = nd.L + (size_t)(n + a) * nd.ld;
+    for (int c = lane; c < k; c += 32) {
+      T s = T(0);
+      for (int j = 0; j < n; ++j) s += row[j] * f[(size_t)j * k + c];
+      wud[(size_t)a * k + c] -= s;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(sync + nd.syncOff + 1, 1);
+  }
+  launch_done(&sync[SYNC_TICK_F], &sync[SYNC_DONE_F]);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) interior_backward_k(const SNode<T>* __restrict__ nodes,
+                                                           const RowBlock* __restrict__ work,
+                                                           const int* __restrict__ rows, int* __restrict__ sync,
+                                                           int epoch, int k, T* __restrict__ ipart,
+                                                           const T* __restrict__ yin, T* __restrict__ w) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ int sLast, sTicket;
+  int* err = sync;
+  if (threadIdx.x == 0) sTicket = atomicAdd(&sync[SYNC_TICK_B], 1);
+  __syncthreads();
+  if (sTicket >= (int)gridDim.x) {
+    if (threadIdx.x == 0) atomicExch(err, 2);
+    return;
+  }
+  const RowBlock wk = work[sTicket];
+  const SNode<T>& nd = nodes[wk.node];
+  if (nd.parentI >= 0 && (threadIdx.x >> 5) == 0) wait_geq(sync + nodes[nd.parentI].syncOff + 2, epoch, err);
+  __syncthreads();
+  const int n = nd.n, a0 = wk.b * ICH, a1 = min(nd.m, a0 + ICH);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* f = reinterpret_cast<T*>(smraw);   // n x k
+  T* t = f + (size_t)n * k;             // 64 x k
+  const int nch = (nd.m + ICH - 1) / ICH;
+  if (nch > 0) {
+    // part[j][c] = sum_{a in chunk} L21[a][j] x_{rows[a]}[c]: a warp per j
+    const int* rw = rows + nd.rowsOff;
+    const T* L21 = nd.L + (size_t)n * nd.ld;
+    T* part = ipart + (nd.zpOff + (size_t)wk.b * n) * k;
+    for (int j = warp; j < n; j += 8)
+      for (int c = lane; c < k; c += 32) {
+        T s = T(0);
+        for (int a = a0; a < a1; ++a) s += L21[(size_t)a * nd.ld + j] * __ldcg(w + (size_t)rw[a] * k + c);
+        part[(size_t)j * k + c] = s;
+      }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      sLast = (atomicAdd(sync + nd.syncOff, 1) == nch - 1);
+      __threadfence();
+    }
+    __syncthreads();
+    if (!sLast) {
+      launch_done(&sync[SYNC_TICK_B], &sync[SYNC_DONE_B]);
+      return;
+    }
+  }
+  for (int idx = threadIdx.x; idx < n * k; idx += blockDim.x) {
+    T s = T(0);
+    for (int c = 0; c < nch; ++c) s += __ldcg(ipart + (nd.zpOff + (size_t)c * n) * k + idx);
+    f[idx] = yin[(size_t)nd.c0 * k + idx] - s;
+  }
+  __syncthreads();
+  trsv_dinv_t_k<T>(nd.L, nd.ld, n, nd.Dinv, f, t, k);
+  for (int idx = threadIdx.x; idx < n * k; idx += blockDim.x) w[(size_t)nd.c0 * k + idx] = f[idx];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (nch > 0) sync[nd.syncOff] = 0;
+    st_release(sync + nd.syncOff + 2, epoch);
+  }
+  launch_done(&sync[SYNC_TICK_B], &sync[SYNC_DONE_B]);
+}
+
+// w[c0 + i][c] += fixed-order sum of row i's contributions (a warp per row).
+template <class T>
+__global__ void __launch_bounds__(256) compressed_gather_k(const SNode<T>* __restrict__ nodes,
+                                                           const int* __restrict__ lvl,
+                                                           const long long* __restrict__ cstart,
+                                                           const long long* __restrict__ ent, int k,
+                                                           const T* __restrict__ wu, T* __restrict__ w) {
+  const SNode<T>& nd = nodes[lvl[blockIdx.y]];
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= nd.n) return;
+  const long long* cs = cstart + nd.cOff;
+  for (int c = lane; c < k; c += 32) {
+    T acc = T(0);
+    for (long long e = cs[i]; e < cs[i + 1]; ++e) acc += wu[ent[e] * k + c];
+    w[(size_t)(nd.c0 + i) * k + c] += acc;
+  }
+}
+
+// X_R (m x k) of every compressed supernode of a level into its u region.
+template <class T>
+__global__ void __launch_bounds__(256) compressed_gather_xr_k(const SNode<T>* __restrict__ nodes,
+                                                              const int* __restrict__ lvl,
+                                                              const int* __restrict__ rows, int k,
+                                                              const T* __restrict__ w, T* __restrict__ wu) {
+  const SNode<T>& nd = nodes[lvl[blockIdx.y]];
+  const int lane = threadIdx.x & 31;
+  const int a = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (a >= nd.m || nd.r == 0) return;
+  const int g = rows[nd.rowsOff + a];
+  T* dst = wu + (nd.wuOff + 2 * nd.r + a) * k;
+  for (int c = lane; c < k; c += 32) dst[c] = w[(size_t)g * k + c];
+}
+
+template <class A, class B>
+__global__ void convert_k_kernel(const A* __restrict__ src, B* __restrict__ dst, long long count) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = (B)src[i];
+}
+
+}  // namespace
+
+template <class T>
+int SolveEngine<T>::batch_capacity() const {
+  const size_t per = sizeof(T) * (size_t)(maxNI_ + 64);
+  const int bySmem = (int)std::min<size_t>(64, (200 * 1024) / std::max<size_t>(per, 1));
+  return std::max(1, bySmem);
+}
+
+template <class T>
+void SolveEngine<T>::plan_batch(int k) {
+  if (k == kB_) return;
+  const Symbolic& S = F_.S;
+  cudaStream_t st = F_.stream;
+  dWuB_.alloc(sizeof(T) * std::max(1LL, wuTotal_ * k));
+  dYB_.alloc(sizeof(T) * std::max<long long>(1, (long long)S.n * k));
+  dIpB_.alloc(sizeof(T) * std::max(1LL, ipTotal_ * k));
+  dSyncB_.alloc(sizeof(int) * syncInts_);
+  RSCHOL_CUDA(cudaMemsetAsync(dSyncB_.p, 0, sizeof(int) * syncInts_, st));
+  dWB_.alloc(sizeof(T) * std::max<long long>(1, (long long)S.n * k));   // the working copy of W
+  epochB_ = 0;
+  // batched GEMMs of the compressed levels
+  const bool tc = std::is_same<T, float>::value && F_.tensor_cores();
+  std::vector<GemmTask<T>> tasks;
+  bSteps_.assign(6 * cLevels_.size(), {});
+  T* wu = dWuB_.as<T>();
+  T* yb = dYB_.as<T>();
+  T* w = dWB_.as<T>();
+  auto mk = [&](const T* A, int lda, bool tA, const T* B, int ldb, T* C, int ldc, int M, int N, int K, T alpha,
+                T beta) {
+    GemmTask<T> g{};
+    g.A = A;
+    g.B = B;
+    g.C = C;
+    g.M = M;
+    g.N = N;
+    g.K = K;
+    g.lda = lda;
+    g.ldb = ldb;
+    g.ldc = ldc;
+    g.tA = tA;
+    g.tB = 0;
+    g.alpha = alpha;
+    g.beta = beta;
+    g.tilesN = (N + 63) / 64;
+    g.split = 1;
+    g.kSplit = 1;
+    g.kLen = K;
+    return g;
+  };
+  auto flush = [&](std::vector<GemmTask<T>>& batch, int slot) {
+    if (batch.empty()) return;
+    int maxK = 0;
+    for (auto& g : batch) maxK = std::max(maxK, g.K);
+    const bool useTc = tc && maxK >= 128;
+    const int rpt = useTc ? 128 : 64;
+    int tiles = 0;
+    for (auto& g : batch) {
+      g.tileBase = tiles;
+      tiles += ((g.M + rpt - 1) / rpt) * g.tilesN;
+    }
+    bSteps_[slot].push_back(XStep{(long long)tasks.size(), (int)batch.size(), tiles, useTc ? 1 : 0});
+    tasks.insert(tasks.end(), batch.begin(), batch.end());
+    batch.clear();
+  };
+  const int L = (int)cLevels_.size();
+  for (int l = 0; l < L; ++l) {
+    std::vector<GemmTask<T>> gy, gz, gu, gs, gg, gx;
+    for (int q = 0; q < cLevels_[l].second; ++q) {
+      const int j = F_.compressedLevels[l][q];
+      const SNode<T>& nd = nodes_[j];
+      const int n = nd.n, m = nd.m, r = nd.r;
+      T* z = wu + nd.wuOff * k;
+      T* sv = wu + (nd.wuOff + r) * k;
+      T* u = wu + (nd.wuOff + 2 * r) * k;
+      T* yj = yb + (size_t)nd.c0 * k;
+      T* wj = w + (size_t)nd.c0 * k;
+      for (int ib = 0; ib < nd.nb; ++ib) {   // Y = X F by row blocks
+        const int h = std::min(64, n - ib * 64), K = std::min(n, (ib + 1) * 64);
+        gy.push_back(mk(nd.X + (size_t)ib * 64 * n, n, false, wj, k, yj + (size_t)ib * 64 * k, k, h, k, K, T(1),
+                        T(0)));
+      }
+      if (r > 0) {
+        gz.push_back(mk(nd.U, r, true, yj, k, z, k, r, k, n, T(1), T(0)));
+        if (m > 0 && l + 1 < L) gu.push_back(mk(nd.V, r, false, z, k, u, k, m, k, r, T(-1), T(0)));
+        if (m > 0) {
+          gs.push_back(mk(nd.V, r, true, u, k, sv, k, r, k, m, T(1), T(0)));
+          gg.push_back(mk(nd.U, r, false, sv, k, yj, k, n, k, r, T(-1), T(1)));
+        }
+      }
+      for (int jb = 0; jb < nd.nb; ++jb) {   // X = X^T G by column blocks
+        const int h = std::min(64, n - jb * 64), K = n - jb * 64;
+        gx.push_back(mk(nd.X + (size_t)jb * 64 * n + jb * 64, n, true, yj + (size_t)jb * 64 * k, k,
+                        wj + (size_t)jb * 64 * k, k, h, k, K, T(1), T(0)));
+      }
+    }
+    flush(gy, 6 * l + 0);
+    flush(gz, 6 * l + 1);
+    flush(gu, 6 * l + 2);
+    flush(gs, 6 * l + 3);
+    flush(gg, 6 * l + 4);
+    flush(gx, 6 * l + 5);
+  }
+  dBGemm_.alloc(std::max<size_t>(16, tasks.size() * sizeof(GemmTask<T>)));
+  if (!tasks.empty())
+    RSCHOL_CUDA(cudaMemcpyAsync(dBGemm_.p, tasks.data(), tasks.size() * sizeof(GemmTask<T>), cudaMemcpyHostToDevice,
+                                st));
+  RSCHOL_CUDA(cudaStreamSynchronize(st));
+  kB_ = k;
+}
+
+template <class T>
+void SolveEngine<T>::apply_batch(double* W64, int k, cudaStream_t st) {
+  if (k <= 0) return;
+  if (k > batch_capacity()) throw std::runtime_error("apply_batch: more right-hand sides than one pass handles");
+  plan_batch(k);
+  const int n = F_.S.n;
+  const long long nk = (long long)n * k;
+  T* w = dWB_.as<T>();
+  convert_k_kernel<double, T><<<(unsigned)std::min<long long>((nk + 255) / 256, 4096), 256, 0, st>>>(W64, w, nk);
+  RSCHOL_LAUNCH_CHECK();
+  if (++epochB_ >= (1 << 24)) {
+    RSCHOL_CUDA(cudaMemsetAsync(dSyncB_.p, 0, sizeof(int) * syncInts_, st));
+    epochB_ = 1;
+  }
+  int* sync = dSyncB_.as<int>();
+  const size_t smem = sizeof(T) * (size_t)(maxNI_ + 64) * k;
+  static bool configured = false;
+  if (!configured) {
+    RSCHOL_CUDA(cudaFuncSetAttribute(interior_forward_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    RSCHOL_CUDA(cudaFuncSetAttribute(interior_backward_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    configured = true;
+  }
+  if (nIWork_ > 0) {
+    interior_forward_k<T><<<nIWork_, 256, smem, st>>>(dNodes_.as<SNode<T>>(), dIWork_.as<RowBlock>(), dRel_.as<int>(),
+                                                       dChild_.as<int>(), sync, epochB_, k, w, dYB_.as<T>(),
+                                                       dWuB_.as<T>());
+    RSCHOL_LAUNCH_CHECK();
+  }
+  const int* lvl = dLevelNodes_.as<int>();
+  const GemmTask<T>* bg = dBGemm_.as<GemmTask<T>>();
+  auto gemm = [&](int slot) {
+    for (const XStep& x : bSteps_[slot]) {
+      if constexpr (std::is_same<T, float>::value) {
+        if (x.tc) launch_gemm_tc(bg + x.off, x.count, x.tiles, F_.dFlag.template as<int>() + 1, st);
+        else launch_gemm<T>(bg + x.off, x.count, x.tiles, st);
+      } else {
+        launch_gemm<T>(bg + x.off, x.count, x.tiles, st);
+      }
+    }
+  };
+  const int L = (int)cLevels_.size();
+  for (int l = 0; l < L; ++l) {
+    const int* lv = lvl + cLevels_[l].first;
+    compressed_gather_k<T><<<dim3(cRowGrid_[l], cLevels_[l].second), 256, 0, st>>>(
+        dNodes_.as<SNode<T>>(), lv, dCStart_.as<long long>(), dCEnt_.as<long long>(), k, dWuB_.as<T>(), w);
+    RSCHOL_LAUNCH_CHECK();
+    gemm(6 * l + 0);
+    gemm(6 * l + 1);
+    gemm(6 * l + 2);
+  }
+  for (int l = L - 1; l >= 0; --l) {
+    const int* lv = lvl + cLevels_[l].first;
+    compressed_gather_xr_k<T><<<dim3(cMRowGrid_[l], cLevels_[l].second), 256, 0, st>>>(
+        dNodes_.as<SNode<T>>(), lv, dRows_.as<int>(), k, w, dWuB_.as<T>());
+    RSCHOL_LAUNCH_CHECK();
+    gemm(6 * l + 3);
+    gemm(6 * l + 4);
+    gemm(6 * l + 5);
+  }
+  if (nIWork_ > 0) {
+    interior_backward_k<T><<<nIWork_, 256, smem, st>>>(dNodes_.as<SNode<T>>(), dIWorkB_.as<RowBlock>(),
+                                                        dRows_.as<int>(), sync, epochB_, k, dIpB_.as<T>(),
+                                                        dYB_.as<T>(), w);
+    RSCHOL_LAUNCH_CHECK();
+  }
+  convert_k_kernel<T, double><<<(unsigned)std::min<long long>((nk + 255) / 256, 4096), 256, 0, st>>>(w, W64, nk);
+  RSCHOL_LAUNCH_CHECK();
+}
+
+template <class T>
+int SolveEngine<T>::take_error_batch(cudaStream_t st) {
+  int e = 0;
+  if (!dSyncB_.p) return 0;
+  RSCHOL_CUDA(cudaMemcpyAsync(&e, dSyncB_.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  RSCHOL_CUDA(cudaStreamSynchronize(st));
+  if (e) {
+    RSCHOL_CUDA(cudaMemsetAsync(dSyncB_.p, 0, sizeof(int) * syncInts_, st));
+    RSCHOL_CUDA(cudaStreamSynchronize(st));
+    epochB_ = 0;
+  }
+  return e;
+}
+
+template int SolveEngine<double>::batch_capacity() const;
+template int SolveEngine<float>::batch_capacity() const;
+template void SolveEngine<double>::plan_batch(int);
+template void SolveEngine<float>::plan_batch(int);
+template void SolveEngine<double>::apply_batch(double*, int, cudaStream_t);
+template void SolveEngine<float>::apply_batch(double*, int, cudaStream_t);
+template int SolveEngine<double>::take_error_batch(cudaStream_t);
+template int SolveEngine<float>::take_error_batch(cudaStream_t);
+
+}  // namespace rschol

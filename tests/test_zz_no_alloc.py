@@ -1,9 +1,10 @@
 """The allocation-free preconditioner apply against the allocating one.
 
-rschol_precond_apply_device_noalloc runs the same kernels on the same factor
-as rschol_precond_apply_device; only the permuted work vector differs (a
-static device array instead of a buffer allocated on first use).  Two calls
-in a row, both precisions, two right-hand sides per call.
+rschol_precond_apply_device_noalloc runs the same single-vector kernels on
+the same factor as rschol_precond_apply_device called with one right-hand
+side; only the permuted work vector differs (a static device array instead
+of a buffer allocated on first use).  Two calls in a row, both precisions,
+two right-hand sides per no-alloc call.
 """
 import numpy as np
 import pytest
@@ -29,7 +30,8 @@ def test_noalloc_apply_matches_device_apply(precision):
         x_ref = torch.zeros_like(b)
         x_na = torch.full_like(b, float("nan"))
         torch.cuda.synchronize()   # the library works on its own stream
-        assert lib.rschol_precond_apply_device(G.h, b.data_ptr(), x_ref.data_ptr(), 2) == 0
+        for k in range(2):   # one right-hand side per call: the same single-vector kernels
+            assert lib.rschol_precond_apply_device(G.h, b[k].data_ptr(), x_ref[k].data_ptr(), 1) == 0
         assert lib.rschol_precond_apply_device_noalloc(G.h, b.data_ptr(), x_na.data_ptr(), 2) == 0
         ref, got = x_ref.cpu().numpy(), x_na.cpu().numpy()
         assert np.all(np.isfinite(got))
