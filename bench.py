@@ -40,6 +40,10 @@ CONFIGS = {
            ("elasticity", 48, 0, 0, 2), 1),
     "c4": ("2D 5-point variable-coefficient 1024^2, log-normal sigma=2 seed 3, 64 RHS",
            ("diffusion", 2, 1024, 2.0, 3), 64),
+    # serving stream (run_serving): a pool of matrices, Poisson arrivals
+    "c5": ("serving stream: 2000 requests, Poisson arrivals at 200/s, pool of 2D grids (side 64-1024) and 3D "
+           "grids (side 16-96), log-normal sigma=1 seed per matrix id, 1-16 RHS per request, to 1e-8",
+           None, 0),
     # a smaller case of c2 for multi-pass ncu captures (a few hundred MB on the device)
     "c2s": ("3D 7-point variable-coefficient diffusion 40^3, log-normal sigma=1 seed 1, harmonic faces",
             ("diffusion", 3, 40, 1.0, 1), 1),
@@ -153,6 +157,19 @@ def cpu_oracle_solve(prob, params):
 def run_reference(args):
     rank, world, dist = dist_setup(args.gpus)
     if rank != 0:
+        return 0
+    if args.config == "c5":
+        stream = serving_stream(args.requests, 200.0, seed=5)
+        probs, rhs = serving_pool([m for m in range(len(SERVING_POOL)) if SERVING_POOL[m][1] <= 32])
+        small = tuple(np.array(v)[[i for i in range(len(stream[0])) if int(stream[1][i]) in probs]] for v in stream)
+        vals = [serving_cpu_sample(small, probs, rhs, 20.0) for _ in range(max(1, args.steps // 5))]
+        cpu = vals[-1]
+        print(json.dumps({"impl": "reference", "metric": "serving: solve requests/s to 1e-8 relative residual",
+                          "value": cpu["value"], "unit": "requests/s", "n_gpus": args.gpus, "steps": len(vals),
+                          "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f64", "data": "synthetic", "config": {"workload": "c5"}, "cpu_baseline": cpu,
+                          "e2e": {"value": cpu["value"], "unit": "requests/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
         return 0
     prob = make_problem(args.config)
     params = dict()
@@ -406,6 +423,145 @@ def run_ours(args):
     return 0
 
 
+# ---- the serving stream ------------------------------------------------------
+SERVING_POOL = [(2, side) for side in (64, 128, 256, 512, 768, 1024)] + \
+               [(3, side) for side in (16, 32, 48, 64, 80, 96)]
+SERVING_RHS_POOL = 32   # random right-hand sides kept per matrix; a request takes a window of them
+
+
+def serving_stream(count, rate, seed):
+    """Arrival times, matrix ids, RHS counts and RHS offsets from one MT19937 stream."""
+    rng = np.random.RandomState(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
+    mids = rng.randint(0, len(SERVING_POOL), count)
+    nrhs = rng.randint(1, 17, count)
+    offs = rng.randint(0, SERVING_RHS_POOL - 16 + 1, count)
+    return arrivals, mids, nrhs, offs
+
+
+def serving_pool(ids):
+    import rank_structured_cholesky_gb300 as rs
+    probs, rhs = {}, {}
+    for m in ids:
+        dim, side = SERVING_POOL[m]
+        probs[m] = rs.diffusion(dim, side, sigma=1.0, seed=100 + m, nrhs=1)
+        rhs[m] = np.random.RandomState(1000 + m).standard_normal((SERVING_RHS_POOL, probs[m].n))
+    return probs, rhs
+
+
+def serve_stream(rs, precision, device, probs, rhs, stream, workers, budget, eps=1e-8):
+    """Submit the stream in real time, collect every result; returns the measurements."""
+    arrivals, mids, nrhs, offs = stream
+    srv = rs.Server(workers=workers, hbm_budget_bytes=budget, precision=precision, device=device)
+    rids = [None] * len(arrivals)
+    results = [None] * len(arrivals)
+    ready = threading.Semaphore(0)
+
+    def collect():
+        for i in range(len(arrivals)):
+            ready.acquire()
+            results[i] = srv.wait(rids[i])
+
+    th = threading.Thread(target=collect)
+    th.start()
+    t0 = time.perf_counter()
+    for i in range(len(arrivals)):
+        delay = t0 + arrivals[i] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        m = int(mids[i])
+        p = probs[m]
+        B = rhs[m][offs[i]:offs[i] + nrhs[i]]
+        rids[i] = srv.submit(m, p.colptr, p.rowind, p.vals, B, p.xyz, eps=eps)
+        ready.release()
+    th.join()
+    wall = time.perf_counter() - t0
+    stats = srv.stats()
+    srv.close()
+    lat = np.array([r[3]["latency"] for r in results])
+    status = [r[0] for r in results]
+    true_res = max(max(q["true_residual"] for q in r[2]) for r in results)
+    hits = [r[3]["cache_hit"] for r in results]
+    lat_hit = lat[np.array(hits, bool)] if any(hits) else lat
+    return {"value": len(arrivals) / wall, "rhs_per_s": float(np.sum(nrhs)) / wall, "wall_s": wall,
+            "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+            "p50_ms_cache_hits": 1e3 * float(np.percentile(lat_hit, 50)),
+            "p99_ms_cache_hits": 1e3 * float(np.percentile(lat_hit, 99)),
+            "failed": int(sum(1 for st in status if st != 0)), "max_true_residual": float(true_res),
+            "cache": {k: stats[k] for k in ("hits", "misses", "evictions", "peak_cached_bytes")},
+            "h2d_bytes": int(sum(8 * probs[int(m)].n * int(k) for m, k in zip(mids, nrhs))),
+            "iterations_mean": float(np.mean([q["iterations"] for r in results for q in r[2]]))}
+
+
+def serving_cpu_sample(stream, probs, rhs, seconds):
+    """The CPU oracle on the stream's requests for the smaller pool matrices
+    (factor cached per matrix, as the server does) for about `seconds`."""
+    from oracle import pyoracle as po
+    small = [i for i in range(len(stream[0])) if probs[int(stream[1][i])].n <= 40000]
+    facs, done, t0 = {}, 0, time.perf_counter()
+    for i in small:
+        m = int(stream[1][i])
+        if m not in facs:
+            p = probs[m]
+            facs[m] = po.OracleFactor(p.colptr, p.rowind, p.vals, p.xyz, dict())
+            assert facs[m].factor() == 0
+        for j in range(int(stream[2][i])):
+            facs[m].pcg(rhs[m][stream[3][i] + j], 1e-8, 10000)
+        done += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    el = time.perf_counter() - t0
+    return {"value": done / el, "unit": "requests/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "the first %d requests of the stream whose matrix has n <= 40000 (of %d such), FP64 "
+                      "oracle factor cached per matrix + PCG per RHS, threaded BLAS; larger matrices cost more"
+                      % (done, len(small))}
+
+
+def run_serving(args):
+    import torch
+    import rank_structured_cholesky_gb300 as rs
+    rank, world, dist = dist_setup(args.gpus)
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    count, rate = args.requests, 200.0
+    stream = serving_stream(count, rate, seed=5)
+    probs, rhs = serving_pool(sorted(set(int(m) for m in stream[1])))
+    budget = args.hbm_budget_gb * 1e9
+    prec = 0 if args.precision == "fp64" else 1
+    # warm-up: a short stream on the two smallest matrices (CUDA context, module loading)
+    warm = (np.arange(args.warmup * 4) * 0.002, np.array([0, 6] * (args.warmup * 2)),
+            np.full(args.warmup * 4, 4), np.zeros(args.warmup * 4, int))
+    wprobs, wrhs = serving_pool([0, 6])
+    serve_stream(rs, prec, local, wprobs, wrhs, warm, args.workers, budget)
+    with ClockSampler(local) as clocks:
+        main = serve_stream(rs, prec, local, probs, rhs, stream, args.workers, budget)
+    plain = None
+    if args.precision == "mixed" and not args.no_fp64_plain:
+        plain = serve_stream(rs, 0, local, probs, rhs, stream, args.workers, budget)
+    hbm, bf16, src = peaks()
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline and world == 1:
+        cpu = serving_cpu_sample(stream, probs, rhs, 20.0)
+    if rank == 0:
+        line = {
+            "metric": "serving: solve requests/s to 1e-8 relative residual", "value": main["value"],
+            "unit": "requests/s", "n_gpus": world, "steps": 1, "warmup": args.warmup,
+            "ms_per_step": 1e3 * main["wall_s"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == 0 else "f32 factor / f64 pcg", "data": "synthetic",
+            "config": {"workload": "c5", "description": CONFIGS["c5"][0], "requests": count, "rate_per_s": rate,
+                       "pool": ["%dD side %d (n=%d)" % (d, sd, probs[m].n) for m, (d, sd) in enumerate(SERVING_POOL)
+                                if m in probs],
+                       "workers": args.workers, "hbm_budget_gb": args.hbm_budget_gb, "precision": args.precision,
+                       "l2": "inputs larger than L2 (largest matrices)"},
+            "e2e": {"value": main["value"], "unit": "requests/s", "h2d_bytes_per_step": main["h2d_bytes"],
+                    "d2h_bytes_per_step": main["h2d_bytes"]},
+            "p50_ms": main["p50_ms"], "p99_ms": main["p99_ms"], "serving": main, "plain_fp64": plain,
+            "cpu_baseline": cpu, "clocks": clocks.summary(), "peak_source": src,
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def profile_phases(lib, F, ctx, stream, d_b, nrhs, torch):
     """CUDA-event timings of one preconditioner apply and one SpMV, launch counts."""
     out = np.zeros(16)
@@ -426,12 +582,17 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--requests", type=int, default=2000, help="c5: requests in the stream")
+    ap.add_argument("--workers", type=int, default=8, help="c5: server worker threads")
+    ap.add_argument("--hbm-budget-gb", type=float, default=200.0, help="c5: device bytes for cached factors")
     ap.add_argument("--profile", action="store_true",
                     help="warm up, then run the steps between cudaProfilerStart/Stop (for ncu), no timing line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "c5":
+        return run_serving(args)
     return run_ours(args)
 
 

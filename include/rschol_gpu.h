@@ -123,6 +123,58 @@ int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x
  *   - the first call on a device looks up the array's address
  *     (cudaGetSymbolAddress, with that device current); make that first call
  *     before any stream capture that would include this function. */
+/* ---- continuous batching on one factor (no reference counterpart) --------
+ * A session keeps the Krylov state of up to max_columns right-hand sides of
+ * one factor on the device (clamped to the factor's batch capacity, at most
+ * 64; rschol_session_columns gives the value used).  rschol_session_add
+ * queues a request of nrhs right-hand sides (b, x: host, stacked column after
+ * column, in the original order; both must stay valid until the request is
+ * done); its columns join the block at the next step as room allows.  Every
+ * rschol_session_step advances each active column by one iteration of
+ * PCG_SOLVER::solvePCG (src/rschol/linearalgebra/PCG_SOLVER.cpp:226-363,
+ * the recurrences of rschol_pcg), retires the columns that meet their
+ * stopping test (x written) and lists in done_tags (room for
+ * rschol_session_columns entries) the requests whose every column is done;
+ * rschol_session_result then gives their rschol_pcg_info and forgets them.
+ * A column's iterates do not depend on the other columns in the block.
+ * One thread at a time drives a session and its factor; the factor must
+ * outlive the session. */
+typedef struct rschol_session rschol_session;
+rschol_session* rschol_session_create(rschol_factor* f, int max_columns);
+int rschol_session_columns(const rschol_session* s);
+int rschol_session_add(rschol_session* s, long long tag, int nrhs, const double* b, double* x, double eps, int maxit);
+int rschol_session_step(rschol_session* s, long long* done_tags, int* ndone);
+int rschol_session_result(rschol_session* s, long long tag, rschol_pcg_info* info);
+int rschol_session_counts(const rschol_session* s, int* active, int* queued);
+void rschol_session_destroy(rschol_session* s);
+
+/* ---- serving loop (no reference counterpart: the reference's pcg_solver
+ * driver solves one system per process) --------------------------------------
+ * Continuous batching over many systems: requests (matrix id, CSC matrix as
+ * for rschol_factor_create, 1..64 right-hand sides stacked column after
+ * column) join the PCG session of their matrix's cached factor at the next
+ * iteration boundary; `workers` threads step the sessions of different
+ * matrices concurrently, each on its factor's own stream.  Factors are
+ * cached on the device by matrix id within hbm_budget_bytes of live device
+ * bytes (idle factors are evicted least recently used first; a factor that
+ * does not fit next to busy ones waits, one larger than the budget fails its
+ * requests with RSCHOL_E_OOM).  A request's result is the same alone and in
+ * a mix.  submit copies its arguments and returns a request id (> 0) or
+ * -status (only the request that builds a factor reads colptr/rowind/vals/
+ * xyz); wait blocks until the request is done and returns its status, x
+ * (stacked), info per right-hand side and times[5] = queued s (including
+ * the factorisation it waited for), factorisation s (0 on a cache hit), PCG
+ * s, latency s, cache hit (0/1).  stats[8] = completed, cache hits, misses,
+ * evictions, cached bytes, peak cached bytes, cached factors, waiting
+ * requests.  destroy finishes every submitted request first. */
+typedef struct rschol_server rschol_server;
+rschol_server* rschol_server_create(const rschol_params* p, int workers, double hbm_budget_bytes);
+int rschol_server_submit(rschol_server* s, int matrix_id, int n, const int* colptr, const int* rowind,
+                         const double* vals, const double* xyz, int nrhs, const double* b, double eps, int maxit);
+int rschol_server_wait(rschol_server* s, int request_id, double* x, rschol_pcg_info* info, double* times);
+int rschol_server_stats(rschol_server* s, double* stats);
+void rschol_server_destroy(rschol_server* s);
+
 /* Diagnostics (no reference counterpart): CUDA-event timing of every step of
  * the numeric factorisation while enabled.  out (may be null) receives, for
  * step kinds 0..6 (GEMM, POTRF, TRSM, extend-add, QR, identity basis, -),
@@ -162,6 +214,9 @@ void rschol_pcg_pysolve(int nrow, const int* jc, const int* ir, const double* pr
 
 /* ---- introspection (parity tests, benchmarks) ---------------------------- */
 int rschol_factor_n(const rschol_factor* f);
+/* live device bytes of the factor: factor arrays, solve and PCG work vectors
+ * (the work vectors grow with the number of right-hand sides per call) */
+double rschol_factor_device_bytes(const rschol_factor* f);
 int rschol_factor_num_nodes(const rschol_factor* f);
 /* info[0..7] = c0, c1, compressed, m (all rows), n_stored, rank, hodlr nodes, interior block */
 int rschol_factor_node_info(const rschol_factor* f, int node, int* info);

@@ -32,12 +32,15 @@ EXPORTED = [
     "rschol_default_params", "rschol_create", "rschol_destroy", "rschol_last_error", "rschol_factor_create",
     "rschol_refactor", "rschol_refactor_device", "rschol_stream", "rschol_profile", "rschol_factor_free", "rschol_precond_apply", "rschol_precond_apply_device",
     "rschol_precond_apply_device_noalloc", "rschol_selftest_gemm", "rschol_step_timing", "rschol_pcg",
-    "rschol_pcg_device", "rschol_pcg_pysolve", "rschol_factor_n", "rschol_factor_num_nodes",
+    "rschol_pcg_device", "rschol_pcg_pysolve", "rschol_factor_n", "rschol_factor_device_bytes", "rschol_factor_num_nodes",
     "rschol_factor_node_info", "rschol_factor_node_l11", "rschol_factor_node_l21", "rschol_factor_perm",
     "rschol_factor_describe", "rschol_factor_stats", "rschol_problem_diffusion", "rschol_problem_elasticity",
     "rschol_problem_n", "rschol_problem_nnz", "rschol_problem_nrhs", "rschol_problem_get", "rschol_problem_free",
     "rschol_mt_draws", "rschol_mt_gaussians", "rschol_block_rank", "rschol_separator_tree", "rschol_etree_counts",
-    "rschol_relaxed_supernodes",
+    "rschol_relaxed_supernodes", "rschol_session_create", "rschol_session_columns", "rschol_session_add",
+    "rschol_session_step", "rschol_session_result", "rschol_session_counts", "rschol_session_destroy",
+    "rschol_server_create", "rschol_server_submit", "rschol_server_wait",
+    "rschol_server_stats", "rschol_server_destroy",
 ]
 
 
@@ -96,6 +99,7 @@ def load_library():
         "rschol_pcg_device": (I, [P, P, P, I, D, I, ctypes.POINTER(PcgInfo)]),
         "rschol_pcg_pysolve": (None, [I, pI, pI, pD, pD, pD]),
         "rschol_factor_n": (I, [P]),
+        "rschol_factor_device_bytes": (D, [P]),
         "rschol_factor_num_nodes": (I, [P]),
         "rschol_factor_node_info": (I, [P, I, pI]),
         "rschol_factor_node_l11": (I, [P, I, pD]),
@@ -116,6 +120,18 @@ def load_library():
         "rschol_separator_tree": (I, [I, P, I, P, P]),
         "rschol_etree_counts": (None, [I, P, P, P, P]),
         "rschol_relaxed_supernodes": (I, [I, P, P, I, P, P, P, P, I, P, P]),
+        "rschol_session_create": (P, [P, I]),
+        "rschol_session_columns": (I, [P]),
+        "rschol_session_add": (I, [P, LL, I, pD, pD, D, I]),
+        "rschol_session_step": (I, [P, ctypes.POINTER(LL), pI]),
+        "rschol_session_result": (I, [P, LL, ctypes.POINTER(PcgInfo)]),
+        "rschol_session_counts": (I, [P, pI, pI]),
+        "rschol_session_destroy": (None, [P]),
+        "rschol_server_create": (P, [ctypes.POINTER(Params), I, D]),
+        "rschol_server_submit": (I, [P, I, I, pI, pI, pD, pD, I, pD, D, I]),
+        "rschol_server_wait": (I, [P, I, pD, ctypes.POINTER(PcgInfo), pD]),
+        "rschol_server_stats": (I, [P, pD]),
+        "rschol_server_destroy": (None, [P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -289,11 +305,137 @@ class GpuFactor:
         s = np.zeros(8)
         load_library().rschol_factor_stats(self.h, _dp(s))
         return dict(symbolic_s=s[0], numeric_s=s[1], attempts=int(s[2]), diag_rank_constant=s[3],
-                    factor_launches=int(s[4]), device_bytes=s[5], gaussian_draws=int(s[6]), factor_flops=s[7])
+                    factor_launches=int(s[4]), device_bytes=s[5], gaussian_draws=int(s[6]), factor_flops=s[7],
+                    live_device_bytes=load_library().rschol_factor_device_bytes(self.h))
 
     def close(self):
         if getattr(self, "h", None):
             load_library().rschol_factor_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Session:
+    """Continuous-batching PCG on one GpuFactor (rschol_session_*).
+
+    ``add`` queues a request of right-hand sides; ``step`` runs one PCG
+    iteration of every active column and returns the requests finished in
+    it as {tag: (status, x, info)}.
+    """
+
+    def __init__(self, factor, max_columns=64):
+        self.factor = factor
+        self.h = load_library().rschol_session_create(factor.h, max_columns)
+        if not self.h:
+            raise RscholError(4, factor.ctx.last_error())
+        self.columns = load_library().rschol_session_columns(self.h)
+        self._reqs = {}
+
+    def add(self, tag, b, eps=1e-8, maxit=10000):
+        b = np.ascontiguousarray(b, np.float64)
+        nrhs = 1 if b.ndim == 1 else b.shape[0]
+        x = np.zeros_like(b)
+        st = load_library().rschol_session_add(self.h, tag, nrhs, _dp(b), _dp(x), eps, maxit)
+        if st != RSCHOL_OK:
+            raise RscholError(st, "rschol_session_add")
+        self._reqs[tag] = (b, x, nrhs)   # the buffers stay alive until the request is done
+
+    def step(self):
+        lib = load_library()
+        tags = (ctypes.c_longlong * self.columns)()
+        nd = ctypes.c_int(0)
+        st = lib.rschol_session_step(self.h, tags, ctypes.byref(nd))
+        if st != RSCHOL_OK:
+            raise RscholError(st, self.factor.ctx.last_error())
+        out = {}
+        for i in range(nd.value):
+            b, x, nrhs = self._reqs.pop(tags[i])
+            infos = (PcgInfo * nrhs)()
+            rs = lib.rschol_session_result(self.h, tags[i], infos)
+            info = [dict(iterations=q.iterations, residual=q.residual, true_residual=q.true_residual,
+                         seconds=q.seconds) for q in infos]
+            out[tags[i]] = (rs, x, info)
+        return out
+
+    def counts(self):
+        a, q = ctypes.c_int(0), ctypes.c_int(0)
+        load_library().rschol_session_counts(self.h, ctypes.byref(a), ctypes.byref(q))
+        return a.value, q.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            load_library().rschol_session_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop over many systems on one GPU (no reference counterpart).
+
+    Requests are (matrix id, CSC matrix, right-hand sides); factors are cached
+    on the device by matrix id within ``hbm_budget_bytes`` and reused by later
+    requests for the same id; ``workers`` threads serve requests concurrently.
+    ``submit`` returns a request id, ``wait`` its solution, PCG info and times.
+    """
+
+    def __init__(self, params=None, workers=4, hbm_budget_bytes=64e9, **overrides):
+        lib = load_library()
+        self.params = params if params is not None else default_params(**overrides)
+        self.h = lib.rschol_server_create(ctypes.byref(self.params), workers, float(hbm_budget_bytes))
+        if not self.h:
+            raise RscholError(1, "rschol_server_create: bad arguments")
+        self._shapes = {}
+
+    def submit(self, matrix_id, colptr, rowind, vals, b, xyz=None, eps=1e-8, maxit=10000):
+        colptr = np.ascontiguousarray(colptr, np.int32)
+        rowind = np.ascontiguousarray(rowind, np.int32)
+        vals = np.ascontiguousarray(vals, np.float64)
+        b = np.ascontiguousarray(b, np.float64)
+        n = len(colptr) - 1
+        nrhs = 1 if b.ndim == 1 else b.shape[0]
+        xp = None
+        if xyz is not None:
+            xyz = np.ascontiguousarray(xyz, np.float64)
+            xp = _dp(xyz)
+        rid = load_library().rschol_server_submit(self.h, int(matrix_id), n, _ip(colptr), _ip(rowind), _dp(vals), xp,
+                                                  nrhs, _dp(b), eps, maxit)
+        if rid <= 0:
+            raise RscholError(-rid, "rschol_server_submit rejected the request")
+        self._shapes[rid] = b.shape
+        return rid
+
+    def wait(self, rid):
+        shape = self._shapes.pop(rid)
+        nrhs = 1 if len(shape) == 1 else shape[0]
+        x = np.zeros(shape)
+        infos = (PcgInfo * nrhs)()
+        times = np.zeros(5)
+        st = load_library().rschol_server_wait(self.h, rid, _dp(x), infos, _dp(times))
+        info = [dict(iterations=i.iterations, residual=i.residual, true_residual=i.true_residual,
+                     seconds=i.seconds) for i in infos]
+        t = dict(queued=times[0], factor=times[1], pcg=times[2], latency=times[3], cache_hit=bool(times[4]))
+        return st, x, info, t
+
+    def stats(self):
+        s = np.zeros(8)
+        load_library().rschol_server_stats(self.h, _dp(s))
+        keys = ["completed", "hits", "misses", "evictions", "cached_bytes", "peak_cached_bytes", "cached_factors",
+                "queued"]
+        return dict(zip(keys, s.tolist()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load_library().rschol_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

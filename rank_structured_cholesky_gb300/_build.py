@@ -20,7 +20,7 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_OUT = os.path.join(ORACLE_DIR, "_build")
 ORACLE_LIB = os.path.join(ORACLE_OUT, "liboracle.so")
 
-HOST_SRC = ["host/ordering.cpp", "host/symbolic.cpp", "host/problems.cpp", "host/capi_host.cpp"]
+HOST_SRC = ["host/ordering.cpp", "host/symbolic.cpp", "host/problems.cpp", "host/capi_host.cpp", "host/server.cpp"]
 CUDA_SRC = ["cuda/dense.cu", "cuda/gemm_tc.cu", "cuda/factor.cu", "cuda/solve.cu", "cuda/solve_batch.cu", "cuda/pcg.cu", "cuda/pcg_batch.cu", "cuda/capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -68,7 +68,8 @@ def build_library(verbose=False, jobs=None):
         if src.endswith(".cu"):
             cmd = [nvcc] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-c", path, "-o", obj]
         else:
-            cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-c", path, "-o", obj]
+            cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "include")
+            cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-I" + cuda_inc, "-c", path, "-o", obj]
         cmds.append(cmd)
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
         for out in ex.map(_run, cmds):

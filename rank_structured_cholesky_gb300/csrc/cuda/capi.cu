@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <sstream>
@@ -145,7 +146,12 @@ struct ImplT : Impl {
 
 }  // namespace
 
+namespace rschol {
+thread_local std::atomic<long long>* g_devAccount = nullptr;
+}
+
 struct rschol_factor {
+  std::atomic<long long> devBytes{0};   // live device bytes of this factor (first member: destroyed last)
   rschol_ctx* ctx = nullptr;
   Params prm;
   int precision = RSCHOL_FP64;
@@ -261,6 +267,7 @@ int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* r
   for (int k = 0; k < nnz; ++k)
     if (rowind[k] < 0 || rowind[k] >= n) return fail(ctx, RSCHOL_E_BAD_INPUT, "row index out of range");
   std::unique_ptr<rschol_factor> f(new rschol_factor());
+  AccountScope acct(&f->devBytes);
   f->ctx = ctx;
   f->prm = to_params(ctx->prm);
   f->precision = ctx->prm.precision;
@@ -329,6 +336,7 @@ int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* r
 
 int rschol_refactor(rschol_factor* f, const double* vals) {
   if (!f || !vals) return RSCHOL_E_BAD_INPUT;
+  AccountScope acct(&f->devBytes);
   try {
     std::vector<double> lower(f->lowerSrc.size());
     for (size_t k = 0; k < lower.size(); ++k) lower[k] = vals[f->lowerSrc[k]];
@@ -353,6 +361,7 @@ static void ensure_batch(rschol_factor* f, int k);
 
 int rschol_refactor_device(rschol_factor* f, const double* d_vals) {
   if (!f || !d_vals) return RSCHOL_E_BAD_INPUT;
+  AccountScope acct(&f->devBytes);
   try {
     cudaStream_t s = f->ctx->stream;
     launch_index_gather(d_vals, f->dLowerSrc.as<int>(), f->impl->device_values(), (long long)f->lowerSrc.size(), s);
@@ -371,6 +380,7 @@ void* rschol_stream(rschol_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr
 
 int rschol_profile(rschol_factor* f, const double* d_b, double* out) {
   if (!f || !d_b || !out) return RSCHOL_E_BAD_INPUT;
+  AccountScope acct(&f->devBytes);
   try {
     cudaStream_t s = f->ctx->stream;
     ensure_vecs(f, 1);
@@ -442,6 +452,7 @@ static void ensure_vecs(rschol_factor* f, int nrhs) {
 
 int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs) {
   if (!f || !d_b || !d_x || nrhs <= 0) return RSCHOL_E_BAD_INPUT;
+  AccountScope acct(&f->devBytes);
   try {
     ensure_vecs(f, 1);
     const int n = f->Afull.n;
@@ -472,6 +483,7 @@ int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x
 
 int rschol_precond_apply(rschol_factor* f, const double* b, double* x, int nrhs) {
   if (!f || !b || !x || nrhs <= 0) return RSCHOL_E_BAD_INPUT;
+  AccountScope acct(&f->devBytes);
   try {
     ensure_vecs(f, nrhs);
     const size_t bytes = sizeof(double) * (size_t)f->Afull.n * nrhs;
@@ -489,6 +501,7 @@ int rschol_precond_apply(rschol_factor* f, const double* b, double* x, int nrhs)
 int rschol_pcg_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs, double eps, int maxit,
                       rschol_pcg_info* info) {
   if (!f || !d_b || !d_x || nrhs <= 0 || maxit < 0) return RSCHOL_E_BAD_INPUT;
+  AccountScope acct(&f->devBytes);
   int status = RSCHOL_OK;
   try {
     ensure_vecs(f, 1);
@@ -544,6 +557,7 @@ int rschol_pcg_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs
 int rschol_pcg(rschol_factor* f, const double* b, double* x, int nrhs, double eps, int maxit,
                rschol_pcg_info* info) {
   if (!f || !b || !x || nrhs <= 0) return RSCHOL_E_BAD_INPUT;
+  AccountScope acct(&f->devBytes);
   try {
     ensure_vecs(f, nrhs);
     const size_t bytes = sizeof(double) * (size_t)f->Afull.n * nrhs;
@@ -579,6 +593,7 @@ void rschol_pcg_pysolve(int nrow, const int* jc, const int* ir, const double* pr
 }
 
 int rschol_factor_n(const rschol_factor* f) { return f ? f->Afull.n : 0; }
+double rschol_factor_device_bytes(const rschol_factor* f) { return f ? (double)f->devBytes.load() : 0.0; }
 int rschol_factor_num_nodes(const rschol_factor* f) { return f ? (int)f->S.nodes.size() : 0; }
 
 int rschol_factor_node_info(const rschol_factor* f, int j, int* info) {
@@ -810,3 +825,95 @@ extern "C" int rschol_precond_apply_device_noalloc(rschol_factor* f, const doubl
   }
   return RSCHOL_OK;
 }
+
+// ---- continuous batching: a PCG session on one factor ---------------------
+struct rschol_session {
+  rschol_factor* f = nullptr;
+  std::unique_ptr<PcgSession> ses;
+  struct Req {
+    int nrhs = 0, remaining = 0;
+    bool breakdown = false;
+    std::vector<rschol_pcg_info> info;
+    double t0 = 0;
+  };
+  std::map<long long, Req> reqs;
+};
+
+extern "C" rschol_session* rschol_session_create(rschol_factor* f, int max_columns) {
+  if (!f || max_columns < 1 || max_columns > 64) return nullptr;
+  AccountScope acct(&f->devBytes);
+  try {
+    Impl* impl = f->impl.get();
+    cudaStream_t s = f->ctx->stream;
+    const int k = std::min(max_columns, std::max(1, std::min(64, impl->batch_capacity())));
+    std::unique_ptr<rschol_session> out(new rschol_session());
+    out->f = f;
+    out->ses.reset(new PcgSession(
+        *f->pcg, k, f->dPerm.as<int>(), [impl, s](double* w, int kk) { impl->apply_batch(w, kk, s); },
+        [impl, s]() { return impl->apply_batch_error(s); }));
+    return out.release();
+  } catch (const std::exception& e) {
+    fail(f->ctx, RSCHOL_E_CUDA, e.what());
+    return nullptr;
+  }
+}
+
+extern "C" int rschol_session_columns(const rschol_session* s) { return s ? s->ses->kmax() : 0; }
+
+extern "C" int rschol_session_add(rschol_session* s, long long tag, int nrhs, const double* b, double* x, double eps,
+                                  int maxit) {
+  if (!s || !b || !x || nrhs < 1 || maxit < 1 || s->reqs.count(tag)) return RSCHOL_E_BAD_INPUT;
+  const int n = s->f->Afull.n;
+  rschol_session::Req& r = s->reqs[tag];
+  r.nrhs = r.remaining = nrhs;
+  r.info.assign(nrhs, rschol_pcg_info{});
+  r.t0 = now_s();
+  for (int c = 0; c < nrhs; ++c) s->ses->add(tag, c, b + (size_t)c * n, x + (size_t)c * n, eps, maxit);
+  return RSCHOL_OK;
+}
+
+extern "C" int rschol_session_step(rschol_session* s, long long* done_tags, int* ndone) {
+  if (!s || !ndone) return RSCHOL_E_BAD_INPUT;
+  *ndone = 0;
+  AccountScope acct(&s->f->devBytes);
+  try {
+    std::vector<PcgSession::Column> fin = s->ses->step();
+    const double t = now_s();
+    for (const PcgSession::Column& c : fin) {
+      rschol_session::Req& r = s->reqs[c.tag];
+      rschol_pcg_info& i = r.info[c.col];
+      i.iterations = c.iterations;
+      i.residual = c.residual;
+      i.true_residual = c.trueResidual;
+      i.seconds = t - r.t0;
+      if (c.breakdown) r.breakdown = true;
+      if (--r.remaining == 0 && done_tags) done_tags[(*ndone)++] = c.tag;
+    }
+  } catch (const WaitTimeout&) {
+    return fail(s->f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);
+  } catch (const std::exception& e) {
+    return fail(s->f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+  return RSCHOL_OK;
+}
+
+extern "C" int rschol_session_result(rschol_session* s, long long tag, rschol_pcg_info* info) {
+  if (!s) return RSCHOL_E_BAD_INPUT;
+  auto it = s->reqs.find(tag);
+  if (it == s->reqs.end() || it->second.remaining > 0) return RSCHOL_E_BAD_INPUT;
+  if (info)
+    for (int c = 0; c < it->second.nrhs; ++c) info[c] = it->second.info[c];
+  const int st = it->second.breakdown ? RSCHOL_E_BREAKDOWN : RSCHOL_OK;
+  s->reqs.erase(it);
+  return st;
+}
+
+extern "C" int rschol_session_counts(const rschol_session* s, int* active, int* queued) {
+  if (!s) return RSCHOL_E_BAD_INPUT;
+  if (active) *active = s->ses->active();
+  if (queued) *queued = s->ses->queued();
+  return RSCHOL_OK;
+}
+
+extern "C" void rschol_session_destroy(rschol_session* s) { delete s; }
+

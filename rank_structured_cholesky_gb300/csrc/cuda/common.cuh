@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -22,16 +23,42 @@ struct CudaError : std::runtime_error {
 
 #define RSCHOL_LAUNCH_CHECK() RSCHOL_CUDA(cudaGetLastError())
 
+// Live device bytes are charged to the account current on the allocating
+// thread (each factor has one, made current by its entry points) and credited
+// back to the same account on release, from whichever thread releases.
+extern thread_local std::atomic<long long>* g_devAccount;
+
+struct AccountScope {
+  std::atomic<long long>* prev;
+  explicit AccountScope(std::atomic<long long>* a) : prev(g_devAccount) { g_devAccount = a; }
+  ~AccountScope() { g_devAccount = prev; }
+  AccountScope(const AccountScope&) = delete;
+  AccountScope& operator=(const AccountScope&) = delete;
+};
+
 // Device allocation owned by the host object that created it.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  std::atomic<long long>* acct = nullptr;   // the account charged for these bytes
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
-  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes), acct(o.acct) {
+    o.p = nullptr;
+    o.bytes = 0;
+    o.acct = nullptr;
+  }
   DevBuf& operator=(DevBuf&& o) noexcept {
-    if (this != &o) { release(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+    if (this != &o) {
+      release();
+      p = o.p;
+      bytes = o.bytes;
+      acct = o.acct;
+      o.p = nullptr;
+      o.bytes = 0;
+      o.acct = nullptr;
+    }
     return *this;
   }
   ~DevBuf() { release(); }
@@ -44,11 +71,17 @@ struct DevBuf {
       throw CudaError(std::string("cudaMalloc(") + std::to_string(b) + "): " + cudaGetErrorString(e));
     }
     bytes = b;
+    acct = g_devAccount;
+    if (acct) acct->fetch_add((long long)b);
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      if (acct) acct->fetch_sub((long long)bytes);
+    }
     p = nullptr;
     bytes = 0;
+    acct = nullptr;
   }
   template <class T> T* as() const { return reinterpret_cast<T*>(p); }
 };

@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <climits>
+#include <mutex>
 #include <type_traits>
 
 #include "common.cuh"
@@ -683,20 +684,18 @@ template <class T> void launch_potrf(const PotrfTask<T>* d, int n, int* flag, cu
 }
 template <class T> void launch_trsm(const TrsmTask<T>* d, int n, int chunks, cudaStream_t s) {
   if (n <= 0 || chunks <= 0) return;
-  static bool configured = false;   // per instantiation
+  static std::once_flag once;   // per instantiation; callers may be on several threads
   if constexpr (std::is_same<T, float>::value) {
     const int smem = (int)(3 * sizeof(T) * 64 * 65);
-    if (!configured) {
+    std::call_once(once, [&] {
       RSCHOL_CUDA(cudaFuncSetAttribute(trsm_inv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-      configured = true;
-    }
+    });
     trsm_inv_kernel<T><<<chunks, 256, smem, s>>>(d, n);
   } else {
     const int smem = (int)(2 * sizeof(T) * 64 * 65);
-    if (!configured) {
+    std::call_once(once, [&] {
       RSCHOL_CUDA(cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-      configured = true;
-    }
+    });
     trsm_kernel<T><<<chunks, 256, smem, s>>>(d, n);
   }
   RSCHOL_LAUNCH_CHECK();
@@ -717,11 +716,10 @@ void launch_scatter(const double* A, const long long* si, const long long* di, l
 }
 template <class T> int launch_householder_qr(const QrTask<T>* d, int n, int maxRows, int maxR, cudaStream_t s) {
   if (n <= 0 || maxR <= 0) return 0;
-  static bool attr = false;
-  if (!attr) {
+  static std::once_flag once;
+  std::call_once(once, [] {
     RSCHOL_CUDA(cudaFuncSetAttribute(qr_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, QR_SMEM_MAX));
-    attr = true;
-  }
+  });
   const long long tiles = (long long)((maxRows + 31) / 32) * ((maxR + 31) / 32);
   qr_to_colmajor<T><<<dim3((unsigned)std::min<long long>(tiles, 64), n), 256, 0, s>>>(d);
   RSCHOL_LAUNCH_CHECK();

@@ -18,6 +18,7 @@
 // MMAs per K step, FP32 accuracy up to the dropped A_lo B_lo term), for the
 // Schur-complement updates whose errors the factor cannot absorb.
 #include <cstdint>
+#include <mutex>
 
 #include "common.cuh"
 #include "dense.cuh"
@@ -327,11 +328,10 @@ __global__ void gemm_splitk_reduce(const GemmTask<float>* __restrict__ tasks, co
 
 void launch_gemm_tc(const GemmTask<float>* d, int nTasks, int tiles, int* dErr, cudaStream_t s) {
   if (nTasks <= 0 || tiles <= 0) return;
-  static bool configured = false;
-  if (!configured) {
+  static std::once_flag once;
+  std::call_once(once, [] {
     RSCHOL_CUDA(cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
-    configured = true;
-  }
+  });
   gemm_tc_kernel<<<tiles, TC_THREADS, TC_SMEM, s>>>(d, nTasks, dErr);
   RSCHOL_LAUNCH_CHECK();
 }

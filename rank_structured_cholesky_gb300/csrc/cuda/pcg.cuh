@@ -14,7 +14,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <deque>
 #include <functional>
+#include <stdexcept>
 #include <vector>
 
 #include "common.cuh"
@@ -52,6 +54,7 @@ class PcgEngine {
   int n;
 
  private:
+  friend class PcgSession;
   cudaStream_t stream_;
   DevBuf rowptr_, colind_, vals_, r_, d_, q_, s_, part_, scal_;
   double* hScal_ = nullptr;   // pinned
@@ -61,6 +64,61 @@ class PcgEngine {
   int kB_ = 0;
   DevBuf rB_, dB_, qB_, sB_, partB_, scalB_;
   double* hScalB_ = nullptr;   // pinned, k x S_COUNT
+};
+
+// Continuous batching on one factor (one thread drives a session).  Columns
+// are queued by add() and join the block at the next step(); every step()
+// advances each active column by one PCG iteration (the reference's
+// recurrences, rotated so that a column can join at the preconditioner
+// step) and retires the columns that meet their stopping test, writing x to
+// the column's host pointer.  Up to kmax columns are active at a time.
+struct WaitTimeout : std::runtime_error {
+  WaitTimeout() : std::runtime_error("preconditioner solve: a bounded wait gave up") {}
+};
+
+class PcgSession {
+ public:
+  struct Column {
+    long long tag = 0;
+    int col = 0;
+    const double* b = nullptr;   // host, original order, n values
+    double* xOut = nullptr;      // host, original order, n values
+    double eps = 1e-8;
+    int maxit = 0;
+    int iterations = 0;
+    double residual = 0, trueResidual = 0;
+    bool breakdown = false, finished = false;
+  };
+  // apply(W, k): in-place M^{-1} of an n x k permuted block;
+  // applyError(): 0, or non-zero when a wait of the last applies gave up.
+  PcgSession(PcgEngine& pcg, int kmax, const int* dPerm, std::function<void(double*, int)> apply,
+             std::function<int()> applyError);
+  ~PcgSession();
+  void add(long long tag, int col, const double* b, double* x, double eps, int maxit);
+  std::vector<Column> step();
+  int active() const {   // retired columns leave the block at the next step
+    int a = 0;
+    for (const Column& c : cols_) a += c.finished ? 0 : 1;
+    return a;
+  }
+  int queued() const { return (int)queue_.size(); }
+  int kmax() const { return kmax_; }
+  long long launches = 0;
+
+ private:
+  PcgEngine& pcg_;
+  int kmax_;
+  const int* perm_;
+  std::function<void(double*, int)> apply_;
+  std::function<int()> applyError_;
+  std::vector<Column> cols_;
+  std::deque<Column> queue_;
+  DevBuf x_[2], r_[2], d_[2], b_[2], s_, q_, part_, sc_;
+  int cap_[2] = {0, 0}, capS_ = 0;   // columns the blocks hold
+  int cur_ = 0;
+  void reserve_set(int set, int k);
+  double* hsc_ = nullptr;   // pinned, per column scalars
+  std::vector<double> hscNew_;
 };
 
 // permuted <-> original order for k right-hand sides: the stacked vectors

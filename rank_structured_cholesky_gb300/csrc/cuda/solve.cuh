@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <stdexcept>
+#include <map>
 #include <vector>
 
 #include "factor.cuh"
@@ -138,14 +139,21 @@ class SolveEngine {
   std::vector<size_t> smemIF_, smemIB_;
   long long launchesPerApply_ = 0;
   double bytesPerApply_ = 0;
-  // batched apply (planned for k right-hand sides on first use)
+  // batched apply: work buffers sized for the widest k seen (they only grow,
+  // so a changing width frees nothing and never synchronises the device);
+  // the GEMM task lists are built once per width and kept
   void plan_batch(int k);
   long long wuTotal_ = 0, ipTotal_ = 0;
   int maxNI_ = 0;                      // largest interior supernode width
   std::vector<int> cMRowGrid_;         // per compressed level: 8-row blocks of the largest m
-  int kB_ = 0, epochB_ = 0;
-  DevBuf dWuB_, dYB_, dIpB_, dSyncB_, dWB_, dBGemm_;
-  std::vector<std::vector<XStep>> bSteps_;   // [6 * level + phase]
+  int kB_ = 0, kAllocB_ = 0, epochB_ = 0;
+  DevBuf dWuB_, dYB_, dIpB_, dSyncB_, dWB_;
+  struct BatchPlan {
+    DevBuf tasks;
+    std::vector<std::vector<XStep>> steps;   // [6 * level + phase]
+  };
+  std::map<int, BatchPlan> bPlans_;
+  const BatchPlan* bPlan_ = nullptr;
 };
 
 }  // namespace rschol

@@ -12,6 +12,7 @@
 // Factor bytes are read once per apply whatever k is; vector bytes scale
 // with k.
 #include <algorithm>
+#include <mutex>
 #include <stdexcept>
 #include <type_traits>
 
@@ -261,17 +262,31 @@ void SolveEngine<T>::plan_batch(int k) {
   if (k == kB_) return;
   const Symbolic& S = F_.S;
   cudaStream_t st = F_.stream;
-  dWuB_.alloc(sizeof(T) * std::max(1LL, wuTotal_ * k));
-  dYB_.alloc(sizeof(T) * std::max<long long>(1, (long long)S.n * k));
-  dIpB_.alloc(sizeof(T) * std::max(1LL, ipTotal_ * k));
-  dSyncB_.alloc(sizeof(int) * syncInts_);
-  RSCHOL_CUDA(cudaMemsetAsync(dSyncB_.p, 0, sizeof(int) * syncInts_, st));
-  dWB_.alloc(sizeof(T) * std::max<long long>(1, (long long)S.n * k));   // the working copy of W
-  epochB_ = 0;
+  if (k > kAllocB_) {
+    dWuB_.alloc(sizeof(T) * std::max(1LL, wuTotal_ * k));
+    dYB_.alloc(sizeof(T) * std::max<long long>(1, (long long)S.n * k));
+    dIpB_.alloc(sizeof(T) * std::max(1LL, ipTotal_ * k));
+    if (!dSyncB_.p) {
+      dSyncB_.alloc(sizeof(int) * syncInts_);
+      RSCHOL_CUDA(cudaMemsetAsync(dSyncB_.p, 0, sizeof(int) * syncInts_, st));
+      epochB_ = 0;
+    }
+    dWB_.alloc(sizeof(T) * std::max<long long>(1, (long long)S.n * k));   // the working copy of W
+    kAllocB_ = k;
+    bPlans_.clear();   // the task lists point into the old buffers
+  }
+  auto found = bPlans_.find(k);
+  if (found != bPlans_.end()) {
+    bPlan_ = &found->second;
+    kB_ = k;
+    return;
+  }
+  BatchPlan& plan = bPlans_[k];
   // batched GEMMs of the compressed levels
   const bool tc = std::is_same<T, float>::value && F_.tensor_cores();
   std::vector<GemmTask<T>> tasks;
-  bSteps_.assign(6 * cLevels_.size(), {});
+  auto& steps = plan.steps;
+  steps.assign(6 * cLevels_.size(), {});
   T* wu = dWuB_.as<T>();
   T* yb = dYB_.as<T>();
   T* w = dWB_.as<T>();
@@ -308,7 +323,7 @@ void SolveEngine<T>::plan_batch(int k) {
       g.tileBase = tiles;
       tiles += ((g.M + rpt - 1) / rpt) * g.tilesN;
     }
-    bSteps_[slot].push_back(XStep{(long long)tasks.size(), (int)batch.size(), tiles, useTc ? 1 : 0});
+    steps[slot].push_back(XStep{(long long)tasks.size(), (int)batch.size(), tiles, useTc ? 1 : 0});
     tasks.insert(tasks.end(), batch.begin(), batch.end());
     batch.clear();
   };
@@ -350,11 +365,12 @@ void SolveEngine<T>::plan_batch(int k) {
     flush(gg, 6 * l + 4);
     flush(gx, 6 * l + 5);
   }
-  dBGemm_.alloc(std::max<size_t>(16, tasks.size() * sizeof(GemmTask<T>)));
+  plan.tasks.alloc(std::max<size_t>(16, tasks.size() * sizeof(GemmTask<T>)));
   if (!tasks.empty())
-    RSCHOL_CUDA(cudaMemcpyAsync(dBGemm_.p, tasks.data(), tasks.size() * sizeof(GemmTask<T>), cudaMemcpyHostToDevice,
-                                st));
+    RSCHOL_CUDA(cudaMemcpyAsync(plan.tasks.p, tasks.data(), tasks.size() * sizeof(GemmTask<T>),
+                                cudaMemcpyHostToDevice, st));
   RSCHOL_CUDA(cudaStreamSynchronize(st));
+  bPlan_ = &plan;
   kB_ = k;
 }
 
@@ -374,12 +390,11 @@ void SolveEngine<T>::apply_batch(double* W64, int k, cudaStream_t st) {
   }
   int* sync = dSyncB_.as<int>();
   const size_t smem = sizeof(T) * (size_t)(maxNI_ + 64) * k;
-  static bool configured = false;
-  if (!configured) {
+  static std::once_flag once;
+  std::call_once(once, [] {
     RSCHOL_CUDA(cudaFuncSetAttribute(interior_forward_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     RSCHOL_CUDA(cudaFuncSetAttribute(interior_backward_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    configured = true;
-  }
+  });
   if (nIWork_ > 0) {
     interior_forward_k<T><<<nIWork_, 256, smem, st>>>(dNodes_.as<SNode<T>>(), dIWork_.as<RowBlock>(), dRel_.as<int>(),
                                                        dChild_.as<int>(), sync, epochB_, k, w, dYB_.as<T>(),
@@ -387,9 +402,9 @@ void SolveEngine<T>::apply_batch(double* W64, int k, cudaStream_t st) {
     RSCHOL_LAUNCH_CHECK();
   }
   const int* lvl = dLevelNodes_.as<int>();
-  const GemmTask<T>* bg = dBGemm_.as<GemmTask<T>>();
+  const GemmTask<T>* bg = bPlan_->tasks.template as<GemmTask<T>>();
   auto gemm = [&](int slot) {
-    for (const XStep& x : bSteps_[slot]) {
+    for (const XStep& x : bPlan_->steps[slot]) {
       if constexpr (std::is_same<T, float>::value) {
         if (x.tc) launch_gemm_tc(bg + x.off, x.count, x.tiles, F_.dFlag.template as<int>() + 1, st);
         else launch_gemm<T>(bg + x.off, x.count, x.tiles, st);
