@@ -1,8 +1,8 @@
 // Batched PCG: k right-hand sides in lockstep on one factor (the c4 form of
 // PCG_SOLVER::solvePCG, src/rschol/linearalgebra/PCG_SOLVER.cpp:226-363).
-// Vectors are n x k row-major blocks; every kernel keeps one partial sum per
-// column and block, reduced in a fixed order, so each column's arithmetic is
-// reproducible.  A column that reaches its tolerance keeps alpha = 0 from
+// Vectors are n x k row-major blocks; every column sum follows one fixed
+// order that depends on n alone (below), so each column's arithmetic is
+// reproducible and the same whatever k is.  A column that reaches its tolerance keeps alpha = 0 from
 // then on (x and r frozen), as if its own loop had stopped.
 #include <algorithm>
 #include <cmath>
@@ -20,67 +20,142 @@ constexpr int KMAX = 64;
 enum { S_DELTA = 0, S_ALPHA, S_BETA, S_RREL, S_BNORM, S_DQ, S_ACTIVE, S_BREAK, S_FRESH, S_COUNT };
 enum { F_ALPHA = 0, F_RNORM, F_BETA, F_DELTA0, F_BNORM, F_TRUE, F_SLOT };
 
-// Per-column block sums: each thread holds up to two columns (lane, lane+32)
-// of its rows; warps add in smem in warp order.  part[blockIdx.x * k + c].
-__device__ void block_sum_cols(const double (&acc)[2], int k, double* part) {
-  __shared__ double red[BT / 32][KMAX];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int q = 0; q < 2; ++q)
-    if (lane + 32 * q < k) red[warp][lane + 32 * q] = acc[q];
-  __syncthreads();
-  if (threadIdx.x < k) {
-    double s = 0.0;
-    for (int w = 0; w < BT / 32; ++w) s += red[w][threadIdx.x];
-    part[(size_t)blockIdx.x * k + threadIdx.x] = s;
+// Row tiles and the order of every column sum.  Rows are cut into tiles of
+// 32.  A tile's 32 row values meet in a pairwise tree (rows s and s ^ 1,
+// then pairs of pairs, ...); warp w of the fixed grid adds the sums of tiles
+// w, w + W, w + 2W, ... (W warps) in order; the 8 warps of a block are added
+// in order; finish_k_kernel adds the blocks.  This order depends on n alone.
+// How lanes cover (tile row, column) pairs depends on k: with KP (k rounded
+// up to a power of two) columns, KL = min(KP, 32) lanes run along the
+// columns and G = 32 / KL along the tile rows.  For G > 1 each lane holds
+// rows g + G j of a tile and the tree is a butterfly (across lanes, then
+// within the lane); for G = 1 a lane walks the tile's rows in order and
+// builds the same tree on a five-entry stack (two columns per lane at KP =
+// 64).  So every lane has work at any k, loads are coalesced along rows
+// (small k) or along columns (large k), and a column's arithmetic does not
+// depend on k.
+template <int KP>
+struct Lay {
+  static constexpr int CPL = KP > 32 ? 2 : 1;   // columns per lane
+  static constexpr int KL = KP > 32 ? 32 : KP;  // lanes along the columns
+  static constexpr int G = 32 / KL;             // lanes along the tile rows
+  static constexpr int SPL = 32 / G;            // tile rows per lane
+};
+
+// trailing one bits of s: the tree level a stack entry is stored at
+__host__ __device__ constexpr int trailing_ones(int s) { return (s & 1) ? 1 + trailing_ones(s >> 1) : 0; }
+
+// Rows S.. of a tile for the G = 1 layout: push row S's value on the stack,
+// combining it with the stored left subtrees (compile-time indices).
+template <int S, int CPL, class Leaf>
+__device__ __forceinline__ void tree_rows(int row0, int n, int k, int cl, double (&st)[CPL][5], double (&W)[CPL],
+                                          Leaf& leaf) {
+  if constexpr (S < 32) {
+    const int row = row0 + S;
+#pragma unroll
+    for (int q = 0; q < CPL; ++q) {
+      const int c = cl + 32 * q;
+      double v = (row < n && c < k) ? leaf(row, c) : 0.0;
+#pragma unroll
+      for (int b = 0; b < trailing_ones(S); ++b) v = st[q][b] + v;
+      if constexpr (S < 31) st[q][trailing_ones(S)] = v;
+      else W[q] += v;
+    }
+    tree_rows<S + 1, CPL>(row0, n, k, cl, st, W, leaf);
   }
 }
 
-// y = A x (a warp per row, lanes across the columns), and the partials of
-// the column dots x . y.
+// Column sums of leaf(row, c) over the rows of this warp's tiles, reduced
+// to part[blockIdx.x * k + c].  Every thread of the block must call it.
+template <int KP, class Leaf>
+__device__ __forceinline__ void tile_sums(int n, int k, Leaf&& leaf, double* part) {
+  using L = Lay<KP>;
+  __shared__ double red[BT / 32][KMAX];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane / L::KL, cl = lane % L::KL;
+  const int nt = (n + 31) / 32;
+  double W[L::CPL];
+#pragma unroll
+  for (int q = 0; q < L::CPL; ++q) W[q] = 0.0;
+  for (int tile = blockIdx.x * (BT / 32) + warp; tile < nt; tile += gridDim.x * (BT / 32)) {
+    if constexpr (L::G == 1) {
+      double st[L::CPL][5];
+      tree_rows<0, L::CPL>(tile * 32, n, k, cl, st, W, leaf);
+    } else {
+      double v[L::SPL];
+#pragma unroll
+      for (int j = 0; j < L::SPL; ++j) {
+        const int row = tile * 32 + g + L::G * j;
+        v[j] = (row < n && cl < k) ? leaf(row, cl) : 0.0;
+      }
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        if (o < L::G) {   // partner row in lane ^ (o * KL)
+#pragma unroll
+          for (int j = 0; j < L::SPL; ++j) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o * L::KL);
+        } else {          // partner row in this lane
+          const int jo = o / L::G;
+#pragma unroll
+          for (int j = 0; j < L::SPL; ++j)
+            if ((j & jo) == 0) {
+              const double t = v[j] + v[j ^ jo];
+              v[j] = t;
+              v[j ^ jo] = t;
+            }
+        }
+      }
+      W[0] += v[0];
+    }
+  }
+  if (g == 0)
+#pragma unroll
+    for (int q = 0; q < L::CPL; ++q)
+      if (cl + 32 * q < k) red[warp][cl + 32 * q] = W[q];
+  __syncthreads();
+  if ((int)threadIdx.x < k) {
+    double t = 0.0;
+    for (int w = 0; w < BT / 32; ++w) t += red[w][threadIdx.x];
+    part[(size_t)blockIdx.x * k + threadIdx.x] = t;
+  }
+}
+
+// y = A x, and the partials of the column dots x . y.  Each y value is the
+// serial sum over its row's nonzeros.
+template <int KP>
 __global__ void __launch_bounds__(BT) spmv_k_kernel(int n, int k, const int* __restrict__ rp,
                                                      const int* __restrict__ ci, const double* __restrict__ v,
                                                      const double* __restrict__ x, double* __restrict__ y,
                                                      double* __restrict__ part) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double acc[2] = {0.0, 0.0};
-  for (int row = blockIdx.x * (BT / 32) + warp; row < n; row += gridDim.x * (BT / 32)) {
-    double s[2] = {0.0, 0.0};
-    for (int p = rp[row]; p < rp[row + 1]; ++p) {
-      const double a = v[p];
-      const double* xr = x + (size_t)ci[p] * k;
-      for (int q = 0; q < 2; ++q)
-        if (lane + 32 * q < k) s[q] += a * xr[lane + 32 * q];
-    }
-    for (int q = 0; q < 2; ++q)
-      if (lane + 32 * q < k) {
-        const size_t o = (size_t)row * k + lane + 32 * q;
-        y[o] = s[q];
-        acc[q] += x[o] * s[q];
-      }
-  }
-  block_sum_cols(acc, k, part);
+  tile_sums<KP>(n, k, [&](int row, int c) {
+    double s = 0.0;
+    for (int p = rp[row]; p < rp[row + 1]; ++p) s += v[p] * x[(size_t)ci[p] * k + c];
+    const size_t o = (size_t)row * k + c;
+    y[o] = s;
+    return x[o] * s;
+  }, part);
 }
 
+template <int KP>
 __global__ void __launch_bounds__(BT) dot_k_kernel(const double* __restrict__ a, const double* __restrict__ b, int n,
                                                    int k, double* __restrict__ part) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double acc[2] = {0.0, 0.0};
-  for (int row = blockIdx.x * (BT / 32) + warp; row < n; row += gridDim.x * (BT / 32))
-    for (int q = 0; q < 2; ++q)
-      if (lane + 32 * q < k) {
-        const size_t o = (size_t)row * k + lane + 32 * q;
-        acc[q] += a[o] * b[o];
-      }
-  block_sum_cols(acc, k, part);
+  tile_sums<KP>(n, k, [&](int row, int c) {
+    const size_t o = (size_t)row * k + c;
+    return a[o] * b[o];
+  }, part);
 }
 
-// Column scalars from the block partials (thread c: column c, fixed order).
-__global__ void finish_k_kernel(const double* __restrict__ part, int count, int k, double* __restrict__ sc,
-                                int mode) {
-  const int c = threadIdx.x;
+// Column scalars from the block partials: a warp per column, lane l adds
+// blocks l, l + 32, ... in order, then a fixed butterfly over the lanes.
+__global__ void __launch_bounds__(256) finish_k_kernel(const double* __restrict__ part, int count, int k,
+                                                       double* __restrict__ sc, int mode) {
+  const int lane = threadIdx.x & 31;
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (c >= k) return;
   double t = 0.0;
-  for (int b = 0; b < count; ++b) t += part[(size_t)b * k + c];
+  for (int b = lane; b < count; b += 32) t += part[(size_t)b * k + c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane != 0) return;
   double* s = sc + (size_t)c * S_COUNT;
   switch (mode) {
     case F_ALPHA:
@@ -116,53 +191,83 @@ __global__ void finish_k_kernel(const double* __restrict__ part, int count, int 
   }
 }
 
+template <int KP>
 __global__ void __launch_bounds__(BT) update_xr_k_kernel(double* __restrict__ x, double* __restrict__ r,
                                                          const double* __restrict__ d, const double* __restrict__ q,
                                                          const double* __restrict__ sc, int n, int k,
                                                          double* __restrict__ part) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double al[2] = {0.0, 0.0};
-  for (int qq = 0; qq < 2; ++qq)
-    if (lane + 32 * qq < k) al[qq] = sc[(size_t)(lane + 32 * qq) * S_COUNT + S_ALPHA];
-  double acc[2] = {0.0, 0.0};
-  for (int row = blockIdx.x * (BT / 32) + warp; row < n; row += gridDim.x * (BT / 32))
-    for (int qq = 0; qq < 2; ++qq)
-      if (lane + 32 * qq < k) {
-        const size_t o = (size_t)row * k + lane + 32 * qq;
-        x[o] += al[qq] * d[o];
-        const double ri = r[o] - al[qq] * q[o];
-        r[o] = ri;
-        acc[qq] += ri * ri;
-      }
-  block_sum_cols(acc, k, part);
+  tile_sums<KP>(n, k, [&](int row, int c) {
+    const double al = sc[(size_t)c * S_COUNT + S_ALPHA];
+    const size_t o = (size_t)row * k + c;
+    x[o] += al * d[o];
+    const double ri = r[o] - al * q[o];
+    r[o] = ri;
+    return ri * ri;
+  }, part);
 }
 
 __global__ void __launch_bounds__(BT) update_d_k_kernel(double* __restrict__ d, const double* __restrict__ s,
                                                         const double* __restrict__ sc, int n, int k) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double be[2] = {0.0, 0.0};
-  for (int qq = 0; qq < 2; ++qq)
-    if (lane + 32 * qq < k) be[qq] = sc[(size_t)(lane + 32 * qq) * S_COUNT + S_BETA];
-  for (int row = blockIdx.x * (BT / 32) + warp; row < n; row += gridDim.x * (BT / 32))
-    for (int qq = 0; qq < 2; ++qq)
-      if (lane + 32 * qq < k) {
-        const size_t o = (size_t)row * k + lane + 32 * qq;
-        d[o] = s[o] + be[qq] * d[o];
-      }
+  const long long tot = (long long)n * k;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(e % k);
+    d[e] = s[e] + sc[(size_t)c * S_COUNT + S_BETA] * d[e];
+  }
 }
 
+template <int KP>
 __global__ void __launch_bounds__(BT) residual_k_kernel(const double* __restrict__ b, const double* __restrict__ q,
                                                         int n, int k, double* __restrict__ part) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double acc[2] = {0.0, 0.0};
-  for (int row = blockIdx.x * (BT / 32) + warp; row < n; row += gridDim.x * (BT / 32))
-    for (int qq = 0; qq < 2; ++qq)
-      if (lane + 32 * qq < k) {
-        const size_t o = (size_t)row * k + lane + 32 * qq;
-        const double e = b[o] - q[o];
-        acc[qq] += e * e;
-      }
-  block_sum_cols(acc, k, part);
+  tile_sums<KP>(n, k, [&](int row, int c) {
+    const size_t o = (size_t)row * k + c;
+    const double e = b[o] - q[o];
+    return e * e;
+  }, part);
+}
+
+int kp_of(int k) {
+  int p = 1;
+  while (p < k) p <<= 1;
+  return p;
+}
+
+#define RSCHOL_KP_SWITCH(k, LAUNCH)                                         \
+  switch (kp_of(k)) {                                                       \
+    case 1: LAUNCH(1); break;                                               \
+    case 2: LAUNCH(2); break;                                               \
+    case 4: LAUNCH(4); break;                                               \
+    case 8: LAUNCH(8); break;                                               \
+    case 16: LAUNCH(16); break;                                             \
+    case 32: LAUNCH(32); break;                                             \
+    case 64: LAUNCH(64); break;                                             \
+    default: throw std::runtime_error("batched PCG: more than 64 columns"); \
+  }
+
+void spmv_k(cudaStream_t st, int n, int k, const int* rp, const int* ci, const double* v, const double* x, double* y,
+            double* part) {
+#define L_(KP) spmv_k_kernel<KP><<<BBLOCKS, BT, 0, st>>>(n, k, rp, ci, v, x, y, part)
+  RSCHOL_KP_SWITCH(k, L_)
+#undef L_
+}
+void dot_k(cudaStream_t st, const double* a, const double* b, int n, int k, double* part) {
+#define L_(KP) dot_k_kernel<KP><<<BBLOCKS, BT, 0, st>>>(a, b, n, k, part)
+  RSCHOL_KP_SWITCH(k, L_)
+#undef L_
+}
+void update_xr_k(cudaStream_t st, double* x, double* r, const double* d, const double* q, const double* sc, int n,
+                 int k, double* part) {
+#define L_(KP) update_xr_k_kernel<KP><<<BBLOCKS, BT, 0, st>>>(x, r, d, q, sc, n, k, part)
+  RSCHOL_KP_SWITCH(k, L_)
+#undef L_
+}
+void residual_k(cudaStream_t st, const double* b, const double* q, int n, int k, double* part) {
+#define L_(KP) residual_k_kernel<KP><<<BBLOCKS, BT, 0, st>>>(b, q, n, k, part)
+  RSCHOL_KP_SWITCH(k, L_)
+#undef L_
+}
+void update_d_k(cudaStream_t st, double* d, const double* s, const double* sc, int n, int k) {
+  const long long tot = (long long)n * k;
+  update_d_k_kernel<<<(unsigned)std::min<long long>((tot + BT - 1) / BT, BBLOCKS * 4), BT, 0, st>>>(d, s, sc, n, k);
 }
 
 __global__ void gather_k_kernel(const double* __restrict__ src, const int* __restrict__ perm,
@@ -268,27 +373,27 @@ std::vector<PcgResult> PcgEngine::solve_batch(const double* B, double* X, int k,
   RSCHOL_CUDA(cudaMemsetAsync(sc, 0, sizeof(double) * S_COUNT * k, st));
   RSCHOL_CUDA(cudaMemsetAsync(X, 0, sizeof(double) * nk, st));
   RSCHOL_CUDA(cudaMemcpyAsync(r, B, sizeof(double) * nk, cudaMemcpyDeviceToDevice, st));
-  dot_k_kernel<<<BBLOCKS, BT, 0, st>>>(B, B, n, k, part);
-  finish_k_kernel<<<1, KMAX, 0, st>>>(part, BBLOCKS, k, sc, F_BNORM);
+  dot_k(st, B, B, n, k, part);
+  finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_BNORM);
   RSCHOL_CUDA(cudaMemcpyAsync(s, r, sizeof(double) * nk, cudaMemcpyDeviceToDevice, st));
   apply(s);
-  dot_k_kernel<<<BBLOCKS, BT, 0, st>>>(r, s, n, k, part);
-  finish_k_kernel<<<1, KMAX, 0, st>>>(part, BBLOCKS, k, sc, F_DELTA0);
+  dot_k(st, r, s, n, k, part);
+  finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_DELTA0);
   RSCHOL_CUDA(cudaMemcpyAsync(d, s, sizeof(double) * nk, cudaMemcpyDeviceToDevice, st));
   RSCHOL_LAUNCH_CHECK();
   launches += 4;
   std::vector<char> active(k, 1);
   int nActive = k, i = 0;
   while (i < maxit && nActive > 0) {
-    spmv_k_kernel<<<BBLOCKS, BT, 0, st>>>(n, k, rp, ci, v, d, q, part);
-    finish_k_kernel<<<1, KMAX, 0, st>>>(part, BBLOCKS, k, sc, F_ALPHA);
-    update_xr_k_kernel<<<BBLOCKS, BT, 0, st>>>(X, r, d, q, sc, n, k, part);
-    finish_k_kernel<<<1, KMAX, 0, st>>>(part, BBLOCKS, k, sc, F_RNORM);
+    spmv_k(st, n, k, rp, ci, v, d, q, part);
+    finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_ALPHA);
+    update_xr_k(st, X, r, d, q, sc, n, k, part);
+    finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_RNORM);
     RSCHOL_CUDA(cudaMemcpyAsync(s, r, sizeof(double) * nk, cudaMemcpyDeviceToDevice, st));
     apply(s);
-    dot_k_kernel<<<BBLOCKS, BT, 0, st>>>(r, s, n, k, part);
-    finish_k_kernel<<<1, KMAX, 0, st>>>(part, BBLOCKS, k, sc, F_BETA);
-    update_d_k_kernel<<<BBLOCKS, BT, 0, st>>>(d, s, sc, n, k);
+    dot_k(st, r, s, n, k, part);
+    finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_BETA);
+    update_d_k(st, d, s, sc, n, k);
     RSCHOL_LAUNCH_CHECK();
     launches += 7;
     RSCHOL_CUDA(cudaMemcpyAsync(hScalB_, sc, sizeof(double) * S_COUNT * k, cudaMemcpyDeviceToHost, st));
@@ -315,9 +420,9 @@ std::vector<PcgResult> PcgEngine::solve_batch(const double* B, double* X, int k,
                                       sizeof(double), cudaMemcpyHostToDevice, st));
   }
   // true residuals ||b - A x|| / ||b||
-  spmv_k_kernel<<<BBLOCKS, BT, 0, st>>>(n, k, rp, ci, v, X, q, part);
-  residual_k_kernel<<<BBLOCKS, BT, 0, st>>>(B, q, n, k, part);
-  finish_k_kernel<<<1, KMAX, 0, st>>>(part, BBLOCKS, k, sc, F_TRUE);
+  spmv_k(st, n, k, rp, ci, v, X, q, part);
+  residual_k(st, B, q, n, k, part);
+  finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_TRUE);
   RSCHOL_LAUNCH_CHECK();
   launches += 3;
   RSCHOL_CUDA(cudaMemcpyAsync(hScalB_, sc, sizeof(double) * S_COUNT * k, cudaMemcpyDeviceToHost, st));
@@ -429,8 +534,8 @@ std::vector<PcgSession::Column> PcgSession::step() {
       std::copy(hscNew_.begin(), hscNew_.begin() + (size_t)k * S_COUNT, hsc_);
       RSCHOL_CUDA(cudaMemcpyAsync(sc_.p, hsc_, sizeof(double) * S_COUNT * k, cudaMemcpyHostToDevice, st));
       if (m > 0) {   // ||b|| of every column (the same value again for the old ones)
-        dot_k_kernel<<<BBLOCKS, BT, 0, st>>>(b_[cur_].as<double>(), b_[cur_].as<double>(), n, k, part_.as<double>());
-        finish_k_kernel<<<1, KMAX, 0, st>>>(part_.as<double>(), BBLOCKS, k, sc_.as<double>(), F_BNORM);
+        dot_k(st, b_[cur_].as<double>(), b_[cur_].as<double>(), n, k, part_.as<double>());
+        finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part_.as<double>(), BBLOCKS, k, sc_.as<double>(), F_BNORM);
         RSCHOL_LAUNCH_CHECK();
       }
     }
@@ -452,14 +557,14 @@ std::vector<PcgSession::Column> PcgSession::step() {
   // 2. s = M^{-1} r; t = r.s; d = s + beta d
   RSCHOL_CUDA(cudaMemcpyAsync(S, R, nkBytes, cudaMemcpyDeviceToDevice, st));
   apply_(S, k);
-  dot_k_kernel<<<BBLOCKS, BT, 0, st>>>(R, S, n, k, part);
-  finish_k_kernel<<<1, KMAX, 0, st>>>(part, BBLOCKS, k, sc, F_SLOT);
-  update_d_k_kernel<<<BBLOCKS, BT, 0, st>>>(D, S, sc, n, k);
+  dot_k(st, R, S, n, k, part);
+  finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_SLOT);
+  update_d_k(st, D, S, sc, n, k);
   // 3. q = A d; alpha; x += alpha d; r -= alpha q; ||r|| / ||b||
-  spmv_k_kernel<<<BBLOCKS, BT, 0, st>>>(n, k, rp, ci, v, D, Q, part);
-  finish_k_kernel<<<1, KMAX, 0, st>>>(part, BBLOCKS, k, sc, F_ALPHA);
-  update_xr_k_kernel<<<BBLOCKS, BT, 0, st>>>(X, R, D, Q, sc, n, k, part);
-  finish_k_kernel<<<1, KMAX, 0, st>>>(part, BBLOCKS, k, sc, F_RNORM);
+  spmv_k(st, n, k, rp, ci, v, D, Q, part);
+  finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_ALPHA);
+  update_xr_k(st, X, R, D, Q, sc, n, k, part);
+  finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_RNORM);
   RSCHOL_LAUNCH_CHECK();
   launches += 8;
   RSCHOL_CUDA(cudaMemcpyAsync(hsc_, sc, sizeof(double) * S_COUNT * k, cudaMemcpyDeviceToHost, st));
@@ -480,9 +585,9 @@ std::vector<PcgSession::Column> PcgSession::step() {
   }
   if (fin.empty()) return done;
   // 5. finished columns: true residual ||b - A x|| / ||b|| and x in the original order
-  spmv_k_kernel<<<BBLOCKS, BT, 0, st>>>(n, k, rp, ci, v, X, Q, part);
-  residual_k_kernel<<<BBLOCKS, BT, 0, st>>>(B, Q, n, k, part);
-  finish_k_kernel<<<1, KMAX, 0, st>>>(part, BBLOCKS, k, sc, F_TRUE);
+  spmv_k(st, n, k, rp, ci, v, X, Q, part);
+  residual_k(st, B, Q, n, k, part);
+  finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_TRUE);
   ColMap fmap{};
   for (size_t c = 0; c < fin.size(); ++c) fmap.src[c] = fin[c];
   const long long nf = (long long)n * (long long)fin.size();

@@ -89,6 +89,8 @@ struct XStep {       // one batched GEMM launch (X = L11^{-1} doubling, batched 
   long long off;
   int count, tiles;
   int tc;            // on the tensor cores
+  long long redOff = 0;   // batched apply: K-slice sums after the launch (first, count, grid)
+  int redCount = 0, redGrid = 0;
 };
 
 template <class T>
@@ -149,7 +151,7 @@ class SolveEngine {
   int kB_ = 0, kAllocB_ = 0, epochB_ = 0;
   DevBuf dWuB_, dYB_, dIpB_, dSyncB_, dWB_;
   struct BatchPlan {
-    DevBuf tasks;
+    DevBuf tasks, sums, ws;   // GEMM tasks, K-slice sums and their slice products
     std::vector<std::vector<XStep>> steps;   // [6 * level + phase]
   };
   std::map<int, BatchPlan> bPlans_;

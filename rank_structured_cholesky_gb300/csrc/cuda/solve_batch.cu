@@ -3,7 +3,7 @@
 //
 // Same operator and schedule as SolveEngine::apply_inplace, with every vector
 // widened to k columns: the interior supernodes run in one ticketed launch
-// per direction (a warp per row, lanes across the right-hand sides), and the
+// per direction (a thread per (row, right-hand side) pair), and the
 // compressed levels become batched GEMMs on the factor's GEMM kernels:
 //   forward   Y = X F (row blocks of X stop at the diagonal), Z = U^T Y,
 //             U_c = -V Z;
@@ -25,31 +25,34 @@ namespace {
 
 using namespace solvedev;
 
+// The loops below give every (row, right-hand side) pair to one thread,
+// pairs numbered row-major (p = row * k + c) across the block, and form each
+// pair's dot product serially in a fixed order: every column's arithmetic is
+// the same whatever k is, all threads have work even at k = 1, and for wide
+// blocks consecutive threads take consecutive columns of one row.
+
 // f := L^{-1} f for k right-hand sides (f: n x k in shared memory, row
 // stride k) with the inverted 64 x 64 diagonal blocks of L; t: 64 x k
-// shared.  A warp per row, lanes across the right-hand sides.
+// shared.
 template <class T>
 __device__ void trsv_dinv_k(const T* __restrict__ L, int ld, int n, const T* __restrict__ D, T* f, T* t, int k) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int i0 = 0; i0 < n; i0 += 64) {
     const int h = min(64, n - i0);
-    for (int i = warp; i < h; i += nwarp) {
+    for (int p = threadIdx.x; p < h * k; p += blockDim.x) {
+      const int i = p / k, c = p - i * k;
       const T* row = L + (size_t)(i0 + i) * ld;
-      for (int c = lane; c < k; c += 32) {
-        T s = f[(size_t)(i0 + i) * k + c];
-        for (int j = 0; j < i0; ++j) s -= row[j] * f[(size_t)j * k + c];
-        t[(size_t)i * k + c] = s;
-      }
+      T s = f[(size_t)(i0 + i) * k + c];
+      for (int j = 0; j < i0; ++j) s -= row[j] * f[(size_t)j * k + c];
+      t[(size_t)i * k + c] = s;
     }
     __syncthreads();
     const T* Db = D + (size_t)i0 * 64;
-    for (int i = warp; i < h; i += nwarp) {
+    for (int p = threadIdx.x; p < h * k; p += blockDim.x) {
+      const int i = p / k, c = p - i * k;
       const T* row = Db + (size_t)i * h;
-      for (int c = lane; c < k; c += 32) {
-        T s = T(0);
-        for (int j = 0; j <= i; ++j) s += row[j] * t[(size_t)j * k + c];
-        f[(size_t)(i0 + i) * k + c] = s;
-      }
+      T s = T(0);
+      for (int j = 0; j <= i; ++j) s += row[j] * t[(size_t)j * k + c];
+      f[(size_t)(i0 + i) * k + c] = s;
     }
     __syncthreads();
   }
@@ -58,24 +61,23 @@ __device__ void trsv_dinv_k(const T* __restrict__ L, int ld, int n, const T* __r
 // f := L^{-T} f for k right-hand sides, same blocks.
 template <class T>
 __device__ void trsv_dinv_t_k(const T* __restrict__ L, int ld, int n, const T* __restrict__ D, T* f, T* t, int k) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   if (n <= 0) return;
   for (int i0 = ((n - 1) / 64) * 64; i0 >= 0; i0 -= 64) {
     const int h = min(64, n - i0);
-    for (int j = warp; j < h; j += nwarp)
-      for (int c = lane; c < k; c += 32) {
-        T s = f[(size_t)(i0 + j) * k + c];
-        for (int i = i0 + h; i < n; ++i) s -= L[(size_t)i * ld + i0 + j] * f[(size_t)i * k + c];
-        t[(size_t)j * k + c] = s;
-      }
+    for (int p = threadIdx.x; p < h * k; p += blockDim.x) {
+      const int j = p / k, c = p - j * k;
+      T s = f[(size_t)(i0 + j) * k + c];
+      for (int i = i0 + h; i < n; ++i) s -= L[(size_t)i * ld + i0 + j] * f[(size_t)i * k + c];
+      t[(size_t)j * k + c] = s;
+    }
     __syncthreads();
     const T* Db = D + (size_t)i0 * 64;
-    for (int j = warp; j < h; j += nwarp)
-      for (int c = lane; c < k; c += 32) {
-        T s = T(0);
-        for (int i = j; i < h; ++i) s += Db[(size_t)i * h + j] * t[(size_t)i * k + c];
-        f[(size_t)(i0 + j) * k + c] = s;
-      }
+    for (int p = threadIdx.x; p < h * k; p += blockDim.x) {
+      const int j = p / k, c = p - j * k;
+      T s = T(0);
+      for (int i = j; i < h; ++i) s += Db[(size_t)i * h + j] * t[(size_t)i * k + c];
+      f[(size_t)(i0 + j) * k + c] = s;
+    }
     __syncthreads();
   }
 }
@@ -99,7 +101,7 @@ __global__ void __launch_bounds__(256) interior_forward_k(const SNode<T>* __rest
   const RowBlock wk = work[sTicket];
   const SNode<T>& nd = nodes[wk.node];
   const int n = nd.n, a0 = wk.b * ICH, a1 = min(nd.m, a0 + ICH);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int warp = threadIdx.x >> 5;
   T* f = reinterpret_cast<T*>(smraw);   // n x k
   T* t = f + (size_t)n * k;             // 64 x k
   T* wud = wu + nd.wuOff * k;
@@ -128,14 +130,13 @@ __global__ void __launch_bounds__(256) interior_forward_k(const SNode<T>* __rest
   trsv_dinv_k<T>(nd.L, nd.ld, n, nd.Dinv, f, t, k);
   if (wk.b == 0)
     for (int idx = threadIdx.x; idx < n * k; idx += blockDim.x) yout[(size_t)nd.c0 * k + idx] = f[idx];
-  // wud[a][c] -= L21[a] . y[:, c]: a warp per row, lanes across the right-hand sides
-  for (int a = a0 + warp; a < a1; a += 8) {
+  // wud[a][c] -= L21[a] . y[:, c], a thread per (row, column)
+  for (int p = threadIdx.x; p < (a1 - a0) * k; p += blockDim.x) {
+    const int a = a0 + p / k, c = p % k;
     const T* row = nd.L + (size_t)(n + a) * nd.ld;
-    for (int c = lane; c < k; c += 32) {
-      T s = T(0);
-      for (int j = 0; j < n; ++j) s += row[j] * f[(size_t)j * k + c];
-      wud[(size_t)a * k + c] -= s;
-    }
+    T s = T(0);
+    for (int j = 0; j < n; ++j) s += row[j] * f[(size_t)j * k + c];
+    wud[(size_t)a * k + c] -= s;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -165,21 +166,20 @@ __global__ void __launch_bounds__(256) interior_backward_k(const SNode<T>* __res
   if (nd.parentI >= 0 && (threadIdx.x >> 5) == 0) wait_geq(sync + nodes[nd.parentI].syncOff + 2, epoch, err);
   __syncthreads();
   const int n = nd.n, a0 = wk.b * ICH, a1 = min(nd.m, a0 + ICH);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T* f = reinterpret_cast<T*>(smraw);   // n x k
   T* t = f + (size_t)n * k;             // 64 x k
   const int nch = (nd.m + ICH - 1) / ICH;
   if (nch > 0) {
-    // part[j][c] = sum_{a in chunk} L21[a][j] x_{rows[a]}[c]: a warp per j
+    // part[j][c] = sum_{a in chunk} L21[a][j] x_{rows[a]}[c], a thread per (j, column)
     const int* rw = rows + nd.rowsOff;
     const T* L21 = nd.L + (size_t)n * nd.ld;
     T* part = ipart + (nd.zpOff + (size_t)wk.b * n) * k;
-    for (int j = warp; j < n; j += 8)
-      for (int c = lane; c < k; c += 32) {
-        T s = T(0);
-        for (int a = a0; a < a1; ++a) s += L21[(size_t)a * nd.ld + j] * __ldcg(w + (size_t)rw[a] * k + c);
-        part[(size_t)j * k + c] = s;
-      }
+    for (int p = threadIdx.x; p < n * k; p += blockDim.x) {
+      const int j = p / k, c = p - j * k;
+      T s = T(0);
+      for (int a = a0; a < a1; ++a) s += L21[(size_t)a * nd.ld + j] * __ldcg(w + (size_t)rw[a] * k + c);
+      part[(size_t)j * k + c] = s;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
@@ -240,6 +240,34 @@ __global__ void __launch_bounds__(256) compressed_gather_xr_k(const SNode<T>* __
   const int g = rows[nd.rowsOff + a];
   T* dst = wu + (nd.wuOff + 2 * nd.r + a) * k;
   for (int c = lane; c < k; c += 32) dst[c] = w[(size_t)g * k + c];
+}
+
+// Long-K products of the batched apply run as K slices (each slice's product
+// to its own block of a workspace, so many more tiles are in flight at small
+// k); this kernel then forms C = alpha * (slice 0 + slice 1 + ...) + beta * C,
+// slices added in order.  The slicing depends on K alone, so the arithmetic of
+// a column does not depend on how many columns the block has.
+template <class T>
+struct SliceSum {
+  T* C;
+  const T* ws;   // slices x M x N, row stride N
+  int ldc, M, N, slices;
+  T alpha, beta;
+};
+
+template <class T>
+__global__ void __launch_bounds__(256) slice_sum_kernel(const SliceSum<T>* __restrict__ sums) {
+  const SliceSum<T> t = sums[blockIdx.y];
+  const long long mn = (long long)t.M * t.N;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < mn; e += (long long)gridDim.x * blockDim.x) {
+    T s = T(0);
+    for (int q = 0; q < t.slices; ++q) s += t.ws[q * mn + e];
+    const int i = (int)(e / t.N), j = (int)(e - (long long)i * t.N);
+    T* c = t.C + (size_t)i * t.ldc + j;
+    T v = t.alpha * s;
+    if (t.beta != T(0)) v += t.beta * *c;
+    *c = v;
+  }
 }
 
 template <class A, class B>
@@ -312,19 +340,61 @@ void SolveEngine<T>::plan_batch(int k) {
     g.kLen = K;
     return g;
   };
+  // K slicing: tasks with K above kSliceMin run as slices of kSlice
+  constexpr int kSlice = 512, kSliceMin = 768;
+  std::vector<SliceSum<T>> sums;
+  std::vector<std::pair<size_t, long long>> taskWs;   // (task, workspace offset) to patch
+  std::vector<std::pair<size_t, long long>> sumWs;    // (sum, workspace offset) to patch
+  long long wsTotal = 0;
   auto flush = [&](std::vector<GemmTask<T>>& batch, int slot) {
     if (batch.empty()) return;
     int maxK = 0;
     for (auto& g : batch) maxK = std::max(maxK, g.K);
     const bool useTc = tc && maxK >= 128;
     const int rpt = useTc ? 128 : 64;
+    std::vector<GemmTask<T>> run;
+    const long long sum0 = (long long)sums.size();
+    long long maxMN = 0, wsStep = 0;
+    for (const GemmTask<T>& g : batch) {
+      if (g.K <= kSliceMin) {
+        run.push_back(g);
+        continue;
+      }
+      const int ns = (g.K + kSlice - 1) / kSlice;
+      const long long mn = (long long)g.M * g.N;
+      SliceSum<T> sm{g.C, nullptr, g.ldc, g.M, g.N, ns, g.alpha, g.beta};
+      sumWs.push_back({sums.size(), wsStep});
+      sums.push_back(sm);
+      for (int q = 0; q < ns; ++q) {
+        GemmTask<T> t = g;
+        t.K = std::min(kSlice, g.K - q * kSlice);
+        t.kLen = t.K;
+        t.A = g.tA ? g.A + (size_t)q * kSlice * g.lda : g.A + (size_t)q * kSlice;
+        t.B = g.B + (size_t)q * kSlice * g.ldb;
+        t.C = nullptr;
+        t.ldc = g.N;
+        t.alpha = T(1);
+        t.beta = T(0);
+        t.lower = 0;
+        taskWs.push_back({tasks.size() + run.size(), wsStep + q * mn});
+        run.push_back(t);
+      }
+      wsStep += ns * mn;
+      maxMN = std::max(maxMN, mn);
+    }
+    // every step's slice products start at the workspace base: steps run in stream order
+    wsTotal = std::max(wsTotal, wsStep);
     int tiles = 0;
-    for (auto& g : batch) {
+    for (auto& g : run) {
       g.tileBase = tiles;
       tiles += ((g.M + rpt - 1) / rpt) * g.tilesN;
     }
-    steps[slot].push_back(XStep{(long long)tasks.size(), (int)batch.size(), tiles, useTc ? 1 : 0});
-    tasks.insert(tasks.end(), batch.begin(), batch.end());
+    XStep xs{(long long)tasks.size(), (int)run.size(), tiles, useTc ? 1 : 0};
+    xs.redOff = sum0;
+    xs.redCount = (int)(sums.size() - sum0);
+    xs.redGrid = (int)std::min<long long>(64, (maxMN + 255) / 256);
+    steps[slot].push_back(xs);
+    tasks.insert(tasks.end(), run.begin(), run.end());
     batch.clear();
   };
   const int L = (int)cLevels_.size();
@@ -365,6 +435,14 @@ void SolveEngine<T>::plan_batch(int k) {
     flush(gg, 6 * l + 4);
     flush(gx, 6 * l + 5);
   }
+  plan.ws.alloc(sizeof(T) * std::max(1LL, wsTotal));
+  T* ws = plan.ws.template as<T>();
+  for (auto& tw : taskWs) tasks[tw.first].C = ws + tw.second;
+  for (auto& sw : sumWs) sums[sw.first].ws = ws + sw.second;
+  plan.sums.alloc(std::max<size_t>(16, sums.size() * sizeof(SliceSum<T>)));
+  if (!sums.empty())
+    RSCHOL_CUDA(cudaMemcpyAsync(plan.sums.p, sums.data(), sums.size() * sizeof(SliceSum<T>), cudaMemcpyHostToDevice,
+                                st));
   plan.tasks.alloc(std::max<size_t>(16, tasks.size() * sizeof(GemmTask<T>)));
   if (!tasks.empty())
     RSCHOL_CUDA(cudaMemcpyAsync(plan.tasks.p, tasks.data(), tasks.size() * sizeof(GemmTask<T>),
@@ -410,6 +488,11 @@ void SolveEngine<T>::apply_batch(double* W64, int k, cudaStream_t st) {
         else launch_gemm<T>(bg + x.off, x.count, x.tiles, st);
       } else {
         launch_gemm<T>(bg + x.off, x.count, x.tiles, st);
+      }
+      if (x.redCount > 0) {
+        slice_sum_kernel<T><<<dim3(x.redGrid, x.redCount), 256, 0, st>>>(bPlan_->sums.template as<SliceSum<T>>() +
+                                                                         x.redOff);
+        RSCHOL_LAUNCH_CHECK();
       }
     }
   };
