@@ -88,8 +88,8 @@ struct DinvTask {    // invert one lower-triangular diagonal block (h x h, h <= 
 struct XStep {       // one batched GEMM launch (X = L11^{-1} doubling, batched apply)
   long long off;
   int count, tiles;
-  int tc;            // on the tensor cores
-  long long redOff = 0;   // batched apply: K-slice sums after the launch (first, count, grid)
+  int tc;            // on the tensor cores (batched apply: the transposed skinny form)
+  long long redOff = 0;   // batched apply: K-slice sums after the launch (first, count, grid); tiles = units
   int redCount = 0, redGrid = 0;
 };
 

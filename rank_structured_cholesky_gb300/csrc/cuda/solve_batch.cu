@@ -25,64 +25,121 @@ namespace {
 
 using namespace solvedev;
 
-// The loops below give every (row, right-hand side) pair to one thread,
-// pairs numbered row-major (p = row * k + c) across the block, and form each
-// pair's dot product serially in a fixed order: every column's arithmetic is
-// the same whatever k is, all threads have work even at k = 1, and for wide
-// blocks consecutive threads take consecutive columns of one row.
+// Every (row, right-hand side) pair of the interior solves is a dot product
+// formed serially in a fixed order, so each column's arithmetic is the same
+// whatever k is.  pair_dots runs such a family: for r < rows, c < k,
+// acc = init(r, c), then for j = lo(r) .. hi(r) - 1 in order
+// acc += a(r, j) * F(j, c) (acc -= ... when SUB), then out(r, c, acc).  A
+// thread takes a tile of RA rows x RC columns (consecutive threads take
+// consecutive column tiles): 1 x 1 spreads the pairs over all threads at
+// small k, 4 x 4 reuses every load of A and F four times at large k.  The
+// tiling only changes which thread forms a pair, not its arithmetic.
+template <class T, int RA, int RC, bool SUB, class AE, class FV, class Init, class Lo, class Hi, class Out>
+__device__ __forceinline__ void pair_dots(int rows, int k, AE a, FV fv, Init init, Lo lo, Hi hi, Out out) {
+  const int ct = (k + RC - 1) / RC, rt = (rows + RA - 1) / RA;
+  for (int tile = threadIdx.x; tile < rt * ct; tile += blockDim.x) {
+    const int tr = tile / ct;
+    const int r0 = tr * RA, c0 = (tile - tr * ct) * RC;
+    T acc[RA][RC];
+    int l[RA], h[RA];
+    int jlo = 0x7fffffff, jhi = -0x7fffffff;
+#pragma unroll
+    for (int r = 0; r < RA; ++r) {
+      const bool rv = r0 + r < rows;
+      l[r] = rv ? lo(r0 + r) : 0;
+      h[r] = rv ? hi(r0 + r) : 0;
+#pragma unroll
+      for (int q = 0; q < RC; ++q) acc[r][q] = (rv && c0 + q < k) ? init(r0 + r, c0 + q) : T(0);
+      if (rv) {
+        jlo = min(jlo, l[r]);
+        jhi = max(jhi, h[r]);
+      }
+    }
+    bool same = true;   // every row of the tile runs over [jlo, jhi)
+#pragma unroll
+    for (int r = 0; r < RA; ++r) same = same && (r0 + r >= rows || (l[r] == jlo && h[r] == jhi));
+    if (same) {
+      for (int j = jlo; j < jhi; ++j) {
+        T f[RC];
+#pragma unroll
+        for (int q = 0; q < RC; ++q) f[q] = (RC == 1 || c0 + q < k) ? fv(j, c0 + q) : T(0);
+#pragma unroll
+        for (int r = 0; r < RA; ++r) {
+          const T av = (RA == 1 || r0 + r < rows) ? a(r0 + r, j) : T(0);
+#pragma unroll
+          for (int q = 0; q < RC; ++q) {
+            if (SUB) acc[r][q] -= av * f[q];
+            else acc[r][q] += av * f[q];
+          }
+        }
+      }
+    } else {
+      for (int j = jlo; j < jhi; ++j) {
+        T f[RC];
+#pragma unroll
+        for (int q = 0; q < RC; ++q) f[q] = (RC == 1 || c0 + q < k) ? fv(j, c0 + q) : T(0);
+#pragma unroll
+        for (int r = 0; r < RA; ++r)
+          if (j >= l[r] && j < h[r]) {
+            const T av = a(r0 + r, j);
+#pragma unroll
+            for (int q = 0; q < RC; ++q) {
+              if (SUB) acc[r][q] -= av * f[q];
+              else acc[r][q] += av * f[q];
+            }
+          }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < RA; ++r)
+#pragma unroll
+      for (int q = 0; q < RC; ++q)
+        if (r0 + r < rows && c0 + q < k) out(r0 + r, c0 + q, acc[r][q]);
+  }
+}
 
 // f := L^{-1} f for k right-hand sides (f: n x k in shared memory, row
 // stride k) with the inverted 64 x 64 diagonal blocks of L; t: 64 x k
 // shared.
-template <class T>
+template <class T, int RA, int RC>
 __device__ void trsv_dinv_k(const T* __restrict__ L, int ld, int n, const T* __restrict__ D, T* f, T* t, int k) {
   for (int i0 = 0; i0 < n; i0 += 64) {
     const int h = min(64, n - i0);
-    for (int p = threadIdx.x; p < h * k; p += blockDim.x) {
-      const int i = p / k, c = p - i * k;
-      const T* row = L + (size_t)(i0 + i) * ld;
-      T s = f[(size_t)(i0 + i) * k + c];
-      for (int j = 0; j < i0; ++j) s -= row[j] * f[(size_t)j * k + c];
-      t[(size_t)i * k + c] = s;
-    }
+    pair_dots<T, RA, RC, true>(
+        h, k, [&](int i, int j) { return L[(size_t)(i0 + i) * ld + j]; },
+        [&](int j, int c) { return f[(size_t)j * k + c]; }, [&](int i, int c) { return f[(size_t)(i0 + i) * k + c]; },
+        [](int) { return 0; }, [&](int) { return i0; }, [&](int i, int c, T v) { t[(size_t)i * k + c] = v; });
     __syncthreads();
     const T* Db = D + (size_t)i0 * 64;
-    for (int p = threadIdx.x; p < h * k; p += blockDim.x) {
-      const int i = p / k, c = p - i * k;
-      const T* row = Db + (size_t)i * h;
-      T s = T(0);
-      for (int j = 0; j <= i; ++j) s += row[j] * t[(size_t)j * k + c];
-      f[(size_t)(i0 + i) * k + c] = s;
-    }
+    pair_dots<T, RA, RC, false>(
+        h, k, [&](int i, int j) { return Db[(size_t)i * h + j]; }, [&](int j, int c) { return t[(size_t)j * k + c]; },
+        [](int, int) { return T(0); }, [](int) { return 0; }, [](int i) { return i + 1; },
+        [&](int i, int c, T v) { f[(size_t)(i0 + i) * k + c] = v; });
     __syncthreads();
   }
 }
 
 // f := L^{-T} f for k right-hand sides, same blocks.
-template <class T>
+template <class T, int RA, int RC>
 __device__ void trsv_dinv_t_k(const T* __restrict__ L, int ld, int n, const T* __restrict__ D, T* f, T* t, int k) {
   if (n <= 0) return;
   for (int i0 = ((n - 1) / 64) * 64; i0 >= 0; i0 -= 64) {
     const int h = min(64, n - i0);
-    for (int p = threadIdx.x; p < h * k; p += blockDim.x) {
-      const int j = p / k, c = p - j * k;
-      T s = f[(size_t)(i0 + j) * k + c];
-      for (int i = i0 + h; i < n; ++i) s -= L[(size_t)i * ld + i0 + j] * f[(size_t)i * k + c];
-      t[(size_t)j * k + c] = s;
-    }
+    pair_dots<T, RA, RC, true>(
+        h, k, [&](int j, int i) { return L[(size_t)i * ld + i0 + j]; },
+        [&](int i, int c) { return f[(size_t)i * k + c]; }, [&](int j, int c) { return f[(size_t)(i0 + j) * k + c]; },
+        [&](int) { return i0 + h; }, [&](int) { return n; }, [&](int j, int c, T v) { t[(size_t)j * k + c] = v; });
     __syncthreads();
     const T* Db = D + (size_t)i0 * 64;
-    for (int p = threadIdx.x; p < h * k; p += blockDim.x) {
-      const int j = p / k, c = p - j * k;
-      T s = T(0);
-      for (int i = j; i < h; ++i) s += Db[(size_t)i * h + j] * t[(size_t)i * k + c];
-      f[(size_t)(i0 + j) * k + c] = s;
-    }
+    pair_dots<T, RA, RC, false>(
+        h, k, [&](int j, int i) { return Db[(size_t)i * h + j]; }, [&](int i, int c) { return t[(size_t)i * k + c]; },
+        [](int, int) { return T(0); }, [](int j) { return j; }, [&](int) { return h; },
+        [&](int j, int c, T v) { f[(size_t)(i0 + j) * k + c] = v; });
     __syncthreads();
   }
 }
 
-template <class T>
+template <class T, int RA, int RC>
 __global__ void __launch_bounds__(256) interior_forward_k(const SNode<T>* __restrict__ nodes,
                                                           const RowBlock* __restrict__ work,
                                                           const int* __restrict__ rel, const int* __restrict__ child,
@@ -127,16 +184,17 @@ __global__ void __launch_bounds__(256) interior_forward_k(const SNode<T>* __rest
     }
     __syncthreads();
   }
-  trsv_dinv_k<T>(nd.L, nd.ld, n, nd.Dinv, f, t, k);
+  trsv_dinv_k<T, RA, RC>(nd.L, nd.ld, n, nd.Dinv, f, t, k);
   if (wk.b == 0)
     for (int idx = threadIdx.x; idx < n * k; idx += blockDim.x) yout[(size_t)nd.c0 * k + idx] = f[idx];
-  // wud[a][c] -= L21[a] . y[:, c], a thread per (row, column)
-  for (int p = threadIdx.x; p < (a1 - a0) * k; p += blockDim.x) {
-    const int a = a0 + p / k, c = p % k;
-    const T* row = nd.L + (size_t)(n + a) * nd.ld;
-    T s = T(0);
-    for (int j = 0; j < n; ++j) s += row[j] * f[(size_t)j * k + c];
-    wud[(size_t)a * k + c] -= s;
+  // wud[a][c] -= L21[a] . y[:, c]
+  {
+    const T* L21 = nd.L + (size_t)(n + a0) * nd.ld;
+    const int ld = nd.ld;
+    pair_dots<T, RA, RC, false>(
+        a1 - a0, k, [&](int a, int j) { return L21[(size_t)a * ld + j]; },
+        [&](int j, int c) { return f[(size_t)j * k + c]; }, [](int, int) { return T(0); }, [](int) { return 0; },
+        [&](int) { return n; }, [&](int a, int c, T v) { wud[(size_t)(a0 + a) * k + c] -= v; });
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -146,7 +204,7 @@ __global__ void __launch_bounds__(256) interior_forward_k(const SNode<T>* __rest
   launch_done(&sync[SYNC_TICK_F], &sync[SYNC_DONE_F]);
 }
 
-template <class T>
+template <class T, int RA, int RC>
 __global__ void __launch_bounds__(256) interior_backward_k(const SNode<T>* __restrict__ nodes,
                                                            const RowBlock* __restrict__ work,
                                                            const int* __restrict__ rows, int* __restrict__ sync,
@@ -170,16 +228,16 @@ __global__ void __launch_bounds__(256) interior_backward_k(const SNode<T>* __res
   T* t = f + (size_t)n * k;             // 64 x k
   const int nch = (nd.m + ICH - 1) / ICH;
   if (nch > 0) {
-    // part[j][c] = sum_{a in chunk} L21[a][j] x_{rows[a]}[c], a thread per (j, column)
+    // part[j][c] = sum_{a in chunk} L21[a][j] x_{rows[a]}[c] (x written by
+    // other blocks of this launch: loads bypass L1)
     const int* rw = rows + nd.rowsOff;
     const T* L21 = nd.L + (size_t)n * nd.ld;
+    const int ld = nd.ld;
     T* part = ipart + (nd.zpOff + (size_t)wk.b * n) * k;
-    for (int p = threadIdx.x; p < n * k; p += blockDim.x) {
-      const int j = p / k, c = p - j * k;
-      T s = T(0);
-      for (int a = a0; a < a1; ++a) s += L21[(size_t)a * nd.ld + j] * __ldcg(w + (size_t)rw[a] * k + c);
-      part[(size_t)j * k + c] = s;
-    }
+    pair_dots<T, RA, RC, false>(
+        n, k, [&](int j, int a) { return L21[(size_t)a * ld + j]; },
+        [&](int a, int c) { return __ldcg(w + (size_t)rw[a] * k + c); }, [](int, int) { return T(0); },
+        [&](int) { return a0; }, [&](int) { return a1; }, [&](int j, int c, T v) { part[(size_t)j * k + c] = v; });
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
@@ -198,7 +256,7 @@ __global__ void __launch_bounds__(256) interior_backward_k(const SNode<T>* __res
     f[idx] = yin[(size_t)nd.c0 * k + idx] - s;
   }
   __syncthreads();
-  trsv_dinv_t_k<T>(nd.L, nd.ld, n, nd.Dinv, f, t, k);
+  trsv_dinv_t_k<T, RA, RC>(nd.L, nd.ld, n, nd.Dinv, f, t, k);
   for (int idx = threadIdx.x; idx < n * k; idx += blockDim.x) w[(size_t)nd.c0 * k + idx] = f[idx];
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -242,6 +300,148 @@ __global__ void __launch_bounds__(256) compressed_gather_xr_k(const SNode<T>* __
   for (int c = lane; c < k; c += 32) dst[c] = w[(size_t)g * k + c];
 }
 
+// Products of the compressed levels: C (M x k) = alpha op(A) B + beta C
+// with B (K x k, row stride ldb) the block of right-hand sides.  With k <= 64
+// these are streaming products over the factor's X, U and V, so they run on
+// SIMT kernels that read A once, coalesced.  Each output column's sum has a
+// fixed order that depends on K alone (not on k); tasks are cut into units
+// (one block each) of a row group and a group of CW columns (skinny_cw),
+// numbered from each task's unitBase.
+template <class T>
+struct SkinnyTask {
+  const T* A;
+  const T* B;
+  T* C;
+  int M, K, lda, ldb, ldc;
+  T alpha, beta;
+  int unitBase;
+};
+
+template <class T>
+__device__ __forceinline__ int find_skinny(const SkinnyTask<T>* __restrict__ tasks, int count, int u) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tasks[mid].unitBase <= u) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Row form, A row-major M x K.  A block per (16 rows, column group), a warp
+// per two rows; lane l adds kk = l, l + 32, ... in order (zeros past K),
+// then the lanes meet in a fixed butterfly.  Chunks of 256 rows of B are
+// staged in shared memory transposed, so lane l reads its kk without bank
+// conflicts, and each staged value serves both rows of the warp.
+constexpr int SK_CHUNK = 256;   // kk per staged chunk of B (8 per lane)
+
+template <class T, int CW>
+__global__ void __launch_bounds__(256) skinny_rows_kernel(const SkinnyTask<T>* __restrict__ tasks, int count, int k) {
+  __shared__ T Bs[CW][SK_CHUNK + 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int u = blockIdx.x;
+  const SkinnyTask<T> t = tasks[find_skinny(tasks, count, u)];
+  const int cg = (k + CW - 1) / CW;
+  const int local = u - t.unitBase, rb = local / cg, c0 = (local - rb * cg) * CW;
+  const int i0 = rb * 16 + warp * 2;
+  T acc[2][CW];
+#pragma unroll
+  for (int q = 0; q < CW; ++q) acc[0][q] = acc[1][q] = T(0);
+  const T* a0 = t.A + (size_t)min(i0, t.M - 1) * t.lda;
+  const T* a1 = t.A + (size_t)min(i0 + 1, t.M - 1) * t.lda;
+  for (int kk0 = 0; kk0 < t.K; kk0 += SK_CHUNK) {
+    T av[2][SK_CHUNK / 32];
+#pragma unroll
+    for (int s = 0; s < SK_CHUNK / 32; ++s) {
+      const int kk = kk0 + lane + 32 * s;
+      av[0][s] = kk < t.K ? a0[kk] : T(0);
+      av[1][s] = kk < t.K ? a1[kk] : T(0);
+    }
+    for (int e = threadIdx.x; e < SK_CHUNK * CW; e += blockDim.x) {
+      const int l = e / CW, q = e - l * CW;
+      Bs[q][l] = (kk0 + l < t.K && c0 + q < k) ? t.B[(size_t)(kk0 + l) * t.ldb + c0 + q] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < SK_CHUNK / 32; ++s)
+#pragma unroll
+      for (int q = 0; q < CW; ++q) {
+        const T b = Bs[q][lane + 32 * s];
+        acc[0][q] += av[0][s] * b;
+        acc[1][q] += av[1][s] * b;
+      }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int i = i0 + r;
+#pragma unroll
+    for (int q = 0; q < CW; ++q) {
+      const T v = warp_sum(acc[r][q]);
+      if (lane == q && i < t.M && c0 + q < k) {
+        T* c = t.C + (size_t)i * t.ldc + c0 + q;
+        T o = t.alpha * v;
+        if (t.beta != T(0)) o += t.beta * *c;
+        *c = o;
+      }
+    }
+  }
+}
+
+// Transposed form, A stored K x M (op(A)[i][kk] = A[kk][i]).  A block per
+// (64 rows, column group): lanes take rows i0 + lane and i0 + lane + 32
+// (coalesced along A's rows), warp w adds kk = w, w + 8, ... in order, and
+// the 8 warp partials are added in warp order.
+template <class T, int CW>
+__global__ void __launch_bounds__(256) skinny_cols_kernel(const SkinnyTask<T>* __restrict__ tasks, int count, int k) {
+  // warp partials go through shared memory QB columns at a time (<= 32 KB)
+  constexpr int QB = sizeof(T) * 8 * 64 * CW > 32768 ? CW / 2 : CW;
+  __shared__ T red[8][64][QB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int u = blockIdx.x;
+  const SkinnyTask<T> t = tasks[find_skinny(tasks, count, u)];
+  const int cg = (k + CW - 1) / CW;
+  const int local = u - t.unitBase, rb = local / cg, c0 = (local - rb * cg) * CW;
+  const int i0 = rb * 64;
+  const bool v0 = i0 + lane < t.M, v1 = i0 + lane + 32 < t.M;
+  T acc[2][CW];
+#pragma unroll
+  for (int q = 0; q < CW; ++q) acc[0][q] = acc[1][q] = T(0);
+#pragma unroll 8
+  for (int kk = warp; kk < t.K; kk += 8) {
+    const T* arow = t.A + (size_t)kk * t.lda + i0;
+    const T a0 = v0 ? arow[lane] : T(0), a1 = v1 ? arow[lane + 32] : T(0);
+    const T* b = t.B + (size_t)kk * t.ldb + c0;
+#pragma unroll
+    for (int q = 0; q < CW; ++q) {
+      const T bv = c0 + q < k ? b[q] : T(0);
+      acc[0][q] += a0 * bv;
+      acc[1][q] += a1 * bv;
+    }
+  }
+#pragma unroll
+  for (int qb = 0; qb < CW; qb += QB) {
+#pragma unroll
+    for (int q = 0; q < QB; ++q) {
+      red[warp][lane][q] = acc[0][qb + q];
+      red[warp][lane + 32][q] = acc[1][qb + q];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * QB; e += blockDim.x) {
+      const int r = e / QB, q = e - r * QB;
+      if (i0 + r >= t.M || c0 + qb + q >= k) continue;
+      T v = T(0);
+#pragma unroll
+      for (int w = 0; w < 8; ++w) v += red[w][r][q];
+      T* c = t.C + (size_t)(i0 + r) * t.ldc + c0 + qb + q;
+      T o = t.alpha * v;
+      if (t.beta != T(0)) o += t.beta * *c;
+      *c = o;
+    }
+    __syncthreads();
+  }
+}
+
 // Long-K products of the batched apply run as K slices (each slice's product
 // to its own block of a workspace, so many more tiles are in flight at small
 // k); this kernel then forms C = alpha * (slice 0 + slice 1 + ...) + beta * C,
@@ -275,6 +475,16 @@ __global__ void convert_k_kernel(const A* __restrict__ src, B* __restrict__ dst,
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
     dst[i] = (B)src[i];
 }
+
+int skinny_width(int k) {
+  int p = 1;
+  while (p < k) p <<= 1;
+  return p;
+}
+
+// columns per unit: k rounded up to a power of two, at most 16 (row form) or
+// 8 (transposed form, whose B values are broadcast loads)
+int skinny_cw(int k, bool cols) { return std::min(cols ? 8 : 16, skinny_width(k)); }
 
 }  // namespace
 
@@ -310,86 +520,70 @@ void SolveEngine<T>::plan_batch(int k) {
     return;
   }
   BatchPlan& plan = bPlans_[k];
-  // batched GEMMs of the compressed levels
-  const bool tc = std::is_same<T, float>::value && F_.tensor_cores();
-  std::vector<GemmTask<T>> tasks;
+  // products of the compressed levels (skinny SIMT kernels)
+  std::vector<SkinnyTask<T>> tasks;
   auto& steps = plan.steps;
   steps.assign(6 * cLevels_.size(), {});
   T* wu = dWuB_.as<T>();
   T* yb = dYB_.as<T>();
   T* w = dWB_.as<T>();
-  auto mk = [&](const T* A, int lda, bool tA, const T* B, int ldb, T* C, int ldc, int M, int N, int K, T alpha,
-                T beta) {
-    GemmTask<T> g{};
-    g.A = A;
-    g.B = B;
-    g.C = C;
-    g.M = M;
-    g.N = N;
-    g.K = K;
-    g.lda = lda;
-    g.ldb = ldb;
-    g.ldc = ldc;
-    g.tA = tA;
-    g.tB = 0;
-    g.alpha = alpha;
-    g.beta = beta;
-    g.tilesN = (N + 63) / 64;
-    g.split = 1;
-    g.kSplit = 1;
-    g.kLen = K;
-    return g;
+  // column groups: up to 16 columns for the row form, 8 for the transposed form
+  const int cgR = (k + skinny_cw(k, false) - 1) / skinny_cw(k, false);
+  const int cgC = (k + skinny_cw(k, true) - 1) / skinny_cw(k, true);
+  struct Prod {   // one product before it is cut into units
+    const T* A;
+    const T* B;
+    T* C;
+    int M, K, lda, ldb, ldc;
+    bool tA;
+    T alpha, beta;
   };
-  // K slicing: tasks with K above kSliceMin run as slices of kSlice
+  auto mk = [&](const T* A, int lda, bool tA, const T* B, int ldb, T* C, int ldc, int M, int, int K, T alpha,
+                T beta) { return Prod{A, B, C, M, K, lda, ldb, ldc, tA, alpha, beta}; };
+  // K slicing of the transposed form (a thread runs down K): tasks with K
+  // above kSliceMin run as slices of kSlice into a workspace, then a
+  // fixed-order sum; the slicing depends on K alone
   constexpr int kSlice = 512, kSliceMin = 768;
   std::vector<SliceSum<T>> sums;
   std::vector<std::pair<size_t, long long>> taskWs;   // (task, workspace offset) to patch
   std::vector<std::pair<size_t, long long>> sumWs;    // (sum, workspace offset) to patch
   long long wsTotal = 0;
-  auto flush = [&](std::vector<GemmTask<T>>& batch, int slot) {
+  auto flush = [&](std::vector<Prod>& batch, int slot) {
     if (batch.empty()) return;
-    int maxK = 0;
-    for (auto& g : batch) maxK = std::max(maxK, g.K);
-    const bool useTc = tc && maxK >= 128;
-    const int rpt = useTc ? 128 : 64;
-    std::vector<GemmTask<T>> run;
+    const bool cols = batch[0].tA;   // a flush holds one form
+    std::vector<SkinnyTask<T>> run;
     const long long sum0 = (long long)sums.size();
     long long maxMN = 0, wsStep = 0;
-    for (const GemmTask<T>& g : batch) {
-      if (g.K <= kSliceMin) {
-        run.push_back(g);
+    auto add = [&](const Prod& g, T* C, int ldc, T alpha, T beta) {
+      run.push_back(SkinnyTask<T>{g.A, g.B, C, g.M, g.K, g.lda, g.ldb, ldc, alpha, beta, 0});
+    };
+    for (const Prod& g : batch) {
+      if (!cols || g.K <= kSliceMin) {
+        add(g, g.C, g.ldc, g.alpha, g.beta);
         continue;
       }
       const int ns = (g.K + kSlice - 1) / kSlice;
-      const long long mn = (long long)g.M * g.N;
-      SliceSum<T> sm{g.C, nullptr, g.ldc, g.M, g.N, ns, g.alpha, g.beta};
+      const long long mn = (long long)g.M * k;
       sumWs.push_back({sums.size(), wsStep});
-      sums.push_back(sm);
+      sums.push_back(SliceSum<T>{g.C, nullptr, g.ldc, g.M, k, ns, g.alpha, g.beta});
       for (int q = 0; q < ns; ++q) {
-        GemmTask<T> t = g;
+        Prod t = g;
         t.K = std::min(kSlice, g.K - q * kSlice);
-        t.kLen = t.K;
-        t.A = g.tA ? g.A + (size_t)q * kSlice * g.lda : g.A + (size_t)q * kSlice;
+        t.A = g.A + (size_t)q * kSlice * g.lda;
         t.B = g.B + (size_t)q * kSlice * g.ldb;
-        t.C = nullptr;
-        t.ldc = g.N;
-        t.alpha = T(1);
-        t.beta = T(0);
-        t.lower = 0;
         taskWs.push_back({tasks.size() + run.size(), wsStep + q * mn});
-        run.push_back(t);
+        add(t, nullptr, k, T(1), T(0));
       }
       wsStep += ns * mn;
       maxMN = std::max(maxMN, mn);
     }
-    // every step's slice products start at the workspace base: steps run in stream order
-    wsTotal = std::max(wsTotal, wsStep);
-    int tiles = 0;
-    for (auto& g : run) {
-      g.tileBase = tiles;
-      tiles += ((g.M + rpt - 1) / rpt) * g.tilesN;
+    wsTotal = std::max(wsTotal, wsStep);   // every step's slices start at the workspace base
+    int units = 0;   // one block per unit: (16 rows | 64 rows, column group)
+    for (auto& t : run) {
+      t.unitBase = units;
+      units += cols ? (t.M + 63) / 64 * cgC : (t.M + 15) / 16 * cgR;
     }
-    XStep xs{(long long)tasks.size(), (int)run.size(), tiles, useTc ? 1 : 0};
+    XStep xs{(long long)tasks.size(), (int)run.size(), units, cols ? 1 : 0};
     xs.redOff = sum0;
     xs.redCount = (int)(sums.size() - sum0);
     xs.redGrid = (int)std::min<long long>(64, (maxMN + 255) / 256);
@@ -399,7 +593,7 @@ void SolveEngine<T>::plan_batch(int k) {
   };
   const int L = (int)cLevels_.size();
   for (int l = 0; l < L; ++l) {
-    std::vector<GemmTask<T>> gy, gz, gu, gs, gg, gx;
+    std::vector<Prod> gy, gz, gu, gs, gg, gx;
     for (int q = 0; q < cLevels_[l].second; ++q) {
       const int j = F_.compressedLevels[l][q];
       const SNode<T>& nd = nodes_[j];
@@ -443,9 +637,9 @@ void SolveEngine<T>::plan_batch(int k) {
   if (!sums.empty())
     RSCHOL_CUDA(cudaMemcpyAsync(plan.sums.p, sums.data(), sums.size() * sizeof(SliceSum<T>), cudaMemcpyHostToDevice,
                                 st));
-  plan.tasks.alloc(std::max<size_t>(16, tasks.size() * sizeof(GemmTask<T>)));
+  plan.tasks.alloc(std::max<size_t>(16, tasks.size() * sizeof(SkinnyTask<T>)));
   if (!tasks.empty())
-    RSCHOL_CUDA(cudaMemcpyAsync(plan.tasks.p, tasks.data(), tasks.size() * sizeof(GemmTask<T>),
+    RSCHOL_CUDA(cudaMemcpyAsync(plan.tasks.p, tasks.data(), tasks.size() * sizeof(SkinnyTask<T>),
                                 cudaMemcpyHostToDevice, st));
   RSCHOL_CUDA(cudaStreamSynchronize(st));
   bPlan_ = &plan;
@@ -470,25 +664,55 @@ void SolveEngine<T>::apply_batch(double* W64, int k, cudaStream_t st) {
   const size_t smem = sizeof(T) * (size_t)(maxNI_ + 64) * k;
   static std::once_flag once;
   std::call_once(once, [] {
-    RSCHOL_CUDA(cudaFuncSetAttribute(interior_forward_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    RSCHOL_CUDA(cudaFuncSetAttribute(interior_backward_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    const int sm = 200 * 1024;
+#define RSCHOL_SMEM_ATTR(RA, RC)                                                                                \
+  RSCHOL_CUDA(cudaFuncSetAttribute(interior_forward_k<T, RA, RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm)); \
+  RSCHOL_CUDA(cudaFuncSetAttribute(interior_backward_k<T, RA, RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))
+    RSCHOL_SMEM_ATTR(1, 1);
+    RSCHOL_SMEM_ATTR(1, 4);
+    RSCHOL_SMEM_ATTR(2, 4);
+    RSCHOL_SMEM_ATTR(4, 4);
+#undef RSCHOL_SMEM_ATTR
   });
+  // register tiles of (row, column) pairs: enough tiles for the 256 threads
+  // of a block (64 - 128 rows) at every k
+  using IF = decltype(&interior_forward_k<T, 1, 1>);
+  using IB = decltype(&interior_backward_k<T, 1, 1>);
+  IF fwd = interior_forward_k<T, 1, 1>;
+  IB bwd = interior_backward_k<T, 1, 1>;
+  if (k >= 48) {
+    fwd = interior_forward_k<T, 4, 4>;
+    bwd = interior_backward_k<T, 4, 4>;
+  } else if (k >= 24) {
+    fwd = interior_forward_k<T, 2, 4>;
+    bwd = interior_backward_k<T, 2, 4>;
+  } else if (k >= 4) {
+    fwd = interior_forward_k<T, 1, 4>;
+    bwd = interior_backward_k<T, 1, 4>;
+  }
   if (nIWork_ > 0) {
-    interior_forward_k<T><<<nIWork_, 256, smem, st>>>(dNodes_.as<SNode<T>>(), dIWork_.as<RowBlock>(), dRel_.as<int>(),
-                                                       dChild_.as<int>(), sync, epochB_, k, w, dYB_.as<T>(),
-                                                       dWuB_.as<T>());
+    fwd<<<nIWork_, 256, smem, st>>>(dNodes_.as<SNode<T>>(), dIWork_.as<RowBlock>(), dRel_.as<int>(), dChild_.as<int>(),
+                                    sync, epochB_, k, w, dYB_.as<T>(), dWuB_.as<T>());
     RSCHOL_LAUNCH_CHECK();
   }
   const int* lvl = dLevelNodes_.as<int>();
-  const GemmTask<T>* bg = bPlan_->tasks.template as<GemmTask<T>>();
+  const SkinnyTask<T>* bg = bPlan_->tasks.template as<SkinnyTask<T>>();
   auto gemm = [&](int slot) {
     for (const XStep& x : bPlan_->steps[slot]) {
-      if constexpr (std::is_same<T, float>::value) {
-        if (x.tc) launch_gemm_tc(bg + x.off, x.count, x.tiles, F_.dFlag.template as<int>() + 1, st);
-        else launch_gemm<T>(bg + x.off, x.count, x.tiles, st);
-      } else {
-        launch_gemm<T>(bg + x.off, x.count, x.tiles, st);
+      const SkinnyTask<T>* tk = bg + x.off;
+      const int cw = skinny_cw(k, x.tc != 0);
+#define RSCHOL_SKINNY(CW)                                                     \
+  if (x.tc) skinny_cols_kernel<T, CW><<<x.tiles, 256, 0, st>>>(tk, x.count, k); \
+  else skinny_rows_kernel<T, CW><<<x.tiles, 256, 0, st>>>(tk, x.count, k)
+      switch (cw) {
+        case 1: RSCHOL_SKINNY(1); break;
+        case 2: RSCHOL_SKINNY(2); break;
+        case 4: RSCHOL_SKINNY(4); break;
+        case 8: RSCHOL_SKINNY(8); break;
+        default: RSCHOL_SKINNY(16); break;
       }
+#undef RSCHOL_SKINNY
+      RSCHOL_LAUNCH_CHECK();
       if (x.redCount > 0) {
         slice_sum_kernel<T><<<dim3(x.redGrid, x.redCount), 256, 0, st>>>(bPlan_->sums.template as<SliceSum<T>>() +
                                                                          x.redOff);
@@ -516,9 +740,8 @@ void SolveEngine<T>::apply_batch(double* W64, int k, cudaStream_t st) {
     gemm(6 * l + 5);
   }
   if (nIWork_ > 0) {
-    interior_backward_k<T><<<nIWork_, 256, smem, st>>>(dNodes_.as<SNode<T>>(), dIWorkB_.as<RowBlock>(),
-                                                        dRows_.as<int>(), sync, epochB_, k, dIpB_.as<T>(),
-                                                        dYB_.as<T>(), w);
+    bwd<<<nIWork_, 256, smem, st>>>(dNodes_.as<SNode<T>>(), dIWorkB_.as<RowBlock>(), dRows_.as<int>(), sync, epochB_,
+                                    k, dIpB_.as<T>(), dYB_.as<T>(), w);
     RSCHOL_LAUNCH_CHECK();
   }
   convert_k_kernel<T, double><<<(unsigned)std::min<long long>((nk + 255) / 256, 4096), 256, 0, st>>>(w, W64, nk);
