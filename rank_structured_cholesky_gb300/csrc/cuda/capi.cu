@@ -69,6 +69,7 @@ struct Impl {
   virtual double flops() const = 0;
   virtual double apply_bytes() const = 0;
   virtual size_t bytes() const = 0;
+  virtual std::vector<std::array<double, 6>> batch_tuning() const = 0;
   virtual void node_l11(int j, double* out) = 0;
   virtual void node_l21(int j, double* out) = 0;
 };
@@ -108,6 +109,7 @@ struct ImplT : Impl {
   double flops() const override { return fe.flops; }
   double apply_bytes() const override { return se.bytes_per_apply(); }
   size_t bytes() const override { return fe.deviceBytes; }
+  std::vector<std::array<double, 6>> batch_tuning() const override { return se.batch_tuning(); }
   std::vector<T> fetch(const T* d, size_t count) {
     std::vector<T> h(count);
     if (count) RSCHOL_CUDA(cudaMemcpy(h.data(), d, sizeof(T) * count, cudaMemcpyDeviceToHost));
@@ -646,7 +648,14 @@ const char* rschol_factor_describe(rschol_factor* f) {
     << ", \"factor_flops\": " << f->impl->flops() << ", \"apply_bytes\": " << f->impl->apply_bytes()
     << ", \"spmv_bytes\": " << f->pcg->spmvBytes << ", \"device_bytes\": " << f->impl->bytes()
     << ", \"symbolic_s\": " << f->tSymbolic << ", \"numeric_s\": " << f->tNumeric
-    << ", \"attempts\": " << f->attempts << "}";
+    << ", \"attempts\": " << f->attempts << ", \"batch_tuning\": [";
+  bool first = true;
+  for (const auto& row : f->impl->batch_tuning()) {   // per width class: class, RA, RC, cwR, cwC, ms
+    o << (first ? "" : ", ") << "[" << row[0] << ", " << row[1] << ", " << row[2] << ", " << row[3] << ", " << row[4]
+      << ", " << row[5] << "]";
+    first = false;
+  }
+  o << "]}";
   f->desc = o.str();
   return f->desc.c_str();
 }

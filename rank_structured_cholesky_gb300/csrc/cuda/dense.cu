@@ -707,6 +707,16 @@ void launch_extadd(const ExtAddRow<T>* rows, int nRows, const ExtAddSeg* segs, c
   extadd_kernel<T><<<(nRows + 7) / 8, 256, 0, s>>>(rows, nRows, segs, src);
   RSCHOL_LAUNCH_CHECK();
 }
+__global__ void init_flags_kernel(int* flag) {
+  flag[0] = INT_MAX;
+  flag[1] = 0;
+}
+
+void launch_init_flags(int* flag, cudaStream_t s) {
+  init_flags_kernel<<<1, 1, 0, s>>>(flag);
+  RSCHOL_LAUNCH_CHECK();
+}
+
 template <class T>
 void launch_scatter(const double* A, const long long* si, const long long* di, long long count, T* dst,
                     cudaStream_t s) {

@@ -89,6 +89,8 @@ template <class T> void launch_trsm(const TrsmTask<T>* dTasks, int nTasks, int t
 template <class T>
 void launch_extadd(const ExtAddRow<T>* dRows, int nRows, const ExtAddSeg* dSegs, const ExtAddSource<T>* dSources,
                    cudaStream_t s);
+// flag[0] = INT_MAX (no POTRF failure yet), flag[1] = 0 (no tensor-core wait error)
+void launch_init_flags(int* flag, cudaStream_t s);
 template <class T>
 void launch_scatter(const double* Avals, const long long* srcIdx, const long long* dstIdx, long long count,
                     T* dst, cudaStream_t s);

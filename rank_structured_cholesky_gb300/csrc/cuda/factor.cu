@@ -32,6 +32,8 @@ FactorEngine<T>::FactorEngine(const Symbolic& S_, const CSC& A_, const Params& p
   RSCHOL_CUDA(cudaMemcpyAsync(dAvals.p, A.x.data(), sizeof(double) * A.x.size(), cudaMemcpyHostToDevice, stream));
   dFlag.alloc(2 * sizeof(int));
   useTc_ = std::is_same<T, float>::value && tensor_cores_enabled();
+  const char* g = std::getenv("RSCHOL_GRAPHS");
+  useGraphs_ = !(g && g[0] == '0');
   RSCHOL_CUDA(cudaStreamSynchronize(stream));
 }
 
@@ -333,6 +335,8 @@ void FactorEngine<T>::emit_rf(const std::vector<RFJob<T>>& jobs) {
 
 template <class T>
 void FactorEngine<T>::plan() {
+  drop_graphs();   // the captured schedule points into the buffers about to be replaced
+  runsSincePlan_ = 0;
   const int nn = (int)S.nodes.size();
   const int N = S.n;
   steps_.clear();
@@ -834,27 +838,33 @@ void FactorEngine<T>::plan() {
 }
 
 template <class T>
-int FactorEngine<T>::run() {
-  if (!planned_) plan();
+void FactorEngine<T>::drop_graphs() {
+  for (auto& g : graph_)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+// Everything one factorisation queues on the stream, between the status
+// reset and the status read.
+template <class T>
+void FactorEngine<T>::enqueue(bool timing, bool capturing) {
+  const unsigned recFlags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   launches = 0;
   RSCHOL_CUDA(cudaMemsetAsync(dInterior.p, 0, dInterior.bytes, stream));
   RSCHOL_CUDA(cudaMemsetAsync(dCompressed.p, 0, dCompressed.bytes, stream));
-  static const int init[2] = {INT_MAX, 0};   // POTRF code, tensor-core wait error
-  RSCHOL_CUDA(cudaMemcpyAsync(dFlag.p, init, sizeof(init), cudaMemcpyHostToDevice, stream));
+  launch_init_flags(dFlag.as<int>(), stream);   // POTRF code = INT_MAX, tensor-core wait error = 0
   launch_scatter<T>(dAvals.as<double>(), dScatSrc_.as<long long>(), dScatDst_.as<long long>(), nScatI_, interior(),
                     stream);
   launch_scatter<T>(dAvals.as<double>(), dScatSrc_.as<long long>() + nScatI_, dScatDst_.as<long long>() + nScatI_,
                     nScatC_, compressed(), stream);
-  launches += 2;
-  const bool timing = timeSteps && !steps_.empty();
-  if (timing && stepEv_.size() < 2 * steps_.size()) {
-    for (auto e : stepEv_) cudaEventDestroy(e);
-    stepEv_.assign(2 * steps_.size(), nullptr);
-    for (auto& e : stepEv_) RSCHOL_CUDA(cudaEventCreate(&e));
-  }
+  launches += 3;
   for (size_t q = 0; q < steps_.size(); ++q) {
     const Step& st = steps_[q];
-    if (timing) RSCHOL_CUDA(cudaEventRecord(stepEv_[2 * q], stream));
+    // external records inside a capture become event-record nodes, so the
+    // replayed graph still times every step
+    if (timing) RSCHOL_CUDA(cudaEventRecordWithFlags(stepEv_[2 * q], stream, recFlags));
     switch (st.kind) {
       case ST_GEMM:
       case ST_GEMM_REDUCE: gemm_launch(st); break;
@@ -869,10 +879,48 @@ int FactorEngine<T>::run() {
         break;
       case ST_IDENT: launch_set_identity<T>(dIdent_.as<IdentTask<T>>() + st.off, st.count, stream); break;
     }
-    if (timing) RSCHOL_CUDA(cudaEventRecord(stepEv_[2 * q + 1], stream));
+    if (timing) RSCHOL_CUDA(cudaEventRecordWithFlags(stepEv_[2 * q + 1], stream, recFlags));
     ++launches;
   }
   if (post) launches += post();
+}
+
+template <class T>
+int FactorEngine<T>::run() {
+  if (!planned_) plan();
+  const bool timing = timeSteps && !steps_.empty();
+  if (timing && stepEv_.size() < 2 * steps_.size()) {
+    drop_graphs();   // the timing graph records the events it was captured with
+    for (auto e : stepEv_) cudaEventDestroy(e);
+    stepEv_.assign(2 * steps_.size(), nullptr);
+    for (auto& e : stepEv_) RSCHOL_CUDA(cudaEventCreate(&e));
+  }
+  // the first run of a plan is queued directly (one-time kernel attributes
+  // are set outside any capture); later runs replay a captured graph
+  const int g = timing ? 1 : 0;
+  if (useGraphs_ && runsSincePlan_ > 0) {
+    if (!graph_[g]) {
+      RSCHOL_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      cudaGraph_t graph = nullptr;
+      try {
+        enqueue(timing, true);
+      } catch (...) {
+        cudaStreamEndCapture(stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+      }
+      RSCHOL_CUDA(cudaStreamEndCapture(stream, &graph));
+      const cudaError_t e = cudaGraphInstantiate(&graph_[g], graph, 0);
+      cudaGraphDestroy(graph);
+      RSCHOL_CUDA(e);
+      graphLaunches_[g] = launches;
+    }
+    RSCHOL_CUDA(cudaGraphLaunch(graph_[g], stream));
+    launches = graphLaunches_[g];
+  } else {
+    enqueue(timing, false);
+  }
+  ++runsSincePlan_;
   int flag[2] = {0, 0};
   RSCHOL_CUDA(cudaMemcpyAsync(flag, dFlag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
   RSCHOL_CUDA(cudaStreamSynchronize(stream));
@@ -887,8 +935,8 @@ int FactorEngine<T>::run() {
     for (const Step& st : steps_)
       if (st.kind == ST_GEMM)
         for (int k = 0; k < st.count; ++k) {
-          const GemmTask<T>& g = gemm_[st.off + k];
-          stepFlops[ST_GEMM] += 2.0 * g.M * g.N * (double)g.K;
+          const GemmTask<T>& gt = gemm_[st.off + k];
+          stepFlops[ST_GEMM] += 2.0 * gt.M * gt.N * (double)gt.K;
         }
   }
   if (flag[1]) throw CudaError("tensor-core GEMM: an mbarrier wait exceeded its limit");

@@ -90,6 +90,7 @@ class FactorEngine {
  public:
   FactorEngine(const Symbolic& S, const CSC& Alower, const Params& prm, cudaStream_t stream);
   ~FactorEngine() {
+    drop_graphs();
     for (auto e : stepEv_) cudaEventDestroy(e);
   }
 
@@ -173,6 +174,16 @@ class FactorEngine {
   DevBuf dScatSrcC_, dScatDstC_;
   long long nScatI_ = 0, nScatC_ = 0;
   bool planned_ = false;
+  // The schedule is static per plan: from the second run of a plan on, the
+  // whole factorisation (and the solve-side preparation queued by post) is
+  // replayed from a CUDA graph captured once; [1] is the variant with the
+  // per-step timing events.  Off with RSCHOL_GRAPHS=0.
+  bool useGraphs_ = true;
+  int runsSincePlan_ = 0;
+  cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+  long long graphLaunches_[2] = {0, 0};
+  void drop_graphs();
+  void enqueue(bool timing, bool capturing);
 };
 
 }  // namespace rschol

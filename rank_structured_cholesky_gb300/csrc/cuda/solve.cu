@@ -1,4 +1,5 @@
 #include <algorithm>
+#include <cstdlib>
 #include <type_traits>
 
 #include "solve.cuh"
@@ -509,7 +510,10 @@ __global__ void convert_kernel(const A* __restrict__ src, B* __restrict__ dst, i
 }  // namespace
 
 template <class T>
-SolveEngine<T>::SolveEngine(FactorEngine<T>& F) : F_(F) {}
+SolveEngine<T>::SolveEngine(FactorEngine<T>& F) : F_(F) {
+  const char* e = std::getenv("RSCHOL_AUTOTUNE");
+  autotune_ = !(e && e[0] == '0');
+}
 
 template <class T>
 void SolveEngine<T>::plan() {

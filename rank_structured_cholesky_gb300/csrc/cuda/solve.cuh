@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <stdexcept>
+#include <array>
 #include <map>
 #include <vector>
 
@@ -110,6 +111,8 @@ class SolveEngine {
   // contiguous) := M^{-1} W with one pass over the factor; k <=
   // batch_capacity().  take_error_batch: as take_error, for the batched path.
   void apply_batch(double* d_W, int k, cudaStream_t s);
+  // the tile shapes chosen for each width class so far: (class, RA, RC, cwR, cwC, ms) rows
+  std::vector<std::array<double, 6>> batch_tuning() const;
   int batch_capacity() const;
   int take_error_batch(cudaStream_t s);
   long long launches_per_apply() const { return launchesPerApply_; }
@@ -144,7 +147,21 @@ class SolveEngine {
   // batched apply: work buffers sized for the widest k seen (they only grow,
   // so a changing width frees nothing and never synchronises the device);
   // the GEMM task lists are built once per width and kept
-  void plan_batch(int k);
+  // Tile shapes of the batched apply (none changes any column's arithmetic):
+  // the interior (row, column) pair tile RA x RC and the column groups of the
+  // two skinny product forms.  Chosen per width class (k rounded up to a
+  // power of two) by timing candidates on first use (RSCHOL_AUTOTUNE=0: fixed
+  // heuristics).
+  struct BatchCfg {
+    int ra = 1, rc = 1, cwR = 1, cwC = 1;
+    double ms = 0;   // the winning candidate's time (0: not timed)
+  };
+  BatchCfg heuristic_cfg(int kp) const;
+  const BatchCfg& config_for(int k, cudaStream_t s);
+  void apply_batch_cfg(double* W64, int k, cudaStream_t s, const BatchCfg& c);
+  std::map<int, BatchCfg> tuned_;
+  bool autotune_ = true;
+  void plan_batch(int k, int cwR, int cwC);
   long long wuTotal_ = 0, ipTotal_ = 0;
   int maxNI_ = 0;                      // largest interior supernode width
   std::vector<int> cMRowGrid_;         // per compressed level: 8-row blocks of the largest m

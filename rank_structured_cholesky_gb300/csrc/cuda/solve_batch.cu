@@ -496,8 +496,9 @@ int SolveEngine<T>::batch_capacity() const {
 }
 
 template <class T>
-void SolveEngine<T>::plan_batch(int k) {
-  if (k == kB_) return;
+void SolveEngine<T>::plan_batch(int k, int cwR, int cwC) {
+  const int key = k * 256 + cwR * 16 + cwC;   // cwR <= 16, cwC <= 8
+  if (key == kB_) return;
   const Symbolic& S = F_.S;
   cudaStream_t st = F_.stream;
   if (k > kAllocB_) {
@@ -513,13 +514,13 @@ void SolveEngine<T>::plan_batch(int k) {
     kAllocB_ = k;
     bPlans_.clear();   // the task lists point into the old buffers
   }
-  auto found = bPlans_.find(k);
+  auto found = bPlans_.find(key);
   if (found != bPlans_.end()) {
     bPlan_ = &found->second;
-    kB_ = k;
+    kB_ = key;
     return;
   }
-  BatchPlan& plan = bPlans_[k];
+  BatchPlan& plan = bPlans_[key];
   // products of the compressed levels (skinny SIMT kernels)
   std::vector<SkinnyTask<T>> tasks;
   auto& steps = plan.steps;
@@ -527,9 +528,9 @@ void SolveEngine<T>::plan_batch(int k) {
   T* wu = dWuB_.as<T>();
   T* yb = dYB_.as<T>();
   T* w = dWB_.as<T>();
-  // column groups: up to 16 columns for the row form, 8 for the transposed form
-  const int cgR = (k + skinny_cw(k, false) - 1) / skinny_cw(k, false);
-  const int cgC = (k + skinny_cw(k, true) - 1) / skinny_cw(k, true);
+  // column groups of the two product forms
+  const int cgR = (k + cwR - 1) / cwR;
+  const int cgC = (k + cwC - 1) / cwC;
   struct Prod {   // one product before it is cut into units
     const T* A;
     const T* B;
@@ -643,14 +644,101 @@ void SolveEngine<T>::plan_batch(int k) {
                                 cudaMemcpyHostToDevice, st));
   RSCHOL_CUDA(cudaStreamSynchronize(st));
   bPlan_ = &plan;
-  kB_ = k;
+  kB_ = key;
+}
+
+template <class T>
+typename SolveEngine<T>::BatchCfg SolveEngine<T>::heuristic_cfg(int kp) const {
+  BatchCfg c;
+  if (kp >= 48) c.ra = 4, c.rc = 4;
+  else if (kp >= 24) c.ra = 2, c.rc = 4;
+  else if (kp >= 4) c.ra = 1, c.rc = 4;
+  c.cwR = skinny_cw(kp, false);
+  c.cwC = skinny_cw(kp, true);
+  return c;
+}
+
+// The width class of k is kp = k rounded up to a power of two (<= the batch
+// capacity); its shapes are timed once, at k = kp, on a zero block: first the
+// interior pair tile, then the row-form and the transposed-form column
+// groups, each over a handful of candidates, the fastest of two timed
+// applies after one warm-up.
+template <class T>
+const typename SolveEngine<T>::BatchCfg& SolveEngine<T>::config_for(int k, cudaStream_t st) {
+  const int kp = std::min(skinny_width(k), std::max(k, batch_capacity()));
+  auto it = tuned_.find(kp);
+  if (it != tuned_.end()) return it->second;
+  BatchCfg best = heuristic_cfg(kp);
+  if (autotune_) {
+    const size_t bytes = sizeof(double) * (size_t)std::max(1, F_.S.n) * kp;
+    DevBuf zero;
+    zero.alloc(bytes);
+    RSCHOL_CUDA(cudaMemsetAsync(zero.p, 0, bytes, st));
+    cudaEvent_t e0, e1;
+    RSCHOL_CUDA(cudaEventCreate(&e0));
+    RSCHOL_CUDA(cudaEventCreate(&e1));
+    auto time_cfg = [&](const BatchCfg& c) {
+      apply_batch_cfg(zero.as<double>(), kp, st, c);   // warm-up (plans this shape)
+      float bestMs = 1e30f;
+      for (int rep = 0; rep < 2; ++rep) {
+        RSCHOL_CUDA(cudaEventRecord(e0, st));
+        apply_batch_cfg(zero.as<double>(), kp, st, c);
+        RSCHOL_CUDA(cudaEventRecord(e1, st));
+        RSCHOL_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        RSCHOL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        bestMs = std::min(bestMs, ms);
+      }
+      return (double)bestMs;
+    };
+    best.ms = time_cfg(best);
+    auto consider = [&](BatchCfg c) {
+      if (c.ra == best.ra && c.rc == best.rc && c.cwR == best.cwR && c.cwC == best.cwC) return;
+      c.ms = time_cfg(c);
+      if (c.ms < best.ms) best = c;
+    };
+    const int tiles[4][2] = {{1, 1}, {1, 4}, {2, 4}, {4, 4}};
+    for (auto& tl : tiles) {
+      BatchCfg c = best;
+      c.ra = tl[0];
+      c.rc = tl[1];
+      consider(c);
+    }
+    for (int cw = 4; cw <= std::min(16, kp); cw *= 2) {
+      BatchCfg c = best;
+      c.cwR = cw;
+      consider(c);
+    }
+    for (int cw = 2; cw <= std::min(8, kp); cw *= 2) {
+      BatchCfg c = best;
+      c.cwC = cw;
+      consider(c);
+    }
+    RSCHOL_CUDA(cudaEventDestroy(e0));
+    RSCHOL_CUDA(cudaEventDestroy(e1));
+  }
+  return tuned_[kp] = best;
+}
+
+template <class T>
+std::vector<std::array<double, 6>> SolveEngine<T>::batch_tuning() const {
+  std::vector<std::array<double, 6>> out;
+  for (const auto& kv : tuned_)
+    out.push_back({(double)kv.first, (double)kv.second.ra, (double)kv.second.rc, (double)kv.second.cwR,
+                   (double)kv.second.cwC, kv.second.ms});
+  return out;
 }
 
 template <class T>
 void SolveEngine<T>::apply_batch(double* W64, int k, cudaStream_t st) {
   if (k <= 0) return;
   if (k > batch_capacity()) throw std::runtime_error("apply_batch: more right-hand sides than one pass handles");
-  plan_batch(k);
+  apply_batch_cfg(W64, k, st, config_for(k, st));
+}
+
+template <class T>
+void SolveEngine<T>::apply_batch_cfg(double* W64, int k, cudaStream_t st, const BatchCfg& cfg) {
+  plan_batch(k, cfg.cwR, cfg.cwC);
   const int n = F_.S.n;
   const long long nk = (long long)n * k;
   T* w = dWB_.as<T>();
@@ -674,19 +762,18 @@ void SolveEngine<T>::apply_batch(double* W64, int k, cudaStream_t st) {
     RSCHOL_SMEM_ATTR(4, 4);
 #undef RSCHOL_SMEM_ATTR
   });
-  // register tiles of (row, column) pairs: enough tiles for the 256 threads
-  // of a block (64 - 128 rows) at every k
+  // register tiles of (row, column) pairs (BatchCfg)
   using IF = decltype(&interior_forward_k<T, 1, 1>);
   using IB = decltype(&interior_backward_k<T, 1, 1>);
   IF fwd = interior_forward_k<T, 1, 1>;
   IB bwd = interior_backward_k<T, 1, 1>;
-  if (k >= 48) {
+  if (cfg.ra == 4) {
     fwd = interior_forward_k<T, 4, 4>;
     bwd = interior_backward_k<T, 4, 4>;
-  } else if (k >= 24) {
+  } else if (cfg.ra == 2) {
     fwd = interior_forward_k<T, 2, 4>;
     bwd = interior_backward_k<T, 2, 4>;
-  } else if (k >= 4) {
+  } else if (cfg.rc == 4) {
     fwd = interior_forward_k<T, 1, 4>;
     bwd = interior_backward_k<T, 1, 4>;
   }
@@ -700,7 +787,7 @@ void SolveEngine<T>::apply_batch(double* W64, int k, cudaStream_t st) {
   auto gemm = [&](int slot) {
     for (const XStep& x : bPlan_->steps[slot]) {
       const SkinnyTask<T>* tk = bg + x.off;
-      const int cw = skinny_cw(k, x.tc != 0);
+      const int cw = x.tc ? cfg.cwC : cfg.cwR;
 #define RSCHOL_SKINNY(CW)                                                     \
   if (x.tc) skinny_cols_kernel<T, CW><<<x.tiles, 256, 0, st>>>(tk, x.count, k); \
   else skinny_rows_kernel<T, CW><<<x.tiles, 256, 0, st>>>(tk, x.count, k)
@@ -764,8 +851,16 @@ int SolveEngine<T>::take_error_batch(cudaStream_t st) {
 
 template int SolveEngine<double>::batch_capacity() const;
 template int SolveEngine<float>::batch_capacity() const;
-template void SolveEngine<double>::plan_batch(int);
-template void SolveEngine<float>::plan_batch(int);
+template void SolveEngine<double>::plan_batch(int, int, int);
+template void SolveEngine<float>::plan_batch(int, int, int);
+template SolveEngine<double>::BatchCfg SolveEngine<double>::heuristic_cfg(int) const;
+template SolveEngine<float>::BatchCfg SolveEngine<float>::heuristic_cfg(int) const;
+template const SolveEngine<double>::BatchCfg& SolveEngine<double>::config_for(int, cudaStream_t);
+template const SolveEngine<float>::BatchCfg& SolveEngine<float>::config_for(int, cudaStream_t);
+template void SolveEngine<double>::apply_batch_cfg(double*, int, cudaStream_t, const BatchCfg&);
+template void SolveEngine<float>::apply_batch_cfg(double*, int, cudaStream_t, const BatchCfg&);
+template std::vector<std::array<double, 6>> SolveEngine<double>::batch_tuning() const;
+template std::vector<std::array<double, 6>> SolveEngine<float>::batch_tuning() const;
 template void SolveEngine<double>::apply_batch(double*, int, cudaStream_t);
 template void SolveEngine<float>::apply_batch(double*, int, cudaStream_t);
 template int SolveEngine<double>::take_error_batch(cudaStream_t);
