@@ -227,6 +227,8 @@ def timed_solves(lib, rs, torch, prob, precision, device, local, steps, warmup, 
     d_b = torch.from_numpy(np.ascontiguousarray(prob.rhs[:nrhs])).to(device)
     d_x = torch.zeros_like(d_b)
     infos = (rs.PcgInfo * nrhs)()
+    if nrhs > 1:   # tile shapes of the batched apply, timed once before any timed work
+        F.autotune(nrhs)
     torch.cuda.synchronize()
 
     def refactor():

@@ -123,6 +123,16 @@ int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x
  *   - the first call on a device looks up the array's address
  *     (cudaGetSymbolAddress, with that device current); make that first call
  *     before any stream capture that would include this function. */
+/* Autotuner of the batched apply (no reference counterpart): times the
+ * candidate tile shapes (interior (row, column) pair tiles, column groups of
+ * the compressed-level products) of every width class (number of
+ * right-hand sides rounded up to a power of two) up to max_columns and keeps
+ * the fastest for this factor; run it while the GPU is otherwise quiet.  No
+ * candidate changes any result: every shape forms each column's sums in the
+ * same order.  Untuned classes use fixed shapes.  The choices are listed in
+ * rschol_factor_describe ("batch_tuning": class, RA, RC, cwR, cwC, ms). */
+int rschol_factor_autotune(rschol_factor* f, int max_columns);
+
 /* ---- continuous batching on one factor (no reference counterpart) --------
  * A session keeps the Krylov state of up to max_columns right-hand sides of
  * one factor on the device (clamped to the factor's batch capacity, at most

@@ -37,7 +37,7 @@ EXPORTED = [
     "rschol_factor_describe", "rschol_factor_stats", "rschol_problem_diffusion", "rschol_problem_elasticity",
     "rschol_problem_n", "rschol_problem_nnz", "rschol_problem_nrhs", "rschol_problem_get", "rschol_problem_free",
     "rschol_mt_draws", "rschol_mt_gaussians", "rschol_block_rank", "rschol_separator_tree", "rschol_etree_counts",
-    "rschol_relaxed_supernodes", "rschol_session_create", "rschol_session_columns", "rschol_session_add",
+    "rschol_relaxed_supernodes", "rschol_factor_autotune", "rschol_session_create", "rschol_session_columns", "rschol_session_add",
     "rschol_session_step", "rschol_session_result", "rschol_session_counts", "rschol_session_destroy",
     "rschol_server_create", "rschol_server_submit", "rschol_server_wait",
     "rschol_server_stats", "rschol_server_destroy",
@@ -120,6 +120,7 @@ def load_library():
         "rschol_separator_tree": (I, [I, P, I, P, P]),
         "rschol_etree_counts": (None, [I, P, P, P, P]),
         "rschol_relaxed_supernodes": (I, [I, P, P, I, P, P, P, P, I, P, P]),
+        "rschol_factor_autotune": (I, [P, I]),
         "rschol_session_create": (P, [P, I]),
         "rschol_session_columns": (I, [P]),
         "rschol_session_add": (I, [P, LL, I, pD, pD, D, I]),
@@ -266,6 +267,12 @@ class GpuFactor:
         info = [dict(iterations=i.iterations, residual=i.residual, true_residual=i.true_residual,
                      seconds=i.seconds) for i in infos]
         return x, (info[0] if nrhs == 1 else info)
+
+    def autotune(self, max_columns=64):
+        """Time the batched apply's tile shapes for every width class up to max_columns."""
+        st = load_library().rschol_factor_autotune(self.h, max_columns)
+        if st != RSCHOL_OK:
+            raise RscholError(st, self.ctx.last_error())
 
     def num_nodes(self):
         return load_library().rschol_factor_num_nodes(self.h)

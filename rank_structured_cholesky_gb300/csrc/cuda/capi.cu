@@ -70,6 +70,7 @@ struct Impl {
   virtual double apply_bytes() const = 0;
   virtual size_t bytes() const = 0;
   virtual std::vector<std::array<double, 6>> batch_tuning() const = 0;
+  virtual void autotune_batch(int kmax, cudaStream_t s) = 0;
   virtual void node_l11(int j, double* out) = 0;
   virtual void node_l21(int j, double* out) = 0;
 };
@@ -110,6 +111,7 @@ struct ImplT : Impl {
   double apply_bytes() const override { return se.bytes_per_apply(); }
   size_t bytes() const override { return fe.deviceBytes; }
   std::vector<std::array<double, 6>> batch_tuning() const override { return se.batch_tuning(); }
+  void autotune_batch(int kmax, cudaStream_t s) override { se.autotune_batch(kmax, s); }
   std::vector<T> fetch(const T* d, size_t count) {
     std::vector<T> h(count);
     if (count) RSCHOL_CUDA(cudaMemcpy(h.data(), d, sizeof(T) * count, cudaMemcpyDeviceToHost));
@@ -847,6 +849,19 @@ struct rschol_session {
   };
   std::map<long long, Req> reqs;
 };
+
+extern "C" int rschol_factor_autotune(rschol_factor* f, int max_columns) {
+  if (!f || max_columns < 1) return RSCHOL_E_BAD_INPUT;
+  AccountScope acct(&f->devBytes);
+  try {
+    f->impl->autotune_batch(std::min(64, max_columns), f->ctx->stream);
+    RSCHOL_CUDA(cudaStreamSynchronize(f->ctx->stream));
+    if (f->impl->apply_batch_error(f->ctx->stream)) return fail(f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);
+  } catch (const std::exception& e) {
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+  return RSCHOL_OK;
+}
 
 extern "C" rschol_session* rschol_session_create(rschol_factor* f, int max_columns) {
   if (!f || max_columns < 1 || max_columns > 64) return nullptr;

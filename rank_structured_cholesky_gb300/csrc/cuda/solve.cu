@@ -512,7 +512,7 @@ __global__ void convert_kernel(const A* __restrict__ src, B* __restrict__ dst, i
 template <class T>
 SolveEngine<T>::SolveEngine(FactorEngine<T>& F) : F_(F) {
   const char* e = std::getenv("RSCHOL_AUTOTUNE");
-  autotune_ = !(e && e[0] == '0');
+  autotune_ = e && e[0] == '1';
 }
 
 template <class T>

@@ -111,6 +111,9 @@ class SolveEngine {
   // contiguous) := M^{-1} W with one pass over the factor; k <=
   // batch_capacity().  take_error_batch: as take_error, for the batched path.
   void apply_batch(double* d_W, int k, cudaStream_t s);
+  // Time the candidate tile shapes of every width class up to kmax on this
+  // stream (run it while the GPU is otherwise quiet) and keep the fastest.
+  void autotune_batch(int kmax, cudaStream_t s);
   // the tile shapes chosen for each width class so far: (class, RA, RC, cwR, cwC, ms) rows
   std::vector<std::array<double, 6>> batch_tuning() const;
   int batch_capacity() const;
@@ -149,15 +152,16 @@ class SolveEngine {
   // the GEMM task lists are built once per width and kept
   // Tile shapes of the batched apply (none changes any column's arithmetic):
   // the interior (row, column) pair tile RA x RC and the column groups of the
-  // two skinny product forms.  Chosen per width class (k rounded up to a
-  // power of two) by timing candidates on first use (RSCHOL_AUTOTUNE=0: fixed
-  // heuristics).
+  // two skinny product forms, per width class (k rounded up to a power of
+  // two).  Fixed heuristics unless the class was tuned by autotune_batch
+  // (or, with RSCHOL_AUTOTUNE=1, on first use).
   struct BatchCfg {
     int ra = 1, rc = 1, cwR = 1, cwC = 1;
     double ms = 0;   // the winning candidate's time (0: not timed)
   };
   BatchCfg heuristic_cfg(int kp) const;
-  const BatchCfg& config_for(int k, cudaStream_t s);
+  const BatchCfg& config_for(int k, cudaStream_t s, bool tune);
+  int width_class(int k) const;
   void apply_batch_cfg(double* W64, int k, cudaStream_t s, const BatchCfg& c);
   std::map<int, BatchCfg> tuned_;
   bool autotune_ = true;

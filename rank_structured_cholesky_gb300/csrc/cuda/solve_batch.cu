@@ -649,12 +649,13 @@ void SolveEngine<T>::plan_batch(int k, int cwR, int cwC) {
 
 template <class T>
 typename SolveEngine<T>::BatchCfg SolveEngine<T>::heuristic_cfg(int kp) const {
+  // what the tuner picks on 2D and 3D diffusion factors of 0.26 - 1 M
+  // unknowns: 1 x 1 pair tiles up to 16 columns, 2 x 4 above; row-form groups
+  // of up to 16 columns; transposed-form groups of 4, 8 from 16 columns on
   BatchCfg c;
-  if (kp >= 48) c.ra = 4, c.rc = 4;
-  else if (kp >= 24) c.ra = 2, c.rc = 4;
-  else if (kp >= 4) c.ra = 1, c.rc = 4;
-  c.cwR = skinny_cw(kp, false);
-  c.cwC = skinny_cw(kp, true);
+  if (kp >= 32) c.ra = 2, c.rc = 4;
+  c.cwR = std::min(16, skinny_width(kp));
+  c.cwC = std::min(kp >= 16 ? 8 : 4, skinny_width(kp));
   return c;
 }
 
@@ -664,12 +665,17 @@ typename SolveEngine<T>::BatchCfg SolveEngine<T>::heuristic_cfg(int kp) const {
 // groups, each over a handful of candidates, the fastest of two timed
 // applies after one warm-up.
 template <class T>
-const typename SolveEngine<T>::BatchCfg& SolveEngine<T>::config_for(int k, cudaStream_t st) {
-  const int kp = std::min(skinny_width(k), std::max(k, batch_capacity()));
+int SolveEngine<T>::width_class(int k) const {
+  return std::min(skinny_width(k), std::max(k, batch_capacity()));
+}
+
+template <class T>
+const typename SolveEngine<T>::BatchCfg& SolveEngine<T>::config_for(int k, cudaStream_t st, bool tune) {
+  const int kp = width_class(k);
   auto it = tuned_.find(kp);
-  if (it != tuned_.end()) return it->second;
+  if (it != tuned_.end() && (it->second.ms > 0 || !tune)) return it->second;
   BatchCfg best = heuristic_cfg(kp);
-  if (autotune_) {
+  if (tune) {
     const size_t bytes = sizeof(double) * (size_t)std::max(1, F_.S.n) * kp;
     DevBuf zero;
     zero.alloc(bytes);
@@ -721,6 +727,12 @@ const typename SolveEngine<T>::BatchCfg& SolveEngine<T>::config_for(int k, cudaS
 }
 
 template <class T>
+void SolveEngine<T>::autotune_batch(int kmax, cudaStream_t st) {
+  kmax = std::min(kmax, batch_capacity());
+  for (int k = 1; k <= kmax; k = width_class(k) + 1) config_for(k, st, true);
+}
+
+template <class T>
 std::vector<std::array<double, 6>> SolveEngine<T>::batch_tuning() const {
   std::vector<std::array<double, 6>> out;
   for (const auto& kv : tuned_)
@@ -733,7 +745,7 @@ template <class T>
 void SolveEngine<T>::apply_batch(double* W64, int k, cudaStream_t st) {
   if (k <= 0) return;
   if (k > batch_capacity()) throw std::runtime_error("apply_batch: more right-hand sides than one pass handles");
-  apply_batch_cfg(W64, k, st, config_for(k, st));
+  apply_batch_cfg(W64, k, st, config_for(k, st, autotune_));
 }
 
 template <class T>
@@ -855,8 +867,12 @@ template void SolveEngine<double>::plan_batch(int, int, int);
 template void SolveEngine<float>::plan_batch(int, int, int);
 template SolveEngine<double>::BatchCfg SolveEngine<double>::heuristic_cfg(int) const;
 template SolveEngine<float>::BatchCfg SolveEngine<float>::heuristic_cfg(int) const;
-template const SolveEngine<double>::BatchCfg& SolveEngine<double>::config_for(int, cudaStream_t);
-template const SolveEngine<float>::BatchCfg& SolveEngine<float>::config_for(int, cudaStream_t);
+template const SolveEngine<double>::BatchCfg& SolveEngine<double>::config_for(int, cudaStream_t, bool);
+template const SolveEngine<float>::BatchCfg& SolveEngine<float>::config_for(int, cudaStream_t, bool);
+template int SolveEngine<double>::width_class(int) const;
+template int SolveEngine<float>::width_class(int) const;
+template void SolveEngine<double>::autotune_batch(int, cudaStream_t);
+template void SolveEngine<float>::autotune_batch(int, cudaStream_t);
 template void SolveEngine<double>::apply_batch_cfg(double*, int, cudaStream_t, const BatchCfg&);
 template void SolveEngine<float>::apply_batch_cfg(double*, int, cudaStream_t, const BatchCfg&);
 template std::vector<std::array<double, 6>> SolveEngine<double>::batch_tuning() const;

@@ -1,10 +1,10 @@
 """The batched apply's autotuner picks tile shapes only, never arithmetic.
 
-Each width class (k rounded up to a power of two) is tuned on first use by
-timing candidate shapes; the candidates differ in which thread forms which
+rschol_factor_autotune times candidate shapes for each width class (k rounded
+up to a power of two); the candidates differ in which thread forms which
 (row, column) sum, not in the order of any sum.  So the tuned factor must
-give bitwise the same batched applies as one that keeps the fixed shapes
-(RSCHOL_AUTOTUNE=0), at every width.
+give bitwise the same batched applies as one that keeps the fixed shapes, at
+every width.
 """
 import numpy as np
 import pytest
@@ -17,14 +17,14 @@ PARAMS = dict(max_dense_block=30, max_diag_block=60, nd_leaf=16)
 
 
 @pytest.mark.parametrize("precision", [rs.FP64, rs.MIXED])
-def test_autotuned_shapes_give_identical_results(precision, monkeypatch):
+def test_autotuned_shapes_give_identical_results(precision):
     prob = rs.diffusion(3, 14, sigma=1.0, seed=21)
     rng = np.random.default_rng(3)
     factors = {}
     for mode in ("1", "0"):
-        monkeypatch.setenv("RSCHOL_AUTOTUNE", mode)
         factors[mode] = rs.GpuFactor(rs.Context(precision=precision, **PARAMS), prob.colptr, prob.rowind, prob.vals,
                                      prob.xyz)
+    factors["1"].autotune(64)
     for k in (2, 3, 8, 16, 40):
         B = rng.standard_normal((k, prob.n))
         x_tuned = factors["1"].apply(B)
