@@ -545,80 +545,141 @@ __global__ void __launch_bounds__(QRP_THREADS) qr_panel_kernel(const QrTask<T>* 
   }
 }
 
-// Apply the block reflector of panel j0 to a group of QA_CW columns.
+// Apply the block reflector of panel j0 to the other columns, in parallel
+// over (row block of QA_RB rows, group of QA_CW columns):
 //   mode 0 (factor): W[j0:n, c] := (I - V T^T V^T) W[j0:n, c], c >= j0 + pw
 //   mode 1 (form Q): Y[j0:n, c] := (I - V T V^T) Y[j0:n, c],   c >= j0
+// in three launches: Zpart = V^T A per row block; Z = the row-block partials
+// added in order, M = T^T Z (or T Z); A -= V M per row block.  ws holds
+// Zpart (tasks x cgMax x rbMax x 16 x 16) and then M (tasks x cgMax x 16 x 16).
+constexpr int QA_RB = 256;   // rows per block of the apply
+
 template <class T>
-__global__ void __launch_bounds__(256) qr_apply_kernel(const QrTask<T>* __restrict__ tasks, int j0, int mode) {
+struct QrApplyView {
+  const T* V;   // panel reflectors, column-major (ld n), V[p][i] at V[p * n + i], unit diagonal implied
+  T* A;
+  int n, r, nr, pw, c0, cw;
+  int mode;
+  __device__ size_t aidx(int j0, int i, int c) const {
+    return mode == 0 ? (size_t)(c0 + c) * n + j0 + i : (size_t)(j0 + i) * r + c0 + c;
+  }
+  __device__ T v(int i, int p) const {   // reflector p at panel row i (i counted from j0)
+    if (p >= pw) return T(0);
+    return i == p ? T(1) : (i > p ? V[(size_t)p * n + i] : T(0));
+  }
+};
+
+template <class T>
+__device__ __forceinline__ bool qr_view(const QrTask<T>& t, int j0, int mode, int cg, QrApplyView<T>& w) {
+  const int n = t.n, r = t.r;
+  if (j0 >= r) return false;
+  w.n = n;
+  w.r = r;
+  w.pw = min(QR_PB, r - j0);
+  w.nr = n - j0;
+  w.mode = mode;
+  w.c0 = (mode == 0 ? j0 + w.pw : j0) + cg * QA_CW;
+  if (w.c0 >= r) return false;
+  w.cw = min(QA_CW, r - w.c0);
+  w.V = t.W + (size_t)j0 * n + j0;
+  w.A = mode == 0 ? t.W : t.Y;
+  return true;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) qr_zpart_kernel(const QrTask<T>* __restrict__ tasks, int j0, int mode,
+                                                       T* __restrict__ ws, int cgMax, int rbMax) {
   __shared__ T Vs[QA_ROWS][QR_PB + 1];
   __shared__ T As[QA_ROWS][QA_CW + 1];
-  __shared__ T Z[QR_PB][QA_CW + 1];
-  __shared__ T M[QR_PB][QA_CW + 1];
-  __shared__ T Ts[QR_PB][QR_PB + 1];
   const QrTask<T> t = tasks[blockIdx.y];
-  const int n = t.n, r = t.r;
-  if (j0 >= r) return;
-  const int pw = min(QR_PB, r - j0), nr = n - j0;
-  const int c0 = (mode == 0 ? j0 + pw : j0) + blockIdx.x * QA_CW;
-  if (c0 >= r) return;
-  const int cw = min(QA_CW, r - c0);
-  const int tid = threadIdx.x;
-  const T* Vg = t.W + (size_t)j0 * n + j0;
-  auto aidx = [&](int i, int c) -> size_t {
-    return mode == 0 ? (size_t)(c0 + c) * n + j0 + i : (size_t)(j0 + i) * r + c0 + c;
-  };
-  T* A = mode == 0 ? t.W : t.Y;
-  for (int idx = tid; idx < QR_PB * QR_PB; idx += blockDim.x) {
-    const int a = idx / QR_PB, b = idx - a * QR_PB;
-    Ts[a][b] = (a <= b && b < pw) ? Vg[(size_t)b * n + a] : T(0);
-  }
-  auto load_v = [&](int i0, int h) {
+  const int cg = blockIdx.x % cgMax, rb = blockIdx.x / cgMax;
+  QrApplyView<T> w;
+  if (!qr_view(t, j0, mode, cg, w)) return;
+  const int r0 = rb * QA_RB;
+  if (r0 >= w.nr) return;
+  const int r1 = min(w.nr, r0 + QA_RB);
+  const int tid = threadIdx.x, zp = tid % QR_PB, zc = tid / QR_PB;
+  T z = T(0);
+  for (int i0 = r0; i0 < r1; i0 += QA_ROWS) {
+    const int h = min(QA_ROWS, r1 - i0);
     for (int idx = tid; idx < QA_ROWS * QR_PB; idx += blockDim.x) {
       const int p = idx / QA_ROWS, i = idx - p * QA_ROWS;
-      const int gi = i0 + i;
-      T v = T(0);
-      if (i < h && p < pw) v = gi == p ? T(1) : (gi > p ? Vg[(size_t)p * n + gi] : T(0));
-      Vs[i][p] = v;
+      Vs[i][p] = i < h ? w.v(i0 + i, p) : T(0);
     }
-  };
-  auto load_a = [&](int i0, int h) {
     for (int idx = tid; idx < QA_ROWS * QA_CW; idx += blockDim.x) {
       int i, c;
       if (mode == 0) { c = idx / QA_ROWS; i = idx - c * QA_ROWS; }
       else { i = idx / QA_CW; c = idx - i * QA_CW; }
-      As[i][c] = (i < h && c < cw) ? A[aidx(i0 + i, c)] : T(0);
+      As[i][c] = (i < h && c < w.cw) ? w.A[w.aidx(j0, i0 + i, c)] : T(0);
     }
-  };
-  // Z = V^T A (thread: p = tid % 16, c = tid / 16)
-  const int zp = tid % QR_PB, zc = tid / QR_PB;
-  T z = T(0);
-  for (int i0 = 0; i0 < nr; i0 += QA_ROWS) {
-    const int h = min(QA_ROWS, nr - i0);
-    load_v(i0, h);
-    load_a(i0, h);
     __syncthreads();
 #pragma unroll 8
     for (int i = 0; i < QA_ROWS; ++i) z += Vs[i][zp] * As[i][zc];
     __syncthreads();
   }
+  ws[(((size_t)blockIdx.y * cgMax + cg) * rbMax + rb) * (QR_PB * QA_CW) + zp * QA_CW + zc] = z;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) qr_zreduce_kernel(const QrTask<T>* __restrict__ tasks, int j0, int mode,
+                                                         T* __restrict__ ws, int cgMax, int rbMax, long long mOff) {
+  __shared__ T Z[QR_PB][QA_CW + 1];
+  __shared__ T Ts[QR_PB][QR_PB + 1];
+  const QrTask<T> t = tasks[blockIdx.y];
+  const int cg = blockIdx.x;
+  QrApplyView<T> w;
+  if (!qr_view(t, j0, mode, cg, w)) return;
+  const int tid = threadIdx.x, zp = tid % QR_PB, zc = tid / QR_PB;
+  {
+    const int a = tid / QR_PB, b = tid - a * QR_PB;   // T over the upper triangle of the diagonal block
+    Ts[a][b] = (a <= b && b < w.pw) ? w.V[(size_t)b * w.n + a] : T(0);
+  }
+  const int nrb = (w.nr + QA_RB - 1) / QA_RB;
+  const T* zpart = ws + ((size_t)blockIdx.y * cgMax + cg) * rbMax * (QR_PB * QA_CW) + zp * QA_CW + zc;
+  T z = T(0);
+  for (int rb = 0; rb < nrb; ++rb) z += zpart[(size_t)rb * (QR_PB * QA_CW)];
   Z[zp][zc] = z;
   __syncthreads();
-  {
-    T m = T(0);
-    if (mode == 0) {
-      for (int q = 0; q <= zp; ++q) m += Ts[q][zp] * Z[q][zc];   // T^T Z
-    } else {
-      for (int q = zp; q < QR_PB; ++q) m += Ts[zp][q] * Z[q][zc];   // T Z
-    }
-    M[zp][zc] = m;
+  T m = T(0);
+  if (mode == 0) {
+    for (int q = 0; q <= zp; ++q) m += Ts[q][zp] * Z[q][zc];   // T^T Z
+  } else {
+    for (int q = zp; q < QR_PB; ++q) m += Ts[zp][q] * Z[q][zc];   // T Z
   }
-  __syncthreads();
-  // A -= V M (thread: row i = tid % 64, columns 4 (tid / 64) .. +3)
+  ws[mOff + ((size_t)blockIdx.y * cgMax + cg) * (QR_PB * QA_CW) + zp * QA_CW + zc] = m;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) qr_update_kernel(const QrTask<T>* __restrict__ tasks, int j0, int mode,
+                                                        const T* __restrict__ ws, int cgMax, long long mOff) {
+  __shared__ T Vs[QA_ROWS][QR_PB + 1];
+  __shared__ T As[QA_ROWS][QA_CW + 1];
+  __shared__ T M[QR_PB][QA_CW + 1];
+  const QrTask<T> t = tasks[blockIdx.y];
+  const int cg = blockIdx.x % cgMax, rb = blockIdx.x / cgMax;
+  QrApplyView<T> w;
+  if (!qr_view(t, j0, mode, cg, w)) return;
+  const int r0 = rb * QA_RB;
+  if (r0 >= w.nr) return;
+  const int r1 = min(w.nr, r0 + QA_RB);
+  const int tid = threadIdx.x;
+  {
+    const int zp = tid % QR_PB, zc = tid / QR_PB;
+    M[zp][zc] = ws[mOff + ((size_t)blockIdx.y * cgMax + cg) * (QR_PB * QA_CW) + zp * QA_CW + zc];
+  }
   const int ai = tid % QA_ROWS, aq = (tid / QA_ROWS) * 4;
-  for (int i0 = 0; i0 < nr; i0 += QA_ROWS) {
-    const int h = min(QA_ROWS, nr - i0);
-    load_v(i0, h);
-    load_a(i0, h);
+  for (int i0 = r0; i0 < r1; i0 += QA_ROWS) {
+    const int h = min(QA_ROWS, r1 - i0);
+    for (int idx = tid; idx < QA_ROWS * QR_PB; idx += blockDim.x) {
+      const int p = idx / QA_ROWS, i = idx - p * QA_ROWS;
+      Vs[i][p] = i < h ? w.v(i0 + i, p) : T(0);
+    }
+    for (int idx = tid; idx < QA_ROWS * QA_CW; idx += blockDim.x) {
+      int i, c;
+      if (mode == 0) { c = idx / QA_ROWS; i = idx - c * QA_ROWS; }
+      else { i = idx / QA_CW; c = idx - i * QA_CW; }
+      As[i][c] = (i < h && c < w.cw) ? w.A[w.aidx(j0, i0 + i, c)] : T(0);
+    }
     __syncthreads();
 #pragma unroll
     for (int cc = 0; cc < 4; ++cc) {
@@ -632,7 +693,7 @@ __global__ void __launch_bounds__(256) qr_apply_kernel(const QrTask<T>* __restri
       int i, c;
       if (mode == 0) { c = idx / QA_ROWS; i = idx - c * QA_ROWS; }
       else { i = idx / QA_CW; c = idx - i * QA_CW; }
-      if (i < h && c < cw) A[aidx(i0 + i, c)] = As[i][c];
+      if (i < h && c < w.cw) w.A[w.aidx(j0, i0 + i, c)] = As[i][c];
     }
     __syncthreads();
   }
@@ -724,8 +785,24 @@ void launch_scatter(const double* A, const long long* si, const long long* di, l
   scatter_kernel<T><<<grid_for(count, 256), 256, 0, s>>>(A, si, di, count, dst);
   RSCHOL_LAUNCH_CHECK();
 }
-template <class T> int launch_householder_qr(const QrTask<T>* d, int n, int maxRows, int maxR, cudaStream_t s) {
+long long householder_qr_workspace(int nTasks, int maxRows, int maxR) {
+  const long long cgMax = (maxR + QA_CW - 1) / QA_CW, rbMax = (maxRows + QA_RB - 1) / QA_RB;
+  return (long long)nTasks * cgMax * (rbMax + 1) * (QR_PB * QA_CW);
+}
+
+template <class T>
+int launch_householder_qr(const QrTask<T>* d, int n, int maxRows, int maxR, T* ws, cudaStream_t s) {
   if (n <= 0 || maxR <= 0) return 0;
+  const int cgMax = (maxR + QA_CW - 1) / QA_CW, rbMax = (maxRows + QA_RB - 1) / QA_RB;
+  const long long mOff = (long long)n * cgMax * rbMax * (QR_PB * QA_CW);
+  int launches = 0;
+  auto apply = [&](int j0, int mode) {
+    qr_zpart_kernel<T><<<dim3(cgMax * rbMax, n), 256, 0, s>>>(d, j0, mode, ws, cgMax, rbMax);
+    qr_zreduce_kernel<T><<<dim3(cgMax, n), 256, 0, s>>>(d, j0, mode, ws, cgMax, rbMax, mOff);
+    qr_update_kernel<T><<<dim3(cgMax * rbMax, n), 256, 0, s>>>(d, j0, mode, ws, cgMax, mOff);
+    RSCHOL_LAUNCH_CHECK();
+    launches += 3;
+  };
   static std::once_flag once;
   std::call_once(once, [] {
     RSCHOL_CUDA(cudaFuncSetAttribute(qr_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, QR_SMEM_MAX));
@@ -733,7 +810,7 @@ template <class T> int launch_householder_qr(const QrTask<T>* d, int n, int maxR
   const long long tiles = (long long)((maxRows + 31) / 32) * ((maxR + 31) / 32);
   qr_to_colmajor<T><<<dim3((unsigned)std::min<long long>(tiles, 64), n), 256, 0, s>>>(d);
   RSCHOL_LAUNCH_CHECK();
-  int launches = 1;
+  launches += 1;
   const size_t smem = std::min<size_t>((size_t)QR_SMEM_MAX, sizeof(T) * (size_t)maxRows * QR_PB);
   const long long smemElems = (long long)(smem / sizeof(T));
   const int panels = (maxR + QR_PB - 1) / QR_PB;
@@ -742,23 +819,13 @@ template <class T> int launch_householder_qr(const QrTask<T>* d, int n, int maxR
     qr_panel_kernel<T><<<n, QRP_THREADS, smem, s>>>(d, j0, smemElems);
     RSCHOL_LAUNCH_CHECK();
     ++launches;
-    const int trail = maxR - j0 - QR_PB;
-    if (trail > 0) {
-      qr_apply_kernel<T><<<dim3((trail + QA_CW - 1) / QA_CW, n), 256, 0, s>>>(d, j0, 0);
-      RSCHOL_LAUNCH_CHECK();
-      ++launches;
-    }
+    if (maxR - j0 - QR_PB > 0) apply(j0, 0);
   }
   const long long ecount = (long long)maxRows * maxR;
   qr_set_e<T><<<dim3((unsigned)std::max<long long>(1, std::min<long long>((ecount + 255) / 256, 256)), n), 256, 0, s>>>(d);
   RSCHOL_LAUNCH_CHECK();
   ++launches;
-  for (int p = panels - 1; p >= 0; --p) {
-    const int j0 = p * QR_PB;
-    qr_apply_kernel<T><<<dim3((maxR - j0 + QA_CW - 1) / QA_CW, n), 256, 0, s>>>(d, j0, 1);
-    RSCHOL_LAUNCH_CHECK();
-    ++launches;
-  }
+  for (int p = panels - 1; p >= 0; --p) apply(p * QR_PB, 1);
   return launches;
 }
 template <class T> void launch_set_identity(const IdentTask<T>* d, int n, cudaStream_t s) {
@@ -780,7 +847,7 @@ template <class T> void launch_box_muller(const uint32_t* raw, long long count, 
                                  cudaStream_t);                                                          \
   template void launch_scatter<T>(const double*, const long long*, const long long*, long long, T*,      \
                                   cudaStream_t);                                                         \
-  template int launch_householder_qr<T>(const QrTask<T>*, int, int, int, cudaStream_t);                  \
+  template int launch_householder_qr<T>(const QrTask<T>*, int, int, int, T*, cudaStream_t);                  \
   template void launch_set_identity<T>(const IdentTask<T>*, int, cudaStream_t);                          \
   template void launch_box_muller<T>(const uint32_t*, long long, T*, cudaStream_t);
 RSCHOL_INST(double)

@@ -107,7 +107,9 @@ struct QrTask {
   int n, r;
 };
 template <class T>
-int launch_householder_qr(const QrTask<T>* dTasks, int nTasks, int maxRows, int maxR, cudaStream_t s);
+int launch_householder_qr(const QrTask<T>* dTasks, int nTasks, int maxRows, int maxR, T* ws, cudaStream_t s);
+// elements of the workspace launch_householder_qr needs for such a batch
+long long householder_qr_workspace(int nTasks, int maxRows, int maxR);
 template <class T>
 struct IdentTask {
   T* U;

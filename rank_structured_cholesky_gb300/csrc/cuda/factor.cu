@@ -316,6 +316,7 @@ void FactorEngine<T>::emit_rf(const std::vector<RFJob<T>>& jobs) {
     }
     steps_.push_back(Step{ST_QR, (long long)qr_.size(), (int)qt.size(), maxR, maxRows});
     qr_.insert(qr_.end(), qt.begin(), qt.end());
+    qrWs_ = std::max(qrWs_, householder_qr_workspace((int)qt.size(), maxRows, maxR));
   }
   // V = F U
   tiles = 0;
@@ -351,6 +352,7 @@ void FactorEngine<T>::plan() {
   splitBase_.clear();
   wsCur_ = 0;
   qr_.clear();
+  qrWs_ = 0;
   ident_.clear();
   ints_.clear();
   flops = 0;
@@ -808,6 +810,7 @@ void FactorEngine<T>::plan() {
   up(dInts_, ints_.data(), ints_.size() * sizeof(int));
   for (auto& s : eaS_) s.rowRel = dInts_.as<int>() + reinterpret_cast<size_t>(s.rowRel);
   dSplitWs_.alloc(sizeof(float) * std::max(1LL, wsCur_));
+  dQrWs_.alloc(sizeof(T) * std::max(1LL, qrWs_));
   for (size_t q = 0; q < gemm_.size(); ++q)
     if (gemmWsOff_[q] >= 0) gemm_[q].ws = dSplitWs_.as<float>() + gemmWsOff_[q];
   up(dSplitIds_, splitIds_.data(), splitIds_.size() * sizeof(int));
@@ -875,7 +878,8 @@ void FactorEngine<T>::enqueue(bool timing, bool capturing) {
                          dEaS_.as<ExtAddSource<T>>(), stream);
         break;
       case ST_QR:
-        launches += launch_householder_qr<T>(dQr_.as<QrTask<T>>() + st.off, st.count, st.aux, st.grid, stream) - 1;
+        launches += launch_householder_qr<T>(dQr_.as<QrTask<T>>() + st.off, st.count, st.aux, st.grid,
+                                             dQrWs_.as<T>(), stream) - 1;
         break;
       case ST_IDENT: launch_set_identity<T>(dIdent_.as<IdentTask<T>>() + st.off, st.count, stream); break;
     }

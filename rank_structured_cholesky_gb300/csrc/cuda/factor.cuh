@@ -168,6 +168,8 @@ class FactorEngine {
   std::vector<long long> splitBase_;       // ST_GEMM_REDUCE: element prefix sums (nIds + 1 per step)
   long long wsCur_ = 0;
   DevBuf dSplitWs_, dSplitIds_, dSplitBase_;
+  long long qrWs_ = 0;   // elements of the Householder QR workspace (largest QR step)
+  DevBuf dQrWs_;
   std::vector<long long> scatSrc_, scatDst_;
   std::vector<int> scatIsInterior_;
   DevBuf dGemm_, dPotrf_, dTrsm_, dEaR_, dEaSeg_, dEaS_, dQr_, dIdent_, dInts_, dScatSrc_, dScatDst_;
