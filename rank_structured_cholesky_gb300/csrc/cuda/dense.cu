@@ -223,10 +223,14 @@ __global__ void __launch_bounds__(256) trsm_kernel(const TrsmTask<T>* __restrict
 template <class T>
 __global__ void __launch_bounds__(256) potrf_reg_kernel(const PotrfTask<T>* __restrict__ tasks, int* flag) {
   // Right-looking Cholesky of one <= 64 x 64 tile.  Thread (i = tid / 4,
-  // g = tid % 4) keeps row i, columns g, g + 4, ..., in registers; column j
-  // is broadcast through a double-buffered shared array.
+  // g = tid % 4) keeps row i, columns g, g + 4, ..., in registers.  Column j
+  // is published unscaled (u, pivot p = u_j) through a double-buffered shared
+  // array, so one barrier per column suffices: the trailing update is
+  // a_ik -= u_i u_k / p, and the stored columns are scaled by 1 / sqrt(p) at
+  // the end (L_jj = sqrt(p)).
   const PotrfTask<T> t = tasks[blockIdx.x];
   __shared__ T col[2][64];
+  __shared__ T piv[64];
   __shared__ int bad;
   const int n = t.n, tid = threadIdx.x, i = tid >> 2, g = tid & 3;
   T v[16];
@@ -246,38 +250,38 @@ __global__ void __launch_bounds__(256) potrf_reg_kernel(const PotrfTask<T>* __re
       const int j = 4 * q0 + jj;
       if (j < n) {
         T* cj = col[j & 1];
-        if (g == jj && i == j) {
-          T d = v[q0];
-          if (!(d > T(0))) {   // not positive definite (or NaN): keep going, report
-            bad = 1;
-            d = T(1);
+        if (g == jj && i >= j && i < n) {
+          T u = v[q0];
+          if (i == j) {
+            if (!(u > T(0))) {   // not positive definite (or NaN): keep going, report
+              bad = 1;
+              u = T(1);
+              v[q0] = u;
+            }
+            piv[j] = u;
           }
-          d = sqrt(d);
-          v[q0] = d;
-          cj[j] = d;
-        }
-        __syncthreads();
-        if (g == jj && i > j && i < n) {
-          const T x = v[q0] / cj[j];
-          v[q0] = x;
-          cj[i] = x;
+          cj[i] = u;
         }
         __syncthreads();
         if (i > j && i < n) {
-          const T ci = cj[i];
+          const T ui = cj[i] / cj[j];
 #pragma unroll
           for (int q = 0; q < 16; ++q) {
             const int k = g + 4 * q;
-            if (k > j && k <= i) v[q] -= ci * cj[k];
+            if (k > j && k <= i) v[q] -= ui * cj[k];
           }
         }
       }
     }
   }
+  __syncthreads();
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
     const int k = g + 4 * q;
-    if (i < n && k <= i) t.A[(size_t)i * t.ld + k] = v[q];
+    if (i < n && k <= i) {
+      const T d = sqrt(piv[k]);
+      t.A[(size_t)i * t.ld + k] = (k == i) ? d : v[q] / d;
+    }
   }
   if (tid == 0 && bad) atomicMin(flag, t.code);
 }
@@ -285,7 +289,8 @@ __global__ void __launch_bounds__(256) potrf_reg_kernel(const PotrfTask<T>* __re
 template <class T>
 __global__ void __launch_bounds__(256) trsm_inv_kernel(const TrsmTask<T>* __restrict__ tasks, int nTasks) {
   // B (64-row chunk x w) := B L^{-T}: the block inverts its w x w tile
-  // (column c by thread c, forward substitution) and multiplies.
+  // (blocked: 16 x 16 diagonal inverses, then the off-diagonal blocks by
+  // distance from the diagonal) and multiplies.
   int lo = 0, hi = nTasks - 1;
   const int b = blockIdx.x;
   while (lo < hi) {
@@ -294,56 +299,93 @@ __global__ void __launch_bounds__(256) trsm_inv_kernel(const TrsmTask<T>* __rest
     else hi = mid - 1;
   }
   const TrsmTask<T> t = tasks[lo];
-  const int r0 = (b - t.chunkBase) * 64;
-  const int nr = min(64, t.rows - r0);
+  const int rb0 = (b - t.chunkBase) * TRSM_ROWS_F32;   // this block's rows: 4 chunks of 64 share the inverse
   const int w = t.w, tid = threadIdx.x;
   extern __shared__ __align__(16) unsigned char trsm_smem[];
   T (*L)[65] = reinterpret_cast<T (*)[65]>(trsm_smem);
   T (*Li)[65] = reinterpret_cast<T (*)[65]>(trsm_smem + sizeof(T) * 64 * 65);
   T (*X)[65] = reinterpret_cast<T (*)[65]>(trsm_smem + 2 * sizeof(T) * 64 * 65);
+  T (*Tm)[16][17] = reinterpret_cast<T (*)[16][17]>(trsm_smem + 3 * sizeof(T) * 64 * 65);   // 3 blocks
   for (int idx = tid; idx < 64 * 64; idx += blockDim.x) {
     const int i = idx >> 6, j = idx & 63;
-    L[i][j] = (i < w && j <= i) ? t.L[(size_t)i * t.ldl + j] : T(0);
+    // padded to 64 with a unit diagonal: the leading w x w block of the
+    // inverse is L^{-1}
+    L[i][j] = (i < w && j <= i) ? t.L[(size_t)i * t.ldl + j] : (i == j ? T(1) : T(0));
     Li[i][j] = T(0);
-    X[i][j] = (i < nr && j < w) ? t.B[(size_t)(r0 + i) * t.ldb + j] : T(0);
   }
   __syncthreads();
-  if (tid < w) {
-    const int c = tid;
-    for (int r = c; r < w; ++r) {
-      T s = (r == c) ? T(1) : T(0);
-      for (int k = c; k < r; ++k) s -= L[r][k] * Li[k][c];
-      Li[r][c] = s / L[r][r];
+  // Li = L^{-1} in 16 x 16 blocks.  Diagonal blocks: warp b inverts block b
+  // by forward substitution, lane c owning column c of the block.
+  {
+    const int wb = tid >> 5, c = tid & 31;
+    if (wb < 4 && c < 16) {
+      const int o = 16 * wb;
+      for (int r = c; r < 16; ++r) {
+        T s = (r == c) ? T(1) : T(0);
+        for (int k = c; k < r; ++k) s -= L[o + r][o + k] * Li[o + k][o + c];
+        Li[o + r][o + c] = s / L[o + r][o + r];
+      }
     }
   }
   __syncthreads();
-  // out[i][j] = sum_{k <= j} X[i][k] Li[j][k]; thread: rows ty + 16 a, columns tx + 16 c
-  const int tx = tid & 15, ty = tid >> 4;
-  T acc[4][4];
-#pragma unroll
-  for (int a = 0; a < 4; ++a)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) acc[a][c] = T(0);
-  for (int k = 0; k < w; ++k) {
-    T xa[4], lb[4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a) xa[a] = X[ty + 16 * a][k];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) lb[c] = Li[tx + 16 * c][k];
+  // Off-diagonal blocks by distance d = R - C: Li[R][C] = -Li[R][R] sum_{K=C}^{R-1} L[R][K] Li[K][C]
+  for (int d = 1; d < 4; ++d) {
+    const int np = 4 - d;   // block pairs (R, C = R - d)
+    for (int e = tid; e < np * 256; e += blockDim.x) {
+      const int pr = e >> 8, i = (e >> 4) & 15, j = e & 15;
+      const int C = pr, R = pr + d;
+      T s = T(0);
+      for (int k = 16 * C; k < 16 * R; ++k) s += L[16 * R + i][k] * Li[k][16 * C + j];
+      Tm[pr][i][j] = s;
+    }
+    __syncthreads();
+    for (int e = tid; e < np * 256; e += blockDim.x) {
+      const int pr = e >> 8, i = (e >> 4) & 15, j = e & 15;
+      const int C = pr, R = pr + d;
+      T s = T(0);
+      for (int k = 0; k <= i; ++k) s += Li[16 * R + i][16 * R + k] * Tm[pr][k][j];
+      Li[16 * R + i][16 * C + j] = -s;
+    }
+    __syncthreads();
+  }
+  for (int sub = 0; sub < TRSM_ROWS_F32 / 64; ++sub) {
+    const int r0 = rb0 + 64 * sub;
+    if (r0 >= t.rows) break;
+    const int nr = min(64, t.rows - r0);
+    for (int idx = tid; idx < 64 * 64; idx += blockDim.x) {
+      const int i = idx >> 6, j = idx & 63;
+      X[i][j] = (i < nr && j < w) ? t.B[(size_t)(r0 + i) * t.ldb + j] : T(0);
+    }
+    __syncthreads();
+    // out[i][j] = sum_{k <= j} X[i][k] Li[j][k]; thread: rows ty + 16 a, columns tx + 16 c
+    const int tx = tid & 15, ty = tid >> 4;
+    T acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) acc[a][c] = fma(xa[a], lb[c], acc[a][c]);
-  }
+      for (int c = 0; c < 4; ++c) acc[a][c] = T(0);
+    for (int k = 0; k < w; ++k) {
+      T xa[4], lb[4];
 #pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    const int i = ty + 16 * a;
-    if (i >= nr) continue;
+      for (int a = 0; a < 4; ++a) xa[a] = X[ty + 16 * a][k];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const int j = tx + 16 * c;
-      if (j < w) t.B[(size_t)(r0 + i) * t.ldb + j] = acc[a][c];
+      for (int c = 0; c < 4; ++c) lb[c] = Li[tx + 16 * c][k];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[a][c] = fma(xa[a], lb[c], acc[a][c]);
     }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int i = ty + 16 * a;
+      if (i >= nr) continue;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int j = tx + 16 * c;
+        if (j < w) t.B[(size_t)(r0 + i) * t.ldb + j] = acc[a][c];
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -747,7 +789,7 @@ template <class T> void launch_trsm(const TrsmTask<T>* d, int n, int chunks, cud
   if (n <= 0 || chunks <= 0) return;
   static std::once_flag once;   // per instantiation; callers may be on several threads
   if constexpr (std::is_same<T, float>::value) {
-    const int smem = (int)(3 * sizeof(T) * 64 * 65);
+    const int smem = (int)(3 * sizeof(T) * 64 * 65 + 3 * sizeof(T) * 16 * 17);
     std::call_once(once, [&] {
       RSCHOL_CUDA(cudaFuncSetAttribute(trsm_inv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     });

@@ -7,6 +7,7 @@
 // (src/rschol/linearalgebra/MATRIX_FAST.cpp:1758 gemm, 1885 syrk, 2086
 // cholesky, 3049 triangularSolve).
 #pragma once
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -42,7 +43,13 @@ struct PotrfTask {
   int code;
 };
 
-// B (rows x w) := B * L^{-T}, L the w x w (w <= 64) lower tile.
+// B (rows x w) := B * L^{-T}, L the w x w (w <= 64) lower tile.  A launch
+// block takes trsm_rows<T>() rows; chunkBase counts such blocks.  (FP32
+// blocks of 256 rows sharing one tile inverse measured slower than 64: the
+// launches lose more parallelism than the repeated inverses cost.)
+constexpr int TRSM_ROWS_F32 = 64;
+template <class T>
+constexpr int trsm_rows() { return std::is_same<T, float>::value ? TRSM_ROWS_F32 : 64; }
 template <class T>
 struct TrsmTask {
   const T* L;

@@ -180,7 +180,7 @@ void FactorEngine<T>::emit_chol(const std::vector<CholJob<T>>& jobs) {
       int rows = j.nRows - kb - w;
       if (rows <= 0) continue;
       TrsmTask<T> t{j.F + (size_t)kb * j.ld + kb, j.F + (size_t)(kb + w) * j.ld + kb, j.ld, j.ld, w, rows, chunks};
-      chunks += (rows + 63) / 64;
+      chunks += (rows + trsm_rows<T>() - 1) / trsm_rows<T>();
       tt.push_back(t);
       flops += (double)rows * w * w;
     }
@@ -215,7 +215,7 @@ void FactorEngine<T>::emit_trsm(const std::vector<TrsmJob<T>>& jobs) {
       if (j.w <= kb || j.rows <= 0) continue;
       int bw = std::min(NB, j.w - kb);
       tt.push_back(TrsmTask<T>{j.L + (size_t)kb * j.ldl + kb, j.B + kb, j.ldl, j.ldb, bw, j.rows, chunks});
-      chunks += (j.rows + 63) / 64;
+      chunks += (j.rows + trsm_rows<T>() - 1) / trsm_rows<T>();
       flops += (double)j.rows * bw * bw;
     }
     if (!tt.empty()) {
