@@ -29,60 +29,86 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_kernel(const GemmTask<T>* _
   const int row0 = ti * BM, col0 = tj * BN;
   if (t.lower && row0 + BM - 1 < col0) return;
 
-  __shared__ T As[BK][BM + 1];
-  __shared__ T Bs[BK][BN + 1];
+  // Two shared stages: the next K slice is loaded into registers while the
+  // current one is multiplied (one barrier per slice); C is fetched before
+  // the K loop.  Each C entry's K order is the plain ascending one.
+  __shared__ T As[2][BK][BM + 1];
+  __shared__ T Bs[2][BK][BN + 1];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   T acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
-
+  T cpre[4][4];
+  if (t.beta != T(0)) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int gi = row0 + ty + 16 * i, gj = col0 + tx + 16 * j;
+        cpre[i][j] = (gi < t.M && gj < t.N) ? t.C[(size_t)gi * t.ldc + gj] : T(0);
+      }
+  }
+  T ra[4], rb[4];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int i, k;
+      if (!t.tA) { i = (tid >> 4) + 16 * q; k = tid & 15; }
+      else { i = tid & 63; k = (tid >> 6) + 4 * q; }
+      const int gi = row0 + i, gk = k0 + k;
+      ra[q] = (gi < t.M && gk < t.K) ? (t.tA ? t.A[(size_t)gk * t.lda + gi] : t.A[(size_t)gi * t.lda + gk]) : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int j, k;
+      if (!t.tB) { j = tid & 63; k = (tid >> 6) + 4 * q; }
+      else { j = (tid >> 4) + 16 * q; k = tid & 15; }
+      const int gj = col0 + j, gk = k0 + k;
+      rb[q] = (gj < t.N && gk < t.K) ? (t.tB ? t.B[(size_t)gj * t.ldb + gk] : t.B[(size_t)gk * t.ldb + gj]) : T(0);
+    }
+  };
+  auto store = [&](int st) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int i, k;
+      if (!t.tA) { i = (tid >> 4) + 16 * q; k = tid & 15; }
+      else { i = tid & 63; k = (tid >> 6) + 4 * q; }
+      As[st][k][i] = ra[q];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int j, k;
+      if (!t.tB) { j = tid & 63; k = (tid >> 6) + 4 * q; }
+      else { j = (tid >> 4) + 16 * q; k = tid & 15; }
+      Bs[st][k][j] = rb[q];
+    }
+  };
+  if (t.K > 0) {
+    load(0);
+    store(0);
+  }
+  __syncthreads();
+  int st = 0;
   for (int k0 = 0; k0 < t.K; k0 += BK) {
-    if (!t.tA) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        int i = (tid >> 4) + 16 * q, k = tid & 15;
-        int gi = row0 + i, gk = k0 + k;
-        As[k][i] = (gi < t.M && gk < t.K) ? t.A[(size_t)gi * t.lda + gk] : T(0);
-      }
-    } else {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        int i = tid & 63, k = (tid >> 6) + 4 * q;
-        int gi = row0 + i, gk = k0 + k;
-        As[k][i] = (gi < t.M && gk < t.K) ? t.A[(size_t)gk * t.lda + gi] : T(0);
-      }
-    }
-    if (!t.tB) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        int j = tid & 63, k = (tid >> 6) + 4 * q;
-        int gj = col0 + j, gk = k0 + k;
-        Bs[k][j] = (gj < t.N && gk < t.K) ? t.B[(size_t)gk * t.ldb + gj] : T(0);
-      }
-    } else {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        int j = (tid >> 4) + 16 * q, k = tid & 15;
-        int gj = col0 + j, gk = k0 + k;
-        Bs[k][j] = (gj < t.N && gk < t.K) ? t.B[(size_t)gj * t.ldb + gk] : T(0);
-      }
-    }
-    __syncthreads();
+    const bool more = k0 + BK < t.K;
+    if (more) load(k0 + BK);
 #pragma unroll
     for (int k = 0; k < BK; ++k) {
       T a[4], bb[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[k][ty + 16 * i];
+      for (int i = 0; i < 4; ++i) a[i] = As[st][k][ty + 16 * i];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) bb[j] = Bs[k][tx + 16 * j];
+      for (int j = 0; j < 4; ++j) bb[j] = Bs[st][k][tx + 16 * j];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
     }
+    if (more) store(st ^ 1);
     __syncthreads();
+    st ^= 1;
   }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
@@ -94,7 +120,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_kernel(const GemmTask<T>* _
       if (gj >= t.N) continue;
       T* c = t.C + (size_t)gi * t.ldc + gj;
       T v = t.alpha * acc[i][j];
-      if (t.beta != T(0)) v = fma(t.beta, *c, v);
+      if (t.beta != T(0)) v = fma(t.beta, cpre[i][j], v);
       *c = v;
     }
   }
