@@ -63,7 +63,8 @@ void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
   if (batch.empty()) return;
   // Path: the tensor cores for FP32 steps with a real K (rank-64 updates are
   // bound by C traffic, which the SIMT kernel already streams); large-K tasks
-  // of steps with few tiles are split along K to fill the SMs.
+  // of steps with few tiles are split along K (slices of at least 128) to
+  // fill the SMs.
   int maxK = 0;
   for (auto& t : batch) maxK = std::max(maxK, t.K);
   const bool tc = useTc_ && maxK >= 128;
@@ -82,8 +83,8 @@ void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
     t.kSplit = 1;
     t.kLen = t.K;
     long long wsOff = -1;
-    if (tc && !t.lower && t.K >= 1024 && baseTiles < want) {
-      int ks = (int)std::min<long long>(16, std::min<long long>(t.K / 512, (want + baseTiles - 1) / baseTiles));
+    if (tc && !t.lower && t.K >= 256 && baseTiles < want) {
+      int ks = (int)std::min<long long>(16, std::min<long long>(t.K / 128, (want + baseTiles - 1) / baseTiles));
       if (ks > 1) {
         const int kl = ((t.K + ks - 1) / ks + 31) / 32 * 32;
         t.kSplit = (t.K + kl - 1) / kl;
