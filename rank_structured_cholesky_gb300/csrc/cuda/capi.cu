@@ -4,6 +4,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -152,6 +153,13 @@ struct ImplT : Impl {
 
 namespace rschol {
 thread_local std::atomic<long long>* g_devAccount = nullptr;
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("RSCHOL_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
 }
 
 struct rschol_factor {

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <utility>
 
 namespace rschol {
 
@@ -22,6 +23,36 @@ struct CudaError : std::runtime_error {
   } while (0)
 
 #define RSCHOL_LAUNCH_CHECK() RSCHOL_CUDA(cudaGetLastError())
+
+// Programmatic dependent launch.  A kernel launched with launch_k may start
+// while the previous kernel on the stream drains: it first lets its own
+// successor launch, then waits until its predecessor has completed and its
+// writes are visible (griddepcontrol), so every kernel so launched must call
+// pdl_enter() before it touches memory.  (A successor grid launches only after
+// every block of its predecessor has started, so waiting blocks never keep a
+// predecessor's blocks off the SMs.)  Both instructions are no-ops for a
+// kernel launched without the attribute.  RSCHOL_PDL=0 turns it off.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+bool pdl_enabled();
+
+template <class... KArgs, class... Args>
+void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  RSCHOL_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+}
 
 // Live device bytes are charged to the account current on the allocating
 // thread (each factor has one, made current by its entry points) and credited

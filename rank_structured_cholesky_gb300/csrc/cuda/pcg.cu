@@ -32,6 +32,7 @@ template <int TPR>
 __global__ void spmv_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci,
                             const double* __restrict__ v, const double* __restrict__ x, double* __restrict__ y,
                             double* __restrict__ part, int withDot) {
+  pdl_enter();
   const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int row = (int)(g / TPR), lane = (int)(g % TPR);
   double s = 0.0;
@@ -52,6 +53,7 @@ __global__ void spmv_kernel(int n, const int* __restrict__ rp, const int* __rest
 
 __global__ void dot_kernel(const double* __restrict__ a, const double* __restrict__ b, int n,
                            double* __restrict__ part) {
+  pdl_enter();
   double s = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += a[i] * b[i];
   double t = block_sum(s);
@@ -59,6 +61,7 @@ __global__ void dot_kernel(const double* __restrict__ a, const double* __restric
 }
 
 __global__ void finish_kernel(const double* __restrict__ part, int count, double* __restrict__ sc, int mode) {
+  pdl_enter();
   double s = 0.0;
   for (int i = threadIdx.x; i < count; i += blockDim.x) s += part[i];
   double t = block_sum(s);
@@ -83,15 +86,18 @@ __global__ void finish_kernel(const double* __restrict__ part, int count, double
   }
 }
 
+// x += alpha d, r -= alpha q, and rcopy = r (the preconditioner's input)
 __global__ void update_xr_kernel(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ d,
                                  const double* __restrict__ q, const double* __restrict__ sc, int n,
-                                 double* __restrict__ part) {
+                                 double* __restrict__ part, double* __restrict__ rcopy) {
+  pdl_enter();
   const double a = sc[S_ALPHA];
   double s = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     x[i] += a * d[i];
     const double ri = r[i] - a * q[i];
     r[i] = ri;
+    rcopy[i] = ri;
     s += ri * ri;
   }
   double t = block_sum(s);
@@ -100,12 +106,14 @@ __global__ void update_xr_kernel(double* __restrict__ x, double* __restrict__ r,
 
 __global__ void update_d_kernel(double* __restrict__ d, const double* __restrict__ s,
                                 const double* __restrict__ sc, int n) {
+  pdl_enter();
   const double b = sc[S_BETA];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) d[i] = s[i] + b * d[i];
 }
 
 __global__ void residual_kernel(const double* __restrict__ b, const double* __restrict__ q, int n,
                                 double* __restrict__ part) {
+  pdl_enter();
   double s = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double e = b[i] - q[i];
@@ -117,16 +125,19 @@ __global__ void residual_kernel(const double* __restrict__ b, const double* __re
 
 __global__ void gather_kernel(const double* __restrict__ src, const int* __restrict__ perm, double* __restrict__ dst,
                               int n) {
+  pdl_enter();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[perm[i]];
 }
 
 __global__ void scatter_perm_kernel(const double* __restrict__ src, const int* __restrict__ perm,
                                     double* __restrict__ dst, int n) {
+  pdl_enter();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[perm[i]] = src[i];
 }
 
 __global__ void index_gather_kernel(const double* __restrict__ src, const int* __restrict__ idx,
                                     double* __restrict__ dst, long long count) {
+  pdl_enter();
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count;
        k += (long long)gridDim.x * blockDim.x)
     dst[k] = src[idx[k]];
@@ -136,16 +147,16 @@ __global__ void index_gather_kernel(const double* __restrict__ src, const int* _
 
 void launch_index_gather(const double* src, const int* idx, double* dst, long long count, cudaStream_t s) {
   if (count <= 0) return;
-  index_gather_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(src, idx, dst, count);
+  launch_k(index_gather_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, s, src, idx, dst, count);
   RSCHOL_LAUNCH_CHECK();
 }
 
 void launch_gather(const double* src, const int* perm, double* dst, int n, cudaStream_t s) {
-  gather_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(src, perm, dst, n);
+  launch_k(gather_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, s, src, perm, dst, n);
   RSCHOL_LAUNCH_CHECK();
 }
 void launch_scatter_perm(const double* src, const int* perm, double* dst, int n, cudaStream_t s) {
-  scatter_perm_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(src, perm, dst, n);
+  launch_k(scatter_perm_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, s, src, perm, dst, n);
   RSCHOL_LAUNCH_CHECK();
 }
 
@@ -180,10 +191,10 @@ void PcgEngine::set_values(const std::vector<double>& vals) {
 
 void PcgEngine::spmv(const double* x, double* y) {
   switch (tpr_) {
-    case 4: spmv_kernel<4><<<nblk_, VEC_THREADS, 0, stream_>>>(n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
-    case 8: spmv_kernel<8><<<nblk_, VEC_THREADS, 0, stream_>>>(n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
-    case 16: spmv_kernel<16><<<nblk_, VEC_THREADS, 0, stream_>>>(n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
-    default: spmv_kernel<32><<<nblk_, VEC_THREADS, 0, stream_>>>(n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
+    case 4: launch_k(spmv_kernel<4>, dim3(nblk_), dim3(VEC_THREADS), 0, stream_, n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
+    case 8: launch_k(spmv_kernel<8>, dim3(nblk_), dim3(VEC_THREADS), 0, stream_, n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
+    case 16: launch_k(spmv_kernel<16>, dim3(nblk_), dim3(VEC_THREADS), 0, stream_, n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
+    default: launch_k(spmv_kernel<32>, dim3(nblk_), dim3(VEC_THREADS), 0, stream_, n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
   }
   RSCHOL_LAUNCH_CHECK();
   ++launches;
@@ -203,12 +214,12 @@ PcgResult PcgEngine::solve(const double* b, double* x, double eps, int maxit,
   RSCHOL_CUDA(cudaMemsetAsync(sc, 0, sizeof(double) * S_COUNT, st));
   RSCHOL_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
   RSCHOL_CUDA(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-  dot_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(b, b, n, part);
-  finish_kernel<<<1, 1024, 0, st>>>(part, VEC_BLOCKS, sc, F_BNORM);
+  launch_k(dot_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, b, b, n, part);
+  launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, VEC_BLOCKS, sc, F_BNORM);
   RSCHOL_CUDA(cudaMemcpyAsync(s, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   apply(s);
-  dot_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(r, s, n, part);
-  finish_kernel<<<1, 1024, 0, st>>>(part, VEC_BLOCKS, sc, F_DELTA0);
+  launch_k(dot_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, r, s, n, part);
+  launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, VEC_BLOCKS, sc, F_DELTA0);
   RSCHOL_CUDA(cudaMemcpyAsync(d, s, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   launches += 4;
   RSCHOL_LAUNCH_CHECK();
@@ -216,14 +227,13 @@ PcgResult PcgEngine::solve(const double* b, double* x, double eps, int maxit,
   int i = 0;
   while (i < maxit && maxR > eps) {
     spmv(d, q);
-    finish_kernel<<<1, 1024, 0, st>>>(part, nblk_, sc, F_ALPHA);
-    update_xr_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(x, r, d, q, sc, n, part);
-    finish_kernel<<<1, 1024, 0, st>>>(part, VEC_BLOCKS, sc, F_RNORM);
-    RSCHOL_CUDA(cudaMemcpyAsync(s, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, nblk_, sc, F_ALPHA);
+    launch_k(update_xr_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, x, r, d, q, sc, n, part, s);
+    launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, VEC_BLOCKS, sc, F_RNORM);
     apply(s);
-    dot_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(r, s, n, part);
-    finish_kernel<<<1, 1024, 0, st>>>(part, VEC_BLOCKS, sc, F_BETA);
-    update_d_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(d, s, sc, n);
+    launch_k(dot_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, r, s, n, part);
+    launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, VEC_BLOCKS, sc, F_BETA);
+    launch_k(update_d_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, d, s, sc, n);
     RSCHOL_LAUNCH_CHECK();
     launches += 6;
     RSCHOL_CUDA(cudaMemcpyAsync(hScal_, sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
@@ -237,8 +247,8 @@ PcgResult PcgEngine::solve(const double* b, double* x, double eps, int maxit,
   res.residual = maxR;
   // true residual ||b - A x|| / ||b||
   spmv(x, q);
-  residual_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, st>>>(b, q, n, part);
-  finish_kernel<<<1, 1024, 0, st>>>(part, VEC_BLOCKS, sc, F_TRUE);
+  launch_k(residual_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, b, q, n, part);
+  launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, VEC_BLOCKS, sc, F_TRUE);
   RSCHOL_LAUNCH_CHECK();
   launches += 2;
   RSCHOL_CUDA(cudaMemcpyAsync(hScal_, sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));

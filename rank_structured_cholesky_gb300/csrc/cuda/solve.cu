@@ -118,6 +118,7 @@ __global__ void __launch_bounds__(256) interior_forward_chunks(const SNode<T>* _
                                                                int* __restrict__ sync, int epoch,
                                                                const T* __restrict__ w, T* __restrict__ yout,
                                                                T* __restrict__ wu) {
+  pdl_enter();
   extern __shared__ __align__(16) unsigned char smraw[];
   T* f = reinterpret_cast<T*>(smraw);
   __shared__ T tb[64];
@@ -193,6 +194,7 @@ __global__ void __launch_bounds__(256) interior_backward_chunks(const SNode<T>* 
                                                                 int* __restrict__ sync, int epoch,
                                                                 T* __restrict__ ipart, const T* __restrict__ yin,
                                                                 T* __restrict__ w) {
+  pdl_enter();
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ T tb[64];
   __shared__ T red[8][256];
@@ -285,6 +287,7 @@ __global__ void __launch_bounds__(256) compressed_gather_rows(const SNode<T>* __
                                                               const long long* __restrict__ cstart,
                                                               const long long* __restrict__ ent,
                                                               const T* __restrict__ wu, T* __restrict__ w) {
+  pdl_enter();
   const SNode<T>& nd = nodes[lvl[blockIdx.y]];
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -305,6 +308,7 @@ template <class T>
 __global__ void __launch_bounds__(256) compressed_ytile_kernel(const SNode<T>* __restrict__ nodes,
                                                                const XTile* __restrict__ tiles,
                                                                const T* __restrict__ w, T* __restrict__ part) {
+  pdl_enter();
   const XTile tl = tiles[blockIdx.x];
   const SNode<T>& nd = nodes[tl.node];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n = nd.n;
@@ -340,6 +344,7 @@ template <class T>
 __global__ void __launch_bounds__(256) compressed_xtile_kernel(const SNode<T>* __restrict__ nodes,
                                                                const XTile* __restrict__ tiles,
                                                                const T* __restrict__ gv, T* __restrict__ part) {
+  pdl_enter();
   __shared__ T gs[SOLVE_RB];
   const XTile tl = tiles[blockIdx.x];
   const SNode<T>& nd = nodes[tl.node];
@@ -362,6 +367,7 @@ __global__ void __launch_bounds__(256) compressed_y_kernel(const SNode<T>* __res
                                                            const RowBlock* __restrict__ work, int* __restrict__ sync,
                                                            T* __restrict__ zpart, const T* __restrict__ ypart,
                                                            T* __restrict__ yv, T* __restrict__ wu) {
+  pdl_enter();
   __shared__ T yb[SOLVE_RB];
   __shared__ T red[8][256];
   __shared__ int sLast;
@@ -399,6 +405,7 @@ template <class T>
 __global__ void __launch_bounds__(256) compressed_x_reduce(const SNode<T>* __restrict__ nodes,
                                                            const int* __restrict__ lvl, const T* __restrict__ xpart,
                                                            T* __restrict__ w) {
+  pdl_enter();
   const SNode<T>& nd = nodes[lvl[blockIdx.y]];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nd.n) return;
@@ -413,6 +420,7 @@ __global__ void __launch_bounds__(256) compressed_x_reduce(const SNode<T>* __res
 template <class T>
 __global__ void __launch_bounds__(256) compressed_vz_kernel(const SNode<T>* __restrict__ nodes,
                                                             const int* __restrict__ lvl, T* __restrict__ wu) {
+  pdl_enter();
   const SNode<T>& nd = nodes[lvl[blockIdx.y]];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int r = nd.r;
@@ -435,6 +443,7 @@ __global__ void __launch_bounds__(256) compressed_vtx_kernel(const SNode<T>* __r
                                                              const int* __restrict__ rows,
                                                              int* __restrict__ sync, T* __restrict__ spart,
                                                              const T* __restrict__ w, T* __restrict__ sv) {
+  pdl_enter();
   __shared__ T xs[128];
   __shared__ T red[8][256];
   __shared__ int sLast;
@@ -463,6 +472,7 @@ template <class T>
 __global__ void __launch_bounds__(256) compressed_g_kernel(const SNode<T>* __restrict__ nodes,
                                                            const int* __restrict__ lvl, const T* __restrict__ sv,
                                                            T* __restrict__ yv) {
+  pdl_enter();
   const SNode<T>& nd = nodes[lvl[blockIdx.y]];
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -503,6 +513,7 @@ __global__ void __launch_bounds__(64) invert_diag_blocks(const DinvTask<T>* __re
 
 template <class A, class B>
 __global__ void convert_kernel(const A* __restrict__ src, B* __restrict__ dst, int n) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = (B)src[i];
 }
@@ -910,7 +921,7 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
   T* w = std::is_same<T, double>::value ? reinterpret_cast<T*>(w64) : dW_.as<T>();
   const int n = F_.S.n;
   if (!std::is_same<T, double>::value) {
-    convert_kernel<double, T><<<(n + 255) / 256, 256, 0, st>>>(w64, w, n);
+    launch_k(convert_kernel<double, T>, dim3((n + 255) / 256), dim3(256), 0, st, w64, w, n);
     RSCHOL_LAUNCH_CHECK();
   }
   const int* lvl = dLevelNodes_.as<int>();
@@ -920,52 +931,40 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
     epoch_ = 1;
   }
   if (nIWork_ > 0) {
-    interior_forward_chunks<T><<<nIWork_, 256, smemIFmax_, st>>>(dNodes_.as<SNode<T>>(), dIWork_.as<RowBlock>(),
-                                                                  dRel_.as<int>(), dChild_.as<int>(), sync, epoch_, w,
-                                                                  dYi_.as<T>(), dWu_.as<T>());
+    launch_k(interior_forward_chunks<T>, dim3(nIWork_), dim3(256), smemIFmax_, st, dNodes_.as<SNode<T>>(), dIWork_.as<RowBlock>(), dRel_.as<int>(), dChild_.as<int>(), sync, epoch_, w, dYi_.as<T>(), dWu_.as<T>());
     RSCHOL_LAUNCH_CHECK();
   }
   T* yv = dYi_.as<T>();
   for (size_t l = 0; l < cLevels_.size(); ++l) {
     const int* lv = lvl + cLevels_[l].first;
-    compressed_gather_rows<T><<<dim3(cRowGrid_[l], cLevels_[l].second), 256, 0, st>>>(
-        dNodes_.as<SNode<T>>(), lv, dCStart_.as<long long>(), dCEnt_.as<long long>(), dWu_.as<T>(), w);
+    launch_k(compressed_gather_rows<T>, dim3(cRowGrid_[l], cLevels_[l].second), dim3(256), 0, st, dNodes_.as<SNode<T>>(), lv, dCStart_.as<long long>(), dCEnt_.as<long long>(), dWu_.as<T>(), w);
     RSCHOL_LAUNCH_CHECK();
-    compressed_ytile_kernel<T><<<cTiles_[l].second, 256, 0, st>>>(
-        dNodes_.as<SNode<T>>(), dTiles_.as<XTile>() + cTiles_[l].first, w, dXp_.as<T>());
+    launch_k(compressed_ytile_kernel<T>, dim3(cTiles_[l].second), dim3(256), 0, st, dNodes_.as<SNode<T>>(), dTiles_.as<XTile>() + cTiles_[l].first, w, dXp_.as<T>());
     RSCHOL_LAUNCH_CHECK();
-    compressed_y_kernel<T><<<cBlocks_[l], 256, 0, st>>>(dNodes_.as<SNode<T>>(), dTickF_.as<RowBlock>() + tickOff_[l],
-                                                         sync, dZp_.as<T>(), dXp_.as<T>(), yv, dWu_.as<T>());
+    launch_k(compressed_y_kernel<T>, dim3(cBlocks_[l]), dim3(256), 0, st, dNodes_.as<SNode<T>>(), dTickF_.as<RowBlock>() + tickOff_[l], sync, dZp_.as<T>(), dXp_.as<T>(), yv, dWu_.as<T>());
     RSCHOL_LAUNCH_CHECK();
     if (l + 1 < cLevels_.size()) {   // the top level's u feeds no one
-      compressed_vz_kernel<T><<<dim3(cVzGrid_[l], cLevels_[l].second), 256, 0, st>>>(dNodes_.as<SNode<T>>(), lv,
-                                                                                      dWu_.as<T>());
+      launch_k(compressed_vz_kernel<T>, dim3(cVzGrid_[l], cLevels_[l].second), dim3(256), 0, st, dNodes_.as<SNode<T>>(), lv, dWu_.as<T>());
       RSCHOL_LAUNCH_CHECK();
     }
   }
   for (int l = (int)cLevels_.size() - 1; l >= 0; --l) {
     const int* lv = lvl + cLevels_[l].first;
-    compressed_vtx_kernel<T><<<dim3(cMaxCh_[l], cLevels_[l].second), 256, 0, st>>>(
-        dNodes_.as<SNode<T>>(), lv, dRows_.as<int>(), sync, dSp_.as<T>(), w, dWu_.as<T>());
+    launch_k(compressed_vtx_kernel<T>, dim3(cMaxCh_[l], cLevels_[l].second), dim3(256), 0, st, dNodes_.as<SNode<T>>(), lv, dRows_.as<int>(), sync, dSp_.as<T>(), w, dWu_.as<T>());
     RSCHOL_LAUNCH_CHECK();
-    compressed_g_kernel<T><<<dim3(cRowGrid_[l], cLevels_[l].second), 256, 0, st>>>(dNodes_.as<SNode<T>>(), lv,
-                                                                                     dWu_.as<T>(), yv);
+    launch_k(compressed_g_kernel<T>, dim3(cRowGrid_[l], cLevels_[l].second), dim3(256), 0, st, dNodes_.as<SNode<T>>(), lv, dWu_.as<T>(), yv);
     RSCHOL_LAUNCH_CHECK();
-    compressed_xtile_kernel<T><<<cTiles_[l].second, 256, 0, st>>>(
-        dNodes_.as<SNode<T>>(), dTiles_.as<XTile>() + cTiles_[l].first, yv, dXp_.as<T>());
+    launch_k(compressed_xtile_kernel<T>, dim3(cTiles_[l].second), dim3(256), 0, st, dNodes_.as<SNode<T>>(), dTiles_.as<XTile>() + cTiles_[l].first, yv, dXp_.as<T>());
     RSCHOL_LAUNCH_CHECK();
-    compressed_x_reduce<T><<<dim3(cColGrid_[l], cLevels_[l].second), 256, 0, st>>>(dNodes_.as<SNode<T>>(), lv,
-                                                                                     dXp_.as<T>(), w);
+    launch_k(compressed_x_reduce<T>, dim3(cColGrid_[l], cLevels_[l].second), dim3(256), 0, st, dNodes_.as<SNode<T>>(), lv, dXp_.as<T>(), w);
     RSCHOL_LAUNCH_CHECK();
   }
   if (nIWork_ > 0) {
-    interior_backward_chunks<T><<<nIWork_, 256, smemIBmax_, st>>>(dNodes_.as<SNode<T>>(), dIWorkB_.as<RowBlock>(),
-                                                                   dRows_.as<int>(), sync, epoch_, dIp_.as<T>(),
-                                                                   dYi_.as<T>(), w);
+    launch_k(interior_backward_chunks<T>, dim3(nIWork_), dim3(256), smemIBmax_, st, dNodes_.as<SNode<T>>(), dIWorkB_.as<RowBlock>(), dRows_.as<int>(), sync, epoch_, dIp_.as<T>(), dYi_.as<T>(), w);
     RSCHOL_LAUNCH_CHECK();
   }
   if (!std::is_same<T, double>::value) {
-    convert_kernel<T, double><<<(n + 255) / 256, 256, 0, st>>>(w, w64, n);
+    launch_k(convert_kernel<T, double>, dim3((n + 255) / 256), dim3(256), 0, st, w, w64, n);
     RSCHOL_LAUNCH_CHECK();
   }
 }
