@@ -65,6 +65,9 @@ void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
   // bound by C traffic, which the SIMT kernel already streams); large-K tasks
   // of steps with few tiles are split along K (slices of at least 128) to
   // fill the SMs.
+  // (rank-64 updates on the tensor cores measured slower than the SIMT kernel
+  // even with both operands on the asynchronous-copy path: 24.8 vs 17.0 ms of
+  // GEMM time in the c2 factor)
   int maxK = 0;
   for (auto& t : batch) maxK = std::max(maxK, t.K);
   const bool tc = useTc_ && maxK >= 128;
@@ -373,23 +376,26 @@ void FactorEngine<T>::plan() {
     L[hh].push_back(s);
   }
 
-  // ---- arenas
+  // ---- arenas.  Leading dimensions are padded to a multiple of 4, so every
+  // front row and every 64-column panel starts on a 16-byte boundary (the
+  // tensor-core GEMM's asynchronous copies move 16-byte chunks).
+  auto pad4 = [](int x) { return (x + 3) & ~3; };
   frontOff.assign(nn, 0);
   ld.assign(nn, 0);
   long long curI = 0, curC = 0;
   for (auto& lv : interiorLevels)
     for (int d : lv) {
       const Node& nd = S.nodes[d];
-      ld[d] = nd.n + nd.m();
+      ld[d] = pad4(nd.n + nd.m());
       frontOff[d] = curI;
       curI += (long long)ld[d] * ld[d];
     }
   for (auto& lv : compressedLevels)
     for (int j : lv) {
       const Node& nd = S.nodes[j];
-      ld[j] = nd.n;
+      ld[j] = pad4(nd.n);
       frontOff[j] = curC;
-      curC += (long long)(nd.n + nd.m()) * nd.n;
+      curC += (long long)(nd.n + nd.m()) * ld[j];
     }
   rank.assign(nn, 0);
   vOff.assign(nn, -1);
@@ -528,7 +534,7 @@ void FactorEngine<T>::plan() {
       EaTarget t;
       t.F = I0 + frontOff[p];
       t.ld = ld[p];
-      t.rows = ld[p];
+      t.rows = pn.n + pn.m();
       for (int a = 0; a < pn.m(); ++a) pos[pn.rows[a]] = a;
       for (int c : S.children[p]) {
         const Node& cn = S.nodes[c];
@@ -555,7 +561,8 @@ void FactorEngine<T>::plan() {
     std::vector<CholJob<T>> jobs;
     for (int d : lv) {
       const Node& nd = S.nodes[d];
-      jobs.push_back(CholJob<T>{I0 + frontOff[d], ld[d], nd.n, ld[d], ld[d], d + 1});
+      const int nm = nd.n + nd.m();
+      jobs.push_back(CholJob<T>{I0 + frontOff[d], ld[d], nd.n, nm, nm, d + 1});
     }
     emit_chol(jobs);
   }

@@ -62,6 +62,16 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
   return r;
 }
 
+// 16-byte asynchronous copy global -> shared; bytes < 16 zero-fills the rest
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 __device__ __forceinline__ void mbar_init(uint32_t addr, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
 }
@@ -196,8 +206,104 @@ __global__ void __launch_bounds__(TC_THREADS) gemm_tc_kernel(const GemmTask<floa
         *reinterpret_cast<uint32_t*>(base + 2 * TC_A_BYTES + TC_B_BYTES + off) = to_tf32(rb[q] - __uint_as_float(h));
     }
   };
+  // MMAs of one staged K tile (issued by thread 0), then a commit to the
+  // stage's barrier
+  auto mma_stage = [&](int st, int kt) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+    for (int kk = 0; kk < TC_BK / 8; ++kk) {
+      const uint32_t step = (uint32_t)kk * 32u;   // 8 TF32 = 32 bytes along the swizzled row
+      const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+      tc_mma(tmem, tc_smem_desc(aHi(st) + step), tc_smem_desc(bHi(st) + step), acc);
+      if (split) {
+        tc_mma(tmem, tc_smem_desc(aHi(st) + step), tc_smem_desc(bLo(st) + step), 1u);
+        tc_mma(tmem, tc_smem_desc(aLo(st) + step), tc_smem_desc(bHi(st) + step), 1u);
+      }
+    }
+    tc_commit(mb0 + 8u * st);
+  };
+  // Async path: A row-major (K contiguous) and B stored N x K, both 16-byte
+  // aligned with leading dimensions that keep every 4-float chunk aligned.
+  // The tiles arrive by 16-byte cp.async straight into the swizzled layout
+  // (the 128-byte swizzle permutes whole 16-byte chunks), the next tile in
+  // flight while the current one is converted and multiplied; the TF32
+  // rounding (and the split's low parts) is a linear pass over the stage.
+  const bool fast = !t.tA && t.tB &&
+                    ((reinterpret_cast<uintptr_t>(t.A) | reinterpret_cast<uintptr_t>(t.B)) & 15u) == 0 &&
+                    (t.lda & 3) == 0 && (t.ldb & 3) == 0;
+  auto issue_async = [&](int k0, int st) {
+    const uint32_t a0 = aHi(st), b0 = bHi(st);
+    for (int c = tid; c < TC_BM * (TC_BK / 4); c += TC_THREADS) {
+      const int r = c >> 3, ch = c & 7;
+      const int gm = row0 + r, gk = k0 + 4 * ch;
+      const int valid = gm < t.M ? max(0, min(4, kEnd - gk)) : 0;
+      const float* src = valid > 0 ? t.A + (size_t)gm * t.lda + gk : t.A;
+      cp_async16(a0 + tc_off(r, 4 * ch), src, 4 * valid);
+    }
+    for (int c = tid; c < TC_BN * (TC_BK / 4); c += TC_THREADS) {
+      const int r = c >> 3, ch = c & 7;
+      const int gn = col0 + r, gk = k0 + 4 * ch;
+      const int valid = gn < t.N ? max(0, min(4, kEnd - gk)) : 0;
+      const float* src = valid > 0 ? t.B + (size_t)gn * t.ldb + gk : t.B;
+      cp_async16(b0 + tc_off(r, 4 * ch), src, 4 * valid);
+    }
+    cp_async_commit();
+  };
+  auto convert_stage = [&](int st) {
+    unsigned char* base = tc_smem + (sbase - sraw) + (size_t)st * TC_STAGE_BYTES;
+    auto conv = [&](unsigned char* hiB, unsigned char* loB, int words) {
+      for (int w = tid; w < words / 4; w += TC_THREADS) {
+        float4* hp = reinterpret_cast<float4*>(hiB) + w;
+        const float4 v = *hp;
+        float4 h, l;
+        h.x = __uint_as_float(to_tf32(v.x));
+        h.y = __uint_as_float(to_tf32(v.y));
+        h.z = __uint_as_float(to_tf32(v.z));
+        h.w = __uint_as_float(to_tf32(v.w));
+        *hp = h;
+        if (split) {
+          l.x = __uint_as_float(to_tf32(v.x - h.x));
+          l.y = __uint_as_float(to_tf32(v.y - h.y));
+          l.z = __uint_as_float(to_tf32(v.z - h.z));
+          l.w = __uint_as_float(to_tf32(v.w - h.w));
+          *(reinterpret_cast<float4*>(loB) + w) = l;
+        }
+      }
+    };
+    conv(base, base + TC_A_BYTES, TC_BM * TC_BK);
+    conv(base + 2 * TC_A_BYTES, base + 2 * TC_A_BYTES + TC_B_BYTES, TC_BN * TC_BK);
+  };
   uint32_t parity[TC_STAGES] = {0u, 0u};
   int issued = 0;   // k tiles whose MMAs were committed
+  if (fast) {
+    if (nk > 0) issue_async(kBeg, 0);
+    for (int kt = 0; kt < nk; ++kt) {
+      const int st = kt & 1;
+      if (kt + 1 < nk) {
+        if (kt >= 1) {   // stage st ^ 1 held tile kt - 1: its MMAs must be done before it is refilled
+          if (tid == 0 && !mbar_wait(mb0 + 8u * (st ^ 1), parity[st ^ 1])) {
+            atomicExch(err, 1);
+            sAbort = 1;
+          }
+          parity[st ^ 1] ^= 1u;
+        }
+        __syncthreads();
+        if (sAbort) break;
+        issue_async(kBeg + (kt + 1) * TC_BK, st ^ 1);
+        cp_async_wait<1>();   // tile kt has landed (kt + 1 may still be in flight)
+      } else {
+        cp_async_wait<0>();
+      }
+      __syncthreads();
+      convert_stage(st);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) mma_stage(st, kt);
+      issued = kt + 1;
+    }
+    cp_async_wait<0>();   // nothing of this CTA stays in flight
+  }
+  if (!fast) {
   if (nk > 0) load_tiles(kBeg);
   for (int kt = 0; kt < nk; ++kt) {
     const int st = kt & 1;
@@ -213,22 +319,10 @@ __global__ void __launch_bounds__(TC_THREADS) gemm_tc_kernel(const GemmTask<floa
     store_tiles(st);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-      for (int kk = 0; kk < TC_BK / 8; ++kk) {
-        const uint32_t step = (uint32_t)kk * 32u;   // 8 TF32 = 32 bytes along the swizzled row
-        const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
-        tc_mma(tmem, tc_smem_desc(aHi(st) + step), tc_smem_desc(bHi(st) + step), acc);
-        if (split) {
-          tc_mma(tmem, tc_smem_desc(aHi(st) + step), tc_smem_desc(bLo(st) + step), 1u);
-          tc_mma(tmem, tc_smem_desc(aLo(st) + step), tc_smem_desc(bHi(st) + step), 1u);
-        }
-      }
-      tc_commit(mb0 + 8u * st);
-    }
+    if (tid == 0) mma_stage(st, kt);
     issued = kt + 1;
     if (kt + 1 < nk) load_tiles(kBeg + (kt + 1) * TC_BK);
+  }
   }
   // The last commit completes after every earlier MMA of this thread.
   if (tid == 0 && issued > 0) {

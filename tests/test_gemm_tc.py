@@ -17,8 +17,10 @@ pytestmark = pytest.mark.gpu
 SHAPES = [
     (128, 64, 32, 0, 0), (100, 50, 7, 0, 1), (300, 130, 257, 1, 0), (257, 200, 96, 1, 1),
     (64, 300, 1000, 0, 0), (1000, 64, 64, 0, 1), (5, 3, 1, 0, 0),
+    # A plain and B transposed with K a multiple of 4: the cp.async path (ragged M, N and K tails)
+    (200, 130, 96, 0, 1), (130, 70, 36, 0, 1), (64, 64, 44, 0, 1), (257, 129, 500, 0, 1),
     # K >= 1024: four K slices summed by the split-K reduction
-    (300, 104, 2048, 1, 0), (129, 65, 3001, 0, 1),
+    (300, 104, 2048, 1, 0), (129, 65, 3001, 0, 1), (129, 65, 3000, 0, 1),
 ]
 
 
