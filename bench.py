@@ -354,6 +354,16 @@ def run_ours(args):
                  "p50_ms": statistics.median(pf["step_ms"]), "p99_ms": float(np.percentile(pf["step_ms"], 99)),
                  "iterations": pf["iterations"] if nrhs > 1 else pf["iterations"][0],
                  "true_residual": pf["true_residual"], "clocks": pf["clocks"]}
+        # the mixed results against the FP64 path (which matches the FP64 oracle to 1e-7 per apply):
+        # one preconditioner application and the PCG solution, same right-hand side
+        b0 = np.ascontiguousarray(prob.rhs[0])
+        z_mixed, z_fp64 = F.apply(b0), pf["F"].apply(b0)
+        x_mixed, _ = F.pcg(b0, eps=1e-8)
+        x_fp64, _ = pf["F"].pcg(b0, eps=1e-8)
+        plain["mixed_vs_fp64"] = {
+            "apply_rel_error": float(np.linalg.norm(z_mixed - z_fp64) / np.linalg.norm(z_fp64)),
+            "solution_rel_error": float(np.linalg.norm(x_mixed - x_fp64) / np.linalg.norm(x_fp64)),
+            "note": "relative 2-norm differences on rhs[0]; both solves stop at ||r||/||b|| <= 1e-8"}
         del pf
 
     hbm, bf16, src = peaks()
@@ -451,7 +461,7 @@ def serving_pool(ids):
     return probs, rhs
 
 
-def serve_stream(rs, precision, device, probs, rhs, stream, workers, budget, eps=1e-8):
+def serve_stream(rs, precision, device, probs, rhs, stream, workers, budget, eps=1e-8, keep=0):
     """Submit the stream in real time, collect every result; returns the measurements."""
     arrivals, mids, nrhs, offs = stream
     srv = rs.Server(workers=workers, hbm_budget_bytes=budget, precision=precision, device=device)
@@ -485,7 +495,8 @@ def serve_stream(rs, precision, device, probs, rhs, stream, workers, budget, eps
     true_res = max(max(q["true_residual"] for q in r[2]) for r in results)
     hits = [r[3]["cache_hit"] for r in results]
     lat_hit = lat[np.array(hits, bool)] if any(hits) else lat
-    return {"value": len(arrivals) / wall, "rhs_per_s": float(np.sum(nrhs)) / wall, "wall_s": wall,
+    kept = [results[i][1] for i in range(min(keep, len(results)))]   # solutions of the first requests
+    return {"value": len(arrivals) / wall, "rhs_per_s": float(np.sum(nrhs)) / wall, "wall_s": wall, "_kept": kept,
             "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
             "p50_ms_cache_hits": 1e3 * float(np.percentile(lat_hit, 50)),
             "p99_ms_cache_hits": 1e3 * float(np.percentile(lat_hit, 99)),
@@ -536,10 +547,17 @@ def run_serving(args):
     wprobs, wrhs = serving_pool([0, 6])
     serve_stream(rs, prec, local, wprobs, wrhs, warm, args.workers, budget)
     with ClockSampler(local) as clocks:
-        main = serve_stream(rs, prec, local, probs, rhs, stream, args.workers, budget)
+        main = serve_stream(rs, prec, local, probs, rhs, stream, args.workers, budget, keep=50)
     plain = None
     if args.precision == "mixed" and not args.no_fp64_plain:
-        plain = serve_stream(rs, 0, local, probs, rhs, stream, args.workers, budget)
+        plain = serve_stream(rs, 0, local, probs, rhs, stream, args.workers, budget, keep=50)
+        # the mixed results against the FP64 path, request by request (first 50 requests)
+        errs = [np.linalg.norm(a - b) / np.linalg.norm(b) for a, b in zip(main["_kept"], plain["_kept"])]
+        main["solution_rel_error_vs_fp64"] = {"max": float(max(errs)), "median": float(np.median(errs)),
+                                              "requests": len(errs)}
+    for d in (main, plain):
+        if d:
+            d.pop("_kept", None)
     hbm, bf16, src = peaks()
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and world == 1:
