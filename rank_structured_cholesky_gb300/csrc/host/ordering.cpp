@@ -50,17 +50,13 @@ bool geometric_split(NDState& S, const std::vector<int>& set, std::vector<int>& 
   for (int d = 0; d < 3; ++d)
     if (hi[d] - lo[d] > best) { best = hi[d] - lo[d]; axis = d; }
   if (!(best > 0.0)) return false;
-  std::vector<double> vals;
-  vals.reserve(set.size());
-  for (int v : set) vals.push_back(S.xyz[3 * (size_t)v + axis]);
-  std::sort(vals.begin(), vals.end());
-  vals.erase(std::unique(vals.begin(), vals.end()), vals.end());
-  // Choose the plane that best balances the two sides.
+  // The plane through the median coordinate (the element a full sort would
+  // put at size / 2) balances the two sides.
   std::vector<double> all;
   all.reserve(set.size());
   for (int v : set) all.push_back(S.xyz[3 * (size_t)v + axis]);
-  std::sort(all.begin(), all.end());
-  double target = all[all.size() / 2];
+  std::nth_element(all.begin(), all.begin() + all.size() / 2, all.end());
+  const double target = all[all.size() / 2];
   for (int v : set) {
     double c = S.xyz[3 * (size_t)v + axis];
     if (c < target) L.push_back(v);
