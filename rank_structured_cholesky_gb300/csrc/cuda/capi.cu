@@ -95,7 +95,7 @@ struct ImplT : Impl {
   int apply_batch_error(cudaStream_t s) override { return se.take_error_batch(s); }
   void step_timing(bool on, double* out) override {
     if (out)
-      for (int k = 0; k < 7; ++k) {
+      for (int k = 0; k < 8; ++k) {
         out[3 * k] = fe.stepMs[k];
         out[3 * k + 1] = fe.stepCount[k];
         out[3 * k + 2] = fe.stepFlops[k];

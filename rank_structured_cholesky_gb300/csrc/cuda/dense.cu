@@ -7,33 +7,24 @@
 
 #include "common.cuh"
 #include "dense.cuh"
+#include "solve_dev.cuh"
 
 namespace rschol {
 
 namespace {
 
+using solvedev::st_release;
+using solvedev::wait_geq;
+
 constexpr int BM = 64, BN = 64, BK = 16, GEMM_THREADS = 256;
 
+// One 64 x 64 tile of C = alpha op(A) op(B) + beta C at (row0, col0), by
+// the 256 threads of the block.  Two shared stages: the next K slice is
+// loaded into registers while the current one is multiplied (one barrier per
+// slice); C is fetched before the K loop.  Each C entry's K order is the
+// plain ascending one.
 template <class T>
-__global__ void __launch_bounds__(GEMM_THREADS) gemm_kernel(const GemmTask<T>* __restrict__ tasks, int nTasks) {
-  int lo = 0, hi = nTasks - 1;
-  const int b = blockIdx.x;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (tasks[mid].tileBase <= b) lo = mid;
-    else hi = mid - 1;
-  }
-  const GemmTask<T> t = tasks[lo];
-  const int local = b - t.tileBase;
-  const int ti = local / t.tilesN, tj = local - ti * t.tilesN;
-  const int row0 = ti * BM, col0 = tj * BN;
-  if (t.lower && row0 + BM - 1 < col0) return;
-
-  // Two shared stages: the next K slice is loaded into registers while the
-  // current one is multiplied (one barrier per slice); C is fetched before
-  // the K loop.  Each C entry's K order is the plain ascending one.
-  __shared__ T As[2][BK][BM + 1];
-  __shared__ T Bs[2][BK][BN + 1];
+__device__ void gemm_tile(const GemmTask<T>& t, int row0, int col0, T (*As)[BK][BM + 1], T (*Bs)[BK][BN + 1]) {
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   T acc[4][4];
 #pragma unroll
@@ -47,7 +38,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_kernel(const GemmTask<T>* _
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int gi = row0 + ty + 16 * i, gj = col0 + tx + 16 * j;
-        cpre[i][j] = (gi < t.M && gj < t.N) ? t.C[(size_t)gi * t.ldc + gj] : T(0);
+        cpre[i][j] = (gi < t.M && gj < t.N) ? __ldcg(t.C + (size_t)gi * t.ldc + gj) : T(0);
       }
   }
   T ra[4], rb[4];
@@ -58,7 +49,8 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_kernel(const GemmTask<T>* _
       if (!t.tA) { i = (tid >> 4) + 16 * q; k = tid & 15; }
       else { i = tid & 63; k = (tid >> 6) + 4 * q; }
       const int gi = row0 + i, gk = k0 + k;
-      ra[q] = (gi < t.M && gk < t.K) ? (t.tA ? t.A[(size_t)gk * t.lda + gi] : t.A[(size_t)gi * t.lda + gk]) : T(0);
+      ra[q] = (gi < t.M && gk < t.K) ? __ldcg(t.tA ? t.A + (size_t)gk * t.lda + gi : t.A + (size_t)gi * t.lda + gk)
+                                       : T(0);
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -66,7 +58,8 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_kernel(const GemmTask<T>* _
       if (!t.tB) { j = tid & 63; k = (tid >> 6) + 4 * q; }
       else { j = (tid >> 4) + 16 * q; k = tid & 15; }
       const int gj = col0 + j, gk = k0 + k;
-      rb[q] = (gj < t.N && gk < t.K) ? (t.tB ? t.B[(size_t)gj * t.ldb + gk] : t.B[(size_t)gk * t.ldb + gj]) : T(0);
+      rb[q] = (gj < t.N && gk < t.K) ? __ldcg(t.tB ? t.B + (size_t)gj * t.ldb + gk : t.B + (size_t)gk * t.ldb + gj)
+                                       : T(0);
     }
   };
   auto store = [&](int st) {
@@ -124,6 +117,25 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_kernel(const GemmTask<T>* _
       *c = v;
     }
   }
+}
+
+template <class T>
+__global__ void __launch_bounds__(GEMM_THREADS) gemm_kernel(const GemmTask<T>* __restrict__ tasks, int nTasks) {
+  int lo = 0, hi = nTasks - 1;
+  const int b = blockIdx.x;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (tasks[mid].tileBase <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  const GemmTask<T> t = tasks[lo];
+  const int local = b - t.tileBase;
+  const int ti = local / t.tilesN, tj = local - ti * t.tilesN;
+  const int row0 = ti * BM, col0 = tj * BN;
+  if (t.lower && row0 + BM - 1 < col0) return;
+  __shared__ T As[2][BK][BM + 1];
+  __shared__ T Bs[2][BK][BN + 1];
+  gemm_tile<T>(t, row0, col0, As, Bs);
 }
 
 template <class T>
@@ -245,78 +257,217 @@ __global__ void __launch_bounds__(256) trsm_kernel(const TrsmTask<T>* __restrict
 // FP32 variants: a register-resident POTRF (thread (i, g) keeps row i,
 // columns g, g + 4, ... of the tile) and a TRSM that inverts the tile in
 // every block and multiplies; they beat the panel-blocked kernels above in
-// FP32, while FP64 prefers the blocked ones.
+// FP32, while FP64 prefers the blocked ones.  The tile bodies are device
+// functions shared with the fused level kernel below.
+
+// Right-looking Cholesky of one n x n (n <= 64) tile at A (row-major, ld) by
+// the block's 256 threads as a 16 x 16 grid: thread (ti, tk) keeps the 4 x 4
+// entries (ti + 16 a, tk + 16 b) in registers.  Column j is published
+// unscaled (u_i = a_ij for i > j, zeros at rows <= j; the pivot p = a_jj
+// apart) through a double-buffered shared vector laid out by (i % 16, i / 16),
+// so one barrier per column suffices and a thread reads its four row values
+// and its four column values as two 16-byte loads; every thread then runs
+// the same 16 unpredicated FMAs a_ik -= (u_i / p) u_k (the zeros leave
+// finished entries unchanged; entries right of the diagonal are never
+// stored).  Finally L_jj = sqrt(p_j), L_ij = a_ij / sqrt(p_j).  A
+// non-positive pivot is replaced by 1 and reported as atomicMin(flag, code).
+// 1 / p on a POTRF's critical path: the fast reciprocal (MUFU-based,
+// __fdividef, within 2 ulp) in FP32, whose factor carries larger rounding
+// errors anyway; exact division in FP64.
+__device__ __forceinline__ float pivot_recip(float p) { return __fdividef(1.0f, p); }
+__device__ __forceinline__ double pivot_recip(double p) { return 1.0 / p; }
+
 template <class T>
-__global__ void __launch_bounds__(256) potrf_reg_kernel(const PotrfTask<T>* __restrict__ tasks, int* flag) {
-  // Right-looking Cholesky of one <= 64 x 64 tile.  Thread (i = tid / 4,
-  // g = tid % 4) keeps row i, columns g, g + 4, ..., in registers.  Column j
-  // is published unscaled (u, pivot p = u_j) through a double-buffered shared
-  // array, so one barrier per column suffices: the trailing update is
-  // a_ik -= u_i u_k / p, and the stored columns are scaled by 1 / sqrt(p) at
-  // the end (L_jj = sqrt(p)).
-  const PotrfTask<T> t = tasks[blockIdx.x];
-  __shared__ T col[2][64];
+__device__ void potrf_tile_reg(T* A, int ld, int n, int code, int* flag) {
+  __shared__ __align__(16) T col[2][64];
   __shared__ T piv[64];
   __shared__ int bad;
-  const int n = t.n, tid = threadIdx.x, i = tid >> 2, g = tid & 3;
-  T v[16];
+  const int tid = threadIdx.x, ti = tid >> 4, tk = tid & 15;
+  T v[4][4];
 #pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const int k = g + 4 * q;
-    v[q] = (i < n && k <= i) ? t.A[(size_t)i * t.ld + k] : T(0);
-  }
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int i = ti + 16 * a, k = tk + 16 * b;
+      v[a][b] = (i < n && k <= i) ? __ldcg(A + (size_t)i * ld + k) : T(0);
+    }
   if (tid == 0) bad = 0;
   __syncthreads();
-  // column j = 4 q0 + jj lives in slot q0 of the threads with g == jj
-  // (both loops unrolled so that every register index is static)
 #pragma unroll
-  for (int q0 = 0; q0 < 16; ++q0) {
+  for (int b0 = 0; b0 < 4; ++b0) {
+#pragma unroll 1
+    for (int jj = 0; jj < 16; ++jj) {
+      const int j = 16 * b0 + jj;
+      if (j >= n) break;
+      T* cj = col[j & 1];
+      if (tk == jj) {   // the owners of column j: rows ti + 16 a
+        T u[4];
 #pragma unroll
-    for (int jj = 0; jj < 4; ++jj) {
-      const int j = 4 * q0 + jj;
-      if (j < n) {
-        T* cj = col[j & 1];
-        if (g == jj && i >= j && i < n) {
-          T u = v[q0];
+        for (int a = 0; a < 4; ++a) {
+          const int i = ti + 16 * a;
+          u[a] = v[a][b0];
           if (i == j) {
-            if (!(u > T(0))) {   // not positive definite (or NaN): keep going, report
+            T p = u[a];
+            if (!(p > T(0))) {   // not positive definite (or NaN): keep going, report
               bad = 1;
-              u = T(1);
-              v[q0] = u;
+              p = T(1);
             }
-            piv[j] = u;
+            piv[j] = p;
           }
-          cj[i] = u;
+          if (i <= j) u[a] = T(0);
         }
-        __syncthreads();
-        if (i > j && i < n) {
-          const T ui = cj[i] / cj[j];
 #pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const int k = g + 4 * q;
-            if (k > j && k <= i) v[q] -= ui * cj[k];
-          }
-        }
+        for (int a = 0; a < 4; ++a) cj[4 * ti + a] = u[a];
       }
+      __syncthreads();
+      const T rp = pivot_recip(piv[j]);
+      T ur[4], uc[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        ur[a] = cj[4 * ti + a] * rp;
+        uc[a] = cj[4 * tk + a];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) v[a][b] -= ur[a] * uc[b];
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const int k = g + 4 * q;
-    if (i < n && k <= i) {
-      const T d = sqrt(piv[k]);
-      t.A[(size_t)i * t.ld + k] = (k == i) ? d : v[q] / d;
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int i = ti + 16 * a, k = tk + 16 * b;
+      if (i < n && k <= i) {
+        const T d = sqrt(piv[k]);
+        A[(size_t)i * ld + k] = (k == i) ? d : v[a][b] / d;
+      }
+    }
+  if (tid == 0 && bad) atomicMin(flag, code);
+  __syncthreads();
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) potrf_reg_kernel(const PotrfTask<T>* __restrict__ tasks, int* flag) {
+  const PotrfTask<T> t = tasks[blockIdx.x];
+  potrf_tile_reg<T>(t.A, t.ld, t.n, t.code, flag);
+}
+
+// Li := L^{-1}, L the w x w lower tile at Lg (ld ldl) padded to 64 with a
+// unit diagonal (so the leading w x w block of Li is the inverse; only the
+// 16 x 16 blocks that cover it are formed).  Blocked: the 16 x 16 diagonal
+// inverses by forward substitution (warp b inverts block b, lane c keeps
+// column c in registers, the diagonal reciprocals formed up front), then the
+// off-diagonal blocks by distance from the diagonal,
+// Li[R][C] = -Li[R][R] sum_{K=C}^{R-1} L[R][K] Li[K][C], with unrolled
+// fixed-length inner products.  L, Li: 64 x 65 shared; Tm: 3 x 16 x 17
+// shared.  256 threads.
+template <class T>
+__device__ void tile_inverse(const T* Lg, int ldl, int w, T (*L)[65], T (*Li)[65], T (*Tm)[16][17]) {
+  const int tid = threadIdx.x;
+  // tile loads unrolled: all 16 loads of a thread in flight at once
+#pragma unroll
+  for (int idx = tid; idx < 64 * 64; idx += 256) {
+    const int i = idx >> 6, j = idx & 63;
+    L[i][j] = (i < w && j <= i) ? __ldcg(Lg + (size_t)i * ldl + j) : (i == j ? T(1) : T(0));
+    Li[i][j] = T(0);
+  }
+  __syncthreads();
+  const int nb = (w + 15) >> 4;   // 16 x 16 blocks that cover the w x w inverse
+  {
+    const int wb = tid >> 5, c = tid & 15;
+    if (wb < nb && (tid & 31) < 16) {
+      const int o = 16 * wb;
+      T d[16], x[16];
+#pragma unroll
+      for (int r = 0; r < 16; ++r) d[r] = T(1) / L[o + r][o + r];
+      // x = column c of the block inverse: x_r = (delta_rc - sum_{k<r} L_rk x_k) / L_rr;
+      // rows above c come out zero by themselves
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        T s = (r == c) ? T(1) : T(0);
+#pragma unroll
+        for (int k = 0; k < r; ++k) s -= L[o + r][o + k] * x[k];
+        x[r] = s * d[r];
+      }
+#pragma unroll
+      for (int r = 0; r < 16; ++r) Li[o + r][o + c] = x[r];
     }
   }
-  if (tid == 0 && bad) atomicMin(flag, t.code);
+  __syncthreads();
+#pragma unroll
+  for (int d = 1; d < 4; ++d) {
+    if (d >= nb) break;
+    const int np = nb - d;   // block pairs (R, C = R - d)
+    for (int e = tid; e < np * 256; e += 256) {
+      const int pr = e >> 8, i = (e >> 4) & 15, j = e & 15;
+      const int C = pr, R = pr + d;
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k < 16 * d; ++k) s += L[16 * R + i][16 * C + k] * Li[16 * C + k][16 * C + j];
+      Tm[pr][i][j] = s;
+    }
+    __syncthreads();
+    for (int e = tid; e < np * 256; e += 256) {
+      const int pr = e >> 8, i = (e >> 4) & 15, j = e & 15;
+      const int C = pr, R = pr + d;
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) s += Li[16 * R + i][16 * R + k] * Tm[pr][k][j];   // Li[R][R] is lower
+      Li[16 * R + i][16 * C + j] = -s;
+    }
+    __syncthreads();
+  }
+}
+
+// B (nr <= 64 rows x w) := B Li^T with Li = L^{-1} (64 x 65 shared, zero
+// above the diagonal); X: 64 x 65 shared staging.  256 threads.
+template <class T>
+__device__ void trsm_chunk_mul(T* B, int ldb, int nr, int w, T (*X)[65], T (*Li)[65]) {
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int idx = tid; idx < 64 * 64; idx += 256) {
+    const int i = idx >> 6, j = idx & 63;
+    X[i][j] = (i < nr && j < w) ? __ldcg(B + (size_t)i * ldb + j) : T(0);
+  }
+  __syncthreads();
+  // out[i][j] = sum_{k <= j} X[i][k] Li[j][k]; thread: rows ty + 16 a, columns tx + 16 c
+  const int tx = tid & 15, ty = tid >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[a][c] = T(0);
+#pragma unroll 4
+  for (int k = 0; k < w; ++k) {
+    T xa[4], lb[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) xa[a] = X[ty + 16 * a][k];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) lb[c] = Li[tx + 16 * c][k];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[a][c] = fma(xa[a], lb[c], acc[a][c]);
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int i = ty + 16 * a;
+    if (i >= nr) continue;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int j = tx + 16 * c;
+      if (j < w) B[(size_t)i * ldb + j] = acc[a][c];
+    }
+  }
+  __syncthreads();
 }
 
 template <class T>
 __global__ void __launch_bounds__(256) trsm_inv_kernel(const TrsmTask<T>* __restrict__ tasks, int nTasks) {
-  // B (64-row chunk x w) := B L^{-T}: the block inverts its w x w tile
-  // (blocked: 16 x 16 diagonal inverses, then the off-diagonal blocks by
-  // distance from the diagonal) and multiplies.
+  // B (64-row chunk x w) := B L^{-T}: the block inverts its w x w tile and
+  // multiplies.
   int lo = 0, hi = nTasks - 1;
   const int b = blockIdx.x;
   while (lo < hi) {
@@ -325,93 +476,149 @@ __global__ void __launch_bounds__(256) trsm_inv_kernel(const TrsmTask<T>* __rest
     else hi = mid - 1;
   }
   const TrsmTask<T> t = tasks[lo];
-  const int rb0 = (b - t.chunkBase) * TRSM_ROWS_F32;   // this block's rows: 4 chunks of 64 share the inverse
-  const int w = t.w, tid = threadIdx.x;
+  const int rb0 = (b - t.chunkBase) * TRSM_ROWS_F32;
   extern __shared__ __align__(16) unsigned char trsm_smem[];
   T (*L)[65] = reinterpret_cast<T (*)[65]>(trsm_smem);
   T (*Li)[65] = reinterpret_cast<T (*)[65]>(trsm_smem + sizeof(T) * 64 * 65);
   T (*X)[65] = reinterpret_cast<T (*)[65]>(trsm_smem + 2 * sizeof(T) * 64 * 65);
   T (*Tm)[16][17] = reinterpret_cast<T (*)[16][17]>(trsm_smem + 3 * sizeof(T) * 64 * 65);   // 3 blocks
-  for (int idx = tid; idx < 64 * 64; idx += blockDim.x) {
-    const int i = idx >> 6, j = idx & 63;
-    // padded to 64 with a unit diagonal: the leading w x w block of the
-    // inverse is L^{-1}
-    L[i][j] = (i < w && j <= i) ? t.L[(size_t)i * t.ldl + j] : (i == j ? T(1) : T(0));
-    Li[i][j] = T(0);
-  }
-  __syncthreads();
-  // Li = L^{-1} in 16 x 16 blocks.  Diagonal blocks: warp b inverts block b
-  // by forward substitution, lane c owning column c of the block.
-  {
-    const int wb = tid >> 5, c = tid & 31;
-    if (wb < 4 && c < 16) {
-      const int o = 16 * wb;
-      for (int r = c; r < 16; ++r) {
-        T s = (r == c) ? T(1) : T(0);
-        for (int k = c; k < r; ++k) s -= L[o + r][o + k] * Li[o + k][o + c];
-        Li[o + r][o + c] = s / L[o + r][o + r];
-      }
-    }
-  }
-  __syncthreads();
-  // Off-diagonal blocks by distance d = R - C: Li[R][C] = -Li[R][R] sum_{K=C}^{R-1} L[R][K] Li[K][C]
-  for (int d = 1; d < 4; ++d) {
-    const int np = 4 - d;   // block pairs (R, C = R - d)
-    for (int e = tid; e < np * 256; e += blockDim.x) {
-      const int pr = e >> 8, i = (e >> 4) & 15, j = e & 15;
-      const int C = pr, R = pr + d;
-      T s = T(0);
-      for (int k = 16 * C; k < 16 * R; ++k) s += L[16 * R + i][k] * Li[k][16 * C + j];
-      Tm[pr][i][j] = s;
-    }
-    __syncthreads();
-    for (int e = tid; e < np * 256; e += blockDim.x) {
-      const int pr = e >> 8, i = (e >> 4) & 15, j = e & 15;
-      const int C = pr, R = pr + d;
-      T s = T(0);
-      for (int k = 0; k <= i; ++k) s += Li[16 * R + i][16 * R + k] * Tm[pr][k][j];
-      Li[16 * R + i][16 * C + j] = -s;
-    }
-    __syncthreads();
-  }
+  tile_inverse<T>(t.L, t.ldl, t.w, L, Li, Tm);
   for (int sub = 0; sub < TRSM_ROWS_F32 / 64; ++sub) {
     const int r0 = rb0 + 64 * sub;
     if (r0 >= t.rows) break;
-    const int nr = min(64, t.rows - r0);
-    for (int idx = tid; idx < 64 * 64; idx += blockDim.x) {
-      const int i = idx >> 6, j = idx & 63;
-      X[i][j] = (i < nr && j < w) ? t.B[(size_t)(r0 + i) * t.ldb + j] : T(0);
+    trsm_chunk_mul<T>(t.B + (size_t)r0 * t.ldb, t.ldb, min(64, t.rows - r0), t.w, X, Li);
+  }
+}
+
+// Blocked partial Cholesky of every front of a level in one launch.  A job
+// factors the first nDiag columns of a front F (rows x rows, lower, row-major)
+// in panels: the first w0 = nDiag - 64 (P - 1) wide, the others 64, so that
+// every later panel and every trailing block is aligned to the tile grid
+// b(0) = 0, b(t) = w0 + 64 (t - 1).  Panel p is one POTRF of tile (p, p)
+// (which also stores the tile's inverse), one TRSM per row tile a > p, and
+// one update C(a, b) -= X(a) X(b)^T (K = panel width) per lower tile of the
+// trailing block with column tile b below nUpd.  Each piece is a work item;
+// a block takes the next item from a ticket counter (the items are listed in
+// a topological order, so a block only waits on items taken before its own) and
+// waits, bounded, on per-tile completion counters:
+//   POTRF(p)       tile (p, p) updated by the p earlier panels
+//   TRSM(p, a)     POTRF(p) done; tile (a, p) updated by the p earlier panels
+//   GEMM(p, a, b)  TRSM(p, a) and TRSM(p, b) done; tile (a, b) updated by the p earlier panels
+// sync[0] is the ticket, the counters follow (zeroed before every launch);
+// a wait that gives up sets flag[1].  Data written by other blocks is read
+// through L2 (ld.global.cg).
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned smid() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+  return r;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) chol_fused_kernel(const CholFusedJob<T>* __restrict__ jobs,
+                                                         const CholItem* __restrict__ items, int nItems,
+                                                         int* __restrict__ sync, T* __restrict__ ws, int* flag,
+                                                         unsigned long long* __restrict__ trace) {
+  extern __shared__ __align__(16) unsigned char cf_smem[];
+  __shared__ int sTicket, sOk;
+  __shared__ unsigned long long tStart, tReady;
+  int* err = flag + 1;
+  if (threadIdx.x == 0) {
+    sTicket = atomicAdd(sync, 1);
+    if (trace) tStart = globaltimer_ns();
+  }
+  __syncthreads();
+  if (sTicket >= nItems) {   // counters not reset: report, touch nothing
+    if (threadIdx.x == 0) atomicExch(err, 2);
+    return;
+  }
+  const CholItem it = items[sTicket];
+  const CholFusedJob<T> j = jobs[it.job];
+  int* cnt = sync + 1 + j.cnt;     // TR x TU: panels applied to tile (a, b)
+  int* tdone = cnt + j.TR * j.TU;  // TR: panels whose TRSM of row tile a is done
+  int* pdone = tdone + j.TR;       // P: POTRF of panel p done
+  const int p = it.p, a = it.a, b = it.b;
+  auto bnd = [&](int t) { return t == 0 ? 0 : j.w0 + 64 * (t - 1); };
+  const int c0 = bnd(p), wp = bnd(p + 1) - c0;
+  if ((threadIdx.x >> 5) == 0) {
+    bool ok;
+    if (it.kind == CHOL_POTRF) ok = wait_geq(cnt + p * j.TU + p, p, err);
+    else if (it.kind == CHOL_TRSM) ok = wait_geq(pdone + p, 1, err) && wait_geq(cnt + a * j.TU + p, p, err);
+    else
+      ok = wait_geq(tdone + a, p + 1, err) && wait_geq(tdone + b, p + 1, err) &&
+           wait_geq(cnt + a * j.TU + b, p, err);
+    if (threadIdx.x == 0) {
+      sOk = ok;
+      if (trace) tReady = globaltimer_ns();
     }
+  }
+  __syncthreads();
+  if (!sOk) return;
+  T* F = j.F;
+  const int ld = j.ld;
+  int* done;
+  int doneVal;
+  if (it.kind == CHOL_POTRF) {
+    T* A = F + (size_t)c0 * ld + c0;
+    potrf_tile_reg<T>(A, ld, wp, j.code, flag);
+    if (c0 + wp < j.nRows) {   // rows below: the TRSM items multiply by the inverse
+      T (*L)[65] = reinterpret_cast<T (*)[65]>(cf_smem);
+      T (*Li)[65] = reinterpret_cast<T (*)[65]>(cf_smem + sizeof(T) * 64 * 65);
+      T (*Tm)[16][17] = reinterpret_cast<T (*)[16][17]>(cf_smem + 2 * sizeof(T) * 64 * 65);
+      tile_inverse<T>(A, ld, wp, L, Li, Tm);
+      T* out = ws + j.inv + (size_t)p * 4096;
+#pragma unroll
+      for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) out[idx] = Li[idx >> 6][idx & 63];
+    }
+    done = pdone + p;
+    doneVal = 1;
+  } else if (it.kind == CHOL_TRSM) {
+    T (*X)[65] = reinterpret_cast<T (*)[65]>(cf_smem);
+    T (*Li)[65] = reinterpret_cast<T (*)[65]>(cf_smem + sizeof(T) * 64 * 65);
+    const T* in = ws + j.inv + (size_t)p * 4096;
+#pragma unroll
+    for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) Li[idx >> 6][idx & 63] = __ldcg(in + idx);
     __syncthreads();
-    // out[i][j] = sum_{k <= j} X[i][k] Li[j][k]; thread: rows ty + 16 a, columns tx + 16 c
-    const int tx = tid & 15, ty = tid >> 4;
-    T acc[4][4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) acc[a][c] = T(0);
-    for (int k = 0; k < w; ++k) {
-      T xa[4], lb[4];
-#pragma unroll
-      for (int a = 0; a < 4; ++a) xa[a] = X[ty + 16 * a][k];
-#pragma unroll
-      for (int c = 0; c < 4; ++c) lb[c] = Li[tx + 16 * c][k];
-#pragma unroll
-      for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[a][c] = fma(xa[a], lb[c], acc[a][c]);
+    const int r0 = bnd(a);
+    trsm_chunk_mul<T>(F + (size_t)r0 * ld + c0, ld, min(bnd(a + 1), j.nRows) - r0, wp, X, Li);
+    done = tdone + a;
+    doneVal = p + 1;
+  } else {
+    const int r0 = bnd(a), q0 = bnd(b);
+    GemmTask<T> g;
+    g.A = F + (size_t)r0 * ld + c0;
+    g.B = F + (size_t)q0 * ld + c0;
+    g.C = F + (size_t)r0 * ld + q0;
+    g.M = min(bnd(a + 1), j.nRows) - r0;
+    g.N = min(bnd(b + 1), j.nUpd) - q0;
+    g.K = wp;
+    g.lda = g.ldb = g.ldc = ld;
+    g.tA = 0;
+    g.tB = 1;
+    g.lower = 0;
+    g.alpha = T(-1);
+    g.beta = T(1);
+    T (*As)[BK][BM + 1] = reinterpret_cast<T (*)[BK][BM + 1]>(cf_smem);
+    T (*Bs)[BK][BN + 1] = reinterpret_cast<T (*)[BK][BN + 1]>(cf_smem + 2 * sizeof(T) * BK * (BM + 1));
+    gemm_tile<T>(g, 0, 0, As, Bs);
+    done = cnt + a * j.TU + b;
+    doneVal = p + 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    st_release(done, doneVal);
+    if (trace) {   // diagnostics: when the item started, was ready, ended (ns), and its SM
+      unsigned long long* r = trace + 4 * (size_t)sTicket;
+      r[0] = tStart;
+      r[1] = tReady;
+      r[2] = globaltimer_ns();
+      r[3] = smid();
     }
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      const int i = ty + 16 * a;
-      if (i >= nr) continue;
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const int j = tx + 16 * c;
-        if (j < w) t.B[(size_t)(r0 + i) * t.ldb + j] = acc[a][c];
-      }
-    }
-    __syncthreads();
   }
 }
 
@@ -535,11 +742,18 @@ __global__ void __launch_bounds__(QRP_THREADS) qr_panel_kernel(const QrTask<T>* 
   T* P = Wg;
   long long lp = n;
   const bool inSmem = (long long)nr * pw <= smemElems;
-  if (inSmem) {
+  if (inSmem) {   // a thread's loads of all panel columns in flight at once
     P = reinterpret_cast<T*>(smraw);
     lp = nr;
-    for (int c = 0; c < pw; ++c)
-      for (int i = tid; i < nr; i += QRP_THREADS) P[c * lp + i] = Wg[(size_t)c * n + i];
+    for (int i = tid; i < nr; i += QRP_THREADS) {
+      T tmp[QR_PB];
+#pragma unroll
+      for (int c = 0; c < QR_PB; ++c)
+        if (c < pw) tmp[c] = Wg[(size_t)c * n + i];
+#pragma unroll
+      for (int c = 0; c < QR_PB; ++c)
+        if (c < pw) P[c * lp + i] = tmp[c];
+    }
   }
   for (int idx = tid; idx < QR_PB * (QR_PB + 1); idx += QRP_THREADS) (&Ts[0][0])[idx] = T(0);
   __syncthreads();
@@ -830,6 +1044,19 @@ template <class T> void launch_trsm(const TrsmTask<T>* d, int n, int chunks, cud
   RSCHOL_LAUNCH_CHECK();
 }
 template <class T>
+void launch_chol_fused(const CholFusedJob<T>* jobs, const CholItem* items, int nItems, int* sync, long long syncInts,
+                       T* ws, int* flag, unsigned long long* trace, cudaStream_t s) {
+  if (nItems <= 0) return;
+  RSCHOL_CUDA(cudaMemsetAsync(sync, 0, sizeof(int) * (size_t)syncInts, s));
+  const int smem = (int)(sizeof(T) * (3 * 64 * 65 + 3 * 16 * 17));
+  static std::once_flag once;
+  std::call_once(once, [&] {
+    RSCHOL_CUDA(cudaFuncSetAttribute(chol_fused_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  });
+  chol_fused_kernel<T><<<nItems, 256, smem, s>>>(jobs, items, nItems, sync, ws, flag, trace);
+  RSCHOL_LAUNCH_CHECK();
+}
+template <class T>
 void launch_extadd(const ExtAddRow<T>* rows, int nRows, const ExtAddSeg* segs, const ExtAddSource<T>* src,
                    cudaStream_t s) {
   if (nRows <= 0) return;
@@ -911,6 +1138,8 @@ template <class T> void launch_box_muller(const uint32_t* raw, long long count, 
   template void launch_gemm<T>(const GemmTask<T>*, int, int, cudaStream_t);                              \
   template void launch_potrf<T>(const PotrfTask<T>*, int, int*, cudaStream_t);                           \
   template void launch_trsm<T>(const TrsmTask<T>*, int, int, cudaStream_t);                              \
+  template void launch_chol_fused<T>(const CholFusedJob<T>*, const CholItem*, int, int*, long long, T*, int*,  \
+                                     unsigned long long*, cudaStream_t);                                 \
   template void launch_extadd<T>(const ExtAddRow<T>*, int, const ExtAddSeg*, const ExtAddSource<T>*,      \
                                  cudaStream_t);                                                          \
   template void launch_scatter<T>(const double*, const long long*, const long long*, long long, T*,      \

@@ -58,6 +58,32 @@ struct TrsmTask {
   int chunkBase;  // first 64-row chunk of this task in the launch
 };
 
+// Blocked partial Cholesky of several fronts in one launch (tile-level
+// dependencies, ticketed work items): job = the first nDiag columns of the
+// nRows x nRows lower front F; trailing updates reach the columns below nUpd.
+// Panels: the first w0 = nDiag - 64 (P - 1) wide, then 64; tile t spans rows
+// [b(t), b(t + 1)), b(0) = 0, b(t) = w0 + 64 (t - 1); TR / TU tiles cover
+// nRows / nUpd.
+template <class T>
+struct CholFusedJob {
+  T* F;
+  int ld, nDiag, nRows, nUpd, code;
+  int w0, P, TR, TU;
+  int cnt;          // offset of the job's TR x TU + TR + P counters after the ticket
+  long long inv;    // element offset of the job's P inverse tiles (64 x 64) in the workspace
+};
+constexpr int CHOL_POTRF = 0, CHOL_TRSM = 1, CHOL_GEMM = 2;
+struct CholItem {   // one piece of panel p: POTRF, TRSM of row tile a, update of tile (a, b)
+  int job, kind, p, a, b;
+};
+// sync: syncInts ints (zeroed here, on the stream, before the launch); ws:
+// the jobs' inverse tiles; flag[0]: min code of a failed pivot, flag[1]: set
+// when a bounded wait gives up.  trace (diagnostics, may be null): 4 values
+// per item -- start, dependencies met, end (ns of the global timer), SM.
+template <class T>
+void launch_chol_fused(const CholFusedJob<T>* jobs, const CholItem* items, int nItems, int* sync, long long syncInts,
+                       T* ws, int* flag, unsigned long long* trace, cudaStream_t s);
+
 // Extend-add "pull" by target row: a warp owns one target row and adds the
 // rows of its sources in a fixed order (deterministic, no atomics).  Source
 // row a, columns b in [b0, min(b1, a + 1)) (the lower part of a symmetric

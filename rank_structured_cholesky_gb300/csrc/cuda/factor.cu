@@ -32,6 +32,8 @@ FactorEngine<T>::FactorEngine(const Symbolic& S_, const CSC& A_, const Params& p
   RSCHOL_CUDA(cudaMemcpyAsync(dAvals.p, A.x.data(), sizeof(double) * A.x.size(), cudaMemcpyHostToDevice, stream));
   dFlag.alloc(2 * sizeof(int));
   useTc_ = std::is_same<T, float>::value && tensor_cores_enabled();
+  const char* fc = std::getenv("RSCHOL_FUSED_CHOL");
+  fusedChol_ = std::is_same<T, float>::value && !(fc && fc[0] == '0');
   const char* g = std::getenv("RSCHOL_GRAPHS");
   useGraphs_ = !(g && g[0] == '0');
   RSCHOL_CUDA(cudaStreamSynchronize(stream));
@@ -162,6 +164,69 @@ static GemmTask<T> mk_gemm(const T* A, int lda, bool tA, const T* B, int ldb, bo
 
 template <class T>
 void FactorEngine<T>::emit_chol(const std::vector<CholJob<T>>& jobs) {
+  if (fusedChol_) {
+    Step st{ST_CHOL, (long long)cholItems_.size(), 0, 0};
+    const int j0 = (int)cholJobs_.size();
+    long long sync = 1, ws = 0;   // sync[0]: the ticket
+    int maxP = 0;
+    for (const auto& jb : jobs) {
+      if (jb.nDiag <= 0) continue;
+      CholFusedJob<T> c{};
+      c.F = jb.F;
+      c.ld = jb.ld;
+      c.nDiag = jb.nDiag;
+      c.nRows = jb.nRows;
+      c.nUpd = jb.nUpd;
+      c.code = jb.code;
+      c.P = (jb.nDiag + NB - 1) / NB;
+      c.w0 = jb.nDiag - NB * (c.P - 1);
+      auto tiles = [&](int n) { return n <= c.w0 ? 1 : 1 + (n - c.w0 + NB - 1) / NB; };
+      c.TR = tiles(jb.nRows);
+      c.TU = tiles(jb.nUpd);
+      c.cnt = (int)(sync - 1);
+      sync += (long long)c.TR * c.TU + c.TR + c.P;
+      c.inv = ws;
+      ws += (long long)c.P * NB * NB;
+      maxP = std::max(maxP, c.P);
+      cholJobs_.push_back(c);
+      for (int p = 0; p < c.P; ++p) {   // algorithmic flops, counted as the per-panel steps count them
+        const int c0 = p == 0 ? 0 : c.w0 + NB * (p - 1), w = p == 0 ? c.w0 : NB;
+        const int rows = jb.nRows - c0 - w, upd = jb.nUpd - c0 - w;
+        flops += (double)w * w * w / 3.0 + (double)std::max(rows, 0) * w * w;
+        if (rows > 0 && upd > 0) flops += 2.0 * rows * upd * w * (rows == upd ? 0.5 : 1.0);
+      }
+    }
+    const int j1 = (int)cholJobs_.size();
+    // Item order (a topological one, with a look-ahead of one panel): stage p
+    // lists the POTRFs and TRSMs of panel p, the rest R(p - 1) of the previous
+    // panel's updates (column tiles >= p + 1), then L(p), panel p's updates of
+    // column tile p + 1 -- all that POTRF(p + 1) and its TRSMs wait for.  So
+    // the next panel's critical pieces are taken long before the bulk of the
+    // current updates is done.
+    auto updates = [&](int q, int p, int bLo, int bHi) {
+      const CholFusedJob<T>& c = cholJobs_[q];
+      for (int b = std::max(bLo, p + 1); b < std::min(bHi, c.TU); ++b)
+        for (int a = b; a < c.TR; ++a) cholItems_.push_back(CholItem{q, CHOL_GEMM, p, a, b});
+    };
+    for (int p = 0; p <= maxP; ++p) {
+      for (int q = j0; q < j1; ++q)
+        if (p < cholJobs_[q].P) cholItems_.push_back(CholItem{q, CHOL_POTRF, p, p, p});
+      for (int q = j0; q < j1; ++q)
+        if (p < cholJobs_[q].P)
+          for (int a = p + 1; a < cholJobs_[q].TR; ++a) cholItems_.push_back(CholItem{q, CHOL_TRSM, p, a, p});
+      for (int q = j0; q < j1; ++q)
+        if (p >= 1 && p <= cholJobs_[q].P) updates(q, p - 1, p + 1, INT_MAX);   // R(p - 1)
+      for (int q = j0; q < j1; ++q)
+        if (p < cholJobs_[q].P) updates(q, p, p + 1, p + 2);                    // L(p)
+    }
+    st.count = st.grid = (int)(cholItems_.size() - st.off);
+    st.elems = sync;
+    if (st.count == 0) return;
+    cholSync_ = std::max(cholSync_, sync);
+    cholWs_ = std::max(cholWs_, ws);
+    steps_.push_back(st);
+    return;
+  }
   int maxN = 0;
   for (auto& j : jobs) maxN = std::max(maxN, j.nDiag);
   for (int kb = 0; kb < maxN; kb += NB) {
@@ -357,6 +422,9 @@ void FactorEngine<T>::plan() {
   wsCur_ = 0;
   qr_.clear();
   qrWs_ = 0;
+  cholJobs_.clear();
+  cholItems_.clear();
+  cholSync_ = cholWs_ = 0;
   ident_.clear();
   ints_.clear();
   flops = 0;
@@ -819,6 +887,10 @@ void FactorEngine<T>::plan() {
   for (auto& s : eaS_) s.rowRel = dInts_.as<int>() + reinterpret_cast<size_t>(s.rowRel);
   dSplitWs_.alloc(sizeof(float) * std::max(1LL, wsCur_));
   dQrWs_.alloc(sizeof(T) * std::max(1LL, qrWs_));
+  dCholSync_.alloc(sizeof(int) * std::max(1LL, cholSync_));
+  dCholWs_.alloc(sizeof(T) * std::max(1LL, cholWs_));
+  if (const char* tp = std::getenv("RSCHOL_CHOL_TRACE"))   // diagnostics: per-item timeline of the fused steps
+    if (tp[0] && !cholItems_.empty()) dCholTrace_.alloc(4 * sizeof(unsigned long long) * cholItems_.size());
   for (size_t q = 0; q < gemm_.size(); ++q)
     if (gemmWsOff_[q] >= 0) gemm_[q].ws = dSplitWs_.as<float>() + gemmWsOff_[q];
   up(dSplitIds_, splitIds_.data(), splitIds_.size() * sizeof(int));
@@ -833,6 +905,10 @@ void FactorEngine<T>::plan() {
   for (const auto& t : trsm_)
     if (!device_ptr(t.L) || !device_ptr(t.B))
       throw std::runtime_error("factor plan: a TRSM task without a device address");
+  for (const auto& c : cholJobs_)
+    if (!device_ptr(c.F)) throw std::runtime_error("factor plan: a Cholesky job without a device address");
+  up(dCholJobs_, cholJobs_.data(), cholJobs_.size() * sizeof(CholFusedJob<T>));
+  up(dCholItems_, cholItems_.data(), cholItems_.size() * sizeof(CholItem));
   up(dGemm_, gemm_.data(), gemm_.size() * sizeof(GemmTask<T>));
   up(dPotrf_, potrf_.data(), potrf_.size() * sizeof(PotrfTask<T>));
   up(dTrsm_, trsm_.data(), trsm_.size() * sizeof(TrsmTask<T>));
@@ -844,7 +920,9 @@ void FactorEngine<T>::plan() {
   up(dScatSrc_, scatSrc_.data(), scatSrc_.size() * sizeof(long long));
   up(dScatDst_, scatDst_.data(), scatDst_.size() * sizeof(long long));
   RSCHOL_CUDA(cudaStreamSynchronize(stream));
-  deviceBytes += ints_.size() * 4 + gemm_.size() * sizeof(GemmTask<T>) + scatSrc_.size() * 16;
+  deviceBytes += ints_.size() * 4 + gemm_.size() * sizeof(GemmTask<T>) + scatSrc_.size() * 16 +
+                 cholItems_.size() * sizeof(CholItem) + cholJobs_.size() * sizeof(CholFusedJob<T>) +
+                 sizeof(int) * cholSync_ + sizeof(T) * cholWs_;
   planned_ = true;
 }
 
@@ -881,6 +959,11 @@ void FactorEngine<T>::enqueue(bool timing, bool capturing) {
       case ST_GEMM_REDUCE: gemm_launch(st); break;
       case ST_POTRF: launch_potrf<T>(dPotrf_.as<PotrfTask<T>>() + st.off, st.count, dFlag.as<int>(), stream); break;
       case ST_TRSM: launch_trsm<T>(dTrsm_.as<TrsmTask<T>>() + st.off, st.count, st.grid, stream); break;
+      case ST_CHOL:
+        launch_chol_fused<T>(dCholJobs_.as<CholFusedJob<T>>(), dCholItems_.as<CholItem>() + st.off, st.count,
+                             dCholSync_.as<int>(), st.elems, dCholWs_.as<T>(), dFlag.as<int>(),
+                             dCholTrace_.p ? dCholTrace_.as<unsigned long long>() + 4 * st.off : nullptr, stream);
+        break;
       case ST_EXTADD:
         launch_extadd<T>(dEaR_.as<ExtAddRow<T>>() + st.off, st.count, dEaSeg_.as<ExtAddSeg>(),
                          dEaS_.as<ExtAddSource<T>>(), stream);
@@ -950,8 +1033,50 @@ int FactorEngine<T>::run() {
           const GemmTask<T>& gt = gemm_[st.off + k];
           stepFlops[ST_GEMM] += 2.0 * gt.M * gt.N * (double)gt.K;
         }
+    // RSCHOL_STEP_LOG=1: every step of this run on stderr (kind, tasks, grid,
+    // device ms; GEMM: flops and largest M / N / K) for tuning the schedule
+    const char* sl = std::getenv("RSCHOL_STEP_LOG");
+    if (sl && sl[0] == '1') {
+      static const char* names[] = {"gemm", "potrf", "trsm", "extadd", "qr", "ident", "reduce", "chol"};
+      for (size_t q = 0; q < steps_.size(); ++q) {
+        const Step& st = steps_[q];
+        float ms = 0;
+        RSCHOL_CUDA(cudaEventElapsedTime(&ms, stepEv_[2 * q], stepEv_[2 * q + 1]));
+        double f = 0;
+        int mM = 0, mN = 0, mK = 0;
+        if (st.kind == ST_GEMM)
+          for (int k = 0; k < st.count; ++k) {
+            const GemmTask<T>& g = gemm_[st.off + k];
+            f += 2.0 * g.M * g.N * (double)g.K;
+            mM = std::max(mM, g.M);
+            mN = std::max(mN, g.N);
+            mK = std::max(mK, g.K);
+          }
+        std::fprintf(stderr, "step %zu %s tasks %d grid %d aux %d us %.1f gflop %.4f M %d N %d K %d\n", q,
+                     names[st.kind], st.count, st.grid, st.aux, 1e3 * ms, f * 1e-9, mM, mN, mK);
+      }
+    }
   }
-  if (flag[1]) throw CudaError("tensor-core GEMM: an mbarrier wait exceeded its limit");
+  if (dCholTrace_.p) {   // RSCHOL_CHOL_TRACE=<file>: one line per item of the fused steps of this run
+    std::vector<unsigned long long> tr(4 * cholItems_.size());
+    RSCHOL_CUDA(cudaMemcpy(tr.data(), dCholTrace_.p, tr.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    if (FILE* fp = std::fopen(std::getenv("RSCHOL_CHOL_TRACE"), "w")) {
+      for (size_t q = 0; q < steps_.size(); ++q) {
+        const Step& st = steps_[q];
+        if (st.kind != ST_CHOL) continue;
+        for (int t = 0; t < st.count; ++t) {
+          const CholItem& it = cholItems_[st.off + t];
+          const unsigned long long* r = &tr[4 * (st.off + t)];
+          std::fprintf(fp, "%zu %d %d %d %d %d %d %llu %llu %llu %llu\n", q, t, it.job, it.kind, it.p, it.a, it.b,
+                       r[0], r[1], r[2], r[3]);
+        }
+      }
+      std::fclose(fp);
+    }
+  }
+  if (flag[1])
+    throw CudaError(flag[1] == 2 ? "fused Cholesky: ticket counter out of range"
+                                 : "factor: a bounded wait (tensor-core mbarrier or tile counter) exceeded its limit");
   return flag[0] == INT_MAX ? 0 : flag[0];
 }
 

@@ -46,6 +46,7 @@ enum StepKind : int {
   ST_QR,
   ST_IDENT,
   ST_GEMM_REDUCE,   // sum the K-slice partials of the split tensor-core GEMM tasks
+  ST_CHOL,          // fused blocked partial Cholesky of a level (POTRF + TRSM + updates, one launch)
 };
 
 struct Step {
@@ -55,7 +56,7 @@ struct Step {
   int grid;         // tiles / chunks / columns for the launch
   int aux = 0;      // ST_QR: largest row count of the batch (grid: largest rank);
                     // ST_GEMM: 1 on the tensor cores
-  long long elems = 0;   // ST_GEMM_REDUCE: elements of C summed
+  long long elems = 0;   // ST_GEMM_REDUCE: elements of C summed; ST_CHOL: ints of its counters
 };
 
 template <class T>
@@ -170,6 +171,13 @@ class FactorEngine {
   DevBuf dSplitWs_, dSplitIds_, dSplitBase_;
   long long qrWs_ = 0;   // elements of the Householder QR workspace (largest QR step)
   DevBuf dQrWs_;
+  // The blocked Cholesky of each emit_chol call as one ticketed launch (FP32;
+  // RSCHOL_FUSED_CHOL=0 keeps the POTRF / TRSM / GEMM steps per panel).
+  bool fusedChol_ = false;
+  std::vector<CholFusedJob<T>> cholJobs_;
+  std::vector<CholItem> cholItems_;
+  long long cholSync_ = 0, cholWs_ = 0;   // largest counter array (ints) and inverse workspace (elements) of a step
+  DevBuf dCholJobs_, dCholItems_, dCholSync_, dCholWs_, dCholTrace_;
   std::vector<long long> scatSrc_, scatDst_;
   std::vector<int> scatIsInterior_;
   DevBuf dGemm_, dPotrf_, dTrsm_, dEaR_, dEaSeg_, dEaS_, dQr_, dIdent_, dInts_, dScatSrc_, dScatDst_;
