@@ -827,6 +827,120 @@ __global__ void __launch_bounds__(QRP_THREADS) qr_panel_kernel(const QrTask<T>* 
   }
 }
 
+// The same panel factorisation with the panel in registers (FP32, at most
+// 512 R rows): thread t keeps rows t + 512 q (q < R) of the 16 panel
+// columns, so a column step touches shared memory only for its three block
+// reductions (|x|^2 below the diagonal with row kk, the 16 dot products
+// s_c = v^T P[:, c], the T column) -- three barriers per column.  Reflectors,
+// T factor and layout as qr_panel_kernel (the sums run in another fixed order).
+template <int R>
+__global__ void __launch_bounds__(QRP_THREADS, 1) qr_panel_reg_kernel(const QrTask<float>* __restrict__ tasks,
+                                                                      int j0) {
+  constexpr int NW = QRP_THREADS / 32;
+  __shared__ float redA[2][NW];
+  __shared__ float redC[NW][QR_PB];
+  __shared__ float rowk[QR_PB], sred[QR_PB];
+  __shared__ float Ts[QR_PB][QR_PB + 1];
+  const QrTask<float> t = tasks[blockIdx.x];
+  const int n = t.n, r = t.r;
+  if (j0 >= r) return;
+  const int pw = min(QR_PB, r - j0), nr = n - j0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float* Wg = t.W + (size_t)j0 * n + j0;   // panel element (i, c) at Wg[c * n + i]
+  float a[R][QR_PB];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int i = tid + QRP_THREADS * q;
+#pragma unroll
+    for (int c = 0; c < QR_PB; ++c) a[q][c] = (i < nr && c < pw) ? Wg[(size_t)c * n + i] : 0.f;
+  }
+  for (int idx = tid; idx < QR_PB * (QR_PB + 1); idx += QRP_THREADS) (&Ts[0][0])[idx] = 0.f;
+  if (tid < QR_PB) sred[tid] = 0.f;   // columns beyond pw keep s = 0
+#pragma unroll
+  for (int kk = 0; kk < QR_PB; ++kk) {
+    if (kk >= pw) break;
+    // |x|^2 below the diagonal; row kk published (alpha and the unit row of the reflector)
+    float x2 = 0.f;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int i = tid + QRP_THREADS * q;
+      if (i > kk && i < nr) x2 += a[q][kk] * a[q][kk];
+    }
+    x2 = warp_sum_d(x2);
+    if (lane == 0) redA[kk & 1][warp] = x2;
+    if (tid == kk)
+#pragma unroll
+      for (int c = 0; c < QR_PB; ++c) rowk[c] = a[0][c];
+    __syncthreads();
+    x2 = 0.f;
+#pragma unroll
+    for (int q = 0; q < NW; ++q) x2 += redA[kk & 1][q];
+    const float alpha = rowk[kk];
+    float tau = 0.f, scal = 1.f;
+    if (x2 > 0.f) {
+      const float beta = -copysignf(sqrtf(alpha * alpha + x2), alpha);
+      tau = (beta - alpha) / beta;
+      scal = 1.f / (alpha - beta);
+    }
+    float v[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int i = tid + QRP_THREADS * q;
+      v[q] = (i > kk && i < nr) ? a[q][kk] * scal : 0.f;
+      if (i > kk && i < nr) a[q][kk] = v[q];
+    }
+    // s_c = P[kk][c] + sum_{i > kk} v_i P[i][c]
+    float part[QR_PB];
+#pragma unroll
+    for (int c = 0; c < QR_PB; ++c) {
+      part[c] = 0.f;
+#pragma unroll
+      for (int q = 0; q < R; ++q) part[c] += v[q] * a[q][c];
+    }
+    const float ws = warp_transpose_sum16(part);
+    if (lane < QR_PB) redC[warp][lane] = ws;
+    __syncthreads();
+    if (tid < pw) {
+      float sum = 0.f;
+#pragma unroll
+      for (int q = 0; q < NW; ++q) sum += redC[q][tid];
+      sred[tid] = sum + rowk[tid];
+    }
+    __syncthreads();
+    // T column kk (dlarft): T[p][kk] = -tau sum_{q=p}^{kk-1} T[p][q] s_q, T[kk][kk] = tau
+    if (tid < kk) {
+      float sum = 0.f;
+      for (int q = tid; q < kk; ++q) sum += Ts[tid][q] * sred[q];
+      Ts[tid][kk] = -tau * sum;
+    }
+    if (tid == kk) Ts[kk][kk] = tau;
+    // apply H_kk to the columns right of kk
+    if (tau != 0.f) {
+#pragma unroll
+      for (int c = kk + 1; c < QR_PB; ++c) {
+        const float w = tau * sred[c];
+#pragma unroll
+        for (int q = 0; q < R; ++q) a[q][c] -= w * v[q];
+        if (tid == kk) a[0][c] -= w;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int i = tid + QRP_THREADS * q;
+    if (i < nr)
+#pragma unroll
+      for (int c = 0; c < QR_PB; ++c)
+        if (c < pw) Wg[(size_t)c * n + i] = a[q][c];
+  }
+  __syncthreads();
+  // T over the upper triangle of the diagonal block
+  for (int idx = tid; idx < pw * pw; idx += QRP_THREADS) {
+    const int ra = idx / pw, cb = idx - ra * pw;
+    if (ra <= cb) Wg[(size_t)cb * n + ra] = Ts[ra][cb];
+  }
+}
+
 // Apply the block reflector of panel j0 to the other columns, in parallel
 // over (row block of QA_RB rows, group of QA_CW columns):
 //   mode 0 (factor): W[j0:n, c] := (I - V T^T V^T) W[j0:n, c], c >= j0 + pw
@@ -1111,7 +1225,14 @@ int launch_householder_qr(const QrTask<T>* d, int n, int maxRows, int maxR, T* w
   const int panels = (maxR + QR_PB - 1) / QR_PB;
   for (int p = 0; p < panels; ++p) {
     const int j0 = p * QR_PB;
-    qr_panel_kernel<T><<<n, QRP_THREADS, smem, s>>>(d, j0, smemElems);
+    if constexpr (std::is_same<T, float>::value) {
+      if (maxRows <= QRP_THREADS) qr_panel_reg_kernel<1><<<n, QRP_THREADS, 0, s>>>(d, j0);
+      else if (maxRows <= 2 * QRP_THREADS) qr_panel_reg_kernel<2><<<n, QRP_THREADS, 0, s>>>(d, j0);
+      else if (maxRows <= 4 * QRP_THREADS) qr_panel_reg_kernel<4><<<n, QRP_THREADS, 0, s>>>(d, j0);
+      else qr_panel_kernel<T><<<n, QRP_THREADS, smem, s>>>(d, j0, smemElems);
+    } else {
+      qr_panel_kernel<T><<<n, QRP_THREADS, smem, s>>>(d, j0, smemElems);
+    }
     RSCHOL_LAUNCH_CHECK();
     ++launches;
     if (maxR - j0 - QR_PB > 0) apply(j0, 0);

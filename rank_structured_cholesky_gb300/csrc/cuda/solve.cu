@@ -278,25 +278,20 @@ __global__ void __launch_bounds__(256) interior_backward_chunks(const SNode<T>* 
 // the triangular solves are GEMVs: every 64-row (or 64-column) block of a
 // supernode is an independent thread block.
 
-// Right-hand side of every compressed supernode of a level: w[c0 + i] plus
-// the fixed-order contribution list of row i (a warp per row, lanes over the
-// contributions).
+// The pieces of a compressed level, as device functions of one thread block
+// (a warp per row where rows are independent).  Data another block wrote is
+// read through L2 (ld.global.cg).
+
+// w[c0 + i] += the fixed-order contribution list of row i (one warp).
 template <class T>
-__global__ void __launch_bounds__(256) compressed_gather_rows(const SNode<T>* __restrict__ nodes,
-                                                              const int* __restrict__ lvl,
-                                                              const long long* __restrict__ cstart,
-                                                              const long long* __restrict__ ent,
-                                                              const T* __restrict__ wu, T* __restrict__ w) {
-  pdl_enter();
-  const SNode<T>& nd = nodes[lvl[blockIdx.y]];
+__device__ void cgather_row(const SNode<T>& nd, int i, const long long* __restrict__ cstart,
+                            const long long* __restrict__ ent, const T* wu, T* w) {
   const int lane = threadIdx.x & 31;
-  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (i >= nd.n) return;
   const long long* cs = cstart + nd.cOff;
   T acc = T(0);
-  for (long long e = cs[i] + lane; e < cs[i + 1]; e += 32) acc += wu[ent[e]];
+  for (long long e = cs[i] + lane; e < cs[i + 1]; e += 32) acc += __ldcg(wu + ent[e]);
   acc = warp_sum(acc);
-  if (lane == 0) w[nd.c0 + i] += acc;
+  if (lane == 0) w[nd.c0 + i] = __ldcg(w + nd.c0 + i) + acc;
 }
 
 // Partial products of y = X f and x = X^T g over 64 x 256 tiles of X (tiles
@@ -305,19 +300,14 @@ __global__ void __launch_bounds__(256) compressed_gather_rows(const SNode<T>* __
 //   P[i][jb] = sum_{j in column block jb} X[i][j] f_j    (forward)
 //   Q[j][ib] = sum_{i in row block ib} X[i][j] g_i       (backward)
 template <class T>
-__global__ void __launch_bounds__(256) compressed_ytile_kernel(const SNode<T>* __restrict__ nodes,
-                                                               const XTile* __restrict__ tiles,
-                                                               const T* __restrict__ w, T* __restrict__ part) {
-  pdl_enter();
-  const XTile tl = tiles[blockIdx.x];
-  const SNode<T>& nd = nodes[tl.node];
+__device__ void cytile(const SNode<T>& nd, const XTile& tl, const T* w, T* part) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n = nd.n;
   const int i0 = tl.ib * SOLVE_RB + warp * 8, j0 = tl.jb * XT_COLS;
   T fj[8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
     const int j = j0 + lane + 32 * c;
-    fj[c] = (j < n) ? w[nd.c0 + j] : T(0);
+    fj[c] = (j < n) ? __ldcg(w + nd.c0 + j) : T(0);
   }
   T acc[8];
 #pragma unroll
@@ -340,6 +330,138 @@ __global__ void __launch_bounds__(256) compressed_ytile_kernel(const SNode<T>* _
   }
 }
 
+// gs: SOLVE_RB shared.
+template <class T>
+__device__ void cxtile(const SNode<T>& nd, const XTile& tl, const T* gv, T* part, T* gs) {
+  const int n = nd.n, i0 = tl.ib * SOLVE_RB, h = min(SOLVE_RB, n - i0);
+  if (threadIdx.x < SOLVE_RB) gs[threadIdx.x] = (threadIdx.x < h) ? __ldcg(gv + nd.c0 + i0 + threadIdx.x) : T(0);
+  __syncthreads();
+  const int j = tl.jb * XT_COLS + threadIdx.x;
+  if (j < n) {
+    T s = T(0);
+#pragma unroll 16
+    for (int i = 0; i < h; ++i) s += nd.X[(size_t)(i0 + i) * n + j] * gs[i];
+    part[nd.zpOff2 + (size_t)j * nd.nb + tl.ib] = s;
+  }
+  __syncthreads();
+}
+
+// y_i = sum of its tile partials (fixed order) for one 64-row block, then the
+// block's part of z = U^T y; the last block of the supernode to finish sums
+// the parts in fixed order.  yb: SOLVE_RB shared, red: 8 x 256 shared.
+template <class T>
+__device__ void cy_block(const SNode<T>& nd, int b, int* sync, T* zpart, const T* ypart, T* yv, T* wu, T* yb,
+                         T (*red)[256], int* sLast) {
+  const int n = nd.n, i0 = b * SOLVE_RB, h = min(SOLVE_RB, n - i0);
+  if (threadIdx.x < SOLVE_RB) {
+    const int i = threadIdx.x;
+    T s = T(0);
+    if (i < h) {
+      const int jbEnd = min(nd.ncb - 1, (i0 + SOLVE_RB - 1) / XT_COLS);
+      const T* p = ypart + nd.zpOff2 + (size_t)(i0 + i) * nd.ncb;
+      for (int jb = 0; jb <= jbEnd; ++jb) s += __ldcg(p + jb);
+      yv[nd.c0 + i0 + i] = s;
+    }
+    yb[i] = s;
+  }
+  __syncthreads();
+  const int r = nd.r;
+  rows_t_gemv<T>(nd.U + (size_t)i0 * r, r, h, r, yb, zpart + nd.zpOff + (size_t)b * r, red);
+  int* done = sync + nd.syncOff;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    *sLast = (atomicAdd(done, 1) == nd.nb - 1);
+    __threadfence();
+  }
+  __syncthreads();
+  if (!*sLast) return;
+  rows_t_gemv<T>(zpart + nd.zpOff, r, nd.nb, r, nullptr, wu + nd.wuOff, red);
+  if (threadIdx.x == 0) *done = 0;
+  __syncthreads();
+}
+
+// x_j = sum of its tile partials over the row blocks ib >= 4 jb (fixed order).
+template <class T>
+__device__ void cx_reduce_col(const SNode<T>& nd, int j, const T* xpart, T* w) {
+  const T* p = xpart + nd.zpOff2 + (size_t)j * nd.nb;
+  T s = T(0);
+  for (int ib = (j / XT_COLS) * (XT_COLS / SOLVE_RB); ib < nd.nb; ++ib) s += __ldcg(p + ib);
+  w[nd.c0 + j] = s;
+}
+
+// u_a = -(V z)_a, the supernode's contribution to its ancestors' right-hand
+// sides (one warp).
+template <class T>
+__device__ void cvz_row(const SNode<T>& nd, int a, T* wu) {
+  const int lane = threadIdx.x & 31, r = nd.r;
+  const T* z = wu + nd.wuOff;
+  const T* v = nd.V + (size_t)a * r;
+  T s = T(0);
+  for (int k = lane; k < r; k += 32) s += v[k] * __ldcg(z + k);
+  s = warp_sum(s);
+  if (lane == 0) wu[nd.wuOff + 2 * r + a] = -s;
+}
+
+// s = V^T x_R for one 128-row chunk; the last chunk to finish sums the chunk
+// partials in fixed order.  xs: 128 shared, red: 8 x 256 shared.
+template <class T>
+__device__ void cvtx_chunk(const SNode<T>& nd, int ch, const int* __restrict__ rows, int* sync, T* spart,
+                           const T* w, T* sv, T* xs, T (*red)[256], int* sLast) {
+  const int r = nd.r, a0 = ch * 128, ah = min(128, nd.m - a0);
+  const int* rw = rows + nd.rowsOff + a0;
+  for (int a = threadIdx.x; a < ah; a += blockDim.x) xs[a] = __ldcg(w + rw[a]);
+  __syncthreads();
+  rows_t_gemv<T>(nd.V + (size_t)a0 * r, r, ah, r, xs, spart + nd.spOff + (size_t)ch * r, red);
+  int* done = sync + nd.syncOff + 1;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    *sLast = (atomicAdd(done, 1) == nd.nch - 1);
+    __threadfence();
+  }
+  __syncthreads();
+  if (!*sLast) return;
+  rows_t_gemv<T>(spart + nd.spOff, r, nd.nch, r, nullptr, sv + nd.wuOff + r, red);
+  if (threadIdx.x == 0) *done = 0;
+  __syncthreads();
+}
+
+// g_i = y_i - (U s)_i in place (one warp).
+template <class T>
+__device__ void cg_row(const SNode<T>& nd, int i, const T* sv, T* yv) {
+  const int lane = threadIdx.x & 31, r = nd.r;
+  const T* s = sv + nd.wuOff + r;
+  const T* u = nd.U + (size_t)i * r;
+  T acc = T(0);
+  for (int k = lane; k < r; k += 32) acc += u[k] * __ldcg(s + k);
+  acc = warp_sum(acc);
+  if (lane == 0) yv[nd.c0 + i] = __ldcg(yv + nd.c0 + i) - acc;
+}
+
+// One launch per piece and level, chained by programmatic dependent launch.
+// (All levels of a direction as one ticketed launch, with each phase waiting
+// on the previous one through counters, measured slower on c2: 1.19 vs 1.07
+// ms per apply -- the dependent launches already start without gaps.)
+template <class T>
+__global__ void __launch_bounds__(256) compressed_gather_rows(const SNode<T>* __restrict__ nodes,
+                                                              const int* __restrict__ lvl,
+                                                              const long long* __restrict__ cstart,
+                                                              const long long* __restrict__ ent,
+                                                              const T* __restrict__ wu, T* __restrict__ w) {
+  pdl_enter();
+  const SNode<T>& nd = nodes[lvl[blockIdx.y]];
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i < nd.n) cgather_row<T>(nd, i, cstart, ent, wu, w);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) compressed_ytile_kernel(const SNode<T>* __restrict__ nodes,
+                                                               const XTile* __restrict__ tiles,
+                                                               const T* __restrict__ w, T* __restrict__ part) {
+  pdl_enter();
+  const XTile tl = tiles[blockIdx.x];
+  cytile<T>(nodes[tl.node], tl, w, part);
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) compressed_xtile_kernel(const SNode<T>* __restrict__ nodes,
                                                                const XTile* __restrict__ tiles,
@@ -347,21 +469,9 @@ __global__ void __launch_bounds__(256) compressed_xtile_kernel(const SNode<T>* _
   pdl_enter();
   __shared__ T gs[SOLVE_RB];
   const XTile tl = tiles[blockIdx.x];
-  const SNode<T>& nd = nodes[tl.node];
-  const int n = nd.n, i0 = tl.ib * SOLVE_RB, h = min(SOLVE_RB, n - i0);
-  if (threadIdx.x < SOLVE_RB) gs[threadIdx.x] = (threadIdx.x < h) ? gv[nd.c0 + i0 + threadIdx.x] : T(0);
-  __syncthreads();
-  const int j = tl.jb * XT_COLS + threadIdx.x;
-  if (j >= n) return;
-  T s = T(0);
-#pragma unroll 16
-  for (int i = 0; i < h; ++i) s += nd.X[(size_t)(i0 + i) * n + j] * gs[i];
-  part[nd.zpOff2 + (size_t)j * nd.nb + tl.ib] = s;
+  cxtile<T>(nodes[tl.node], tl, gv, part, gs);
 }
 
-// y_i = sum of its tile partials (fixed order) for one 64-row block, then the
-// block's part of z = U^T y; the last block of the supernode to finish sums
-// the parts in fixed order.
 template <class T>
 __global__ void __launch_bounds__(256) compressed_y_kernel(const SNode<T>* __restrict__ nodes,
                                                            const RowBlock* __restrict__ work, int* __restrict__ sync,
@@ -372,35 +482,9 @@ __global__ void __launch_bounds__(256) compressed_y_kernel(const SNode<T>* __res
   __shared__ T red[8][256];
   __shared__ int sLast;
   const RowBlock wk = work[blockIdx.x];
-  const SNode<T>& nd = nodes[wk.node];
-  const int n = nd.n, i0 = wk.b * SOLVE_RB, h = min(SOLVE_RB, n - i0);
-  if (threadIdx.x < SOLVE_RB) {
-    const int i = threadIdx.x;
-    T s = T(0);
-    if (i < h) {
-      const int jbEnd = min(nd.ncb - 1, (i0 + SOLVE_RB - 1) / XT_COLS);
-      const T* p = ypart + nd.zpOff2 + (size_t)(i0 + i) * nd.ncb;
-      for (int jb = 0; jb <= jbEnd; ++jb) s += p[jb];
-      yv[nd.c0 + i0 + i] = s;
-    }
-    yb[i] = s;
-  }
-  __syncthreads();
-  const int r = nd.r;
-  rows_t_gemv<T>(nd.U + (size_t)i0 * r, r, h, r, yb, zpart + nd.zpOff + (size_t)wk.b * r, red);
-  int* done = sync + nd.syncOff;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    sLast = (atomicAdd(done, 1) == nd.nb - 1);
-    __threadfence();
-  }
-  __syncthreads();
-  if (!sLast) return;
-  rows_t_gemv<T>(zpart + nd.zpOff, r, nd.nb, r, nullptr, wu + nd.wuOff, red);
-  if (threadIdx.x == 0) *done = 0;
+  cy_block<T>(nodes[wk.node], wk.b, sync, zpart, ypart, yv, wu, yb, red, &sLast);
 }
 
-// x_j = sum of its tile partials over the row blocks ib >= 4 jb (fixed order).
 template <class T>
 __global__ void __launch_bounds__(256) compressed_x_reduce(const SNode<T>* __restrict__ nodes,
                                                            const int* __restrict__ lvl, const T* __restrict__ xpart,
@@ -408,35 +492,17 @@ __global__ void __launch_bounds__(256) compressed_x_reduce(const SNode<T>* __res
   pdl_enter();
   const SNode<T>& nd = nodes[lvl[blockIdx.y]];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nd.n) return;
-  const T* p = xpart + nd.zpOff2 + (size_t)j * nd.nb;
-  T s = T(0);
-  for (int ib = (j / XT_COLS) * (XT_COLS / SOLVE_RB); ib < nd.nb; ++ib) s += p[ib];
-  w[nd.c0 + j] = s;
+  if (j < nd.n) cx_reduce_col<T>(nd, j, xpart, w);
 }
 
-// u = -V z of every compressed supernode of a level (its contribution to the
-// right-hand sides of its ancestors), a warp per row.
 template <class T>
 __global__ void __launch_bounds__(256) compressed_vz_kernel(const SNode<T>* __restrict__ nodes,
                                                             const int* __restrict__ lvl, T* __restrict__ wu) {
   pdl_enter();
   const SNode<T>& nd = nodes[lvl[blockIdx.y]];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int r = nd.r;
-  const T* z = wu + nd.wuOff;
-  T* u = wu + nd.wuOff + 2 * r;
-  for (int a = blockIdx.x * 8 + warp; a < nd.m; a += gridDim.x * 8) {
-    const T* v = nd.V + (size_t)a * r;
-    T s = T(0);
-    for (int k = lane; k < r; k += 32) s += v[k] * z[k];
-    s = warp_sum(s);
-    if (lane == 0) u[a] = -s;
-  }
+  for (int a = blockIdx.x * 8 + (threadIdx.x >> 5); a < nd.m; a += gridDim.x * 8) cvz_row<T>(nd, a, wu);
 }
 
-// s = V^T x_R of every compressed supernode of a level: 128-row chunks, then
-// the last chunk to finish sums the chunk partials in fixed order.
 template <class T>
 __global__ void __launch_bounds__(256) compressed_vtx_kernel(const SNode<T>* __restrict__ nodes,
                                                              const int* __restrict__ lvl,
@@ -448,42 +514,17 @@ __global__ void __launch_bounds__(256) compressed_vtx_kernel(const SNode<T>* __r
   __shared__ T red[8][256];
   __shared__ int sLast;
   const SNode<T>& nd = nodes[lvl[blockIdx.y]];
-  const int ch = blockIdx.x;
-  if (ch >= nd.nch) return;
-  const int r = nd.r, a0 = ch * 128, ah = min(128, nd.m - a0);
-  const int* rw = rows + nd.rowsOff + a0;
-  for (int a = threadIdx.x; a < ah; a += blockDim.x) xs[a] = w[rw[a]];
-  __syncthreads();
-  rows_t_gemv<T>(nd.V + (size_t)a0 * r, r, ah, r, xs, spart + nd.spOff + (size_t)ch * r, red);
-  int* done = sync + nd.syncOff + 1;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    sLast = (atomicAdd(done, 1) == nd.nch - 1);
-    __threadfence();
-  }
-  __syncthreads();
-  if (!sLast) return;
-  rows_t_gemv<T>(spart + nd.spOff, r, nd.nch, r, nullptr, sv + nd.wuOff + r, red);
-  if (threadIdx.x == 0) *done = 0;
+  if (blockIdx.x < nd.nch) cvtx_chunk<T>(nd, blockIdx.x, rows, sync, spart, w, sv, xs, red, &sLast);
 }
 
-// g = y - U s in place (a warp per row).
 template <class T>
 __global__ void __launch_bounds__(256) compressed_g_kernel(const SNode<T>* __restrict__ nodes,
                                                            const int* __restrict__ lvl, const T* __restrict__ sv,
                                                            T* __restrict__ yv) {
   pdl_enter();
   const SNode<T>& nd = nodes[lvl[blockIdx.y]];
-  const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (i >= nd.n || nd.r == 0 || nd.m == 0) return;
-  const int r = nd.r;
-  const T* s = sv + nd.wuOff + r;
-  const T* u = nd.U + (size_t)i * r;
-  T acc = T(0);
-  for (int k = lane; k < r; k += 32) acc += u[k] * s[k];
-  acc = warp_sum(acc);
-  if (lane == 0) yv[nd.c0 + i] -= acc;
+  if (i < nd.n && nd.r > 0 && nd.m > 0) cg_row<T>(nd, i, sv, yv);
 }
 
 // Inverse of each lower-triangular diagonal block (column c by thread c,
