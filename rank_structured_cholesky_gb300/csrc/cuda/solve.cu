@@ -101,6 +101,93 @@ __device__ void trsv_dinv_t(const T* __restrict__ L, int ld, int n, const T* __r
   }
 }
 
+// Small interior supernodes (n <= IW_N, m <= ICH: one chunk) take a warp
+// each, eight to a block, so the thousands of bottom-level supernodes do not
+// each pay a block's scheduling, ticket and barrier latencies.  The steps and
+// the waits are those of a chunk block below; the per-warp shared buffers
+// hold f (IW_N) and the update vector (ICH).
+constexpr int IW_N = 32;
+
+template <class T>
+__device__ void interior_forward_warp(const SNode<T>* __restrict__ nodes, int s, const int* __restrict__ rel,
+                                      const int* __restrict__ child, int* sync, int epoch, const T* w, T* yout, T* wu,
+                                      T* f, T* u) {
+  const int lane = threadIdx.x & 31;
+  int* err = sync;
+  const SNode<T>& nd = nodes[s];
+  const int n = nd.n, m = nd.m;
+  for (int c = nd.childBegin; c < nd.childEnd; ++c) {   // every child has stored its update vector
+    const SNode<T>& cn = nodes[child[c]];
+    if (!wait_geq(sync + cn.syncOff + 1, epoch * max(1, cn.nch), err)) break;
+  }
+  if (lane < n) f[lane] = w[nd.c0 + lane];
+  for (int a = lane; a < m; a += 32) u[a] = T(0);
+  __syncwarp();
+  for (int c = nd.childBegin; c < nd.childEnd; ++c) {   // children's update vectors, in child order
+    const SNode<T>& cn = nodes[child[c]];
+    const T* wuc = wu + cn.wuOff;
+    const int* rl = rel + cn.relOff;
+    for (int a = lane; a < cn.m; a += 32) {
+      const int t = rl[a];
+      const T v = __ldcg(wuc + a);
+      if (t < n) f[t] += v;
+      else u[t - n] += v;
+    }
+    __syncwarp();
+  }
+  // y = L11^{-1} f through the inverted diagonal block (n x n, row-major)
+  T y = T(0);
+  if (lane < n)
+    for (int j = 0; j <= lane; ++j) y += nd.Dinv[lane * n + j] * f[j];
+  __syncwarp();
+  if (lane < n) {
+    f[lane] = y;
+    yout[nd.c0 + lane] = y;
+  }
+  __syncwarp();
+  T* wud = wu + nd.wuOff;
+  for (int a = lane; a < m; a += 32) {   // u_a -= L21[a] . y
+    const T* row = nd.L + (size_t)(n + a) * nd.ld;
+    T acc = T(0);
+    for (int j = 0; j < n; ++j) acc += row[j] * f[j];
+    wud[a] = u[a] - acc;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    __threadfence();
+    atomicAdd(sync + nd.syncOff + 1, 1);
+  }
+}
+
+template <class T>
+__device__ void interior_backward_warp(const SNode<T>* __restrict__ nodes, int s, const int* __restrict__ rows,
+                                       int* sync, int epoch, const T* yin, T* w, T* f, T* xr) {
+  const int lane = threadIdx.x & 31;
+  int* err = sync;
+  const SNode<T>& nd = nodes[s];
+  const int n = nd.n, m = nd.m;
+  if (nd.parentI >= 0) wait_geq(sync + nodes[nd.parentI].syncOff + 2, epoch, err);   // ancestors solved
+  const int* rw = rows + nd.rowsOff;
+  for (int a = lane; a < m; a += 32) xr[a] = __ldcg(w + rw[a]);
+  __syncwarp();
+  T t = T(0);   // f_j = y_j - (L21^T x_R)_j, lanes over the columns
+  if (lane < n) {
+    for (int a = 0; a < m; ++a) t += nd.L[(size_t)(n + a) * nd.ld + lane] * xr[a];
+    f[lane] = yin[nd.c0 + lane] - t;
+  }
+  __syncwarp();
+  T x = T(0);   // x = L11^{-T} f: x_i = sum_{k >= i} D_ki f_k
+  if (lane < n) {
+    for (int k = lane; k < n; ++k) x += nd.Dinv[k * n + lane] * f[k];
+    w[nd.c0 + lane] = x;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    __threadfence();
+    st_release(sync + nd.syncOff + 2, epoch);   // x of this supernode is final
+  }
+}
+
 // Interior supernodes: all levels in one launch per direction.  A block takes
 // the next (supernode, 128-row chunk of its off-diagonal rows) from a ticket
 // counter, in level order, so it only waits on blocks that started before it:
@@ -117,7 +204,7 @@ __global__ void __launch_bounds__(256) interior_forward_chunks(const SNode<T>* _
                                                                const int* __restrict__ child,
                                                                int* __restrict__ sync, int epoch,
                                                                const T* __restrict__ w, T* __restrict__ yout,
-                                                               T* __restrict__ wu) {
+                                                               T* __restrict__ wu, const int* __restrict__ small) {
   pdl_enter();
   extern __shared__ __align__(16) unsigned char smraw[];
   T* f = reinterpret_cast<T*>(smraw);
@@ -131,6 +218,14 @@ __global__ void __launch_bounds__(256) interior_forward_chunks(const SNode<T>* _
     return;
   }
   const RowBlock wk = work[sTicket];
+  if (wk.node < 0) {   // a group of small supernodes (node = -1 - group, b = count), a warp each
+    const int warp = threadIdx.x >> 5;
+    if (warp < wk.b)
+      interior_forward_warp<T>(nodes, small[8 * (-1 - wk.node) + warp], rel, child, sync, epoch, w, yout, wu,
+                               f + warp * (IW_N + ICH), f + warp * (IW_N + ICH) + IW_N);
+    launch_done(&sync[SYNC_TICK_F], &sync[SYNC_DONE_F]);
+    return;
+  }
   const SNode<T>& nd = nodes[wk.node];
   const int n = nd.n, a0 = wk.b * ICH, a1 = min(nd.m, a0 + ICH);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -193,7 +288,7 @@ __global__ void __launch_bounds__(256) interior_backward_chunks(const SNode<T>* 
                                                                 const int* __restrict__ rows,
                                                                 int* __restrict__ sync, int epoch,
                                                                 T* __restrict__ ipart, const T* __restrict__ yin,
-                                                                T* __restrict__ w) {
+                                                                T* __restrict__ w, const int* __restrict__ small) {
   pdl_enter();
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ T tb[64];
@@ -207,6 +302,14 @@ __global__ void __launch_bounds__(256) interior_backward_chunks(const SNode<T>* 
     return;
   }
   const RowBlock wk = work[sTicket];
+  if (wk.node < 0) {   // a group of small supernodes, a warp each
+    const int warp = threadIdx.x >> 5;
+    T* fw = reinterpret_cast<T*>(smraw) + warp * (IW_N + ICH);
+    if (warp < wk.b)
+      interior_backward_warp<T>(nodes, small[8 * (-1 - wk.node) + warp], rows, sync, epoch, yin, w, fw, fw + IW_N);
+    launch_done(&sync[SYNC_TICK_B], &sync[SYNC_DONE_B]);
+    return;
+  }
   const SNode<T>& nd = nodes[wk.node];
   if (nd.parentI >= 0 && (threadIdx.x >> 5) == 0)   // the parent (and so every ancestor) is solved
     wait_geq(sync + nodes[nd.parentI].syncOff + 2, epoch, err);
@@ -708,6 +811,33 @@ void SolveEngine<T>::plan() {
   for (int l = (int)iLevels_.size() - 1; l >= 0; --l)
     iworkB.insert(iworkB.end(), iwork.begin() + iLevels_[l].first,
                   iwork.begin() + iLevels_[l].first + iLevels_[l].second);
+  // the single-vector apply: per level, the small supernodes in groups of
+  // eight (a warp each), then the chunk blocks of the others
+  std::vector<RowBlock> iworkS, iworkSB;
+  std::vector<int> small;
+  {
+    std::vector<std::pair<size_t, size_t>> lvRange;   // per level: [begin, end) in iworkS
+    bool anySmall = false;
+    for (auto& lv : F_.interiorLevels) {
+      const size_t b0 = iworkS.size();
+      std::vector<int> sm;
+      for (int d : lv)
+        if (S.nodes[d].n <= IW_N && S.nodes[d].m() <= ICH) sm.push_back(d);
+      for (size_t g = 0; g < sm.size(); g += 8) {
+        const int cnt = (int)std::min<size_t>(8, sm.size() - g);
+        iworkS.push_back(RowBlock{-1 - (int)(small.size() / 8), cnt});
+        for (int q = 0; q < 8; ++q) small.push_back(q < cnt ? sm[g + q] : -1);
+        anySmall = true;
+      }
+      for (int d : lv)
+        if (!(S.nodes[d].n <= IW_N && S.nodes[d].m() <= ICH))
+          for (int c = 0; c < std::max(1, nodes_[d].nch); ++c) iworkS.push_back(RowBlock{d, c});
+      lvRange.push_back({b0, iworkS.size()});
+    }
+    for (int l = (int)lvRange.size() - 1; l >= 0; --l)
+      iworkSB.insert(iworkSB.end(), iworkS.begin() + lvRange[l].first, iworkS.begin() + lvRange[l].second);
+    smemWarps_ = anySmall ? sizeof(T) * 8 * (IW_N + ICH) : 0;
+  }
   for (size_t v : smemIB_)
     if (v > 200 * 1024) throw std::runtime_error("interior front too large for the shared-memory solve");
   // compressed levels: (supernode, 64-row block) work lists
@@ -804,6 +934,10 @@ void SolveEngine<T>::plan() {
   up(dIWork_, iwork.data(), iwork.size() * sizeof(RowBlock));
   up(dIWorkB_, iworkB.data(), iworkB.size() * sizeof(RowBlock));
   nIWork_ = (int)iwork.size();
+  up(dIWorkS_, iworkS.data(), iworkS.size() * sizeof(RowBlock));
+  up(dIWorkSB_, iworkSB.data(), iworkSB.size() * sizeof(RowBlock));
+  up(dSmall_, small.data(), small.size() * sizeof(int));
+  nIWorkS_ = (int)iworkS.size();
   wuTotal_ = wuCur;
   ipTotal_ = ipCur;
   maxNI_ = 0;
@@ -971,8 +1105,8 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
     RSCHOL_CUDA(cudaMemsetAsync(dSync_.p, 0, sizeof(int) * syncInts_, st));
     epoch_ = 1;
   }
-  if (nIWork_ > 0) {
-    launch_k(interior_forward_chunks<T>, dim3(nIWork_), dim3(256), smemIFmax_, st, dNodes_.as<SNode<T>>(), dIWork_.as<RowBlock>(), dRel_.as<int>(), dChild_.as<int>(), sync, epoch_, w, dYi_.as<T>(), dWu_.as<T>());
+  if (nIWorkS_ > 0) {
+    launch_k(interior_forward_chunks<T>, dim3(nIWorkS_), dim3(256), std::max(smemIFmax_, smemWarps_), st, dNodes_.as<SNode<T>>(), dIWorkS_.as<RowBlock>(), dRel_.as<int>(), dChild_.as<int>(), sync, epoch_, w, dYi_.as<T>(), dWu_.as<T>(), dSmall_.as<int>());
     RSCHOL_LAUNCH_CHECK();
   }
   T* yv = dYi_.as<T>();
@@ -1000,8 +1134,8 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
     launch_k(compressed_x_reduce<T>, dim3(cColGrid_[l], cLevels_[l].second), dim3(256), 0, st, dNodes_.as<SNode<T>>(), lv, dXp_.as<T>(), w);
     RSCHOL_LAUNCH_CHECK();
   }
-  if (nIWork_ > 0) {
-    launch_k(interior_backward_chunks<T>, dim3(nIWork_), dim3(256), smemIBmax_, st, dNodes_.as<SNode<T>>(), dIWorkB_.as<RowBlock>(), dRows_.as<int>(), sync, epoch_, dIp_.as<T>(), dYi_.as<T>(), w);
+  if (nIWorkS_ > 0) {
+    launch_k(interior_backward_chunks<T>, dim3(nIWorkS_), dim3(256), std::max(smemIBmax_, smemWarps_), st, dNodes_.as<SNode<T>>(), dIWorkSB_.as<RowBlock>(), dRows_.as<int>(), sync, epoch_, dIp_.as<T>(), dYi_.as<T>(), w, dSmall_.as<int>());
     RSCHOL_LAUNCH_CHECK();
   }
   if (!std::is_same<T, double>::value) {

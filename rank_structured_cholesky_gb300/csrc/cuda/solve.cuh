@@ -128,6 +128,11 @@ class SolveEngine {
   DevBuf dDinv_, dDinvTasks_, dZp_, dSp_, dIp_, dYi_, dSync_, dTickF_, dIWork_, dIWorkB_;
   int nIWork_ = 0;
   size_t smemIFmax_ = 8, smemIBmax_ = 8;
+  // single-vector apply: work lists with the small interior supernodes in
+  // groups of eight (a warp each; group members in dSmall_)
+  DevBuf dIWorkS_, dIWorkSB_, dSmall_;
+  int nIWorkS_ = 0;
+  size_t smemWarps_ = 0;
   int epoch_ = 0;                     // apply counter: the interior completion targets
   DevBuf dX_, dT1_, dXGemm_;          // compressed L11^{-1}, its temporaries and GEMM tasks
   DevBuf dXp_, dTiles_;               // tile partials of the X products, tile lists
