@@ -321,10 +321,16 @@ def run_ours(args):
     stats = F.stats()
     desc = F.describe()
 
-    # end to end through the C ABI with host buffers (copies inside the timed region)
-    h_vals = prob.vals
-    h_b = np.ascontiguousarray(prob.rhs[:nrhs])
-    h_x = np.zeros_like(h_b)
+    # end to end through the C ABI with host buffers (copies inside the timed
+    # region, from and to pinned host memory)
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float64).pin_memory()
+        arr = t.numpy()
+        arr[...] = a
+        return t, arr
+    _pv, h_vals = pinned(prob.vals)
+    _pb, h_b = pinned(np.ascontiguousarray(prob.rhs[:nrhs]))
+    _px, h_x = pinned(np.zeros((nrhs, n)))
     infos = (rs.PcgInfo * nrhs)()
 
     def step_e2e():

@@ -177,6 +177,7 @@ struct rschol_factor {
   std::vector<int> permCsrSrc;  // permuted CSR value k = Afull.x[permCsrSrc[k]]
   DevBuf dPerm, dB, dX, dBp, dXp, dLowerSrc, dCsrSrc;
   DevBuf dBk, dXk;   // batched right-hand sides / solutions, n x k row-major, permuted
+  DevBuf dVals;      // rschol_refactor: the caller's values, staged on the device
   int kCap = 0;
   int nrhsCap = 0;
   double tSymbolic = 0, tNumeric = 0;
@@ -350,22 +351,15 @@ int rschol_refactor(rschol_factor* f, const double* vals) {
   if (!f || !vals) return RSCHOL_E_BAD_INPUT;
   AccountScope acct(&f->devBytes);
   try {
-    std::vector<double> lower(f->lowerSrc.size());
-    for (size_t k = 0; k < lower.size(); ++k) lower[k] = vals[f->lowerSrc[k]];
-    f->A.x = lower;
-    f->Afull.x.assign(vals, vals + f->Afull.p[f->Afull.n]);
-    std::vector<double> cv(f->permCsrSrc.size());
-    for (size_t k = 0; k < cv.size(); ++k) cv[k] = vals[f->permCsrSrc[k]];
-    f->impl->set_values(lower.data());
-    f->pcg->set_values(cv);
-    if (f->attempts > 1) {   // the ranks of a previous retry do not carry over
-      assign_ranks(f->S, f->prm, f->prm.rank_constant, f->prm.diag_rank_constant);
-      f->impl->plan();
-    }
-    return numeric_with_retry(f);
+    // one copy of the caller's values, then the device path's gathers into
+    // the factor's lower triangle and the PCG's permuted CSR
+    const size_t nnz = (size_t)f->Afull.p[f->Afull.n];
+    f->dVals.alloc(sizeof(double) * std::max<size_t>(1, nnz));
+    RSCHOL_CUDA(cudaMemcpyAsync(f->dVals.p, vals, sizeof(double) * nnz, cudaMemcpyHostToDevice, f->ctx->stream));
   } catch (const std::exception& e) {
     return fail(f->ctx, RSCHOL_E_CUDA, e.what());
   }
+  return rschol_refactor_device(f, f->dVals.as<double>());
 }
 
 static void ensure_vecs(rschol_factor* f, int nrhs);

@@ -542,14 +542,15 @@ __global__ void __launch_bounds__(256) chol_fused_kernel(const CholFusedJob<T>* 
   int* tdone = cnt + j.TR * j.TU;  // TR: panels whose TRSM of row tile a is done
   int* pdone = tdone + j.TR;       // P: POTRF of panel p done
   const int p = it.p, a = it.a, b = it.b;
-  auto bnd = [&](int t) { return t == 0 ? 0 : j.w0 + 64 * (t - 1); };
+  auto bnd = [&](int t) { return t == 0 ? 0 : j.w0 + 64 * (t - 1); };      // columns (and Cholesky rows)
+  auto rbnd = [&](int t) { return t == 0 ? 0 : j.r1 + 64 * (t - 1); };     // rows
   const int c0 = bnd(p), wp = bnd(p + 1) - c0;
   if ((threadIdx.x >> 5) == 0) {
     bool ok;
-    if (it.kind == CHOL_POTRF) ok = wait_geq(cnt + p * j.TU + p, p, err);
+    if (it.kind == CHOL_POTRF) ok = j.L ? true : wait_geq(cnt + p * j.TU + p, p, err);
     else if (it.kind == CHOL_TRSM) ok = wait_geq(pdone + p, 1, err) && wait_geq(cnt + a * j.TU + p, p, err);
     else
-      ok = wait_geq(tdone + a, p + 1, err) && wait_geq(tdone + b, p + 1, err) &&
+      ok = wait_geq(tdone + a, p + 1, err) && (j.L || wait_geq(tdone + b, p + 1, err)) &&
            wait_geq(cnt + a * j.TU + b, p, err);
     if (threadIdx.x == 0) {
       sOk = ok;
@@ -563,13 +564,15 @@ __global__ void __launch_bounds__(256) chol_fused_kernel(const CholFusedJob<T>* 
   int* done;
   int doneVal;
   if (it.kind == CHOL_POTRF) {
-    T* A = F + (size_t)c0 * ld + c0;
-    potrf_tile_reg<T>(A, ld, wp, j.code, flag);
-    if (c0 + wp < j.nRows) {   // rows below: the TRSM items multiply by the inverse
+    // Cholesky job: factor the diagonal tile; TRSM job: L is factored already
+    T* A = j.L ? const_cast<T*>(j.L) + (size_t)c0 * j.ldl + c0 : F + (size_t)c0 * ld + c0;
+    const int lda = j.L ? j.ldl : ld;
+    if (!j.L) potrf_tile_reg<T>(A, ld, wp, j.code, flag);
+    if (j.L || c0 + wp < j.nRows) {   // rows below: the TRSM items multiply by the inverse
       T (*L)[65] = reinterpret_cast<T (*)[65]>(cf_smem);
       T (*Li)[65] = reinterpret_cast<T (*)[65]>(cf_smem + sizeof(T) * 64 * 65);
       T (*Tm)[16][17] = reinterpret_cast<T (*)[16][17]>(cf_smem + 2 * sizeof(T) * 64 * 65);
-      tile_inverse<T>(A, ld, wp, L, Li, Tm);
+      tile_inverse<T>(A, lda, wp, L, Li, Tm);
       T* out = ws + j.inv + (size_t)p * 4096;
 #pragma unroll
       for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) out[idx] = Li[idx >> 6][idx & 63];
@@ -583,20 +586,21 @@ __global__ void __launch_bounds__(256) chol_fused_kernel(const CholFusedJob<T>* 
 #pragma unroll
     for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) Li[idx >> 6][idx & 63] = __ldcg(in + idx);
     __syncthreads();
-    const int r0 = bnd(a);
-    trsm_chunk_mul<T>(F + (size_t)r0 * ld + c0, ld, min(bnd(a + 1), j.nRows) - r0, wp, X, Li);
+    const int r0 = rbnd(a);
+    trsm_chunk_mul<T>(F + (size_t)r0 * ld + c0, ld, min(rbnd(a + 1), j.nRows) - r0, wp, X, Li);
     done = tdone + a;
     doneVal = p + 1;
   } else {
-    const int r0 = bnd(a), q0 = bnd(b);
+    const int r0 = rbnd(a), q0 = bnd(b);
     GemmTask<T> g;
     g.A = F + (size_t)r0 * ld + c0;
-    g.B = F + (size_t)q0 * ld + c0;
+    g.B = j.L ? j.L + (size_t)q0 * j.ldl + c0 : F + (size_t)q0 * ld + c0;   // TRSM job: X(a) L(b, p)^T
     g.C = F + (size_t)r0 * ld + q0;
-    g.M = min(bnd(a + 1), j.nRows) - r0;
+    g.M = min(rbnd(a + 1), j.nRows) - r0;
     g.N = min(bnd(b + 1), j.nUpd) - q0;
     g.K = wp;
-    g.lda = g.ldb = g.ldc = ld;
+    g.lda = g.ldc = ld;
+    g.ldb = j.L ? j.ldl : ld;
     g.tA = 0;
     g.tB = 1;
     g.lower = 0;

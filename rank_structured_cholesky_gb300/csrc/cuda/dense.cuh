@@ -64,6 +64,10 @@ struct TrsmTask {
 // Panels: the first w0 = nDiag - 64 (P - 1) wide, then 64; tile t spans rows
 // [b(t), b(t + 1)), b(0) = 0, b(t) = w0 + 64 (t - 1); TR / TU tiles cover
 // nRows / nUpd.
+// A TRSM job (L != null) is the same launch's B := B L^{-T} for a factored
+// w x w lower L (ld ldl) and F = B (nRows x w, ld): "POTRF" items only
+// invert L's diagonal tiles (no wait), the updates are X(a) L(b, p)^T, and B's
+// rows are cut at 0, r1 = 64, 128, ... (a Cholesky job has r1 = w0).
 template <class T>
 struct CholFusedJob {
   T* F;
@@ -71,6 +75,8 @@ struct CholFusedJob {
   int w0, P, TR, TU;
   int cnt;          // offset of the job's TR x TU + TR + P counters after the ticket
   long long inv;    // element offset of the job's P inverse tiles (64 x 64) in the workspace
+  const T* L;       // TRSM job: the factored triangle (null for a Cholesky job)
+  int ldl, r1;      // r1: height of the first row tile
 };
 constexpr int CHOL_POTRF = 0, CHOL_TRSM = 1, CHOL_GEMM = 2;
 struct CholItem {   // one piece of panel p: POTRF, TRSM of row tile a, update of tile (a, b)

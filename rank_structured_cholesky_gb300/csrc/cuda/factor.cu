@@ -185,6 +185,7 @@ void FactorEngine<T>::emit_chol(const std::vector<CholJob<T>>& jobs) {
       auto tiles = [&](int n) { return n <= c.w0 ? 1 : 1 + (n - c.w0 + NB - 1) / NB; };
       c.TR = tiles(jb.nRows);
       c.TU = tiles(jb.nUpd);
+      c.r1 = c.w0;
       c.cnt = (int)(sync - 1);
       sync += (long long)c.TR * c.TU + c.TR + c.P;
       c.inv = ws;
@@ -277,6 +278,64 @@ void FactorEngine<T>::emit_chol(const std::vector<CholJob<T>>& jobs) {
 
 template <class T>
 void FactorEngine<T>::emit_trsm(const std::vector<TrsmJob<T>>& jobs) {
+  if (fusedChol_) {   // one ticketed launch (TRSM jobs of the fused Cholesky kernel)
+    Step st{ST_CHOL, (long long)cholItems_.size(), 0, 0};
+    const int j0 = (int)cholJobs_.size();
+    long long sync = 1, ws = 0;
+    int maxP = 0;
+    for (const auto& jb : jobs) {
+      if (jb.w <= 0 || jb.rows <= 0) continue;
+      CholFusedJob<T> c{};
+      c.F = jb.B;
+      c.ld = jb.ldb;
+      c.nDiag = jb.w;
+      c.nRows = jb.rows;
+      c.nUpd = jb.w;
+      c.L = jb.L;
+      c.ldl = jb.ldl;
+      c.r1 = NB;
+      c.P = (jb.w + NB - 1) / NB;
+      c.w0 = jb.w - NB * (c.P - 1);
+      c.TR = (jb.rows + NB - 1) / NB;
+      c.TU = c.P;
+      c.cnt = (int)(sync - 1);
+      sync += (long long)c.TR * c.TU + c.TR + c.P;
+      c.inv = ws;
+      ws += (long long)c.P * NB * NB;
+      maxP = std::max(maxP, c.P);
+      cholJobs_.push_back(c);
+      for (int p = 0; p < c.P; ++p) {   // algorithmic flops, as the per-panel steps count them
+        const int c0 = p == 0 ? 0 : c.w0 + NB * (p - 1), w = p == 0 ? c.w0 : NB;
+        flops += (double)jb.rows * w * w + 2.0 * jb.rows * (double)(jb.w - c0 - w) * w;
+      }
+    }
+    const int j1 = (int)cholJobs_.size();
+    // all diagonal inverses first (no waits), then stage p: the TRSMs of panel
+    // p, the rest of panel p - 1's updates, panel p's updates of column tile p + 1
+    for (int q = j0; q < j1; ++q)
+      for (int p = 0; p < cholJobs_[q].P; ++p) cholItems_.push_back(CholItem{q, CHOL_POTRF, p, p, p});
+    auto updates = [&](int q, int p, int bLo, int bHi) {
+      const CholFusedJob<T>& c = cholJobs_[q];
+      for (int b = std::max(bLo, p + 1); b < std::min(bHi, c.TU); ++b)
+        for (int a = 0; a < c.TR; ++a) cholItems_.push_back(CholItem{q, CHOL_GEMM, p, a, b});
+    };
+    for (int p = 0; p <= maxP; ++p) {
+      for (int q = j0; q < j1; ++q)
+        if (p < cholJobs_[q].P)
+          for (int a = 0; a < cholJobs_[q].TR; ++a) cholItems_.push_back(CholItem{q, CHOL_TRSM, p, a, p});
+      for (int q = j0; q < j1; ++q)
+        if (p >= 1 && p <= cholJobs_[q].P) updates(q, p - 1, p + 1, INT_MAX);
+      for (int q = j0; q < j1; ++q)
+        if (p < cholJobs_[q].P) updates(q, p, p + 1, p + 2);
+    }
+    st.count = st.grid = (int)(cholItems_.size() - st.off);
+    st.elems = sync;
+    if (st.count == 0) return;
+    cholSync_ = std::max(cholSync_, sync);
+    cholWs_ = std::max(cholWs_, ws);
+    steps_.push_back(st);
+    return;
+  }
   int maxW = 0;
   for (auto& j : jobs) maxW = std::max(maxW, j.rows > 0 ? j.w : 0);
   for (int kb = 0; kb < maxW; kb += NB) {
