@@ -203,9 +203,9 @@ def run_reference(args):
     return 0
 
 
-def traffic_from_profiles(kernel):
+def traffic_from_profiles(kernel, workload="c2"):
     """dram bytes per launch of `kernel` from the committed ncu summary, or None."""
-    path = os.path.join(ROOT, "profiles", "%s_c2.md" % kernel)
+    path = os.path.join(ROOT, "profiles", "%s_%s.md" % (kernel, workload))
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -391,19 +391,25 @@ def run_ours(args):
                    "sample": "one full %s solve (symbolic + FP64 factor + PCG to 1e-8, %d iterations) with the "
                              "CPU oracle, threaded BLAS" % (args.config, res["iterations"]),
                    "factor_s": res["factor_s"], "pcg_s": res["pcg_s"], "iterations": res["iterations"]}
-        # roofline of the dominant kernel family (the factor's GEMMs), timed
-        # with CUDA events around every GEMM launch of the instrumented pass
-        # of the K timed steps
+        # rooflines of the dominant kernel (the fused blocked Cholesky / TRSM
+        # launches, chol_fused_kernel, 22.5% of the c2 launch list) and of the
+        # remaining GEMM launches, timed with CUDA events around every factor
+        # step of the instrumented pass of the K timed steps
         c = main["counters"]
-        gemm_ms, gemm_launch, gemm_flops = c[0], c[1], c[2]
         step_total_ms = sum(main["step_ms"])
-        achieved = gemm_flops / (gemm_ms * 1e-3) / 1e12 if gemm_ms > 0 else 0.0
-        roof = {"bound": "tensor", "kernel": "factor GEMMs (gemm_kernel SIMT and gemm_tc_kernel tcgen05)",
-                "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
-                "traffic": traffic_from_profiles("gemm_kernel"), "peak_source": src,
-                "flops_per_launch": gemm_flops / max(gemm_launch, 1),
-                "launch_ms": gemm_ms / max(gemm_launch, 1), "launches_per_step": gemm_launch / args.steps,
-                "share_of_step_time": gemm_ms / step_total_ms if step_total_ms else None}
+
+        def roofline(kernel, ms, launches, flops, traffic, traffic_source):
+            achieved = flops / (ms * 1e-3) / 1e12 if ms > 0 else 0.0
+            return {"bound": "tensor", "kernel": kernel, "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                    "frac": achieved / bf16, "traffic": traffic, "traffic_source": traffic_source,
+                    "peak_source": src, "flops_per_launch": flops / max(launches, 1),
+                    "launch_ms": ms / max(launches, 1), "launches_per_step": launches / args.steps,
+                    "share_of_step_time": ms / step_total_ms if step_total_ms else None}
+        roof = roofline("chol_fused_kernel (blocked Cholesky and TRSM chains of a level, FP32 SIMT, ticketed tiles)",
+                        c[21], c[22], c[23], traffic_from_profiles("chol_fused_kernel", "c2s"),
+                        "dram bytes per launch, averaged over the c2s launches of profiles/chol_fused_kernel_c2s.md")
+        roof_gemm = roofline("factor GEMMs (gemm_kernel SIMT and gemm_tc_kernel tcgen05)", c[0], c[1], c[2],
+                             traffic_from_profiles("gemm_kernel"), "profiles/gemm_kernel_c2.md")
         apply_bytes = phase["apply_bytes"]
         its = main["iterations"][0]
         pcg_bytes = its * (apply_bytes + phase["spmv_bytes"] + 8.0 * 10 * n)
@@ -426,7 +432,7 @@ def run_ours(args):
                     "h2d_bytes_per_step": int(prob.vals.nbytes + h_b.nbytes),
                     "d2h_bytes_per_step": int(h_x.nbytes)},
             "gpu_launches": int(args.steps * (phase["factor_launches"] + phase["pcg_launches"])),
-            "roofline": roof,
+            "roofline": roof, "roofline_gemm": roof_gemm,
             "roofline_pcg": roof_pcg,
             "cpu_baseline": cpu,
             "clocks": main["clocks"],

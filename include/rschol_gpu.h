@@ -188,9 +188,10 @@ void rschol_server_destroy(rschol_server* s);
 /* Diagnostics (no reference counterpart): CUDA-event timing of every step of
  * the numeric factorisation while enabled.  out (may be null, else 24
  * doubles) receives, for step kinds 0..7 (GEMM, POTRF, TRSM, extend-add, QR,
- * identity basis, -, fused blocked Cholesky), 3 values each: device milliseconds, launches and GEMM flops accumulated
- * since timing was last switched on; enable = 1 also resets them when timing
- * was off. */
+ * identity basis, -, fused blocked Cholesky / TRSM), 3 values each: device
+ * milliseconds, launches and algorithmic flops (GEMM and fused steps)
+ * accumulated since timing was last switched on; enable = 1 also resets them
+ * when timing was off. */
 int rschol_step_timing(rschol_factor* f, int enable, double* out);
 
 /* Diagnostics (no reference counterpart): one tensor-core GEMM

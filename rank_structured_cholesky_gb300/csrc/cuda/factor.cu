@@ -33,7 +33,7 @@ FactorEngine<T>::FactorEngine(const Symbolic& S_, const CSC& A_, const Params& p
   dFlag.alloc(2 * sizeof(int));
   useTc_ = std::is_same<T, float>::value && tensor_cores_enabled();
   const char* fc = std::getenv("RSCHOL_FUSED_CHOL");
-  fusedChol_ = std::is_same<T, float>::value && !(fc && fc[0] == '0');
+  fusedChol_ = !(fc && fc[0] == '0');
   const char* g = std::getenv("RSCHOL_GRAPHS");
   useGraphs_ = !(g && g[0] == '0');
   RSCHOL_CUDA(cudaStreamSynchronize(stream));
@@ -168,6 +168,7 @@ template <class T>
 void FactorEngine<T>::emit_chol(const std::vector<CholJob<T>>& jobs) {
   if (fusedChol_) {
     Step st{ST_CHOL, (long long)cholItems_.size(), 0, 0};
+    const double flops0 = flops;
     const int j0 = (int)cholJobs_.size();
     long long sync = 1, ws = 0;   // sync[0]: the ticket
     int maxP = 0;
@@ -224,6 +225,7 @@ void FactorEngine<T>::emit_chol(const std::vector<CholJob<T>>& jobs) {
     }
     st.count = st.grid = (int)(cholItems_.size() - st.off);
     st.elems = sync;
+    st.flops = flops - flops0;
     if (st.count == 0) return;
     cholSync_ = std::max(cholSync_, sync);
     cholWs_ = std::max(cholWs_, ws);
@@ -280,6 +282,7 @@ template <class T>
 void FactorEngine<T>::emit_trsm(const std::vector<TrsmJob<T>>& jobs) {
   if (fusedChol_) {   // one ticketed launch (TRSM jobs of the fused Cholesky kernel)
     Step st{ST_CHOL, (long long)cholItems_.size(), 0, 0};
+    const double flops0 = flops;
     const int j0 = (int)cholJobs_.size();
     long long sync = 1, ws = 0;
     int maxP = 0;
@@ -330,6 +333,7 @@ void FactorEngine<T>::emit_trsm(const std::vector<TrsmJob<T>>& jobs) {
     }
     st.count = st.grid = (int)(cholItems_.size() - st.off);
     st.elems = sync;
+    st.flops = flops - flops0;
     if (st.count == 0) return;
     cholSync_ = std::max(cholSync_, sync);
     cholWs_ = std::max(cholWs_, ws);
@@ -1087,6 +1091,7 @@ int FactorEngine<T>::run() {
       const int k = steps_[q].kind == ST_GEMM_REDUCE ? (int)ST_GEMM : steps_[q].kind;
       stepMs[k] += ms;
       stepCount[k] += 1;
+      stepFlops[k] += steps_[q].flops;
     }
     for (const Step& st : steps_)
       if (st.kind == ST_GEMM)

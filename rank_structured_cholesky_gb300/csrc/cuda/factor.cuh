@@ -57,6 +57,7 @@ struct Step {
   int aux = 0;      // ST_QR: largest row count of the batch (grid: largest rank);
                     // ST_GEMM: 1 on the tensor cores
   long long elems = 0;   // ST_GEMM_REDUCE: elements of C summed; ST_CHOL: ints of its counters
+  double flops = 0;      // ST_CHOL: algorithmic flops of the launch
 };
 
 template <class T>
@@ -171,8 +172,9 @@ class FactorEngine {
   DevBuf dSplitWs_, dSplitIds_, dSplitBase_;
   long long qrWs_ = 0;   // elements of the Householder QR workspace (largest QR step)
   DevBuf dQrWs_;
-  // The blocked Cholesky of each emit_chol call as one ticketed launch (FP32;
-  // RSCHOL_FUSED_CHOL=0 keeps the POTRF / TRSM / GEMM steps per panel).
+  // The blocked Cholesky of each emit_chol call, and the blocked TRSM of each
+  // emit_trsm call, as one ticketed launch (RSCHOL_FUSED_CHOL=0 keeps the
+  // POTRF / TRSM / GEMM steps per panel).
   bool fusedChol_ = false;
   std::vector<CholFusedJob<T>> cholJobs_;
   std::vector<CholItem> cholItems_;
