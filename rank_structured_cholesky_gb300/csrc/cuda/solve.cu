@@ -545,7 +545,9 @@ __device__ void cg_row(const SNode<T>& nd, int i, const T* sv, T* yv) {
 // One launch per piece and level, chained by programmatic dependent launch.
 // (All levels of a direction as one ticketed launch, with each phase waiting
 // on the previous one through counters, measured slower on c2: 1.19 vs 1.07
-// ms per apply -- the dependent launches already start without gaps.)
+// ms per apply -- the dependent launches already start without gaps; running
+// the y and x reductions at the tail of the tile launches, by the last tile
+// of each block, measured the same: 0.936 vs 0.919 ms.)
 template <class T>
 __global__ void __launch_bounds__(256) compressed_gather_rows(const SNode<T>* __restrict__ nodes,
                                                               const int* __restrict__ lvl,
