@@ -206,3 +206,19 @@ def test_batched_pcg_many_columns_and_groups():
     for k in range(70):
         assert np.linalg.norm(B[k] - A @ X[k]) / np.linalg.norm(B[k]) <= 1e-8
     assert abs(infos[0]["iterations"] - i1["iterations"]) <= 1
+
+
+@pytest.mark.parametrize("precision,tol", [(rs.FP64, APPLY_TOL), (rs.MIXED, 1e-3)])
+def test_fused_and_per_panel_factor_paths_agree(precision, tol, oracles, monkeypatch):
+    """The fused level launches (default) and the per-panel POTRF / TRSM / GEMM
+    steps (RSCHOL_FUSED_CHOL=0) block the same factorisation differently; both
+    must match the oracle's preconditioner, and each other, within the apply
+    tolerance of their precision."""
+    prob, params, O = oracles("3d16")
+    b = prob.rhs[0]
+    y_fused = gpu_factor(prob, params, precision=precision).apply(b)
+    monkeypatch.setenv("RSCHOL_FUSED_CHOL", "0")
+    y_panel = gpu_factor(prob, params, precision=precision).apply(b)
+    y_ref = O.apply(b)
+    assert rel(y_fused, y_ref) < tol and rel(y_panel, y_ref) < tol
+    assert rel(y_fused, y_panel) < tol
