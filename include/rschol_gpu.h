@@ -133,6 +133,18 @@ int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x
  * rschol_factor_describe ("batch_tuning": class, RA, RC, cwR, cwC, ms). */
 int rschol_factor_autotune(rschol_factor* f, int max_columns);
 
+/* Autotuner of the factor's schedule (no reference counterpart): times
+ * `repeats` numeric factorisations of the factor's current values under each
+ * candidate -- FP32 GEMM steps on the tensor cores (128 x 64 tiles) from
+ * K >= 128, from K >= 256, or none (64 x 64 SIMT tiles); the blocked Cholesky
+ * and TRSM chains of a level as one fused launch of 64 x 64 tile items or as
+ * one launch per 64-column panel -- keeps the fastest and leaves the factor
+ * refactored with it.  The candidates differ only in rounding.  Run it while
+ * the GPU is otherwise quiet, before creating sessions on the factor.  The
+ * choice is listed in rschol_factor_describe ("schedule": tc_min_k (-1: none),
+ * fused, tuned_ms). */
+int rschol_factor_tune_schedule(rschol_factor* f, int repeats);
+
 /* ---- continuous batching on one factor (no reference counterpart) --------
  * A session keeps the Krylov state of up to max_columns right-hand sides of
  * one factor on the device (clamped to the factor's batch capacity, at most

@@ -37,7 +37,7 @@ EXPORTED = [
     "rschol_factor_describe", "rschol_factor_stats", "rschol_problem_diffusion", "rschol_problem_elasticity",
     "rschol_problem_n", "rschol_problem_nnz", "rschol_problem_nrhs", "rschol_problem_get", "rschol_problem_free",
     "rschol_mt_draws", "rschol_mt_gaussians", "rschol_block_rank", "rschol_separator_tree", "rschol_etree_counts",
-    "rschol_relaxed_supernodes", "rschol_factor_autotune", "rschol_session_create", "rschol_session_columns", "rschol_session_add",
+    "rschol_relaxed_supernodes", "rschol_factor_autotune", "rschol_factor_tune_schedule", "rschol_session_create", "rschol_session_columns", "rschol_session_add",
     "rschol_session_step", "rschol_session_result", "rschol_session_counts", "rschol_session_destroy",
     "rschol_server_create", "rschol_server_submit", "rschol_server_wait",
     "rschol_server_stats", "rschol_server_destroy",
@@ -121,6 +121,7 @@ def load_library():
         "rschol_etree_counts": (None, [I, P, P, P, P]),
         "rschol_relaxed_supernodes": (I, [I, P, P, I, P, P, P, P, I, P, P]),
         "rschol_factor_autotune": (I, [P, I]),
+        "rschol_factor_tune_schedule": (I, [P, I]),
         "rschol_session_create": (P, [P, I]),
         "rschol_session_columns": (I, [P]),
         "rschol_session_add": (I, [P, LL, I, pD, pD, D, I]),
@@ -273,6 +274,14 @@ class GpuFactor:
         st = load_library().rschol_factor_autotune(self.h, max_columns)
         if st != RSCHOL_OK:
             raise RscholError(st, self.ctx.last_error())
+
+    def tune_schedule(self, repeats=2):
+        """Time the factor's candidate schedules (tensor-core GEMM threshold, fused or
+        per-panel blocked Cholesky) and keep the fastest; the factor stays factored."""
+        st = load_library().rschol_factor_tune_schedule(self.h, repeats)
+        if st != RSCHOL_OK:
+            raise RscholError(st, self.ctx.last_error())
+        return self.describe()["schedule"]
 
     def num_nodes(self):
         return load_library().rschol_factor_num_nodes(self.h)

@@ -1,6 +1,7 @@
 // C ABI (include/rschol_gpu.h): FactorPreconditioner / PCG_SOLVER /
 // pcg_pysolve replacements on one GB300.
 #include <algorithm>
+#include <climits>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -72,6 +73,9 @@ struct Impl {
   virtual size_t bytes() const = 0;
   virtual std::vector<std::array<double, 6>> batch_tuning() const = 0;
   virtual void autotune_batch(int kmax, cudaStream_t s) = 0;
+  virtual void set_schedule(int tcMinK, bool fused) = 0;
+  virtual int tc_min_k() const = 0;
+  virtual bool fused_chol() const = 0;
   virtual void node_l11(int j, double* out) = 0;
   virtual void node_l21(int j, double* out) = 0;
 };
@@ -87,6 +91,9 @@ struct ImplT : Impl {
     fe.plan();
     se.plan();
   }
+  void set_schedule(int tcMinK, bool fused) override { fe.set_schedule(tcMinK, fused); }
+  int tc_min_k() const override { return fe.tc_min_k(); }
+  bool fused_chol() const override { return fe.fused_chol(); }
   int run() override { return fe.run(); }
   void apply(double* w, cudaStream_t s) override { se.apply_inplace(w, s); }
   int apply_error(cudaStream_t s) override { return se.take_error(s); }
@@ -183,6 +190,7 @@ struct rschol_factor {
   double tSymbolic = 0, tNumeric = 0;
   int attempts = 0;
   double diagRankConstant = 0.5;
+  double tunedMs = 0;   // rschol_factor_tune_schedule: the chosen schedule's factorisation time
   std::string desc;
 };
 
@@ -652,7 +660,10 @@ const char* rschol_factor_describe(rschol_factor* f) {
     << ", \"factor_flops\": " << f->impl->flops() << ", \"apply_bytes\": " << f->impl->apply_bytes()
     << ", \"spmv_bytes\": " << f->pcg->spmvBytes << ", \"device_bytes\": " << f->impl->bytes()
     << ", \"symbolic_s\": " << f->tSymbolic << ", \"numeric_s\": " << f->tNumeric
-    << ", \"attempts\": " << f->attempts << ", \"batch_tuning\": [";
+    << ", \"attempts\": " << f->attempts << ", \"schedule\": {\"tc_min_k\": "
+    << (f->impl->tc_min_k() == INT_MAX ? -1 : f->impl->tc_min_k())
+    << ", \"fused\": " << (f->impl->fused_chol() ? "true" : "false") << ", \"tuned_ms\": " << f->tunedMs
+    << "}, \"batch_tuning\": [";
   bool first = true;
   for (const auto& row : f->impl->batch_tuning()) {   // per width class: class, RA, RC, cwR, cwC, ms
     o << (first ? "" : ", ") << "[" << row[0] << ", " << row[1] << ", " << row[2] << ", " << row[3] << ", " << row[4]
@@ -863,6 +874,57 @@ extern "C" int rschol_factor_autotune(rschol_factor* f, int max_columns) {
     return fail(f->ctx, RSCHOL_E_CUDA, e.what());
   }
   return RSCHOL_OK;
+}
+
+extern "C" int rschol_factor_tune_schedule(rschol_factor* f, int repeats) {
+  if (!f || repeats < 1) return RSCHOL_E_BAD_INPUT;
+  AccountScope acct(&f->devBytes);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  try {
+    cudaStream_t s = f->ctx->stream;
+    RSCHOL_CUDA(cudaEventCreate(&e0));
+    RSCHOL_CUDA(cudaEventCreate(&e1));
+    std::vector<int> ks = {INT_MAX};
+    if (f->precision == RSCHOL_MIXED) ks = {128, 256, INT_MAX};
+    int bestK = f->impl->tc_min_k();
+    bool bestFused = f->impl->fused_chol();
+    double best = 1e300;
+    for (int k : ks)
+      for (bool fused : {true, false}) {
+        f->impl->set_schedule(k, fused);
+        f->impl->plan();
+        // the first run launches directly, the second captures the graph;
+        // the timed ones replay it, as every later refactorisation does
+        if (f->impl->run() != 0 || f->impl->run() != 0) continue;
+        double ms = 0;
+        bool ok = true;
+        for (int r = 0; r < repeats && ok; ++r) {
+          RSCHOL_CUDA(cudaEventRecord(e0, s));
+          ok = f->impl->run() == 0;
+          RSCHOL_CUDA(cudaEventRecord(e1, s));
+          RSCHOL_CUDA(cudaEventSynchronize(e1));
+          float t = 0;
+          RSCHOL_CUDA(cudaEventElapsedTime(&t, e0, e1));
+          ms += t;
+        }
+        if (ok && ms / repeats < best) {
+          best = ms / repeats;
+          bestK = k;
+          bestFused = fused;
+        }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    e0 = e1 = nullptr;
+    f->impl->set_schedule(bestK, bestFused);
+    f->impl->plan();
+    f->tunedMs = best < 1e300 ? best : 0;
+  } catch (const std::exception& e) {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return fail(f->ctx, RSCHOL_E_CUDA, e.what());
+  }
+  return numeric_with_retry(f);
 }
 
 extern "C" rschol_session* rschol_session_create(rschol_factor* f, int max_columns) {

@@ -74,7 +74,7 @@ void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
   // updates gained, the K = 64 steps turned latency-bound in the epilogue)
   int maxK = 0;
   for (auto& t : batch) maxK = std::max(maxK, t.K);
-  const bool tc = useTc_ && maxK >= 128;
+  const bool tc = useTc_ && maxK >= tcMinK_;
   const int rowsPerTile = tc ? 128 : 64;
   long long baseTiles = 0;
   for (auto& t : batch) baseTiles += (long long)((t.M + rowsPerTile - 1) / rowsPerTile) * ((t.N + 63) / 64);

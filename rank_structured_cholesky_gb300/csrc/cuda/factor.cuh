@@ -150,9 +150,20 @@ class FactorEngine {
   void gemm1(const GemmTask<T>& t);   // a single-task GEMM step
   void gemm_launch(const Step& st);    // SIMT kernel, or the tensor cores for FP32
   bool useTc_ = false;
+  int tcMinK_ = 128;
 
  public:
   bool tensor_cores() const { return useTc_; }   // FP32 GEMMs on tcgen05
+  // Schedule options timed by the factor tuner (taking effect at the next
+  // plan()): FP32 GEMM steps go to the tensor cores from K >= tcMinK
+  // (INT_MAX: never); fused level launches for the blocked Cholesky and TRSM
+  // chains, or one launch per 64-column panel.
+  void set_schedule(int tcMinK, bool fused) {
+    tcMinK_ = tcMinK;
+    fusedChol_ = fused;
+  }
+  int tc_min_k() const { return tcMinK_; }
+  bool fused_chol() const { return fusedChol_; }
 
   std::vector<Step> steps_;
   std::vector<cudaEvent_t> stepEv_;

@@ -35,3 +35,18 @@ def test_autotuned_shapes_give_identical_results(precision):
     assert {int(row[0]) for row in tuning} >= {2, 4, 8, 16, 64}
     assert all(row[5] > 0 for row in tuning)                 # every class was timed
     assert all(row[5] == 0 for row in factors["0"].describe()["batch_tuning"])
+
+
+@pytest.mark.parametrize("precision", [rs.FP64, rs.MIXED])
+def test_schedule_tuner_leaves_a_working_factor(precision):
+    """rschol_factor_tune_schedule times the factor's candidate schedules (tensor-core
+    threshold, fused or per-panel blocked Cholesky), keeps the fastest and leaves the
+    factor refactored with it: PCG still reaches 1e-8 in the same iteration count +-1."""
+    prob = rs.diffusion(3, 16, sigma=1.0, seed=3)
+    G = rs.GpuFactor(rs.Context(precision=precision, **PARAMS), prob.colptr, prob.rowind, prob.vals, prob.xyz)
+    _, i0 = G.pcg(prob.rhs[0], 1e-8, 500)
+    sch = G.tune_schedule(2)
+    assert sch["tuned_ms"] > 0 and isinstance(sch["fused"], bool)
+    assert sch["tc_min_k"] in ((128, 256, -1) if precision == rs.MIXED else (-1, 128))
+    _, i1 = G.pcg(prob.rhs[0], 1e-8, 500)
+    assert i1["true_residual"] <= 1e-8 and abs(i1["iterations"] - i0["iterations"]) <= 1
