@@ -105,7 +105,7 @@ __device__ void trsv_dinv_t(const T* __restrict__ L, int ld, int n, const T* __r
 // each, eight to a block, so the thousands of bottom-level supernodes do not
 // each pay a block's scheduling, ticket and barrier latencies.  (Widening
 // this to n <= 64, m <= 320 -- a warp per supernode of the next two levels --
-// measured slower on c2: 1.15 vs 0.92 ms per apply.)  The steps and
+// measured slower on c2: 1.15 vs 0.92 ms per apply; to m <= 192, the same.)  The steps and
 // the waits are those of a chunk block below; the per-warp shared buffers
 // hold f (IW_N) and the update vector (ICH).
 constexpr int IW_N = 32;
