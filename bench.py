@@ -399,10 +399,16 @@ def run_ours(args):
         c = main["counters"]
         step_total_ms = sum(main["step_ms"])
 
+        # context for FP32 SIMT work: 152 SMs x 128 FP32 lanes x 2 flops x the SM clock sampled in the run
+        sm_mhz = (main["clocks"] or {}).get("sm_mhz") or 2070.0
+        fp32_nominal = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+
         def roofline(kernel, ms, launches, flops, traffic, traffic_source):
             achieved = flops / (ms * 1e-3) / 1e12 if ms > 0 else 0.0
             return {"bound": "tensor", "kernel": kernel, "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                    "frac": achieved / bf16, "traffic": traffic, "traffic_source": traffic_source,
+                    "frac": achieved / bf16, "fp32_simt_nominal": fp32_nominal,
+                    "frac_of_fp32_simt_nominal": achieved / fp32_nominal,
+                    "traffic": traffic, "traffic_source": traffic_source,
                     "peak_source": src, "flops_per_launch": flops / max(launches, 1),
                     "launch_ms": ms / max(launches, 1), "launches_per_step": launches / args.steps,
                     "share_of_step_time": ms / step_total_ms if step_total_ms else None}
