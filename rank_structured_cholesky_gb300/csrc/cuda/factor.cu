@@ -140,8 +140,6 @@ void FactorEngine<T>::gemm1(const GemmTask<T>& t) {
   flush_gemm(b, tiles);
 }
 
-static inline GemmTask<double> gemm_zero_d() { return GemmTask<double>{}; }
-
 template <class T>
 static GemmTask<T> mk_gemm(const T* A, int lda, bool tA, const T* B, int ldb, bool tB, T* C, int ldc, int M, int N,
                            int K, T alpha, T beta, bool lower = false) {
