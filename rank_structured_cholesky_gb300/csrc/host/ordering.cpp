@@ -4,6 +4,7 @@
 #include <cfloat>
 #include <cmath>
 #include <functional>
+#include <future>
 #include <numeric>
 #include <stdexcept>
 
@@ -137,16 +138,67 @@ void graph_split(NDState& S, const std::vector<int>& set, std::vector<int>& L,
   std::sort(sep.begin(), sep.end());
 }
 
-int dissect(NDState& S, std::vector<int> set) {
-  if ((int)set.size() <= S.leaf) return new_component(S, std::move(set), 0);
-  std::vector<int> L, R, sep;
+// Split set into L, R and the separator; false: keep it as one component.
+bool split(NDState& S, const std::vector<int>& set, std::vector<int>& L, std::vector<int>& R,
+           std::vector<int>& sep) {
+  if ((int)set.size() <= S.leaf) return false;
   bool ok = false;
   if (S.xyz) ok = geometric_split(S, set, L, R, sep);
   if (!ok) { L.clear(); R.clear(); sep.clear(); graph_split(S, set, L, R, sep); }
-  if (sep.empty() || (L.empty() && R.empty())) return new_component(S, std::move(set), 0);
+  return !(sep.empty() || (L.empty() && R.empty()));
+}
+
+int dissect(NDState& S, std::vector<int> set) {
+  std::vector<int> L, R, sep;
+  if (!split(S, set, L, R, sep)) return new_component(S, std::move(set), 0);
   std::vector<int> kids;
   if (!L.empty()) kids.push_back(dissect(S, std::move(L)));
   if (!R.empty()) kids.push_back(dissect(S, std::move(R)));
+  int c = new_component(S, std::move(sep), (int)kids.size());
+  for (int k : kids) S.compParent[k] = c;
+  return c;
+}
+
+// Move the components of a subtree dissected in its own state Sub (root
+// subRoot) to the end of S; returns the root's index in S.  The splits do
+// not depend on the scratch stamps, so a subtree comes out exactly as the
+// serial recursion makes it, and appending L's subtree, then R's, then the
+// separator keeps the serial postorder.
+int adopt(NDState& S, NDState& Sub, int subRoot) {
+  const int base = (int)S.compMembers.size();
+  for (size_t k = 0; k < Sub.compMembers.size(); ++k) {
+    S.compMembers.push_back(std::move(Sub.compMembers[k]));
+    S.compParent.push_back(Sub.compParent[k] >= 0 ? Sub.compParent[k] + base : -1);
+    S.compChildren.push_back(Sub.compChildren[k]);
+  }
+  return subRoot + base;
+}
+
+// The top `depth` levels of the recursion with the two halves dissected
+// concurrently, each in a state of its own; below that (or for small sets)
+// the serial recursion.
+int dissect_parallel(NDState& S, std::vector<int> set, int depth) {
+  if (depth <= 0 || set.size() < 20000) return dissect(S, std::move(set));
+  std::vector<int> L, R, sep;
+  if (!split(S, set, L, R, sep)) return new_component(S, std::move(set), 0);
+  auto fresh = [&]() {
+    NDState T;
+    T.A = S.A;
+    T.xyz = S.xyz;
+    T.leaf = S.leaf;
+    T.mark.assign(S.mark.size(), 0);
+    return T;
+  };
+  NDState SL = fresh(), SR = fresh();
+  int rootL = -1, rootR = -1;
+  std::future<int> fl;
+  if (!L.empty())
+    fl = std::async(std::launch::async, [&SL, &L, depth]() { return dissect_parallel(SL, std::move(L), depth - 1); });
+  if (!R.empty()) rootR = dissect_parallel(SR, std::move(R), depth - 1);
+  if (fl.valid()) rootL = fl.get();
+  std::vector<int> kids;
+  if (rootL >= 0) kids.push_back(adopt(S, SL, rootL));
+  if (rootR >= 0) kids.push_back(adopt(S, SR, rootR));
   int c = new_component(S, std::move(sep), (int)kids.size());
   for (int k : kids) S.compParent[k] = c;
   return c;
@@ -163,8 +215,9 @@ void nested_dissection(const CSC& A, const double* xyz, int ndLeaf, std::vector<
   S.mark.assign(A.n, 0);
   std::vector<int> all(A.n);
   std::iota(all.begin(), all.end(), 0);
-  // Disconnected pieces are handled by the bisection itself.
-  if (A.n > 0) dissect(S, std::move(all));
+  // Disconnected pieces are handled by the bisection itself.  The top four
+  // levels run their two halves concurrently (up to 16 threads).
+  if (A.n > 0) dissect_parallel(S, std::move(all), 4);
   perm.clear();
   perm.reserve(A.n);
   comps.assign(S.compMembers.size(), Component());
