@@ -952,8 +952,10 @@ void FactorEngine<T>::plan() {
   dQrWs_.alloc(sizeof(T) * std::max(1LL, qrWs_));
   dCholSync_.alloc(sizeof(int) * std::max(1LL, cholSync_));
   dCholWs_.alloc(sizeof(T) * std::max(1LL, cholWs_));
-  if (const char* tp = std::getenv("RSCHOL_CHOL_TRACE"))   // diagnostics: per-item timeline of the fused steps
-    if (tp[0] && !cholItems_.empty()) dCholTrace_.alloc(4 * sizeof(unsigned long long) * cholItems_.size());
+  {   // diagnostics: per-item timeline of the fused steps, sized for this plan (or none)
+    const char* tp = std::getenv("RSCHOL_CHOL_TRACE");
+    dCholTrace_.alloc(tp && tp[0] && !cholItems_.empty() ? 4 * sizeof(unsigned long long) * cholItems_.size() : 0);
+  }
   for (size_t q = 0; q < gemm_.size(); ++q)
     if (gemmWsOff_[q] >= 0) gemm_[q].ws = dSplitWs_.as<float>() + gemmWsOff_[q];
   up(dSplitIds_, splitIds_.data(), splitIds_.size() * sizeof(int));
@@ -1121,10 +1123,11 @@ int FactorEngine<T>::run() {
       }
     }
   }
-  if (dCholTrace_.p) {   // RSCHOL_CHOL_TRACE=<file>: one line per item of the fused steps of this run
+  const char* tracePath = std::getenv("RSCHOL_CHOL_TRACE");
+  if (dCholTrace_.p && tracePath && tracePath[0]) {   // one line per item of the fused steps of this run
     std::vector<unsigned long long> tr(4 * cholItems_.size());
     RSCHOL_CUDA(cudaMemcpy(tr.data(), dCholTrace_.p, tr.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-    if (FILE* fp = std::fopen(std::getenv("RSCHOL_CHOL_TRACE"), "w")) {
+    if (FILE* fp = std::fopen(tracePath, "w")) {
       for (size_t q = 0; q < steps_.size(); ++q) {
         const Step& st = steps_[q];
         if (st.kind != ST_CHOL) continue;
