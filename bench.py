@@ -32,32 +32,45 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIGS = {
-    # name: (description, generator kwargs, nrhs)
-    "c1": ("2D 5-point Poisson 128x128, Dirichlet, seed 0", ("diffusion", 2, 128, 0.0, 0), 1),
+    # name: (description, generator spec, nrhs, factor parameters beyond the reference driver's defaults)
+    "c1": ("2D 5-point Poisson 128x128, Dirichlet, seed 0; ND leaves <= 64, separators above 16 columns compressed "
+           "(HODLR leaves <= 32), ranks <= 32 with oversampling 10",
+           ("diffusion", 2, 128, 0.0, 0), 1,
+           dict(nd_leaf=64, max_dense_block=16, max_diag_block=32, rank_cap=32, oversampling=10)),
     "c2": ("3D 7-point variable-coefficient diffusion 64^3, log-normal sigma=1 seed 1, harmonic faces",
-           ("diffusion", 3, 64, 1.0, 1), 1),
-    "c3": ("3D Q1 hex linear elasticity 48^3 elements, E=1 nu=0.3, x=0 face clamped, seed 2",
-           ("elasticity", 48, 0, 0, 2), 1),
+           ("diffusion", 3, 64, 1.0, 1), 1, dict()),
+    "c3": ("3D Q1 hex linear elasticity 48^3 elements, E=1 nu=0.3, x=0 face clamped, seed 2; ranks <= 64",
+           ("elasticity", 48, 0, 0, 2), 1, dict(rank_cap=64)),
     "c4": ("2D 5-point variable-coefficient 1024^2, log-normal sigma=2 seed 3, 64 RHS",
-           ("diffusion", 2, 1024, 2.0, 3), 64),
+           ("diffusion", 2, 1024, 2.0, 3), 64, dict()),
     # serving stream (run_serving): a pool of matrices, Poisson arrivals
     "c5": ("serving stream: 2000 requests, Poisson arrivals at 200/s, pool of 2D grids (side 64-1024) and 3D "
            "grids (side 16-96), log-normal sigma=1 seed per matrix id, 1-16 RHS per request, to 1e-8",
-           None, 0),
+           None, 0, dict()),
     # a smaller case of c2 for multi-pass ncu captures (a few hundred MB on the device)
     "c2s": ("3D 7-point variable-coefficient diffusion 40^3, log-normal sigma=1 seed 1, harmonic faces",
-            ("diffusion", 3, 40, 1.0, 1), 1),
+            ("diffusion", 3, 40, 1.0, 1), 1, dict()),
 }
 
 
-def make_problem(cfg):
-    import rank_structured_cholesky_gb300 as rs
-    _, spec, nrhs = CONFIGS[cfg]
+def config_params(cfg):
+    return dict(CONFIGS[cfg][3])
+
+
+def make_problem(cfg, cpu_only=False):
+    """The workload's system.  cpu_only builds it with the CPU oracle's copy
+    of the generators (the same arrays), so that the CPU arm never loads the
+    GPU library."""
+    _, spec, nrhs, _ = CONFIGS[cfg]
+    if cpu_only:
+        from oracle import pyoracle as gen
+    else:
+        import rank_structured_cholesky_gb300 as gen
     if spec[0] == "diffusion":
         _, dim, nx, sigma, seed = spec
-        return rs.diffusion(dim, nx, sigma=sigma, seed=seed, nrhs=nrhs)
+        return gen.diffusion(dim, nx, sigma=sigma, seed=seed, nrhs=nrhs)
     _, ne, _, _, seed = spec
-    return rs.elasticity(ne, seed=seed, nrhs=nrhs)
+    return gen.elasticity(ne, seed=seed, nrhs=nrhs)
 
 
 def peaks():
@@ -160,7 +173,7 @@ def run_reference(args):
         return 0
     if args.config == "c5":
         stream = serving_stream(args.requests, 200.0, seed=5)
-        probs, rhs = serving_pool([m for m in range(len(SERVING_POOL)) if SERVING_POOL[m][1] <= 32])
+        probs, rhs = serving_pool([m for m in range(len(SERVING_POOL)) if SERVING_POOL[m][1] <= 32], cpu_only=True)
         small = tuple(np.array(v)[[i for i in range(len(stream[0])) if int(stream[1][i]) in probs]] for v in stream)
         vals = [serving_cpu_sample(small, probs, rhs, 20.0) for _ in range(max(1, args.steps // 5))]
         cpu = vals[-1]
@@ -171,8 +184,8 @@ def run_reference(args):
                           "e2e": {"value": cpu["value"], "unit": "requests/s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}), flush=True)
         return 0
-    prob = make_problem(args.config)
-    params = dict()
+    prob = make_problem(args.config, cpu_only=True)
+    params = config_params(args.config)
     cores = os.cpu_count()
     for _ in range(args.warmup):
         cpu_oracle_solve(prob, params)
@@ -190,7 +203,7 @@ def run_reference(args):
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": args.config, "description": CONFIGS[args.config][0], "n": prob.n,
-                   "parallelism": "single process, threaded BLAS"},
+                   "params": params, "parallelism": "single process, threaded BLAS"},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
                          "sample": "full %s solve per step (symbolic + factor + PCG to 1e-8)" % args.config},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -215,9 +228,9 @@ def traffic_from_profiles(kernel, workload="c2"):
     return None
 
 
-def timed_solves(lib, rs, torch, prob, precision, device, local, steps, warmup, dist, step_timing):
+def timed_solves(lib, rs, torch, prob, params, precision, device, local, steps, warmup, dist, step_timing):
     """K timed factor + PCG steps (device-resident inputs) for one precision."""
-    ctx = rs.Context(precision=precision, device=local)
+    ctx = rs.Context(**params, precision=precision, device=local)
     t0 = time.perf_counter()
     F = rs.GpuFactor(ctx, prob.colptr, prob.rowind, prob.vals, prob.xyz)
     setup_s = time.perf_counter() - t0
@@ -293,7 +306,7 @@ def run_ours(args):
 
     if args.profile:
         # ncu --profile-from-start off: capture exactly the K steps
-        ctx = rs.Context(precision=args.precision, device=local)
+        ctx = rs.Context(**config_params(args.config), precision=args.precision, device=local)
         F = rs.GpuFactor(ctx, prob.colptr, prob.rowind, prob.vals, prob.xyz)
         d_vals = torch.from_numpy(prob.vals).to(device)
         d_b = torch.from_numpy(np.ascontiguousarray(prob.rhs[:nrhs])).to(device)
@@ -317,7 +330,9 @@ def run_ours(args):
                               "iterations": [infos[k].iterations for k in range(nrhs)]}), flush=True)
         return 0
 
-    main = timed_solves(lib, rs, torch, prob, args.precision, device, local, args.steps, args.warmup, dist, True)
+    params = config_params(args.config)
+    main = timed_solves(lib, rs, torch, prob, params, args.precision, device, local, args.steps, args.warmup, dist,
+                        True)
     F, ctx, stream = main["F"], main["ctx"], main["stream"]
     stats = F.stats()
     desc = F.describe()
@@ -360,7 +375,7 @@ def run_ours(args):
     # the plain FP64 path on the same workload, for the mixed-precision speed-up
     plain = None
     if args.precision == "mixed" and not args.no_fp64_plain:
-        pf = timed_solves(lib, rs, torch, prob, "fp64", device, local, args.steps, args.warmup, dist, False)
+        pf = timed_solves(lib, rs, torch, prob, params, "fp64", device, local, args.steps, args.warmup, dist, False)
         plain = {"value": world * args.steps / pf["total_s"], "unit": "solves/s",
                  "ms_per_step": 1e3 * pf["total_s"] / args.steps,
                  "factor_ms": statistics.median(pf["factor_ms"]), "pcg_ms": statistics.median(pf["pcg_ms"]),
@@ -386,7 +401,7 @@ def run_ours(args):
         cpu = None
         if not args.no_cpu_baseline and world == 1:
             cores = os.cpu_count()
-            res = cpu_oracle_solve(prob, dict())
+            res = cpu_oracle_solve(prob, params)
             t = res["symbolic_s"] + res["factor_s"] + res["pcg_s"]
             cpu = {"value": 1.0 / t, "unit": "solves/s", "cores": cores, "kind": "port",
                    "sample": "one full %s solve (symbolic + FP64 factor + PCG to 1e-8, %d iterations) with the "
@@ -433,7 +448,7 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32 factor / f64 pcg",
             "data": "synthetic",
             "config": {"workload": args.config, "description": CONFIGS[args.config][0], "n": n, "nrhs": nrhs,
-                       "precision": args.precision, "parallelism": "replicas" if world > 1 else "single GPU",
+                       "params": params, "precision": args.precision, "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (factor arena %.0f MB)" % (stats["device_bytes"] / 1e6)},
             "e2e": {"value": world * args.steps / e2e_s, "unit": "solves/s",
                     "h2d_bytes_per_step": int(prob.vals.nbytes + h_b.nbytes),
@@ -478,12 +493,15 @@ def serving_stream(count, rate, seed):
     return arrivals, mids, nrhs, offs
 
 
-def serving_pool(ids):
-    import rank_structured_cholesky_gb300 as rs
+def serving_pool(ids, cpu_only=False):
+    if cpu_only:
+        from oracle import pyoracle as gen
+    else:
+        import rank_structured_cholesky_gb300 as gen
     probs, rhs = {}, {}
     for m in ids:
         dim, side = SERVING_POOL[m]
-        probs[m] = rs.diffusion(dim, side, sigma=1.0, seed=100 + m, nrhs=1)
+        probs[m] = gen.diffusion(dim, side, sigma=1.0, seed=100 + m, nrhs=1)
         rhs[m] = np.random.RandomState(1000 + m).standard_normal((SERVING_RHS_POOL, probs[m].n))
     return probs, rhs
 

@@ -103,11 +103,12 @@ int rschol_profile(rschol_factor* f, const double* d_b, double* out);
 
 /* x = M^{-1} b for nrhs column-major right-hand sides.
  * Replaces FactorPreconditioner::solve (FactorPreconditioner.cpp:135-162),
- * PRECONDITIONER::solve (src/rschol/linearalgebra/PRECONDITIONER.h:290-292). */
+ * PRECONDITIONER::solve (src/rschol/linearalgebra/PRECONDITIONER.h:56). */
 int rschol_precond_apply(rschol_factor* f, const double* b, double* x, int nrhs);
 int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs);
 
-/* Same result as rschol_precond_apply_device, but the call allocates no
+/* The same preconditioner application as rschol_precond_apply_device called
+ * once per right-hand side (nrhs = 1 each time), but the call allocates no
  * device memory: for callers that apply the preconditioner inside their own
  * solver loop and cannot let a call allocate (cudaMalloc synchronises the
  * device and stalls their other streams, or their memory budget is fixed).
@@ -120,9 +121,13 @@ int rschol_precond_apply_device(rschol_factor* f, const double* d_b, double* d_x
  *     streams) race on it, so serialise them;
  *   - nothing in it has to start at zero: each right-hand side is written
  *     completely before it is read;
- *   - the first call on a device looks up the array's address
- *     (cudaGetSymbolAddress, with that device current); make that first call
- *     before any stream capture that would include this function. */
+ *   - rschol_create looks up the array's device address (once per device,
+ *     with that device current), so the call itself only reads a pointer;
+ *   - like the other entry points it synchronises the context stream before
+ *     returning. */
+#define RSCHOL_NOALLOC_MAX_N 2097152
+int rschol_precond_apply_device_noalloc(rschol_factor* f, const double* d_b, double* d_x, int nrhs);
+
 /* Autotuner of the batched apply (no reference counterpart): times the
  * candidate tile shapes (interior (row, column) pair tiles, column groups of
  * the compressed-level products) of every width class (number of
@@ -213,14 +218,11 @@ int rschol_step_timing(rschol_factor* f, int enable, double* out);
  * sum_k |a_ik b_kj| (+ |beta c_ij|), out[1]: largest absolute error. */
 int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int split, int lower, double* out);
 
-#define RSCHOL_NOALLOC_MAX_N 2097152
-int rschol_precond_apply_device_noalloc(rschol_factor* f, const double* d_b, double* d_x, int nrhs);
-
 /* Preconditioned CG from x0 = 0 with the factor as M, stopping at
  * ||r|| / ||b|| <= eps or maxit iterations; nrhs right-hand sides are solved
  * together, sharing the factor.
  * Replaces PCG_SOLVER(A, eps, iters) + solvePCG(x, b, M)
- * (src/rschol/linearalgebra/PCG_SOLVER.h:344-417, PCG_SOLVER.cpp:226-363).
+ * (src/rschol/linearalgebra/PCG_SOLVER.h:52-65, PCG_SOLVER.cpp:226-363).
  * info may be NULL; otherwise it receives nrhs entries. */
 int rschol_pcg(rschol_factor* f, const double* b, double* x, int nrhs, double eps, int maxit,
                rschol_pcg_info* info);

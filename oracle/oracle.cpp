@@ -773,6 +773,44 @@ using oracle::Factor;
 
 extern "C" {
 
+// The synthetic problems of the library (rank_structured_cholesky_gb300/
+// csrc/host/problems.cpp, compiled into this oracle too), so that CPU-only
+// callers need not load the GPU library to build their inputs.
+void* oracle_problem_diffusion(int dim, int nx, int ny, int nz, double sigma, unsigned seed, int nrhs) {
+  try {
+    return new rschol::Problem(rschol::make_diffusion(dim, nx, ny, nz, sigma, seed, nrhs));
+  } catch (const std::exception&) {
+    return nullptr;
+  }
+}
+
+void* oracle_problem_elasticity(int ne, double E, double nu, unsigned seed, int nrhs) {
+  try {
+    return new rschol::Problem(rschol::make_elasticity(ne, E, nu, seed, nrhs));
+  } catch (const std::exception&) {
+    return nullptr;
+  }
+}
+
+// sizes[0..2] = n, nnz, nrhs
+void oracle_problem_sizes(const void* p, long long* sizes) {
+  const rschol::Problem& P = *(const rschol::Problem*)p;
+  sizes[0] = P.n;
+  sizes[1] = (long long)P.rowind.size();
+  sizes[2] = P.nrhs;
+}
+
+void oracle_problem_get(const void* p, int* colptr, int* rowind, double* vals, double* xyz, double* rhs) {
+  const rschol::Problem& P = *(const rschol::Problem*)p;
+  std::memcpy(colptr, P.colptr.data(), sizeof(int) * P.colptr.size());
+  std::memcpy(rowind, P.rowind.data(), sizeof(int) * P.rowind.size());
+  std::memcpy(vals, P.vals.data(), sizeof(double) * P.vals.size());
+  std::memcpy(xyz, P.xyz.data(), sizeof(double) * P.xyz.size());
+  std::memcpy(rhs, P.rhs.data(), sizeof(double) * P.rhs.size());
+}
+
+void oracle_problem_free(void* p) { delete (rschol::Problem*)p; }
+
 void oracle_set_blas(void* dgemm, void* dtrsm, void* dpotrf, void* dgeqrf, void* dorgqr) {
   oracle::g_blas.gemm = (oracle::dgemm_t)dgemm;
   oracle::g_blas.trsm = (oracle::dtrsm_t)dtrsm;

@@ -55,6 +55,13 @@ def load(use_blas=True):
     lib.oracle_times.argtypes = [P, pD]
     lib.oracle_gaussians.argtypes = [P, ctypes.c_longlong, pD]
     lib.oracle_set_blas.argtypes = [P, P, P, P, P]
+    lib.oracle_problem_diffusion.restype = P
+    lib.oracle_problem_diffusion.argtypes = [I, I, I, I, D, ctypes.c_uint, I]
+    lib.oracle_problem_elasticity.restype = P
+    lib.oracle_problem_elasticity.argtypes = [I, D, D, ctypes.c_uint, I]
+    lib.oracle_problem_sizes.argtypes = [P, ctypes.POINTER(ctypes.c_longlong)]
+    lib.oracle_problem_get.argtypes = [P, P, P, P, P, P]
+    lib.oracle_problem_free.argtypes = [P]
     if use_blas:
         try:
             import scipy.linalg.cython_blas as cb
@@ -78,6 +85,39 @@ def _ip(a):
 
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Problem:
+    """A synthetic system built by the oracle library (the same generators as
+    the GPU library's rschol_problem_*), with the fields of
+    rank_structured_cholesky_gb300.Problem."""
+
+    def __init__(self, handle):
+        lib = load()
+        if not handle:
+            raise RuntimeError("problem generation failed")
+        sz = (ctypes.c_longlong * 3)()
+        lib.oracle_problem_sizes(handle, sz)
+        n, nnz, nrhs = int(sz[0]), int(sz[1]), int(sz[2])
+        self.n, self.nrhs = n, nrhs
+        self.colptr = np.zeros(n + 1, np.int32)
+        self.rowind = np.zeros(nnz, np.int32)
+        self.vals = np.zeros(nnz)
+        self.xyz = np.zeros(3 * n)
+        rhs = np.zeros(n * max(nrhs, 1))
+        lib.oracle_problem_get(handle, self.colptr.ctypes.data, self.rowind.ctypes.data, self.vals.ctypes.data,
+                               self.xyz.ctypes.data, rhs.ctypes.data)
+        lib.oracle_problem_free(handle)
+        self.rhs = rhs.reshape(max(nrhs, 1), n)
+
+
+def diffusion(dim, nx, sigma=0.0, seed=0, nrhs=1):
+    nz = nx if dim == 3 else 1
+    return Problem(load().oracle_problem_diffusion(dim, nx, nx, nz, sigma, seed, nrhs))
+
+
+def elasticity(ne, E=1.0, nu=0.3, seed=2, nrhs=1):
+    return Problem(load().oracle_problem_elasticity(ne, E, nu, seed, nrhs))
 
 
 class OracleFactor:

@@ -89,19 +89,67 @@ def build_oracle():
     return ORACLE_LIB
 
 
+def reference_dir():
+    """Root of the reference's sources (RSCHOL_REFERENCE_DIR, by default the
+    read-only checkout this recipe was written against), or None where they
+    are absent."""
+    root = os.environ.get("RSCHOL_REFERENCE_DIR", "/root/reference")
+    return root if os.path.isdir(os.path.join(root, "src", "rschol")) else None
+
+
+REF_SHIM = os.path.join(ORACLE_DIR, "ref_shim")
+REF_OUT = os.path.join(ORACLE_DIR, "_ref")
+REF_PCG_LIB = os.path.join(REF_OUT, "libref_pcg.so")
+REF_SEPTREE = os.path.join(REF_OUT, "ref_septree_kat")
+REF_MT = os.path.join(REF_OUT, "mt_ref_kat")
+
+
 def build_reference_tools():
-    """Compile the reference's own MERSENNETWISTER header into a known-answer
-    tool under oracle/_ref/ (only where the reference sources are present)."""
-    ref_hdr_dir = "/root/reference/src/rschol/util"
-    if not os.path.exists(os.path.join(ref_hdr_dir, "MERSENNETWISTER.h")):
+    """Compile checking tools from the reference's own sources where they lie
+    (only where they are present), into oracle/_ref/:
+
+    * mt_ref_kat        -- draws of src/rschol/util/MERSENNETWISTER.h;
+    * ref_septree_kat   -- src/rschol/datastructure/SeparatorTree.h/.cpp, as
+                           NestedDissection::ReorderNestedSeparators builds it;
+    * libref_pcg.so     -- PCG_SOLVER::solvePCG with VECTOR_FAST.cpp and
+                           SPARSE_MATRIX.cpp, preconditioner by callback.
+
+    oracle/ref_shim/ stands in for Boost's names, the CMake-written config.h
+    and CBLAS level 1; none of the reference's code is changed or copied.
+    Returns the MT tool's path, or None without the reference sources."""
+    root = reference_dir()
+    if root is None:
         return None
-    out_dir = os.path.join(ORACLE_DIR, "_ref")
-    os.makedirs(out_dir, exist_ok=True)
-    exe = os.path.join(out_dir, "mt_ref_kat")
-    src = os.path.join(ORACLE_DIR, "ref_mt_kat.cpp")
-    if _stale(exe, [src]):
-        _run(["g++", "-O2", "-std=c++11", "-I", ref_hdr_dir, src, "-o", exe])
-    return exe
+    src = os.path.join(root, "src")
+    os.makedirs(os.path.join(REF_OUT, "obj"), exist_ok=True)
+    mt_src = os.path.join(ORACLE_DIR, "ref_mt_kat.cpp")
+    if _stale(REF_MT, [mt_src]):
+        _run(["g++", "-O2", "-std=c++11", "-I", os.path.join(src, "rschol", "util"), mt_src, "-o", REF_MT])
+    shim_files = [os.path.join(d, f) for d, _, fs in os.walk(REF_SHIM) for f in fs]
+    inc = ["-I", REF_SHIM, "-I", src]
+    st_src = os.path.join(ORACLE_DIR, "ref_septree_kat.cpp")
+    st_deps = [st_src] + shim_files + [os.path.join(src, "rschol", "datastructure", f)
+                                       for f in ("SeparatorTree.h", "SeparatorTree.cpp")]
+    if _stale(REF_SEPTREE, st_deps):
+        _run(["g++", "-O2", "-std=c++11", "-w"] + inc + [st_src, "-o", REF_SEPTREE])
+    la = os.path.join(src, "rschol", "linearalgebra")
+    ref_srcs = [os.path.join(la, f) for f in ("PCG_SOLVER.cpp", "VECTOR_FAST.cpp", "SPARSE_MATRIX.cpp")]
+    tool = os.path.join(ORACLE_DIR, "ref_pcg_tool.cpp")
+    blas = os.path.join(REF_SHIM, "cblas_level1.c")
+    if _stale(REF_PCG_LIB, ref_srcs + [tool, blas] + shim_files):
+        hidden = ["-fPIC", "-fvisibility=hidden", "-ffunction-sections", "-fdata-sections"]
+        objs, cmds = [], []
+        for s_ in ref_srcs + [tool]:
+            o = os.path.join(REF_OUT, "obj", os.path.basename(s_) + ".o")
+            objs.append(o)
+            cmds.append(["g++", "-O2", "-std=c++11", "-w"] + hidden + inc + ["-I", la, "-c", s_, "-o", o])
+        o = os.path.join(REF_OUT, "obj", "cblas_level1.o")
+        objs.append(o)
+        cmds.append(["gcc", "-O2"] + hidden + ["-c", blas, "-o", o])
+        with cf.ThreadPoolExecutor(max_workers=4) as ex:
+            list(ex.map(_run, cmds))
+        _run(["g++", "-shared", "-Wl,--gc-sections", "-Wl,--no-undefined", "-o", REF_PCG_LIB] + objs + ["-lz"])
+    return REF_MT
 
 
 def build_all(verbose=False):

@@ -28,7 +28,12 @@ struct rschol_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   int device = 0;
+  double* noallocWork = nullptr;   // device address of the static work vector of this device
 };
+
+// Looks up (once per device, that device current) the device address of the
+// static work vector of rschol_precond_apply_device_noalloc.
+static cudaError_t noalloc_lookup(int device, double** addr);
 
 namespace {
 
@@ -236,6 +241,15 @@ rschol_ctx* rschol_create(const rschol_params* p) {
   if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     c->err = "CUDA device initialisation failed";
     c->stream = nullptr;
+    return c;
+  }
+  // the allocation-free apply's static work vector: its device address is
+  // looked up here, with the device current, so that the apply only reads it
+  const cudaError_t e = noalloc_lookup(c->device, &c->noallocWork);
+  if (e != cudaSuccess) {
+    c->err = std::string("cudaGetSymbolAddress of the static work vector: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+    c->noallocWork = nullptr;
   }
   return c;
 }
@@ -797,7 +811,10 @@ extern "C" int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int spl
 
 // ---- allocation-free preconditioner apply ----------------------------------
 // The permuted work vector lives in a file-scope device array instead of a
-// buffer allocated on first use, so the call itself never allocates.
+// buffer allocated on first use, so the call itself never allocates.  Its
+// device address is looked up when a context is created (rschol_create):
+// under lazy module loading the lookup loads this file's module, which
+// allocates the array, so it must not happen inside the apply.
 namespace {
 constexpr int kNoAllocMaxN = RSCHOL_NOALLOC_MAX_N;
 constexpr int kNoAllocMaxDevices = 64;
@@ -806,6 +823,21 @@ std::mutex g_noalloc_mu;
 void* g_noalloc_addr[kNoAllocMaxDevices] = {};
 }  // namespace
 
+static cudaError_t noalloc_lookup(int device, double** addr) {
+  *addr = nullptr;
+  if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    // the caller (rschol_create) has made `device` current
+    void* a = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&a, g_noalloc_work);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[device] = a;
+  }
+  *addr = static_cast<double*>(g_noalloc_addr[device]);
+  return cudaSuccess;
+}
+
 extern "C" int rschol_precond_apply_device_noalloc(rschol_factor* f, const double* d_b, double* d_x, int nrhs) {
   if (!f || !d_b || !d_x || nrhs <= 0) return RSCHOL_E_BAD_INPUT;
   const int n = f->Afull.n;
@@ -813,29 +845,12 @@ extern "C" int rschol_precond_apply_device_noalloc(rschol_factor* f, const doubl
     return fail(f->ctx, RSCHOL_E_BAD_INPUT,
                 "rschol_precond_apply_device_noalloc: n = " + std::to_string(n) + " exceeds the static work vector (" +
                     std::to_string(kNoAllocMaxN) + " unknowns); use rschol_precond_apply_device");
-  const int dev = f->ctx->device;
-  if (dev < 0 || dev >= kNoAllocMaxDevices)
-    return fail(f->ctx, RSCHOL_E_UNSUPPORTED, "rschol_precond_apply_device_noalloc: device ordinal out of range");
+  double* work = f->ctx->noallocWork;
+  if (!work)
+    return fail(f->ctx, RSCHOL_E_CUDA,
+                "rschol_precond_apply_device_noalloc: the static work vector's address was not found when the "
+                "context was created");
   try {
-    double* work = nullptr;
-    {
-      std::lock_guard<std::mutex> lock(g_noalloc_mu);
-      if (!g_noalloc_addr[dev]) {
-        // once per device, with that device current
-        int prev = -1;
-        RSCHOL_CUDA(cudaGetDevice(&prev));
-        RSCHOL_CUDA(cudaSetDevice(dev));
-        void* addr = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_work);
-        if (prev >= 0 && prev != dev) cudaSetDevice(prev);
-        if (e != cudaSuccess)
-          return fail(f->ctx, RSCHOL_E_CUDA,
-                      std::string("rschol_precond_apply_device_noalloc: cudaGetSymbolAddress: ") +
-                          cudaGetErrorString(e));
-        g_noalloc_addr[dev] = addr;
-      }
-      work = static_cast<double*>(g_noalloc_addr[dev]);
-    }
     cudaStream_t s = f->ctx->stream;
     for (int k = 0; k < nrhs; ++k) {
       launch_gather(d_b + (size_t)k * n, f->dPerm.as<int>(), work, n, s);

@@ -24,3 +24,15 @@ def test_reference_arm_prints_the_contract_line():
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+
+
+def test_reference_arm_does_not_load_the_gpu_library():
+    """The CPU arm builds its inputs with the oracle's generators: the GPU
+    library must not be mapped into its process."""
+    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--config', 'c1', '--steps', '1', "
+            "'--warmup', '0']; import bench; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('GPU_LIB_MAPPED' if 'librschol_gb300' in maps else 'GPU_LIB_ABSENT')")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert "GPU_LIB_ABSENT" in out.stdout

@@ -13,8 +13,9 @@ Tolerances (FP64 path), relative Frobenius / 2-norm error against the oracle:
     loops differs by 3.1e-6 on the 2d48 case);
   * APPLY_TOL = 1e-7 for one preconditioner application.
 PCG reaches ||r||/||b|| <= 1e-8 in the oracle's iteration count +-1.  Mixed
-precision (FP32 factor, FP64 PCG) must reach the same 1e-8 residual; its
-error against the FP64 oracle is asserted below 1e-3.
+precision (FP32 factor, FP64 PCG) must reach the same 1e-8 residual in the
+FP64 oracle's iteration count +-1; its error against the FP64 oracle is
+asserted below 1e-3.  Every supernode's blocks are compared.
 """
 import os
 
@@ -69,8 +70,6 @@ def test_factor_blocks_match_oracle(case, oracles):
     for j in range(G.num_nodes()):
         gi, oi = G.node_info(j), O.node_info(j)
         assert (gi["c0"], gi["c1"], gi["compressed"]) == (oi["c0"], oi["c1"], oi["compressed"])
-        if not gi["compressed"] and j % 5:
-            continue
         tol = COMPRESSED_TOL if gi["compressed"] else EXACT_TOL
         assert rel(G.node_l11(j), O.node_l11(j)) < tol, ("l11", j, gi)
         l21o = O.node_l21(j)
@@ -116,7 +115,7 @@ def test_mixed_precision_reaches_fp64_accuracy(case, oracles):
     x, info = G.pcg(prob.rhs[0], 1e-8, 2000)
     assert info["true_residual"] <= 1e-8
     _, it, _, _ = O.pcg(prob.rhs[0], 1e-8, 2000)
-    assert info["iterations"] <= it + 3
+    assert abs(info["iterations"] - it) <= 1, (info, it)
     # error of the FP32 factor against the FP64 oracle, stated as a bound
     assert rel(G.apply(prob.rhs[0]), O.apply(prob.rhs[0])) < 1e-3
 

@@ -4,7 +4,10 @@ rschol_precond_apply_device_noalloc runs the same single-vector kernels on
 the same factor as rschol_precond_apply_device called with one right-hand
 side; only the permuted work vector differs (a static device array instead
 of a buffer allocated on first use).  Two calls in a row, both precisions,
-two right-hand sides per no-alloc call.
+two right-hand sides per no-alloc call.  The device's free memory is the
+same before and after the first no-alloc call of a fresh context: the
+static array's address is looked up when the context is created, so the
+call itself loads and allocates nothing.
 """
 import numpy as np
 import pytest
@@ -26,6 +29,16 @@ def test_noalloc_apply_matches_device_apply(precision):
     n = prob.n
     assert n <= 2097152
     b = torch.tensor(np.stack(prob.rhs), dtype=torch.float64, device="cuda")
+    x_warm = torch.zeros_like(b)
+    x_first = torch.zeros_like(b)
+    torch.cuda.synchronize()
+    # the single-vector kernels are loaded by one allocating apply first
+    assert lib.rschol_precond_apply_device(G.h, b[0].data_ptr(), x_warm[0].data_ptr(), 1) == 0
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    assert lib.rschol_precond_apply_device_noalloc(G.h, b.data_ptr(), x_first.data_ptr(), 2) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
     for _ in range(2):
         x_ref = torch.zeros_like(b)
         x_na = torch.full_like(b, float("nan"))
