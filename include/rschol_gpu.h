@@ -19,13 +19,14 @@ extern "C" {
 enum rschol_status {
   RSCHOL_OK = 0,
   RSCHOL_E_BAD_INPUT = 1,
-  RSCHOL_E_NOT_PD_AFTER_RETRY = 2, /* IndefiniteDiagonalError after all retries */
+  RSCHOL_E_NOT_PD_AFTER_RETRY = 2, /* IndefiniteDiagonalError of a compressed supernode after all retries */
   RSCHOL_E_OOM = 3,
   RSCHOL_E_CUDA = 4,
   RSCHOL_E_BREAKDOWN = 5,          /* PCG breakdown: d' A d == 0 */
-  RSCHOL_E_TIMEOUT = 6,            /* a bounded wait between thread blocks of the solve gave up */
+  RSCHOL_E_TIMEOUT = 6,            /* a bounded wait between thread blocks of the factor or solve gave up */
   RSCHOL_E_NO_DEVICE = 7,
-  RSCHOL_E_UNSUPPORTED = 8
+  RSCHOL_E_UNSUPPORTED = 8,
+  RSCHOL_E_NOT_PD = 9              /* non-positive pivot in an uncompressed supernode (the reference aborts) */
 };
 
 enum rschol_precision {

@@ -855,8 +855,13 @@ void* oracle_create(int n, const int* colptr, const int* rowind, const double* v
 
 void oracle_free(void* h) { delete (Factor*)h; }
 
-// Numeric factorisation with the reference's retry policy.  Returns 0 or
-// the 1-based index of the node whose diagonal was not positive definite.
+// Numeric factorisation with the reference's retry policy
+// (SparseSolver.cpp:174-214): an indefinite diagonal of a compressed node
+// (IndefiniteDiagonalError from its DiagonalBlock, DiagonalBlock.cpp:372-376,
+// 429-435) is retried with a larger diagonal rank constant; a non-positive
+// pivot of an uncompressed node is where the reference aborts
+// (Supernode.cpp:3681-3689), so it is returned at once.  Returns 0 or the
+// 1-based index of the node whose diagonal was not positive definite.
 int oracle_factor(void* h) {
   Factor& F = *(Factor*)h;
   double t0 = oracle::now();
@@ -868,6 +873,7 @@ int oracle_factor(void* h) {
     F.attempts++;
     status = oracle::numeric(F);
     if (status == 0) break;
+    if (!F.S.nodes[status - 1].compressed) break;
     dc *= F.prm.rank_alpha;
   }
   F.diagRankConstant = dc;

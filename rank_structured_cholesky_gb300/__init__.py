@@ -4,7 +4,7 @@ Python host mirror of the reference's interface for this path
 (jeffchadwick/rank_structured_cholesky):
 
 * ``FactorPreconditioner.initialize / solve``  -- src/rschol/solver/FactorPreconditioner.h:92-113
-* ``PCGSolver(A, eps, iterations).solve_pcg``   -- src/rschol/linearalgebra/PCG_SOLVER.h:344-417
+* ``PCGSolver(A, eps, iterations).solve_pcg``   -- src/rschol/linearalgebra/PCG_SOLVER.h:52-65
 * ``solve(A, b)``                               -- src/python/rschol.pyx:38-53 (``rschol.solve``)
 
 All compute runs in the native library (``_build/librschol_gb300.so``, C ABI
@@ -23,7 +23,7 @@ RSCHOL_OK = 0
 STATUS_NAMES = {
     0: "RSCHOL_OK", 1: "RSCHOL_E_BAD_INPUT", 2: "RSCHOL_E_NOT_PD_AFTER_RETRY", 3: "RSCHOL_E_OOM",
     4: "RSCHOL_E_CUDA", 5: "RSCHOL_E_BREAKDOWN", 6: "RSCHOL_E_TIMEOUT", 7: "RSCHOL_E_NO_DEVICE",
-    8: "RSCHOL_E_UNSUPPORTED",
+    8: "RSCHOL_E_UNSUPPORTED", 9: "RSCHOL_E_NOT_PD",
 }
 FP64, MIXED = 0, 1
 

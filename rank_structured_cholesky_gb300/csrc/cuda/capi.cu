@@ -262,6 +262,12 @@ void rschol_destroy(rschol_ctx* c) {
 
 const char* rschol_last_error(const rschol_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
+// SparseSolver::factorNumeric (SparseSolver.cpp:174-214): retries only the
+// IndefiniteDiagonalError of a compressed supernode's diagonal (its
+// DiagonalBlock, DiagonalBlock.cpp:372-376 and 429-435) with a larger
+// diagonal rank constant.  A non-positive pivot in an uncompressed
+// supernode's exact Cholesky is where the reference aborts
+// (Supernode.cpp:3681-3689): returned at once as RSCHOL_E_NOT_PD.
 static int numeric_with_retry(rschol_factor* f) {
   rschol_ctx* ctx = f->ctx;
   double t0 = now_s();
@@ -276,15 +282,23 @@ static int numeric_with_retry(rschol_factor* f) {
       assign_ranks(f->S, f->prm, f->prm.rank_constant, dc);
       f->impl->plan();
     }
-    status = f->impl->run();
+    status = f->impl->run();   // 0, or 1 + the first supernode with a non-positive pivot
     if (status == 0) break;
+    const int node = status - 1;
+    if (node >= 0 && node < (int)f->S.nodes.size() && !f->S.nodes[node].compressed) {
+      f->diagRankConstant = dc;
+      f->tNumeric = now_s() - t0;
+      return fail(ctx, RSCHOL_E_NOT_PD,
+                  "matrix not positive definite: non-positive pivot in the diagonal of uncompressed supernode " +
+                      std::to_string(node));
+    }
     dc *= f->prm.rank_alpha;
   }
   f->diagRankConstant = dc;
   f->tNumeric = now_s() - t0;
   if (status != 0)
     return fail(ctx, RSCHOL_E_NOT_PD_AFTER_RETRY,
-                "indefinite diagonal block (code " + std::to_string(status) + ") after " +
+                "indefinite diagonal block of compressed supernode " + std::to_string(status - 1) + " after " +
                     std::to_string(f->attempts) + " attempts");
   return RSCHOL_OK;
 }
@@ -358,6 +372,9 @@ int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* r
                            cudaMemcpyHostToDevice));
     int st = numeric_with_retry(f.get());
     if (st != RSCHOL_OK) return st;
+  } catch (const FactorWaitTimeout& e) {
+    cudaGetLastError();
+    return fail(ctx, RSCHOL_E_TIMEOUT, e.what());
   } catch (const CudaError& e) {
     cudaGetLastError();
     std::string m = e.what();
@@ -399,6 +416,8 @@ int rschol_refactor_device(rschol_factor* f, const double* d_vals) {
       f->impl->plan();
     }
     return numeric_with_retry(f);
+  } catch (const FactorWaitTimeout& e) {
+    return fail(f->ctx, RSCHOL_E_TIMEOUT, e.what());
   } catch (const std::exception& e) {
     return fail(f->ctx, RSCHOL_E_CUDA, e.what());
   }

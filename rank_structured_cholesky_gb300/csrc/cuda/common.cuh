@@ -14,6 +14,13 @@ struct CudaError : std::runtime_error {
   explicit CudaError(const std::string& s) : std::runtime_error(s) {}
 };
 
+// A bounded wait inside a factorisation kernel (a fused-Cholesky tile
+// counter or a tensor-core mbarrier) gave up: the kernel returned early and
+// the factor is invalid, but the context stays usable.
+struct FactorWaitTimeout : CudaError {
+  explicit FactorWaitTimeout(const std::string& s) : CudaError(s) {}
+};
+
 #define RSCHOL_CUDA(call)                                                                          \
   do {                                                                                             \
     cudaError_t e_ = (call);                                                                       \

@@ -544,16 +544,18 @@ __global__ void __launch_bounds__(256) chol_fused_kernel(const CholFusedJob<T>* 
   int* tdone = cnt + j.TR * j.TU;  // TR: panels whose TRSM of row tile a is done
   int* pdone = tdone + j.TR;       // P: POTRF of panel p done
   const int p = it.p, a = it.a, b = it.b;
+  const int lim = flag[2];   // polls before a wait gives up (set with the flags before the factorisation)
   auto bnd = [&](int t) { return t == 0 ? 0 : j.w0 + 64 * (t - 1); };      // columns (and Cholesky rows)
   auto rbnd = [&](int t) { return t == 0 ? 0 : j.r1 + 64 * (t - 1); };     // rows
   const int c0 = bnd(p), wp = bnd(p + 1) - c0;
   if ((threadIdx.x >> 5) == 0) {
     bool ok;
-    if (it.kind == CHOL_POTRF) ok = j.L ? true : wait_geq(cnt + p * j.TU + p, p, err);
-    else if (it.kind == CHOL_TRSM) ok = wait_geq(pdone + p, 1, err) && wait_geq(cnt + a * j.TU + p, p, err);
+    if (it.kind == CHOL_POTRF) ok = j.L ? true : wait_geq(cnt + p * j.TU + p, p, err, lim);
+    else if (it.kind == CHOL_TRSM)
+      ok = wait_geq(pdone + p, 1, err, lim) && wait_geq(cnt + a * j.TU + p, p, err, lim);
     else
-      ok = wait_geq(tdone + a, p + 1, err) && (j.L || wait_geq(tdone + b, p + 1, err)) &&
-           wait_geq(cnt + a * j.TU + b, p, err);
+      ok = wait_geq(tdone + a, p + 1, err, lim) && (j.L || wait_geq(tdone + b, p + 1, err, lim)) &&
+           wait_geq(cnt + a * j.TU + b, p, err, lim);
     if (threadIdx.x == 0) {
       sOk = ok;
       if (trace) tReady = globaltimer_ns();
@@ -1183,13 +1185,14 @@ void launch_extadd(const ExtAddRow<T>* rows, int nRows, const ExtAddSeg* segs, c
   extadd_kernel<T><<<(nRows + 7) / 8, 256, 0, s>>>(rows, nRows, segs, src);
   RSCHOL_LAUNCH_CHECK();
 }
-__global__ void init_flags_kernel(int* flag) {
+__global__ void init_flags_kernel(int* flag, int waitLimit) {
   flag[0] = INT_MAX;
   flag[1] = 0;
+  flag[2] = waitLimit;
 }
 
-void launch_init_flags(int* flag, cudaStream_t s) {
-  init_flags_kernel<<<1, 1, 0, s>>>(flag);
+void launch_init_flags(int* flag, int waitLimit, cudaStream_t s) {
+  init_flags_kernel<<<1, 1, 0, s>>>(flag, waitLimit);
   RSCHOL_LAUNCH_CHECK();
 }
 

@@ -84,7 +84,7 @@ struct CholItem {   // one piece of panel p: POTRF, TRSM of row tile a, update o
 };
 // sync: syncInts ints (zeroed here, on the stream, before the launch); ws:
 // the jobs' inverse tiles; flag[0]: min code of a failed pivot, flag[1]: set
-// when a bounded wait gives up.  trace (diagnostics, may be null): 4 values
+// when a bounded wait gives up, flag[2]: polls before a wait gives up.  trace (diagnostics, may be null): 4 values
 // per item -- start, dependencies met, end (ns of the global timer), SM.
 template <class T>
 void launch_chol_fused(const CholFusedJob<T>* jobs, const CholItem* items, int nItems, int* sync, long long syncInts,
@@ -129,7 +129,9 @@ template <class T>
 void launch_extadd(const ExtAddRow<T>* dRows, int nRows, const ExtAddSeg* dSegs, const ExtAddSource<T>* dSources,
                    cudaStream_t s);
 // flag[0] = INT_MAX (no POTRF failure yet), flag[1] = 0 (no tensor-core wait error)
-void launch_init_flags(int* flag, cudaStream_t s);
+// flag[0] = INT_MAX (no failed pivot), flag[1] = 0 (no wait gave up),
+// flag[2] = waitLimit (polls before a fused-Cholesky wait gives up).
+void launch_init_flags(int* flag, int waitLimit, cudaStream_t s);
 template <class T>
 void launch_scatter(const double* Avals, const long long* srcIdx, const long long* dstIdx, long long count,
                     T* dst, cudaStream_t s);

@@ -9,6 +9,7 @@
 #include <type_traits>
 
 #include "../host/rng.h"
+#include "solve_dev.cuh"
 #include "factor.cuh"
 
 namespace rschol {
@@ -30,7 +31,14 @@ FactorEngine<T>::FactorEngine(const Symbolic& S_, const CSC& A_, const Params& p
     : S(S_), A(A_), prm(p), stream(s) {
   dAvals.alloc(sizeof(double) * std::max<size_t>(1, A.x.size()));
   RSCHOL_CUDA(cudaMemcpyAsync(dAvals.p, A.x.data(), sizeof(double) * A.x.size(), cudaMemcpyHostToDevice, stream));
-  dFlag.alloc(2 * sizeof(int));
+  dFlag.alloc(3 * sizeof(int));
+  waitLimit_ = solvedev::SPIN_LIMIT;
+  if (const char* wl = std::getenv("RSCHOL_WAIT_LIMIT")) {
+    const long v = std::strtol(wl, nullptr, 10);
+    if (v >= 16 && v <= (1L << 26)) waitLimit_ = (int)v;
+  }
+  const char* drop = std::getenv("RSCHOL_TEST_DROP_CHOL_ITEM");
+  dropItemTest_ = drop && drop[0] == '1';
   useTc_ = std::is_same<T, float>::value && tensor_cores_enabled();
   const char* fc = std::getenv("RSCHOL_FUSED_CHOL");
   fusedChol_ = !(fc && fc[0] == '0');
@@ -220,6 +228,14 @@ void FactorEngine<T>::emit_chol(const std::vector<CholJob<T>>& jobs) {
         if (p >= 1 && p <= cholJobs_[q].P) updates(q, p - 1, p + 1, INT_MAX);   // R(p - 1)
       for (int q = j0; q < j1; ++q)
         if (p < cholJobs_[q].P) updates(q, p, p + 1, p + 2);                    // L(p)
+    }
+    if (dropItemTest_ && !droppedItem_) {   // test switch: one POTRF whose TRSMs then wait in vain
+      for (size_t k = (size_t)st.off; k < cholItems_.size(); ++k)
+        if (cholItems_[k].kind == CHOL_POTRF && cholJobs_[cholItems_[k].job].TR > cholItems_[k].p + 1) {
+          cholItems_.erase(cholItems_.begin() + (long)k);
+          droppedItem_ = true;
+          break;
+        }
     }
     st.count = st.grid = (int)(cholItems_.size() - st.off);
     st.elems = sync;
@@ -470,6 +486,7 @@ template <class T>
 void FactorEngine<T>::plan() {
   drop_graphs();   // the captured schedule points into the buffers about to be replaced
   runsSincePlan_ = 0;
+  droppedItem_ = false;
   const int nn = (int)S.nodes.size();
   const int N = S.n;
   steps_.clear();
@@ -1008,7 +1025,7 @@ void FactorEngine<T>::enqueue(bool timing, bool capturing) {
   launches = 0;
   RSCHOL_CUDA(cudaMemsetAsync(dInterior.p, 0, dInterior.bytes, stream));
   RSCHOL_CUDA(cudaMemsetAsync(dCompressed.p, 0, dCompressed.bytes, stream));
-  launch_init_flags(dFlag.as<int>(), stream);   // POTRF code = INT_MAX, tensor-core wait error = 0
+  launch_init_flags(dFlag.as<int>(), waitLimit_, stream);   // POTRF code = INT_MAX, no wait error, poll limit
   launch_scatter<T>(dAvals.as<double>(), dScatSrc_.as<long long>(), dScatDst_.as<long long>(), nScatI_, interior(),
                     stream);
   launch_scatter<T>(dAvals.as<double>(), dScatSrc_.as<long long>() + nScatI_, dScatDst_.as<long long>() + nScatI_,
@@ -1141,9 +1158,8 @@ int FactorEngine<T>::run() {
       std::fclose(fp);
     }
   }
-  if (flag[1])
-    throw CudaError(flag[1] == 2 ? "fused Cholesky: ticket counter out of range"
-                                 : "factor: a bounded wait (tensor-core mbarrier or tile counter) exceeded its limit");
+  if (flag[1] == 2) throw CudaError("fused Cholesky: ticket counter out of range");
+  if (flag[1]) throw FactorWaitTimeout("factor: a bounded wait (tensor-core mbarrier or tile counter) exceeded its limit");
   return flag[0] == INT_MAX ? 0 : flag[0];
 }
 

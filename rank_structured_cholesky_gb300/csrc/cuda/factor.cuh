@@ -197,6 +197,13 @@ class FactorEngine {
   DevBuf dScatSrcC_, dScatDstC_;
   long long nScatI_ = 0, nScatC_ = 0;
   bool planned_ = false;
+  // Polls before a bounded wait of the fused Cholesky gives up
+  // (RSCHOL_WAIT_LIMIT, default solvedev::SPIN_LIMIT).  The test switch
+  // RSCHOL_TEST_DROP_CHOL_ITEM=1 leaves the first POTRF item that TRSM items
+  // depend on out of the plan, so that their waits run out: it exercises the
+  // give-up path (RSCHOL_E_TIMEOUT, context still usable) and nothing else.
+  int waitLimit_ = 0;
+  bool dropItemTest_ = false, droppedItem_ = false;
   // The schedule is static per plan: from the second run of a plan on, the
   // whole factorisation (and the solve-side preparation queued by post) is
   // replayed from a CUDA graph captured once; [1] is the variant with the

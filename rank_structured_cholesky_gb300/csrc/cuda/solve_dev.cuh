@@ -29,11 +29,11 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
 
 // Warp-uniform bounded wait for *p >= target.  Returns false when the wait
-// gave up (after SPIN_LIMIT polls, or as soon as another block reported an
+// gave up (after `limit` polls, or as soon as another block reported an
 // error); the error word is then set.
-__device__ __forceinline__ bool wait_geq(const int* p, int target, int* err) {
+__device__ __forceinline__ bool wait_geq(const int* p, int target, int* err, int limit = SPIN_LIMIT) {
   if (__all_sync(FULL, ld_acquire(p) >= target)) return true;
-  for (int it = 1; it <= SPIN_LIMIT; ++it) {
+  for (int it = 1; it <= limit; ++it) {
     __nanosleep(64);
     if (__all_sync(FULL, ld_acquire(p) >= target)) return true;
     if ((it & 63) == 0 && __any_sync(FULL, ld_volatile(err) != 0)) return false;

@@ -143,16 +143,39 @@ def test_refactor_same_pattern_matches_fresh_factor():
     assert info["true_residual"] <= 1e-8
 
 
-def test_indefinite_matrix_reports_status():
+def indefinite_case(compressed):
+    """A 2D Poisson matrix with one negative diagonal entry placed in an
+    uncompressed (compressed=False) or a compressed supernode, found with the
+    oracle's symbolic plan (the same host code as the library's)."""
     prob = rs.diffusion(2, 12, sigma=0.0)
+    params = dict(max_dense_block=8, max_diag_block=32)
+    O = po.OracleFactor(prob.colptr, prob.rowind, prob.vals, prob.xyz, params)
+    assert O.factor() == 0
+    perm = O.perm()
+    node = next(j for j in range(O.num_nodes()) if bool(O.node_info(j)["compressed"]) == compressed)
+    row = int(perm[O.node_info(node)["c0"]])
     vals = prob.vals.copy()
-    for p in range(prob.colptr[70], prob.colptr[71]):
-        if prob.rowind[p] == 70:
+    for p in range(prob.colptr[row], prob.colptr[row + 1]):
+        if prob.rowind[p] == row:
             vals[p] = -4.0
-    ctx = rs.Context(max_dense_block=8, max_diag_block=32)
+    return prob, params, vals, node
+
+
+@pytest.mark.parametrize("compressed", [False, True])
+def test_indefinite_matrix_reports_status(compressed):
+    """The reference's retry policy: an indefinite diagonal of a compressed
+    supernode is retried (10 attempts, then RSCHOL_E_NOT_PD_AFTER_RETRY); a
+    non-positive pivot of an uncompressed one is where the reference aborts
+    (RSCHOL_E_NOT_PD at once).  The oracle reports the same node."""
+    prob, params, vals, node = indefinite_case(compressed)
+    ctx = rs.Context(**params)
     with pytest.raises(rs.RscholError) as e:
         rs.GpuFactor(ctx, prob.colptr, prob.rowind, vals, prob.xyz)
-    assert e.value.status == 2   # RSCHOL_E_NOT_PD_AFTER_RETRY
+    assert e.value.status == (2 if compressed else 9), str(e.value)
+    assert ("supernode %d" % node) in ctx.last_error()
+    O = po.OracleFactor(prob.colptr, prob.rowind, vals, prob.xyz, params)
+    assert O.factor() == node + 1
+    assert O.times()["attempts"] == (10 if compressed else 1)
 
 
 def test_pcg_pysolve_drop_in():

@@ -80,21 +80,6 @@ def test_identity_basis_fallback_is_exact():
     assert it <= 2 and true < 1e-10
 
 
-def test_indefinite_matrix_exhausts_retries():
-    prob = rs.diffusion(2, 12, sigma=0.0)
-    vals = prob.vals.copy()
-    # make one diagonal entry negative: no rank constant can rescue it
-    for j in range(prob.n):
-        for p in range(prob.colptr[j], prob.colptr[j + 1]):
-            if prob.rowind[p] == j and j == 70:
-                vals[p] = -4.0
-    F = po.OracleFactor(prob.colptr, prob.rowind, vals, prob.xyz, dict(max_dense_block=8, max_diag_block=32))
-    assert F.factor() != 0
-    t = F.times()
-    assert t["attempts"] == 10
-    assert abs(t["diag_rank_constant"] - 0.5 * 1.25 ** 10) < 1e-12
-
-
 def test_recursive_hodlr_diagonal_runs():
     prob, params = make("3d20h")
     F = po.OracleFactor(prob.colptr, prob.rowind, prob.vals, prob.xyz, params)
@@ -103,3 +88,18 @@ def test_recursive_hodlr_diagonal_runs():
     assert max(hn) >= 7    # at least one diagonal with >= 4 leaves
     x, it, rec, true = F.pcg(prob.rhs[0], 1e-8, 500)
     assert true <= 1e-8
+
+
+@pytest.mark.parametrize("compressed", [False, True])
+def test_oracle_retry_policy(compressed):
+    """Indefinite diagonal of a compressed node: 10 attempts with a growing
+    diagonal rank constant; of an uncompressed node: no retry (the
+    reference aborts there)."""
+    from tests.test_gpu_parity import indefinite_case
+    prob, params, vals, node = indefinite_case(compressed)
+    O = po.OracleFactor(prob.colptr, prob.rowind, vals, prob.xyz, params)
+    assert O.factor() == node + 1
+    t = O.times()
+    assert t["attempts"] == (10 if compressed else 1)
+    if compressed:
+        assert abs(t["diag_rank_constant"] - 0.5 * 1.25 ** 10) < 1e-9
