@@ -61,6 +61,7 @@ Params to_params(const rschol_params& p) {
 
 struct Impl {
   virtual ~Impl() = default;
+  unsigned long long planGen = 0;   // bumped by every plan(): the solve's buffers may have moved
   virtual void plan() = 0;
   virtual int run() = 0;
   virtual void apply(double* d_w, cudaStream_t s) = 0;
@@ -95,6 +96,7 @@ struct ImplT : Impl {
   void plan() override {
     fe.plan();
     se.plan();
+    ++planGen;
   }
   void set_schedule(int tcMinK, bool fused) override { fe.set_schedule(tcMinK, fused); }
   int tc_min_k() const override { return fe.tc_min_k(); }
@@ -446,8 +448,8 @@ int rschol_profile(rschol_factor* f, const double* d_b, double* out) {
     launch_gather(d_b, f->dPerm.as<int>(), f->dBp.as<double>(), n, s);
     Impl* impl = f->impl.get();
     RSCHOL_CUDA(cudaEventRecord(e[5], s));
-    PcgResult r = f->pcg->solve(f->dBp.as<double>(), f->dXp.as<double>(), 1e-8, 10000,
-                                [impl, s](double* w) { impl->apply(w, s); });
+    PcgResult r = f->pcg->solve_graph(f->dBp.as<double>(), f->dXp.as<double>(), 1e-8, 10000,
+                                      [impl, s](double* w) { impl->apply(w, s); }, impl->planGen);
     RSCHOL_CUDA(cudaEventRecord(e[6], s));
     RSCHOL_CUDA(cudaEventSynchronize(e[6]));
     float ms[6];
@@ -559,7 +561,7 @@ int rschol_pcg_device(rschol_factor* f, const double* d_b, double* d_x, int nrhs
       auto apply = [impl, s](double* w) { impl->apply(w, s); };
       double t0 = now_s();
       launch_gather(d_b, f->dPerm.as<int>(), f->dBp.as<double>(), n, s);
-      PcgResult r = f->pcg->solve(f->dBp.as<double>(), f->dXp.as<double>(), eps, maxit, apply);
+      PcgResult r = f->pcg->solve_graph(f->dBp.as<double>(), f->dXp.as<double>(), eps, maxit, apply, impl->planGen);
       launch_scatter_perm(f->dXp.as<double>(), f->dPerm.as<int>(), d_x, n, s);
       RSCHOL_CUDA(cudaStreamSynchronize(s));
       if (f->impl->apply_error(s)) return fail(f->ctx, RSCHOL_E_TIMEOUT, kSolveWaitMsg);

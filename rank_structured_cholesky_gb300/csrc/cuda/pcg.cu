@@ -1,5 +1,6 @@
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "pcg.cuh"
 
@@ -11,7 +12,7 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr int VEC_THREADS = 256;
 constexpr int VEC_BLOCKS = 152 * 8;   // fixed grid: 8 CTAs per SM on 152 SMs
 
-enum { S_DELTA = 0, S_ALPHA, S_BETA, S_RREL, S_BNORM, S_DQ, S_DELTA_NEW, S_BREAK, S_COUNT };
+enum { S_DELTA = 0, S_ALPHA, S_BETA, S_RREL, S_BNORM, S_DQ, S_DELTA_NEW, S_BREAK, S_ITERS, S_TRUE, S_COUNT };
 enum { F_ALPHA = 0, F_RNORM, F_BETA, F_DELTA0, F_BNORM, F_TRUE };
 
 __device__ __forceinline__ double block_sum(double v) {
@@ -82,7 +83,7 @@ __global__ void finish_kernel(const double* __restrict__ part, int count, double
     }
     case F_DELTA0: sc[S_DELTA] = t; break;
     case F_BNORM: sc[S_BNORM] = sqrt(t); break;
-    case F_TRUE: sc[S_RREL] = sqrt(t) / sc[S_BNORM]; break;
+    case F_TRUE: sc[S_TRUE] = sqrt(t) / sc[S_BNORM]; break;
   }
 }
 
@@ -121,6 +122,24 @@ __global__ void residual_kernel(const double* __restrict__ b, const double* __re
   }
   double t = block_sum(s);
   if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// Control of the captured solve's WHILE node: the first iteration runs when
+// maxit > 0 (the reference's loop starts with maxR = 2 eps > eps); after each
+// iteration another follows while ||r|| / ||b|| > eps and iterations < maxit
+// (a NaN residual stops it, as the host loop does).  ctl = {eps, maxit}.
+__global__ void pcg_start_kernel(const double* __restrict__ ctl, cudaGraphConditionalHandle h) {
+  pdl_enter();
+  cudaGraphSetConditional(h, ctl[1] > 0.5 ? 1u : 0u);
+}
+
+__global__ void pcg_control_kernel(double* __restrict__ sc, const double* __restrict__ ctl,
+                                   cudaGraphConditionalHandle h) {
+  pdl_enter();
+  const double it = sc[S_ITERS] + 1.0;
+  sc[S_ITERS] = it;
+  const double r = sc[S_RREL];
+  cudaGraphSetConditional(h, (it < ctl[1] && r > ctl[0]) ? 1u : 0u);
 }
 
 __global__ void gather_kernel(const double* __restrict__ src, const int* __restrict__ perm, double* __restrict__ dst,
@@ -176,13 +195,26 @@ PcgEngine::PcgEngine(int n_, const std::vector<int>& rowptr, const std::vector<i
   part_.alloc(sizeof(double) * std::max(nblk_, VEC_BLOCKS));
   scal_.alloc(sizeof(double) * S_COUNT);
   RSCHOL_CUDA(cudaMallocHost((void**)&hScal_, sizeof(double) * S_COUNT));
+  ctl_.alloc(sizeof(double) * 2);
+  RSCHOL_CUDA(cudaMallocHost((void**)&hCtl_, sizeof(double) * 2));
+  const char* g = std::getenv("RSCHOL_PCG_GRAPH");
+  useGraph_ = !(g && g[0] == '0');
   spmvBytes = 12.0 * colind.size() + 4.0 * (n + 1) + 16.0 * n;
   RSCHOL_CUDA(cudaStreamSynchronize(s));
 }
 
 PcgEngine::~PcgEngine() {
+  drop_graph();
   if (hScal_) cudaFreeHost(hScal_);
   if (hScalB_) cudaFreeHost(hScalB_);
+  if (hCtl_) cudaFreeHost(hCtl_);
+}
+
+void PcgEngine::drop_graph() {
+  if (gExec_) cudaGraphExecDestroy(gExec_);
+  gExec_ = nullptr;
+  gB_ = nullptr;
+  gX_ = nullptr;
 }
 
 void PcgEngine::set_values(const std::vector<double>& vals) {
@@ -200,17 +232,14 @@ void PcgEngine::spmv(const double* x, double* y) {
   ++launches;
 }
 
-PcgResult PcgEngine::solve(const double* b, double* x, double eps, int maxit,
-                           const std::function<void(double*)>& apply) {
-  PcgResult res;
+// x0 = 0, r = b, ||b||, s = M^{-1} r, delta = r.s, d = s
+void PcgEngine::prologue(const double* b, double* x, const std::function<void(double*)>& apply) {
   double* r = r_.as<double>();
   double* d = d_.as<double>();
-  double* q = q_.as<double>();
   double* s = s_.as<double>();
   double* part = part_.as<double>();
   double* sc = scal_.as<double>();
   cudaStream_t st = stream_;
-  launches = 0;
   RSCHOL_CUDA(cudaMemsetAsync(sc, 0, sizeof(double) * S_COUNT, st));
   RSCHOL_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
   RSCHOL_CUDA(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
@@ -223,20 +252,53 @@ PcgResult PcgEngine::solve(const double* b, double* x, double eps, int maxit,
   RSCHOL_CUDA(cudaMemcpyAsync(d, s, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   launches += 4;
   RSCHOL_LAUNCH_CHECK();
+}
+
+// q = A d, alpha, x += alpha d, r -= alpha q (s = r), ||r||, s = M^{-1} r,
+// beta, d = s + beta d
+void PcgEngine::iteration(double* x, const std::function<void(double*)>& apply) {
+  double* r = r_.as<double>();
+  double* d = d_.as<double>();
+  double* q = q_.as<double>();
+  double* s = s_.as<double>();
+  double* part = part_.as<double>();
+  double* sc = scal_.as<double>();
+  cudaStream_t st = stream_;
+  spmv(d, q);
+  launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, nblk_, sc, F_ALPHA);
+  launch_k(update_xr_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, x, r, d, q, sc, n, part, s);
+  launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, VEC_BLOCKS, sc, F_RNORM);
+  apply(s);
+  launch_k(dot_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, r, s, n, part);
+  launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, VEC_BLOCKS, sc, F_BETA);
+  launch_k(update_d_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, d, s, sc, n);
+  RSCHOL_LAUNCH_CHECK();
+  launches += 6;
+}
+
+// true residual ||b - A x|| / ||b||
+void PcgEngine::epilogue(const double* b, const double* x) {
+  double* q = q_.as<double>();
+  double* part = part_.as<double>();
+  double* sc = scal_.as<double>();
+  spmv(x, q);
+  launch_k(residual_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, stream_, b, q, n, part);
+  launch_k(finish_kernel, dim3(1), dim3(1024), 0, stream_, part, VEC_BLOCKS, sc, F_TRUE);
+  RSCHOL_LAUNCH_CHECK();
+  launches += 2;
+}
+
+PcgResult PcgEngine::solve(const double* b, double* x, double eps, int maxit,
+                           const std::function<void(double*)>& apply) {
+  PcgResult res;
+  cudaStream_t st = stream_;
+  launches = 0;
+  prologue(b, x, apply);
   double maxR = 2.0 * eps;
   int i = 0;
   while (i < maxit && maxR > eps) {
-    spmv(d, q);
-    launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, nblk_, sc, F_ALPHA);
-    launch_k(update_xr_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, x, r, d, q, sc, n, part, s);
-    launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, VEC_BLOCKS, sc, F_RNORM);
-    apply(s);
-    launch_k(dot_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, r, s, n, part);
-    launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, VEC_BLOCKS, sc, F_BETA);
-    launch_k(update_d_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, d, s, sc, n);
-    RSCHOL_LAUNCH_CHECK();
-    launches += 6;
-    RSCHOL_CUDA(cudaMemcpyAsync(hScal_, sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
+    iteration(x, apply);
+    RSCHOL_CUDA(cudaMemcpyAsync(hScal_, scal_.p, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
     RSCHOL_CUDA(cudaStreamSynchronize(st));
     maxR = hScal_[S_RREL];
     if (hScal_[S_BREAK] != 0.0) res.breakdown = true;
@@ -245,15 +307,94 @@ PcgResult PcgEngine::solve(const double* b, double* x, double eps, int maxit,
   }
   res.iterations = i;
   res.residual = maxR;
-  // true residual ||b - A x|| / ||b||
-  spmv(x, q);
-  launch_k(residual_kernel, dim3(VEC_BLOCKS), dim3(VEC_THREADS), 0, st, b, q, n, part);
-  launch_k(finish_kernel, dim3(1), dim3(1024), 0, st, part, VEC_BLOCKS, sc, F_TRUE);
-  RSCHOL_LAUNCH_CHECK();
-  launches += 2;
-  RSCHOL_CUDA(cudaMemcpyAsync(hScal_, sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
+  epilogue(b, x);
+  RSCHOL_CUDA(cudaMemcpyAsync(hScal_, scal_.p, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
   RSCHOL_CUDA(cudaStreamSynchronize(st));
-  res.trueResidual = hScal_[S_RREL];
+  res.trueResidual = hScal_[S_TRUE];
+  return res;
+}
+
+PcgResult PcgEngine::solve_graph(const double* b, double* x, double eps, int maxit,
+                                 const std::function<void(double*)>& apply, unsigned long long key) {
+  if (!useGraph_) return solve(b, x, eps, maxit, apply);
+  cudaStream_t st = stream_;
+  if (!gExec_ || gB_ != b || gX_ != x || gKey_ != key) {
+    drop_graph();
+    // three captures into one graph: the prologue, the WHILE node's body,
+    // the epilogue after the WHILE node
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    cudaGraph_t g = nullptr;
+    RSCHOL_CUDA(cudaGraphCreate(&g, 0));
+    struct GraphGuard {
+      cudaGraph_t g;
+      ~GraphGuard() { if (g) cudaGraphDestroy(g); }
+    } guard{g};
+    cudaGraphConditionalHandle h;
+    RSCHOL_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+    auto capture = [&](cudaGraph_t into, const cudaGraphNode_t* deps, size_t nDeps,
+                       const std::function<void()>& body) -> std::vector<cudaGraphNode_t> {
+      RSCHOL_CUDA(cudaStreamBeginCaptureToGraph(st, into, deps, nullptr, nDeps, mode));
+      std::vector<cudaGraphNode_t> leaves;
+      try {
+        body();
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* d = nullptr;
+        const cudaGraphEdgeData* ed = nullptr;   // queried so that programmatic edges are not a lossy query
+        size_t nd = 0;
+        RSCHOL_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &d, &ed, &nd));
+        leaves.assign(d, d + nd);
+      } catch (...) {
+        cudaGraph_t dummy;
+        cudaStreamEndCapture(st, &dummy);
+        throw;
+      }
+      cudaGraph_t out = nullptr;
+      RSCHOL_CUDA(cudaStreamEndCapture(st, &out));
+      return leaves;
+    };
+    const double* ctl = ctl_.as<double>();
+    launches = 0;
+    std::vector<cudaGraphNode_t> pro = capture(g, nullptr, 0, [&] {
+      prologue(b, x, apply);
+      launch_k(pcg_start_kernel, dim3(1), dim3(32), 0, st, ctl, h);
+      ++launches;
+    });
+    gPro_ = launches;
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cond;
+    RSCHOL_CUDA(cudaGraphAddNode(&cond, g, pro.data(), nullptr, pro.size(), &cp));
+    cudaGraph_t bodyGraph = cp.conditional.phGraph_out[0];
+    launches = 0;
+    capture(bodyGraph, nullptr, 0, [&] {
+      iteration(x, apply);
+      launch_k(pcg_control_kernel, dim3(1), dim3(32), 0, st, scal_.as<double>(), ctl, h);
+      ++launches;
+    });
+    gBody_ = launches;
+    launches = 0;
+    capture(g, &cond, 1, [&] { epilogue(b, x); });
+    gEpi_ = launches;
+    RSCHOL_CUDA(cudaGraphInstantiate(&gExec_, g, 0));
+    gB_ = b;
+    gX_ = x;
+    gKey_ = key;
+  }
+  hCtl_[0] = eps;
+  hCtl_[1] = (double)maxit;
+  RSCHOL_CUDA(cudaMemcpyAsync(ctl_.p, hCtl_, sizeof(double) * 2, cudaMemcpyHostToDevice, st));
+  RSCHOL_CUDA(cudaGraphLaunch(gExec_, st));
+  RSCHOL_CUDA(cudaMemcpyAsync(hScal_, scal_.p, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
+  RSCHOL_CUDA(cudaStreamSynchronize(st));
+  PcgResult res;
+  res.iterations = (int)hScal_[S_ITERS];
+  res.residual = res.iterations > 0 ? hScal_[S_RREL] : 2.0 * eps;
+  res.trueResidual = hScal_[S_TRUE];
+  res.breakdown = hScal_[S_BREAK] != 0.0;
+  launches = gPro_ + (long long)res.iterations * gBody_ + gEpi_;
   return res;
 }
 

@@ -41,6 +41,17 @@ class PcgEngine {
   // d_b, d_x: permuted vectors on the device.  apply: in-place M^{-1}.
   PcgResult solve(const double* d_b, double* d_x, double eps, int maxit,
                   const std::function<void(double*)>& apply);
+  // The same solve as one CUDA graph: the prologue, a conditional WHILE
+  // node whose body is one iteration (its last kernel decides on the device
+  // whether another follows: ||r|| / ||b|| > eps and fewer than maxit
+  // iterations), and the true-residual epilogue -- one launch and one
+  // read-back per solve instead of a host round trip per iteration.  Built on
+  // the first solve for a (d_b, d_x, key) triple and replayed while they stay
+  // the same; `key` must change whenever apply's buffers do (a new plan).
+  // Same kernels, same order of operations: results are bitwise those of
+  // solve().  RSCHOL_PCG_GRAPH=0 makes it call solve().
+  PcgResult solve_graph(const double* d_b, double* d_x, double eps, int maxit,
+                        const std::function<void(double*)>& apply, unsigned long long key);
   // k right-hand sides at once: B, X are n x k row-major (the k values of a
   // row contiguous), permuted; apply: in-place M^{-1} of such a block.
   // Every column follows the single-vector recurrences and stops on its own
@@ -58,6 +69,19 @@ class PcgEngine {
   cudaStream_t stream_;
   DevBuf rowptr_, colind_, vals_, r_, d_, q_, s_, part_, scal_;
   double* hScal_ = nullptr;   // pinned
+  // the captured solve (solve_graph) and what it was captured for
+  void prologue(const double* b, double* x, const std::function<void(double*)>& apply);
+  void iteration(double* x, const std::function<void(double*)>& apply);
+  void epilogue(const double* b, const double* x);
+  void drop_graph();
+  cudaGraphExec_t gExec_ = nullptr;
+  const double* gB_ = nullptr;
+  double* gX_ = nullptr;
+  unsigned long long gKey_ = 0;
+  long long gPro_ = 0, gBody_ = 0, gEpi_ = 0;   // own kernel launches of the three parts
+  DevBuf ctl_;                 // eps, maxit of the current solve (read by the graph's control kernels)
+  double* hCtl_ = nullptr;     // pinned
+  bool useGraph_ = true;
   int nblk_ = 0;
   int tpr_ = 8;
   // batched solves (allocated for kB_ right-hand sides on first use)

@@ -133,7 +133,6 @@ class SolveEngine {
   DevBuf dIWorkS_, dIWorkSB_, dSmall_;
   int nIWorkS_ = 0;
   size_t smemWarps_ = 0;
-  int epoch_ = 0;                     // apply counter: the interior completion targets
   DevBuf dX_, dT1_, dXGemm_;          // compressed L11^{-1}, its temporaries and GEMM tasks
   DevBuf dXp_, dTiles_;               // tile partials of the X products, tile lists
   std::vector<std::pair<long long, int>> cTiles_;   // per compressed level: (offset, count) of tiles

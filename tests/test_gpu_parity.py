@@ -244,3 +244,25 @@ def test_fused_and_per_panel_factor_paths_agree(precision, tol, oracles, monkeyp
     y_ref = O.apply(b)
     assert rel(y_fused, y_ref) < tol and rel(y_panel, y_ref) < tol
     assert rel(y_fused, y_panel) < tol
+
+
+@pytest.mark.parametrize("precision", [rs.FP64, rs.MIXED])
+def test_graph_pcg_matches_host_loop(precision, monkeypatch):
+    """The PCG solve captured as one CUDA graph (a conditional WHILE node
+    decides on the device whether another iteration follows) runs the same
+    kernels in the same order as the host-driven loop (RSCHOL_PCG_GRAPH=0):
+    bitwise the same iterates and counts, for any eps / maxit, replayed across
+    calls and with applies in between."""
+    prob, params = make("3d20h")
+    b = prob.rhs[0]
+    monkeypatch.setenv("RSCHOL_PCG_GRAPH", "0")
+    H = gpu_factor(prob, params, precision=precision)
+    monkeypatch.delenv("RSCHOL_PCG_GRAPH")
+    G = gpu_factor(prob, params, precision=precision)
+    for eps, maxit in [(1e-8, 500), (1e-4, 500), (1e-12, 3), (1e-8, 0), (1e-8, 500)]:
+        xh, ih = H.pcg(b, eps, maxit)
+        xg, ig = G.pcg(b, eps, maxit)
+        assert ih["iterations"] == ig["iterations"], (eps, maxit, ih, ig)
+        assert np.array_equal(xh, xg)
+        assert ih["true_residual"] == ig["true_residual"]
+        assert np.array_equal(H.apply(b), G.apply(b))
