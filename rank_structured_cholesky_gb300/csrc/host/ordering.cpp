@@ -6,7 +6,10 @@
 #include <functional>
 #include <future>
 #include <numeric>
+#include <queue>
 #include <stdexcept>
+#include <string>
+#include <cstdlib>
 
 namespace rschol {
 
@@ -22,7 +25,7 @@ struct NDState {
   const double* xyz;
   int leaf;
   std::vector<int> mark;      // scratch: membership stamp
-  std::vector<int> level;     // scratch: BFS level
+  std::vector<int> level;     // scratch: local index of a vertex in the set being split
   int stamp = 0;
   std::vector<std::vector<int>> compMembers;
   std::vector<int> compParent;
@@ -138,13 +141,401 @@ void graph_split(NDState& S, const std::vector<int>& set, std::vector<int>& L,
   std::sort(sep.begin(), sep.end());
 }
 
+// ---------------------------------------------------------------------------
+// Multilevel vertex-separator bisection for matrices without coordinates
+// (the role METIS's node bisection plays inside cholmod_nested_dissection,
+// CHOLMOD_Environment.cpp:326-432): heavy-edge-matching coarsening, greedy
+// graph-growing bisection of the coarsest graph, Fiduccia-Mattheyses
+// refinement of the edge cut at every level on the way back, and a minimum
+// vertex cover of the final cut edges (Koenig's theorem) as the separator.
+// Deterministic: every choice depends on the graph and vertex order only.
+// ---------------------------------------------------------------------------
+struct WGraph {   // weighted undirected graph (CSR, no self loops)
+  int n = 0;
+  std::vector<int> xadj, adj, ew, vw;
+  long long totalW = 0;
+};
+
+// The subgraph of A induced on set (local index k <-> set[k]).
+WGraph induced_graph(NDState& S, const std::vector<int>& set) {
+  WGraph G;
+  G.n = (int)set.size();
+  ++S.stamp;
+  const int in = S.stamp;
+  for (int k = 0; k < G.n; ++k) {
+    S.mark[set[k]] = in;
+    S.level[set[k]] = k;
+  }
+  G.xadj.assign(G.n + 1, 0);
+  for (int k = 0; k < G.n; ++k) {
+    const int v = set[k];
+    int deg = 0;
+    for (int p = S.A->p[v]; p < S.A->p[v + 1]; ++p) {
+      const int w = S.A->i[p];
+      if (w != v && S.mark[w] == in) ++deg;
+    }
+    G.xadj[k + 1] = G.xadj[k] + deg;
+  }
+  G.adj.resize(G.xadj[G.n]);
+  for (int k = 0; k < G.n; ++k) {
+    const int v = set[k];
+    int q = G.xadj[k];
+    for (int p = S.A->p[v]; p < S.A->p[v + 1]; ++p) {
+      const int w = S.A->i[p];
+      if (w != v && S.mark[w] == in) G.adj[q++] = S.level[w];
+    }
+  }
+  G.ew.assign(G.adj.size(), 1);
+  G.vw.assign(G.n, 1);
+  G.totalW = G.n;
+  return G;
+}
+
+// Heavy-edge matching: each unmatched vertex (in order of increasing
+// degree, ties by index) is matched with its unmatched neighbour of heaviest
+// edge (ties: lighter vertex, then lower index).  Returns the coarse graph
+// and cmap (fine -> coarse).
+WGraph coarsen(const WGraph& G, std::vector<int>& cmap) {
+  std::vector<int> order(G.n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return G.xadj[a + 1] - G.xadj[a] < G.xadj[b + 1] - G.xadj[b]; });
+  std::vector<int> match(G.n, -1);
+  for (int v : order) {
+    if (match[v] >= 0) continue;
+    int best = -1, bw = -1, bvw = 0;
+    for (int p = G.xadj[v]; p < G.xadj[v + 1]; ++p) {
+      const int u = G.adj[p];
+      if (match[u] >= 0) continue;
+      if (G.ew[p] > bw || (G.ew[p] == bw && (G.vw[u] < bvw || (G.vw[u] == bvw && u < best)))) {
+        best = u;
+        bw = G.ew[p];
+        bvw = G.vw[u];
+      }
+    }
+    if (best >= 0) {
+      match[v] = best;
+      match[best] = v;
+    } else {
+      match[v] = v;
+    }
+  }
+  cmap.assign(G.n, -1);
+  WGraph C;
+  for (int v = 0; v < G.n; ++v) {
+    if (cmap[v] >= 0) continue;
+    cmap[v] = C.n;
+    if (match[v] != v) cmap[match[v]] = C.n;
+    ++C.n;
+  }
+  C.vw.assign(C.n, 0);
+  for (int v = 0; v < G.n; ++v) C.vw[cmap[v]] += G.vw[v];
+  C.totalW = G.totalW;
+  // coarse adjacency: fine vertices grouped by coarse vertex, edges summed
+  std::vector<int> first(C.n, -1), second(C.n, -1);
+  for (int v = 0; v < G.n; ++v) {
+    const int c = cmap[v];
+    if (first[c] < 0) first[c] = v;
+    else second[c] = v;
+  }
+  std::vector<int> slot(C.n, -1);
+  C.xadj.assign(C.n + 1, 0);
+  std::vector<int> nbr, wgt;
+  for (int c = 0; c < C.n; ++c) {
+    nbr.clear();
+    wgt.clear();
+    for (int v : {first[c], second[c]}) {
+      if (v < 0) continue;
+      for (int p = G.xadj[v]; p < G.xadj[v + 1]; ++p) {
+        const int d = cmap[G.adj[p]];
+        if (d == c) continue;
+        if (slot[d] < 0) {
+          slot[d] = (int)nbr.size();
+          nbr.push_back(d);
+          wgt.push_back(0);
+        }
+        wgt[slot[d]] += G.ew[p];
+      }
+    }
+    for (int d : nbr) slot[d] = -1;
+    C.adj.insert(C.adj.end(), nbr.begin(), nbr.end());
+    C.ew.insert(C.ew.end(), wgt.begin(), wgt.end());
+    C.xadj[c + 1] = (int)C.adj.size();
+  }
+  return C;
+}
+
+long long cut_weight(const WGraph& G, const std::vector<char>& part) {
+  long long cut = 0;
+  for (int v = 0; v < G.n; ++v)
+    for (int p = G.xadj[v]; p < G.xadj[v + 1]; ++p)
+      if (part[v] != part[G.adj[p]]) cut += G.ew[p];
+  return cut / 2;
+}
+
+// Fiduccia-Mattheyses passes on the edge cut: vertices move, highest gain
+// first (ties: lower index), each at most once per pass, while neither side
+// grows beyond maxSide; the pass is rolled back to its best prefix.
+void fm_refine(const WGraph& G, std::vector<char>& part, long long maxSide, int passes) {
+  long long w[2] = {0, 0};
+  for (int v = 0; v < G.n; ++v) w[(int)part[v]] += G.vw[v];
+  std::vector<long long> gain(G.n);
+  std::vector<char> locked(G.n);
+  std::vector<int> moves;
+  for (int pass = 0; pass < passes; ++pass) {
+    for (int v = 0; v < G.n; ++v) {
+      long long g = 0;
+      for (int p = G.xadj[v]; p < G.xadj[v + 1]; ++p) g += part[G.adj[p]] != part[v] ? G.ew[p] : -G.ew[p];
+      gain[v] = g;
+    }
+    std::fill(locked.begin(), locked.end(), 0);
+    using Item = std::pair<long long, int>;   // (gain, -vertex): max gain, then lowest index
+    std::priority_queue<Item> pq;
+    for (int v = 0; v < G.n; ++v) {
+      bool boundary = false;
+      for (int p = G.xadj[v]; p < G.xadj[v + 1] && !boundary; ++p) boundary = part[G.adj[p]] != part[v];
+      if (boundary) pq.push({gain[v], -v});
+    }
+    moves.clear();
+    long long cut = 0, best = 0;   // relative to the pass start
+    size_t bestLen = 0;
+    long long bestImb = std::llabs(w[0] - w[1]);
+    const size_t patience = 64 + (size_t)G.n / 64;
+    while (!pq.empty()) {
+      const Item it = pq.top();
+      pq.pop();
+      const int v = -it.second;
+      if (locked[v] || it.first != gain[v]) continue;   // moved already, or a stale entry
+      const int from = part[v], to = 1 - from;
+      if (w[to] + G.vw[v] > maxSide) continue;
+      locked[v] = 1;
+      part[v] = (char)to;
+      w[from] -= G.vw[v];
+      w[to] += G.vw[v];
+      cut -= gain[v];
+      moves.push_back(v);
+      for (int p = G.xadj[v]; p < G.xadj[v + 1]; ++p) {
+        const int u = G.adj[p];
+        if (locked[u]) continue;
+        gain[u] += part[u] == to ? -2LL * G.ew[p] : 2LL * G.ew[p];
+        pq.push({gain[u], -u});
+      }
+      const long long imb = std::llabs(w[0] - w[1]);
+      if (cut < best || (cut == best && imb < bestImb)) {
+        best = cut;
+        bestLen = moves.size();
+        bestImb = imb;
+      }
+      if (moves.size() - bestLen > patience) break;
+    }
+    for (size_t k = moves.size(); k > bestLen; --k) {   // roll back past the best prefix
+      const int v = moves[k - 1];
+      const int from = part[v], to = 1 - from;
+      part[v] = (char)to;
+      w[from] -= G.vw[v];
+      w[to] += G.vw[v];
+    }
+    if (bestLen == 0) break;
+  }
+}
+
+// Greedy graph growing: side 0 grows breadth-first from `seed` (continuing
+// from the lowest unvisited vertex when a component is exhausted) until it
+// holds half the vertex weight.
+std::vector<char> grow_bisection(const WGraph& G, int seed) {
+  std::vector<char> part(G.n, 1);
+  std::vector<char> seen(G.n, 0);
+  long long w0 = 0;
+  const long long half = G.totalW / 2;
+  std::vector<int> queue;
+  queue.reserve(G.n);
+  size_t head = 0;
+  int nextStart = 0;
+  queue.push_back(seed);
+  seen[seed] = 1;
+  while (w0 < half) {
+    if (head == queue.size()) {
+      while (nextStart < G.n && seen[nextStart]) ++nextStart;
+      if (nextStart >= G.n) break;
+      queue.push_back(nextStart);
+      seen[nextStart] = 1;
+    }
+    const int v = queue[head++];
+    part[v] = 0;
+    w0 += G.vw[v];
+    for (int p = G.xadj[v]; p < G.xadj[v + 1]; ++p) {
+      const int u = G.adj[p];
+      if (!seen[u]) {
+        seen[u] = 1;
+        queue.push_back(u);
+      }
+    }
+  }
+  return part;
+}
+
+// Minimum vertex cover of the cut edges (bipartite: side-0 vs side-1
+// boundary vertices) by a maximum matching and Koenig's construction.
+std::vector<int> cut_cover(const WGraph& G, const std::vector<char>& part) {
+  std::vector<int> mate(G.n, -1);
+  std::vector<int> left;   // side-0 boundary vertices
+  for (int v = 0; v < G.n; ++v) {
+    if (part[v] != 0) continue;
+    for (int p = G.xadj[v]; p < G.xadj[v + 1]; ++p)
+      if (part[G.adj[p]] == 1) { left.push_back(v); break; }
+  }
+  // augmenting paths (iterative DFS from each free left vertex)
+  std::vector<int> visitStamp(G.n, -1), parentL(G.n, -1), iter(G.n, 0);
+  for (size_t k = 0; k < left.size(); ++k) {
+    const int root = left[k];
+    std::vector<int> stack{root};
+    iter[root] = G.xadj[root];
+    visitStamp[root] = (int)k;
+    int freeR = -1;
+    while (!stack.empty() && freeR < 0) {
+      const int v = stack.back();
+      bool pushed = false;
+      while (iter[v] < G.xadj[v + 1]) {
+        const int u = G.adj[iter[v]++];
+        if (part[u] != 1 || visitStamp[u] == (int)k) continue;
+        visitStamp[u] = (int)k;
+        parentL[u] = v;
+        if (mate[u] < 0) { freeR = u; break; }
+        const int w = mate[u];
+        if (visitStamp[w] == (int)k) continue;
+        visitStamp[w] = (int)k;
+        iter[w] = G.xadj[w];
+        stack.push_back(w);
+        pushed = true;
+        break;
+      }
+      if (freeR < 0 && !pushed) stack.pop_back();
+    }
+    for (int u = freeR; u >= 0;) {   // flip the path
+      const int v = parentL[u];
+      const int next = mate[v];
+      mate[v] = u;
+      mate[u] = v;
+      u = next;
+    }
+  }
+  // Z: reachable from free left vertices by alternating paths
+  std::vector<char> inZ(G.n, 0);
+  std::vector<int> stack;
+  for (int v : left)
+    if (mate[v] < 0) { inZ[v] = 1; stack.push_back(v); }
+  while (!stack.empty()) {
+    const int v = stack.back();
+    stack.pop_back();
+    for (int p = G.xadj[v]; p < G.xadj[v + 1]; ++p) {
+      const int u = G.adj[p];
+      if (part[u] != 1 || inZ[u] || mate[v] == u) continue;
+      inZ[u] = 1;
+      const int w = mate[u];
+      if (w >= 0 && !inZ[w]) { inZ[w] = 1; stack.push_back(w); }
+    }
+  }
+  std::vector<int> cover;
+  for (int v = 0; v < G.n; ++v) {
+    bool boundary = false;
+    for (int p = G.xadj[v]; p < G.xadj[v + 1] && !boundary; ++p) boundary = part[G.adj[p]] != part[v];
+    if (!boundary) continue;
+    if ((part[v] == 0 && !inZ[v]) || (part[v] == 1 && inZ[v])) cover.push_back(v);
+  }
+  return cover;
+}
+
+bool bfs_nd() {
+  static const bool bfs = [] {
+    const char* e = std::getenv("RSCHOL_GRAPH_ND");
+    return e && std::string(e) == "bfs";
+  }();
+  return bfs;
+}
+
+void multilevel_split(NDState& S, const std::vector<int>& set, std::vector<int>& L, std::vector<int>& R,
+                      std::vector<int>& sep) {
+  std::vector<WGraph> levels;
+  std::vector<std::vector<int>> maps;
+  levels.push_back(induced_graph(S, set));
+  while (levels.back().n > 120 && levels.size() < 48) {
+    std::vector<int> cmap;
+    WGraph C = coarsen(levels.back(), cmap);
+    if (C.n > (int)(0.92 * levels.back().n)) break;   // matching stalled
+    maps.push_back(std::move(cmap));
+    levels.push_back(std::move(C));
+  }
+  auto maxSide = [](const WGraph& G) {
+    long long mx = 0;
+    for (int w : G.vw) mx = std::max<long long>(mx, w);
+    return std::max((long long)std::ceil(0.55 * (double)G.totalW), (G.totalW + 1) / 2 + mx);
+  };
+  // coarsest level: the best of a few grown bisections
+  const WGraph& C = levels.back();
+  std::vector<char> part;
+  long long bestCut = -1;
+  const int seeds[4] = {0, C.n / 3, (2 * C.n) / 3, C.n - 1};
+  for (int k = 0; k < 4; ++k) {
+    if (k > 0 && seeds[k] == seeds[k - 1]) continue;
+    std::vector<char> p = grow_bisection(C, seeds[k]);
+    fm_refine(C, p, maxSide(C), 8);
+    const long long cut = cut_weight(C, p);
+    if (bestCut < 0 || cut < bestCut) {
+      bestCut = cut;
+      part.swap(p);
+    }
+  }
+  for (int l = (int)levels.size() - 2; l >= 0; --l) {   // project and refine
+    std::vector<char> fine(levels[l].n);
+    for (int v = 0; v < levels[l].n; ++v) fine[v] = part[maps[l][v]];
+    fm_refine(levels[l], fine, maxSide(levels[l]), 4);
+    part.swap(fine);
+  }
+  const WGraph& G = levels.front();
+  std::vector<int> cover = cut_cover(G, part);
+  std::vector<char> inSep(G.n, 0);
+  for (int v : cover) inSep[v] = 1;
+  for (int k = 0; k < G.n; ++k) {
+    if (inSep[k]) sep.push_back(set[k]);
+    else if (part[k] == 0) L.push_back(set[k]);
+    else R.push_back(set[k]);
+  }
+  if (sep.empty() && !L.empty() && !R.empty()) {   // disconnected halves: a one-vertex separator
+    sep.push_back(R.back());
+    R.pop_back();
+  }
+  std::sort(L.begin(), L.end());
+  std::sort(R.begin(), R.end());
+  std::sort(sep.begin(), sep.end());
+}
+
 // Split set into L, R and the separator; false: keep it as one component.
 bool split(NDState& S, const std::vector<int>& set, std::vector<int>& L, std::vector<int>& R,
            std::vector<int>& sep) {
   if ((int)set.size() <= S.leaf) return false;
   bool ok = false;
   if (S.xyz) ok = geometric_split(S, set, L, R, sep);
-  if (!ok) { L.clear(); R.clear(); sep.clear(); graph_split(S, set, L, R, sep); }
+  if (!ok) {
+    // without coordinates: the level-structure bisection and the multilevel
+    // one, keeping the smaller separator (ties: the better balanced split)
+    L.clear();
+    R.clear();
+    sep.clear();
+    graph_split(S, set, L, R, sep);
+    if (!bfs_nd()) {
+      std::vector<int> L2, R2, sep2;
+      multilevel_split(S, set, L2, R2, sep2);
+      const bool valid = !(sep2.empty() || L2.empty() || R2.empty());
+      auto imb = [](const std::vector<int>& a, const std::vector<int>& b) {
+        return std::abs((long long)a.size() - (long long)b.size());
+      };
+      if (valid && (sep2.size() < sep.size() || (sep2.size() == sep.size() && imb(L2, R2) < imb(L, R)))) {
+        L.swap(L2);
+        R.swap(R2);
+        sep.swap(sep2);
+      }
+    }
+  }
   return !(sep.empty() || (L.empty() && R.empty()));
 }
 
@@ -187,6 +578,7 @@ int dissect_parallel(NDState& S, std::vector<int> set, int depth) {
     T.xyz = S.xyz;
     T.leaf = S.leaf;
     T.mark.assign(S.mark.size(), 0);
+    T.level.assign(S.mark.size(), 0);
     return T;
   };
   NDState SL = fresh(), SR = fresh();
@@ -213,6 +605,7 @@ void nested_dissection(const CSC& A, const double* xyz, int ndLeaf, std::vector<
   S.xyz = xyz;
   S.leaf = std::max(1, ndLeaf);
   S.mark.assign(A.n, 0);
+  S.level.assign(A.n, 0);
   std::vector<int> all(A.n);
   std::iota(all.begin(), all.end(), 0);
   // Disconnected pieces are handled by the bisection itself.  The top four
