@@ -15,6 +15,7 @@ namespace {
 
 using solvedev::st_release;
 using solvedev::wait_geq;
+using solvedev::wait_geq_lim;
 
 constexpr int BM = 64, BN = 64, BK = 16, GEMM_THREADS = 256;
 
@@ -544,18 +545,18 @@ __global__ void __launch_bounds__(256) chol_fused_kernel(const CholFusedJob<T>* 
   int* tdone = cnt + j.TR * j.TU;  // TR: panels whose TRSM of row tile a is done
   int* pdone = tdone + j.TR;       // P: POTRF of panel p done
   const int p = it.p, a = it.a, b = it.b;
-  const int lim = flag[2];   // polls before a wait gives up (set with the flags before the factorisation)
+  const int* lim = flag + 2;   // polls before a wait gives up (set with the flags before the factorisation)
   auto bnd = [&](int t) { return t == 0 ? 0 : j.w0 + 64 * (t - 1); };      // columns (and Cholesky rows)
   auto rbnd = [&](int t) { return t == 0 ? 0 : j.r1 + 64 * (t - 1); };     // rows
   const int c0 = bnd(p), wp = bnd(p + 1) - c0;
   if ((threadIdx.x >> 5) == 0) {
     bool ok;
-    if (it.kind == CHOL_POTRF) ok = j.L ? true : wait_geq(cnt + p * j.TU + p, p, err, lim);
+    if (it.kind == CHOL_POTRF) ok = j.L ? true : wait_geq_lim(cnt + p * j.TU + p, p, err, lim);
     else if (it.kind == CHOL_TRSM)
-      ok = wait_geq(pdone + p, 1, err, lim) && wait_geq(cnt + a * j.TU + p, p, err, lim);
+      ok = wait_geq_lim(pdone + p, 1, err, lim) && wait_geq_lim(cnt + a * j.TU + p, p, err, lim);
     else
-      ok = wait_geq(tdone + a, p + 1, err, lim) && (j.L || wait_geq(tdone + b, p + 1, err, lim)) &&
-           wait_geq(cnt + a * j.TU + b, p, err, lim);
+      ok = wait_geq_lim(tdone + a, p + 1, err, lim) && (j.L || wait_geq_lim(tdone + b, p + 1, err, lim)) &&
+           wait_geq_lim(cnt + a * j.TU + b, p, err, lim);
     if (threadIdx.x == 0) {
       sOk = ok;
       if (trace) tReady = globaltimer_ns();

@@ -194,21 +194,22 @@ __device__ void interior_backward_warp(const SNode<T>* __restrict__ nodes, int s
 // the next (supernode, 128-row chunk of its off-diagonal rows) from a ticket
 // counter, in level order, so it only waits on blocks that started before it:
 // forward, on the chunk blocks of the supernode's children (per-supernode
-// completion counters that grow by one per chunk and apply); backward, on
-// the solve of its interior parent (a flag set to the apply's epoch).  Every
-// chunk block assembles and solves the supernode's own n columns (n is small);
-// chunk 0 stores y.
+// completion counters that grow by one per chunk); backward, on the solve of
+// its interior parent (a flag set to 1).  The apply's last kernel clears the
+// counters (clear_piece), so every apply starts from zeros with no host
+// state and the same launches replay unchanged inside a CUDA graph.  Every
+// chunk block assembles and solves the supernode's own n columns (n is
+// small); chunk 0 stores y.
 
 template <class T>
 __global__ void __launch_bounds__(256) interior_forward_chunks(const SNode<T>* __restrict__ nodes,
                                                                const RowBlock* __restrict__ work,
                                                                const int* __restrict__ rel,
                                                                const int* __restrict__ child,
-                                                               int* __restrict__ sync, const int* __restrict__ epochP,
+                                                               int* __restrict__ sync, int epoch,
                                                                const T* __restrict__ w, T* __restrict__ yout,
                                                                T* __restrict__ wu, const int* __restrict__ small) {
   pdl_enter();
-  const int epoch = __ldcg(epochP) + 1;   // this apply's number (advanced by the apply's last kernel)
   extern __shared__ __align__(16) unsigned char smraw[];
   T* f = reinterpret_cast<T*>(smraw);
   __shared__ T tb[64];
@@ -289,11 +290,10 @@ template <class T>
 __global__ void __launch_bounds__(256) interior_backward_chunks(const SNode<T>* __restrict__ nodes,
                                                                 const RowBlock* __restrict__ work,
                                                                 const int* __restrict__ rows,
-                                                                int* __restrict__ sync, const int* __restrict__ epochP,
+                                                                int* __restrict__ sync, int epoch,
                                                                 T* __restrict__ ipart, const T* __restrict__ yin,
                                                                 T* __restrict__ w, const int* __restrict__ small) {
   pdl_enter();
-  const int epoch = __ldcg(epochP) + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ T tb[64];
   __shared__ T red[8][256];
@@ -668,37 +668,25 @@ __global__ void convert_kernel(const A* __restrict__ src, B* __restrict__ dst, i
   if (i < n) dst[i] = (B)src[i];
 }
 
-// The single-vector apply's epoch lives on the device (sync[syncInts], so
-// that a captured apply replays correctly): every interior kernel of an
-// apply targets *epochP + 1, and the apply's last kernel advances it.  Block
-// 0 alone advances it (other blocks may start later and must not see a
-// changed value), and far from overflow restarts it at 0 with every counter
-// zeroed, as a fresh plan has them.
-__device__ __forceinline__ void advance_epoch(int* sync, int syncInts) {
-  if (blockIdx.x != 0) return;
-  const int e = __ldcg(sync + syncInts) + 1;
-  __syncthreads();
-  if (e < (1 << 24)) {
-    if (threadIdx.x == 0) sync[syncInts] = e;
-    return;
-  }
-  for (int i = threadIdx.x; i <= syncInts; i += blockDim.x) sync[i] = 0;
+// Zero the interior completion counters and solved flags after their last
+// reader (the backward launch), grid-stride.
+__device__ __forceinline__ void clear_piece(int* c, int count) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) c[i] = 0;
 }
 
-// last kernel of a mixed-precision apply: w64 = (double) w, epoch advanced
+__global__ void clear_counters(int* __restrict__ c, int count) {
+  pdl_enter();
+  clear_piece(c, count);
+}
+
+// last kernel of a mixed-precision apply: w64 = (double) w and the counters cleared
 template <class T>
-__global__ void convert_out_kernel(const T* __restrict__ src, double* __restrict__ dst, int n, int* sync,
-                                   int syncInts) {
+__global__ void convert_out_kernel(const T* __restrict__ src, double* __restrict__ dst, int n, int* __restrict__ c,
+                                   int count) {
   pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = (double)src[i];
-  advance_epoch(sync, syncInts);
-}
-
-// last kernel of an FP64 apply
-__global__ void epoch_kernel(int* sync, int syncInts) {
-  pdl_enter();
-  advance_epoch(sync, syncInts);
+  if (c) clear_piece(c, count);
 }
 
 }  // namespace
@@ -739,7 +727,7 @@ void SolveEngine<T>::plan() {
       wuCur += nd.m();
       sn.nch = (nd.m() + ICH - 1) / ICH;
       sn.syncOff = syncCur;
-      syncCur += 3;   // backward chunk counter, forward completion count, backward solved epoch
+      syncCur += 3;   // backward chunk counter, forward completion count, backward solved flag
       sn.parentI = (nd.parent >= 0 && !S.nodes[nd.parent].compressed) ? nd.parent : -1;
       sn.zpOff = ipCur;
       ipCur += (long long)sn.nch * nd.n;
@@ -991,15 +979,15 @@ void SolveEngine<T>::plan() {
   up(dTiles_, xtiles.data(), xtiles.size() * sizeof(XTile));
   up(dDinvTasks_, dinvTasks.data(), dinvTasks.size() * sizeof(DinvTask<T>));
   syncInts_ = syncCur;
-  dSync_.alloc(sizeof(int) * (syncCur + 1));   // + the single-vector apply's epoch
-  RSCHOL_CUDA(cudaMemsetAsync(dSync_.p, 0, sizeof(int) * (syncCur + 1), st));
+  dSync_.alloc(sizeof(int) * syncCur);
+  RSCHOL_CUDA(cudaMemsetAsync(dSync_.p, 0, sizeof(int) * syncCur, st));
   if (!std::is_same<T, double>::value) dW_.alloc(sizeof(T) * std::max(1, S.n));
   RSCHOL_CUDA(cudaStreamSynchronize(st));
   const int maxSmem = 200 * 1024;
   RSCHOL_CUDA(cudaFuncSetAttribute(interior_forward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
   RSCHOL_CUDA(cudaFuncSetAttribute(interior_backward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
   launchesPerApply_ = (iLevels_.empty() ? 0 : 2) + 8 * (long long)cLevels_.size() - (cLevels_.empty() ? 0 : 1) +
-                      (std::is_same<T, double>::value ? 1 : 2);
+                      (std::is_same<T, double>::value ? (nIWorkS_ > 0 ? 1 : 0) : 2);
   bytesPerApply_ += 8.0 * 4 * S.n;
 }
 
@@ -1120,8 +1108,8 @@ int SolveEngine<T>::take_error(cudaStream_t st) {
   RSCHOL_CUDA(cudaMemcpyAsync(&e, dSync_.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   RSCHOL_CUDA(cudaStreamSynchronize(st));
   if (e) {
-    // a wait gave up: counters, flags and the epoch are in an unknown state; start over
-    RSCHOL_CUDA(cudaMemsetAsync(dSync_.p, 0, sizeof(int) * (syncInts_ + 1), st));
+    // a wait gave up: counters and flags are in an unknown state; start over
+    RSCHOL_CUDA(cudaMemsetAsync(dSync_.p, 0, sizeof(int) * syncInts_, st));
     RSCHOL_CUDA(cudaStreamSynchronize(st));
   }
   return e;
@@ -1138,9 +1126,9 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
   }
   const int* lvl = dLevelNodes_.as<int>();
   int* sync = dSync_.as<int>();
-  const int* epochP = sync + syncInts_;
+  const int epoch = 1;   // completion targets: every apply starts its counters at zero
   if (nIWorkS_ > 0) {
-    launch_k(interior_forward_chunks<T>, dim3(nIWorkS_), dim3(256), std::max(smemIFmax_, smemWarps_), st, dNodes_.as<SNode<T>>(), dIWorkS_.as<RowBlock>(), dRel_.as<int>(), dChild_.as<int>(), sync, epochP, w, dYi_.as<T>(), dWu_.as<T>(), dSmall_.as<int>());
+    launch_k(interior_forward_chunks<T>, dim3(nIWorkS_), dim3(256), std::max(smemIFmax_, smemWarps_), st, dNodes_.as<SNode<T>>(), dIWorkS_.as<RowBlock>(), dRel_.as<int>(), dChild_.as<int>(), sync, epoch, w, dYi_.as<T>(), dWu_.as<T>(), dSmall_.as<int>());
     RSCHOL_LAUNCH_CHECK();
   }
   T* yv = dYi_.as<T>();
@@ -1169,15 +1157,19 @@ void SolveEngine<T>::apply_inplace(double* w64, cudaStream_t st) {
     RSCHOL_LAUNCH_CHECK();
   }
   if (nIWorkS_ > 0) {
-    launch_k(interior_backward_chunks<T>, dim3(nIWorkS_), dim3(256), std::max(smemIBmax_, smemWarps_), st, dNodes_.as<SNode<T>>(), dIWorkSB_.as<RowBlock>(), dRows_.as<int>(), sync, epochP, dIp_.as<T>(), dYi_.as<T>(), w, dSmall_.as<int>());
+    launch_k(interior_backward_chunks<T>, dim3(nIWorkS_), dim3(256), std::max(smemIBmax_, smemWarps_), st, dNodes_.as<SNode<T>>(), dIWorkSB_.as<RowBlock>(), dRows_.as<int>(), sync, epoch, dIp_.as<T>(), dYi_.as<T>(), w, dSmall_.as<int>());
     RSCHOL_LAUNCH_CHECK();
   }
+  // the interior counters are cleared by the apply's last kernel
+  int* clr = nIWorkS_ > 0 ? sync + SYNC_GLOBAL : nullptr;
+  const int nClr = nIWorkS_ > 0 ? syncInts_ - SYNC_GLOBAL : 0;
   if (!std::is_same<T, double>::value) {
-    launch_k(convert_out_kernel<T>, dim3((n + 255) / 256), dim3(256), 0, st, (const T*)w, w64, n, sync, syncInts_);
-  } else {
-    launch_k(epoch_kernel, dim3(1), dim3(256), 0, st, sync, syncInts_);
+    launch_k(convert_out_kernel<T>, dim3((n + 255) / 256), dim3(256), 0, st, (const T*)w, w64, n, clr, nClr);
+    RSCHOL_LAUNCH_CHECK();
+  } else if (nClr > 0) {
+    launch_k(clear_counters, dim3((nClr + 1023) / 1024), dim3(256), 0, st, clr, nClr);
+    RSCHOL_LAUNCH_CHECK();
   }
-  RSCHOL_LAUNCH_CHECK();
 }
 
 template class SolveEngine<double>;

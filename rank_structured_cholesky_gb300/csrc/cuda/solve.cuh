@@ -51,7 +51,7 @@ struct SNode {
   int childBegin, childEnd;   // interior: children (range in the child list)
   int nb, nch;                // compressed: row blocks of L11; both: 128-row chunks of V / L21
   int syncOff;                // compressed: 2 completion counters; interior: backward chunk
-                              // counter, forward completion count, backward solved epoch
+                              // counter, forward completion count, backward solved flag
   int parentI;                // interior: parent if it is interior, else -1
   long long rowsOff;          // rows of this node in the row arena
   long long wuOff;            // interior: update vector; compressed: z (r), s (r), u = -V z (m)

@@ -42,6 +42,13 @@ __device__ __forceinline__ bool wait_geq(const int* p, int target, int* err, int
   return false;
 }
 
+// Same, with the poll limit read from *limitP only once the first poll has
+// failed (the fast path adds no dependent load to the caller's critical path).
+__device__ __forceinline__ bool wait_geq_lim(const int* p, int target, int* err, const int* limitP) {
+  if (__all_sync(FULL, ld_acquire(p) >= target)) return true;
+  return wait_geq(p, target, err, __ldcg(limitP));
+}
+
 // Every block of a ticketed launch calls this once when it is done; the last
 // one resets the ticket and completion counters for the next launch.
 __device__ __forceinline__ void launch_done(int* tick, int* done) {
