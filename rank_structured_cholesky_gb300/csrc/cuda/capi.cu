@@ -775,7 +775,9 @@ extern "C" int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int spl
     t.lower = lower;
     t.alpha = alpha;
     t.beta = beta;
-    t.tilesN = (N + 63) / 64;
+    const int bn = tc_tile_n(N);
+    t.bn = bn;
+    t.tilesN = (N + bn - 1) / bn;
     t.tileBase = 0;
     t.split = split;
     // K >= 1024 (and not lower): four K slices through the partial workspace
@@ -786,11 +788,11 @@ extern "C" int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int spl
     if (K >= 1024 && !lower) {
       t.kLen = ((K + 3) / 4 + 31) / 32 * 32;
       t.kSplit = (K + t.kLen - 1) / t.kLen;
-      dW.alloc(sizeof(float) * (size_t)t.kSplit * tilesPer * 128 * 64);
+      dW.alloc(sizeof(float) * (size_t)t.kSplit * tilesPer * 128 * bn);
       t.ws = dW.as<float>();
     }
     RSCHOL_CUDA(cudaMemcpy(dT.p, &t, sizeof(t), cudaMemcpyHostToDevice));
-    launch_gemm_tc(dT.as<GemmTask<float>>(), 1, tilesPer * t.kSplit, dE.as<int>(), 0);
+    launch_gemm_tc(dT.as<GemmTask<float>>(), 1, tilesPer * t.kSplit, dE.as<int>(), 0, bn);
     if (t.kSplit > 1) {
       const int id = 0;
       const long long base[2] = {0, (long long)M * N};
@@ -921,7 +923,7 @@ extern "C" int rschol_factor_tune_schedule(rschol_factor* f, int repeats) {
     RSCHOL_CUDA(cudaEventCreate(&e0));
     RSCHOL_CUDA(cudaEventCreate(&e1));
     std::vector<int> ks = {INT_MAX};
-    if (f->precision == RSCHOL_MIXED) ks = {128, 256, INT_MAX};
+    if (f->precision == RSCHOL_MIXED) ks = {32, 128, 256, INT_MAX};
     int bestK = f->impl->tc_min_k();
     bool bestFused = f->impl->fused_chol();
     double best = 1e300;

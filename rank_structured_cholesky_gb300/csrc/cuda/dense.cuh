@@ -31,7 +31,8 @@ struct GemmTask {
   int split;      // tensor-core path: split-precision (3 x TF32) products
   int kSplit;     // tensor-core path: K slices (1: none); slices write partials to ws
   int kLen;       // K per slice (a multiple of 32)
-  float* ws;      // kSplit x tiles x 128 x 64 partials (kSplit > 1)
+  float* ws;      // kSplit x tiles x 128 x bn partials (kSplit > 1)
+  int bn;         // tensor-core path: output tile width of the launch (64 or 128; 0: 64)
 };
 
 // In-place lower Cholesky of one diagonal tile (n <= 64).  On a
@@ -115,10 +116,14 @@ struct ExtAddRow {
 };
 
 template <class T> void launch_gemm(const GemmTask<T>* dTasks, int nTasks, int totalTiles, cudaStream_t s);
-// FP32 tasks on the tensor cores (tcgen05, TF32 or split TF32), 128 x 64
-// output tiles (tileBase / tilesN counted for that tile); *dErr is set if an
-// mbarrier wait gives up.
-void launch_gemm_tc(const GemmTask<float>* dTasks, int nTasks, int totalTiles, int* dErr, cudaStream_t s);
+// FP32 tasks on the tensor cores (tcgen05, TF32 or split TF32), 128 x bn
+// output tiles, bn = 64 or 128 for the whole launch (tileBase / tilesN counted
+// for that width; every task's bn equal to it); *dErr is set if an mbarrier
+// wait gives up.
+void launch_gemm_tc(const GemmTask<float>* dTasks, int nTasks, int totalTiles, int* dErr, cudaStream_t s,
+                    int bn = 64);
+// The tile width of a tensor-core launch whose widest task has N columns.
+inline int tc_tile_n(int maxN) { return maxN > 64 ? 128 : 64; }
 // C = alpha * sum of the K-slice partials + beta * C for the split tasks
 // ids[0..nIds) (elemBase: prefix sums of their M x N, elemBase[nIds] = elems).
 void launch_gemm_splitk_reduce(const GemmTask<float>* dTasks, const int* ids, int nIds, const long long* elemBase,

@@ -58,7 +58,7 @@ void FactorEngine<float>::gemm_launch(const Step& st) {
     launch_gemm_splitk_reduce(dGemm_.as<GemmTask<float>>(), dSplitIds_.as<int>() + st.off, st.count,
                               dSplitBase_.as<long long>() + st.aux, st.elems, stream);
   else if (st.aux)
-    launch_gemm_tc(dGemm_.as<GemmTask<float>>() + st.off, st.count, st.grid, dFlag.as<int>() + 1, stream);
+    launch_gemm_tc(dGemm_.as<GemmTask<float>>() + st.off, st.count, st.grid, dFlag.as<int>() + 1, stream, st.aux);
   else
     launch_gemm<float>(dGemm_.as<GemmTask<float>>() + st.off, st.count, st.grid, stream);
 }
@@ -80,12 +80,16 @@ void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
   // GEMM time in the c2 factor; so did a 128 x 128 SIMT tile with 8 x 8
   // outputs per thread, 15.9 vs 12.1 ms: only the K >= 69 contribution
   // updates gained, the K = 64 steps turned latency-bound in the epilogue)
-  int maxK = 0;
-  for (auto& t : batch) maxK = std::max(maxK, t.K);
+  int maxK = 0, maxN = 0;
+  for (auto& t : batch) {
+    maxK = std::max(maxK, t.K);
+    maxN = std::max(maxN, t.N);
+  }
   const bool tc = useTc_ && maxK >= tcMinK_;
   const int rowsPerTile = tc ? 128 : 64;
+  const int bn = tc ? tc_tile_n(maxN) : 64;   // tile width: 128 x bn on the tensor cores
   long long baseTiles = 0;
-  for (auto& t : batch) baseTiles += (long long)((t.M + rowsPerTile - 1) / rowsPerTile) * ((t.N + 63) / 64);
+  for (auto& t : batch) baseTiles += (long long)((t.M + rowsPerTile - 1) / rowsPerTile) * ((t.N + bn - 1) / bn);
   const long long want = 2LL * 152;   // two blocks per SM
   int tiles = 0;
   std::vector<int> ids;
@@ -93,7 +97,8 @@ void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
   const long long first = (long long)gemm_.size();
   for (size_t q = 0; q < batch.size(); ++q) {
     GemmTask<T>& t = batch[q];
-    t.tilesN = (t.N + 63) / 64;
+    t.tilesN = (t.N + bn - 1) / bn;
+    t.bn = bn;
     const int tilesPer = ((t.M + rowsPerTile - 1) / rowsPerTile) * t.tilesN;
     t.kSplit = 1;
     t.kLen = t.K;
@@ -105,7 +110,7 @@ void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
         t.kSplit = (t.K + kl - 1) / kl;
         t.kLen = kl;
         wsOff = wsCur_;
-        wsCur_ += (long long)t.kSplit * tilesPer * 128 * 64;
+        wsCur_ += (long long)t.kSplit * tilesPer * 128 * bn;
         ids.push_back((int)(first + q));
         base.push_back(base.back() + (long long)t.M * t.N);
       }
@@ -115,7 +120,7 @@ void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
     gemmWsOff_.push_back(wsOff);
   }
   Step st{ST_GEMM, first, (int)batch.size(), tiles};
-  st.aux = tc ? 1 : 0;
+  st.aux = tc ? bn : 0;
   gemm_.insert(gemm_.end(), batch.begin(), batch.end());
   steps_.push_back(st);
   if (!ids.empty()) {

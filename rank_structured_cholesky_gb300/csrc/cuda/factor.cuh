@@ -55,7 +55,7 @@ struct Step {
   int count;        // number of tasks
   int grid;         // tiles / chunks / columns for the launch
   int aux = 0;      // ST_QR: largest row count of the batch (grid: largest rank);
-                    // ST_GEMM: 1 on the tensor cores
+                    // ST_GEMM: the tile width bn on the tensor cores, 0 on the SIMT kernel
   long long elems = 0;   // ST_GEMM_REDUCE: elements of C summed; ST_CHOL: ints of its counters
   double flops = 0;      // ST_CHOL: algorithmic flops of the launch
 };

@@ -1039,12 +1039,19 @@ void SolveEngine<T>::plan_inverse(const std::vector<long long>& xOff) {
   };
   auto flush = [&](std::vector<GemmTask<T>>& batch) {
     if (batch.empty()) return;
+    int maxN = 0;
+    for (auto& t : batch) maxN = std::max(maxN, t.N);
+    const int bn = tc ? tc_tile_n(maxN) : 64;
     int tiles = 0;
     for (auto& t : batch) {
+      t.tilesN = (t.N + bn - 1) / bn;
+      t.bn = bn;
       t.tileBase = tiles;
       tiles += ((t.M + rpt - 1) / rpt) * t.tilesN;
     }
-    xSteps_.push_back(XStep{(long long)tasks.size(), (int)batch.size(), tiles, tc ? 1 : 0});
+    XStep xs{(long long)tasks.size(), (int)batch.size(), tiles, tc ? 1 : 0};
+    xs.bn = bn;
+    xSteps_.push_back(xs);
     tasks.insert(tasks.end(), batch.begin(), batch.end());
     batch.clear();
   };
@@ -1091,7 +1098,7 @@ int SolveEngine<T>::prepare(cudaStream_t st) {
   for (const XStep& x : xSteps_) {
     const GemmTask<T>* d = dXGemm_.as<GemmTask<T>>() + x.off;
     if constexpr (std::is_same<T, float>::value) {
-      if (F_.tensor_cores()) launch_gemm_tc(d, x.count, x.tiles, F_.dFlag.template as<int>() + 1, st);
+      if (F_.tensor_cores()) launch_gemm_tc(d, x.count, x.tiles, F_.dFlag.template as<int>() + 1, st, x.bn);
       else launch_gemm<T>(d, x.count, x.tiles, st);
     } else {
       launch_gemm<T>(d, x.count, x.tiles, st);

@@ -90,6 +90,7 @@ struct XStep {       // one batched GEMM launch (X = L11^{-1} doubling, batched 
   long long off;
   int count, tiles;
   int tc;            // on the tensor cores (batched apply: the transposed skinny form)
+  int bn = 64;       // tensor-core tile width of the launch (X doubling)
   long long redOff = 0;   // batched apply: K-slice sums after the launch (first, count, grid); tiles = units
   int redCount = 0, redGrid = 0;
 };

@@ -21,6 +21,10 @@ SHAPES = [
     (200, 130, 96, 0, 1), (130, 70, 36, 0, 1), (64, 64, 44, 0, 1), (257, 129, 500, 0, 1),
     # K >= 1024: four K slices summed by the split-K reduction
     (300, 104, 2048, 1, 0), (129, 65, 3001, 0, 1), (129, 65, 3000, 0, 1),
+    # 128-wide tiles (N > 64) with either operand layout; unaligned leading
+    # dimensions (no 16-byte loads); the sketch shapes of the factor
+    (300, 128, 64, 0, 0), (333, 100, 37, 1, 1), (250, 127, 130, 1, 0), (3072, 69, 1024, 1, 0),
+    (1024, 104, 3000, 0, 0), (512, 129, 45, 0, 1),
 ]
 
 
@@ -35,7 +39,9 @@ def test_tensor_core_gemm(shape, split):
     assert out[0] < tol, (shape, split, out[0], out[1])
 
 
-def test_tensor_core_gemm_lower_tiles():
+@pytest.mark.parametrize("n", [60, 400])
+def test_tensor_core_gemm_lower_tiles(n):
+    # n = 400: 128-wide tiles, those strictly above the diagonal skipped
     out = (ctypes.c_double * 2)()
-    st = rs.load_library().rschol_selftest_gemm(400, 400, 64, 0, 1, 1, 1, out)
+    st = rs.load_library().rschol_selftest_gemm(n, n, 64, 0, 1, 1, 1, out)
     assert st == 0 and out[0] < 1e-5, (st, out[0])
