@@ -392,7 +392,19 @@ def run_ours(args):
             "apply_rel_error": float(np.linalg.norm(z_mixed - z_fp64) / np.linalg.norm(z_fp64)),
             "solution_rel_error": float(np.linalg.norm(x_mixed - x_fp64) / np.linalg.norm(x_fp64)),
             "note": "relative 2-norm differences on rhs[0]; both solves stop at ||r||/||b|| <= 1e-8"}
-        del pf
+        # mixed precision with the root separator's dense Cholesky in FP64: its cost and its error
+        rf = timed_solves(lib, rs, torch, prob, dict(params, root_fp64=1), "mixed", device, local, args.steps,
+                          args.warmup, dist, False)
+        z_root = rf["F"].apply(b0)
+        x_root, _ = rf["F"].pcg(b0, eps=1e-8)
+        plain["mixed_root_fp64"] = {
+            "value": world * args.steps / rf["total_s"], "unit": "solves/s",
+            "factor_ms": statistics.median(rf["factor_ms"]), "pcg_ms": statistics.median(rf["pcg_ms"]),
+            "iterations": rf["iterations"] if nrhs > 1 else rf["iterations"][0],
+            "true_residual": rf["true_residual"],
+            "apply_rel_error_vs_fp64": float(np.linalg.norm(z_root - z_fp64) / np.linalg.norm(z_fp64)),
+            "solution_rel_error_vs_fp64": float(np.linalg.norm(x_root - x_fp64) / np.linalg.norm(x_fp64))}
+        del pf, rf
 
     hbm, bf16, src = peaks()
     if rank == 0:

@@ -54,6 +54,8 @@ typedef struct rschol_params {
   unsigned seed;             /* generator reseed at every numeric factorisation (152) */
   int precision;             /* enum rschol_precision */
   int device;                /* CUDA device ordinal (0) */
+  int root_fp64;             /* RSCHOL_MIXED only: the dense Cholesky of the root separator's
+                                blocks in FP64, the rest of the factor FP32 (0) */
 } rschol_params;
 
 typedef struct rschol_ctx rschol_ctx;

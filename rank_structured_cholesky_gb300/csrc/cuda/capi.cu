@@ -56,6 +56,7 @@ Params to_params(const rschol_params& p) {
   q.max_factor_attempts = p.max_factor_attempts;
   q.rank_alpha = p.rank_alpha;
   q.seed = p.seed;
+  q.root_fp64 = p.root_fp64;
   return q;
 }
 
@@ -227,6 +228,7 @@ void rschol_default_params(rschol_params* p) {
   p->seed = 152;
   p->precision = RSCHOL_FP64;
   p->device = 0;
+  p->root_fp64 = 0;
 }
 
 rschol_ctx* rschol_create(const rschol_params* p) {
@@ -691,6 +693,7 @@ const char* rschol_factor_describe(rschol_factor* f) {
   std::string s = describe(f->S);
   s.pop_back();
   o << s << ", \"precision\": \"" << (f->precision == RSCHOL_MIXED ? "mixed" : "fp64") << "\""
+    << ", \"root_fp64\": " << ((f->precision == RSCHOL_MIXED && f->prm.root_fp64) ? 1 : 0)
     << ", \"factor_launches\": " << f->impl->launches() << ", \"apply_launches\": " << f->impl->apply_launches()
     << ", \"factor_flops\": " << f->impl->flops() << ", \"apply_bytes\": " << f->impl->apply_bytes()
     << ", \"spmv_bytes\": " << f->pcg->spmvBytes << ", \"device_bytes\": " << f->impl->bytes()

@@ -1186,6 +1186,25 @@ void launch_extadd(const ExtAddRow<T>* rows, int nRows, const ExtAddSeg* segs, c
   extadd_kernel<T><<<(nRows + 7) / 8, 256, 0, s>>>(rows, nRows, segs, src);
   RSCHOL_LAUNCH_CHECK();
 }
+// a block of 256 threads per (task, 64-row slab)
+__global__ void block_convert_kernel(const CvtTask* __restrict__ tasks, int toDouble) {
+  const CvtTask t = tasks[blockIdx.y];
+  const int r0 = blockIdx.x * 64;
+  if (r0 >= t.n) return;
+  const int r1 = min(t.n, r0 + 64);
+  for (int i = r0 + (threadIdx.x >> 5); i < r1; i += 8)
+    for (int j = threadIdx.x & 31; j <= i; j += 32) {
+      if (toDouble) t.D[(size_t)i * t.ldd + j] = (double)t.F[(size_t)i * t.ld + j];
+      else t.F[(size_t)i * t.ld + j] = (float)t.D[(size_t)i * t.ldd + j];
+    }
+}
+
+void launch_block_convert(const CvtTask* d, int nTasks, int maxN, int toDouble, cudaStream_t s) {
+  if (nTasks <= 0 || maxN <= 0) return;
+  block_convert_kernel<<<dim3((maxN + 63) / 64, nTasks), 256, 0, s>>>(d, toDouble);
+  RSCHOL_LAUNCH_CHECK();
+}
+
 __global__ void init_flags_kernel(int* flag, int waitLimit) {
   flag[0] = INT_MAX;
   flag[1] = 0;

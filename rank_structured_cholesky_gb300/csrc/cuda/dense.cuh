@@ -116,6 +116,14 @@ struct ExtAddRow {
 };
 
 template <class T> void launch_gemm(const GemmTask<T>* dTasks, int nTasks, int totalTiles, cudaStream_t s);
+// The lower triangle of an n x n FP32 block (leading dimension ld) to FP64
+// scratch (leading dimension ldd) when toDouble, else back.
+struct CvtTask {
+  float* F;
+  double* D;
+  int ld, ldd, n;
+};
+void launch_block_convert(const CvtTask* dTasks, int nTasks, int maxN, int toDouble, cudaStream_t s);
 // FP32 tasks on the tensor cores (tcgen05, TF32 or split TF32), 128 x bn
 // output tiles, bn = 64 or 128 for the whole launch (tileBase / tilesN counted
 // for that width; every task's bn equal to it); *dErr is set if an mbarrier

@@ -175,80 +175,136 @@ static GemmTask<T> mk_gemm(const T* A, int lda, bool tA, const T* B, int ldb, bo
   return t;
 }
 
+// The blocked partial Cholesky of every job as one ticketed launch (step kind
+// `kind`, jobs and items appended to cjobs / items): shared by the factor's
+// own precision and the FP64 root separator of a mixed factor.
+template <class T>
+template <class U>
+void FactorEngine<T>::emit_fused(const std::vector<CholJob<U>>& jobs, int kind, std::vector<CholFusedJob<U>>& cjobs,
+                                 std::vector<CholItem>& items, long long& syncMax, long long& wsMax) {
+  Step st{kind, (long long)items.size(), 0, 0};
+  const double flops0 = flops;
+  const int j0 = (int)cjobs.size();
+  long long sync = 1, ws = 0;   // sync[0]: the ticket
+  int maxP = 0;
+  for (const auto& jb : jobs) {
+    if (jb.nDiag <= 0) continue;
+    CholFusedJob<U> c{};
+    c.F = jb.F;
+    c.ld = jb.ld;
+    c.nDiag = jb.nDiag;
+    c.nRows = jb.nRows;
+    c.nUpd = jb.nUpd;
+    c.code = jb.code;
+    c.P = (jb.nDiag + NB - 1) / NB;
+    c.w0 = jb.nDiag - NB * (c.P - 1);
+    auto tiles = [&](int n) { return n <= c.w0 ? 1 : 1 + (n - c.w0 + NB - 1) / NB; };
+    c.TR = tiles(jb.nRows);
+    c.TU = tiles(jb.nUpd);
+    c.r1 = c.w0;
+    c.cnt = (int)(sync - 1);
+    sync += (long long)c.TR * c.TU + c.TR + c.P;
+    c.inv = ws;
+    ws += (long long)c.P * NB * NB;
+    maxP = std::max(maxP, c.P);
+    cjobs.push_back(c);
+    for (int p = 0; p < c.P; ++p) {   // algorithmic flops, counted as the per-panel steps count them
+      const int c0 = p == 0 ? 0 : c.w0 + NB * (p - 1), w = p == 0 ? c.w0 : NB;
+      const int rows = jb.nRows - c0 - w, upd = jb.nUpd - c0 - w;
+      flops += (double)w * w * w / 3.0 + (double)std::max(rows, 0) * w * w;
+      if (rows > 0 && upd > 0) flops += 2.0 * rows * upd * w * (rows == upd ? 0.5 : 1.0);
+    }
+  }
+  const int j1 = (int)cjobs.size();
+  // Item order (a topological one, with a look-ahead of one panel): stage p
+  // lists the POTRFs and TRSMs of panel p, the rest R(p - 1) of the previous
+  // panel's updates (column tiles >= p + 1), then L(p), panel p's updates of
+  // column tile p + 1 -- all that POTRF(p + 1) and its TRSMs wait for.  So
+  // the next panel's critical pieces are taken long before the bulk of the
+  // current updates is done.
+  auto updates = [&](int q, int p, int bLo, int bHi) {
+    const CholFusedJob<U>& c = cjobs[q];
+    for (int b = std::max(bLo, p + 1); b < std::min(bHi, c.TU); ++b)
+      for (int a = b; a < c.TR; ++a) items.push_back(CholItem{q, CHOL_GEMM, p, a, b});
+  };
+  for (int p = 0; p <= maxP; ++p) {
+    for (int q = j0; q < j1; ++q)
+      if (p < cjobs[q].P) items.push_back(CholItem{q, CHOL_POTRF, p, p, p});
+    for (int q = j0; q < j1; ++q)
+      if (p < cjobs[q].P)
+        for (int a = p + 1; a < cjobs[q].TR; ++a) items.push_back(CholItem{q, CHOL_TRSM, p, a, p});
+    for (int q = j0; q < j1; ++q)
+      if (p >= 1 && p <= cjobs[q].P) updates(q, p - 1, p + 1, INT_MAX);   // R(p - 1)
+    for (int q = j0; q < j1; ++q)
+      if (p < cjobs[q].P) updates(q, p, p + 1, p + 2);                    // L(p)
+  }
+  if (dropItemTest_ && !droppedItem_) {   // test switch: one POTRF whose TRSMs then wait in vain
+    for (size_t k = (size_t)st.off; k < items.size(); ++k)
+      if (items[k].kind == CHOL_POTRF && cjobs[items[k].job].TR > items[k].p + 1) {
+        items.erase(items.begin() + (long)k);
+        droppedItem_ = true;
+        break;
+      }
+  }
+  st.count = st.grid = (int)(items.size() - st.off);
+  st.elems = sync;
+  st.flops = flops - flops0;
+  if (st.count == 0) return;
+  syncMax = std::max(syncMax, sync);
+  wsMax = std::max(wsMax, ws);
+  steps_.push_back(st);
+}
+
 template <class T>
 void FactorEngine<T>::emit_chol(const std::vector<CholJob<T>>& jobs) {
-  if (fusedChol_) {
-    Step st{ST_CHOL, (long long)cholItems_.size(), 0, 0};
-    const double flops0 = flops;
-    const int j0 = (int)cholJobs_.size();
-    long long sync = 1, ws = 0;   // sync[0]: the ticket
-    int maxP = 0;
+  if (!rootStart_.empty()) {
+    // FP64 root separator of a mixed factor: the root's blocks go through FP64
+    // scratch (converted in, factored, converted back), the others as usual
+    std::vector<CholJob<T>> rest;
+    std::vector<CholJob<double>> root;
+    std::vector<CvtTask> cv;
+    int maxN = 0;
     for (const auto& jb : jobs) {
-      if (jb.nDiag <= 0) continue;
-      CholFusedJob<T> c{};
-      c.F = jb.F;
-      c.ld = jb.ld;
-      c.nDiag = jb.nDiag;
-      c.nRows = jb.nRows;
-      c.nUpd = jb.nUpd;
-      c.code = jb.code;
-      c.P = (jb.nDiag + NB - 1) / NB;
-      c.w0 = jb.nDiag - NB * (c.P - 1);
-      auto tiles = [&](int n) { return n <= c.w0 ? 1 : 1 + (n - c.w0 + NB - 1) / NB; };
-      c.TR = tiles(jb.nRows);
-      c.TU = tiles(jb.nUpd);
-      c.r1 = c.w0;
-      c.cnt = (int)(sync - 1);
-      sync += (long long)c.TR * c.TU + c.TR + c.P;
-      c.inv = ws;
-      ws += (long long)c.P * NB * NB;
-      maxP = std::max(maxP, c.P);
-      cholJobs_.push_back(c);
-      for (int p = 0; p < c.P; ++p) {   // algorithmic flops, counted as the per-panel steps count them
-        const int c0 = p == 0 ? 0 : c.w0 + NB * (p - 1), w = p == 0 ? c.w0 : NB;
-        const int rows = jb.nRows - c0 - w, upd = jb.nUpd - c0 - w;
-        flops += (double)w * w * w / 3.0 + (double)std::max(rows, 0) * w * w;
-        if (rows > 0 && upd > 0) flops += 2.0 * rows * upd * w * (rows == upd ? 0.5 : 1.0);
+      const int node = jb.code - 1;
+      auto it = rootStart_.find(node);
+      if (it == rootStart_.end() || jb.nRows != jb.nDiag) {
+        rest.push_back(jb);
+        continue;
       }
+      // the block's position in the front: its rows and columns start at d0
+      T* const F0 = compressed() + frontOff[node];
+      const long long e = (long long)(jb.F - F0);
+      const int d0 = (int)(e / ld[node]);
+      const int nn = S.nodes[node].n;
+      double* D = dRoot64_.as<double>() + it->second + (long long)d0 * nn + d0;
+      cv.push_back(CvtTask{reinterpret_cast<float*>(jb.F), D, jb.ld, nn, jb.nDiag});
+      root.push_back(CholJob<double>{D, nn, jb.nDiag, jb.nDiag, jb.nDiag, jb.code});
+      maxN = std::max(maxN, jb.nDiag);
     }
-    const int j1 = (int)cholJobs_.size();
-    // Item order (a topological one, with a look-ahead of one panel): stage p
-    // lists the POTRFs and TRSMs of panel p, the rest R(p - 1) of the previous
-    // panel's updates (column tiles >= p + 1), then L(p), panel p's updates of
-    // column tile p + 1 -- all that POTRF(p + 1) and its TRSMs wait for.  So
-    // the next panel's critical pieces are taken long before the bulk of the
-    // current updates is done.
-    auto updates = [&](int q, int p, int bLo, int bHi) {
-      const CholFusedJob<T>& c = cholJobs_[q];
-      for (int b = std::max(bLo, p + 1); b < std::min(bHi, c.TU); ++b)
-        for (int a = b; a < c.TR; ++a) cholItems_.push_back(CholItem{q, CHOL_GEMM, p, a, b});
-    };
-    for (int p = 0; p <= maxP; ++p) {
-      for (int q = j0; q < j1; ++q)
-        if (p < cholJobs_[q].P) cholItems_.push_back(CholItem{q, CHOL_POTRF, p, p, p});
-      for (int q = j0; q < j1; ++q)
-        if (p < cholJobs_[q].P)
-          for (int a = p + 1; a < cholJobs_[q].TR; ++a) cholItems_.push_back(CholItem{q, CHOL_TRSM, p, a, p});
-      for (int q = j0; q < j1; ++q)
-        if (p >= 1 && p <= cholJobs_[q].P) updates(q, p - 1, p + 1, INT_MAX);   // R(p - 1)
-      for (int q = j0; q < j1; ++q)
-        if (p < cholJobs_[q].P) updates(q, p, p + 1, p + 2);                    // L(p)
+    if (!root.empty()) {
+      Step in{ST_CVT, (long long)cvt_.size(), (int)cv.size(), maxN};
+      in.aux = 1;
+      cvt_.insert(cvt_.end(), cv.begin(), cv.end());
+      steps_.push_back(in);
+      emit_fused<double>(root, ST_CHOL64, cholJobs64_, cholItems64_, cholSync64_, cholWs64_);
+      Step out{ST_CVT, (long long)cvt_.size(), (int)cv.size(), maxN};
+      out.aux = 0;
+      cvt_.insert(cvt_.end(), cv.begin(), cv.end());
+      steps_.push_back(out);
     }
-    if (dropItemTest_ && !droppedItem_) {   // test switch: one POTRF whose TRSMs then wait in vain
-      for (size_t k = (size_t)st.off; k < cholItems_.size(); ++k)
-        if (cholItems_[k].kind == CHOL_POTRF && cholJobs_[cholItems_[k].job].TR > cholItems_[k].p + 1) {
-          cholItems_.erase(cholItems_.begin() + (long)k);
-          droppedItem_ = true;
-          break;
-        }
+    if (rest.empty()) return;
+    if (rest.size() != jobs.size()) {
+      emit_chol_t(rest);
+      return;
     }
-    st.count = st.grid = (int)(cholItems_.size() - st.off);
-    st.elems = sync;
-    st.flops = flops - flops0;
-    if (st.count == 0) return;
-    cholSync_ = std::max(cholSync_, sync);
-    cholWs_ = std::max(cholWs_, ws);
-    steps_.push_back(st);
+  }
+  emit_chol_t(jobs);
+}
+
+template <class T>
+void FactorEngine<T>::emit_chol_t(const std::vector<CholJob<T>>& jobs) {
+  if (fusedChol_) {
+    emit_fused<T>(jobs, ST_CHOL, cholJobs_, cholItems_, cholSync_, cholWs_);
     return;
   }
   int maxN = 0;
@@ -510,6 +566,11 @@ void FactorEngine<T>::plan() {
   cholJobs_.clear();
   cholItems_.clear();
   cholSync_ = cholWs_ = 0;
+  cvt_.clear();
+  cholJobs64_.clear();
+  cholItems64_.clear();
+  cholSync64_ = cholWs64_ = 0;
+  rootStart_.clear();
   ident_.clear();
   ints_.clear();
   flops = 0;
@@ -626,6 +687,19 @@ void FactorEngine<T>::plan() {
   dContrib.alloc(sizeof(T) * std::max(1LL, curT));
   dGauss.alloc(sizeof(T) * std::max(1LL, S.totalDraws));
   deviceBytes = sizeof(T) * (curI + curC + curV + curH + curT + S.totalDraws) + sizeof(double) * A.x.size();
+  if (std::is_same<T, float>::value && prm.root_fp64) {
+    // the root separator: compressed supernodes at the top of the tree
+    long long cur = 0;
+    for (int j = 0; j < nn; ++j)
+      if (S.nodes[j].compressed && S.nodes[j].parent < 0) {
+        rootStart_[j] = cur;
+        cur += (long long)S.nodes[j].n * S.nodes[j].n;
+      }
+    dRoot64_.alloc(sizeof(double) * std::max(1LL, cur));
+    deviceBytes += sizeof(double) * cur;
+  } else {
+    dRoot64_.alloc(0);
+  }
   T* const I0 = interior();
   T* const C0 = compressed();
   T* const V0 = vu();
@@ -974,6 +1048,8 @@ void FactorEngine<T>::plan() {
   dQrWs_.alloc(sizeof(T) * std::max(1LL, qrWs_));
   dCholSync_.alloc(sizeof(int) * std::max(1LL, cholSync_));
   dCholWs_.alloc(sizeof(T) * std::max(1LL, cholWs_));
+  dCholSync64_.alloc(cholItems64_.empty() ? 0 : sizeof(int) * std::max(1LL, cholSync64_));
+  dCholWs64_.alloc(cholItems64_.empty() ? 0 : sizeof(double) * std::max(1LL, cholWs64_));
   {   // diagnostics: per-item timeline of the fused steps, sized for this plan (or none)
     const char* tp = std::getenv("RSCHOL_CHOL_TRACE");
     dCholTrace_.alloc(tp && tp[0] && !cholItems_.empty() ? 4 * sizeof(unsigned long long) * cholItems_.size() : 0);
@@ -994,6 +1070,11 @@ void FactorEngine<T>::plan() {
       throw std::runtime_error("factor plan: a TRSM task without a device address");
   for (const auto& c : cholJobs_)
     if (!device_ptr(c.F)) throw std::runtime_error("factor plan: a Cholesky job without a device address");
+  for (const auto& c : cholJobs64_)
+    if (!device_ptr(c.F)) throw std::runtime_error("factor plan: an FP64 Cholesky job without a device address");
+  up(dCholJobs64_, cholJobs64_.data(), cholJobs64_.size() * sizeof(CholFusedJob<double>));
+  up(dCholItems64_, cholItems64_.data(), cholItems64_.size() * sizeof(CholItem));
+  up(dCvt_, cvt_.data(), cvt_.size() * sizeof(CvtTask));
   up(dCholJobs_, cholJobs_.data(), cholJobs_.size() * sizeof(CholFusedJob<T>));
   up(dCholItems_, cholItems_.data(), cholItems_.size() * sizeof(CholItem));
   up(dGemm_, gemm_.data(), gemm_.size() * sizeof(GemmTask<T>));
@@ -1060,6 +1141,12 @@ void FactorEngine<T>::enqueue(bool timing, bool capturing) {
                                              dQrWs_.as<T>(), stream) - 1;
         break;
       case ST_IDENT: launch_set_identity<T>(dIdent_.as<IdentTask<T>>() + st.off, st.count, stream); break;
+      case ST_CVT: launch_block_convert(dCvt_.as<CvtTask>() + st.off, st.count, st.grid, st.aux, stream); break;
+      case ST_CHOL64:
+        launch_chol_fused<double>(dCholJobs64_.as<CholFusedJob<double>>(), dCholItems64_.as<CholItem>() + st.off,
+                                  st.count, dCholSync64_.as<int>(), st.elems, dCholWs64_.as<double>(),
+                                  dFlag.as<int>(), nullptr, stream);
+        break;
     }
     if (timing) RSCHOL_CUDA(cudaEventRecordWithFlags(stepEv_[2 * q + 1], stream, recFlags));
     ++launches;
@@ -1110,7 +1197,10 @@ int FactorEngine<T>::run() {
     for (size_t q = 0; q < steps_.size(); ++q) {
       float ms = 0;
       RSCHOL_CUDA(cudaEventElapsedTime(&ms, stepEv_[2 * q], stepEv_[2 * q + 1]));
-      const int k = steps_[q].kind == ST_GEMM_REDUCE ? (int)ST_GEMM : steps_[q].kind;
+      // per-kind totals: split-K sums with the GEMMs, the FP64 root's
+      // conversions in slot 6, its Cholesky with the fused Cholesky
+      const int kd = steps_[q].kind;
+      const int k = kd == ST_GEMM_REDUCE ? (int)ST_GEMM : kd == ST_CVT ? 6 : kd == ST_CHOL64 ? (int)ST_CHOL : kd;
       stepMs[k] += ms;
       stepCount[k] += 1;
       stepFlops[k] += steps_[q].flops;
@@ -1125,7 +1215,7 @@ int FactorEngine<T>::run() {
     // device ms; GEMM: flops and largest M / N / K) for tuning the schedule
     const char* sl = std::getenv("RSCHOL_STEP_LOG");
     if (sl && sl[0] == '1') {
-      static const char* names[] = {"gemm", "potrf", "trsm", "extadd", "qr", "ident", "reduce", "chol"};
+      static const char* names[] = {"gemm", "potrf", "trsm", "extadd", "qr", "ident", "reduce", "chol", "cvt", "chol64"};
       for (size_t q = 0; q < steps_.size(); ++q) {
         const Step& st = steps_[q];
         float ms = 0;

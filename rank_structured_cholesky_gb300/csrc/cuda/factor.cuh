@@ -29,6 +29,7 @@
 #include <cstdint>
 #include <string>
 #include <functional>
+#include <map>
 #include <vector>
 
 #include "../host/ordering.h"
@@ -47,6 +48,8 @@ enum StepKind : int {
   ST_IDENT,
   ST_GEMM_REDUCE,   // sum the K-slice partials of the split tensor-core GEMM tasks
   ST_CHOL,          // fused blocked partial Cholesky of a level (POTRF + TRSM + updates, one launch)
+  ST_CVT,           // root separator blocks FP32 -> FP64 scratch (aux 1) or back (aux 0); grid: largest block
+  ST_CHOL64,        // fused blocked Cholesky of root separator blocks in FP64 (mixed factor with root_fp64)
 };
 
 struct Step {
@@ -132,6 +135,10 @@ class FactorEngine {
 
  private:
   void emit_chol(const std::vector<CholJob<T>>& jobs);
+  void emit_chol_t(const std::vector<CholJob<T>>& jobs);
+  template <class U>
+  void emit_fused(const std::vector<CholJob<U>>& jobs, int kind, std::vector<CholFusedJob<U>>& cjobs,
+                  std::vector<CholItem>& items, long long& syncMax, long long& wsMax);
   void emit_trsm(const std::vector<TrsmJob<T>>& jobs);
   void emit_rf(const std::vector<RFJob<T>>& jobs);
   struct EaSrc {            // plan-time source of an extend-add
@@ -191,6 +198,16 @@ class FactorEngine {
   std::vector<CholItem> cholItems_;
   long long cholSync_ = 0, cholWs_ = 0;   // largest counter array (ints) and inverse workspace (elements) of a step
   DevBuf dCholJobs_, dCholItems_, dCholSync_, dCholWs_, dCholTrace_;
+  // Mixed factor with Params::root_fp64: the dense Cholesky of the root
+  // separator's blocks runs in FP64 on scratch copies (per root supernode, an
+  // n x n FP64 matrix at rootStart_[node] in dRoot64_).
+  std::map<int, long long> rootStart_;
+  DevBuf dRoot64_, dCvt_;
+  std::vector<CvtTask> cvt_;
+  std::vector<CholFusedJob<double>> cholJobs64_;
+  std::vector<CholItem> cholItems64_;
+  long long cholSync64_ = 0, cholWs64_ = 0;
+  DevBuf dCholJobs64_, dCholItems64_, dCholSync64_, dCholWs64_;
   std::vector<long long> scatSrc_, scatDst_;
   std::vector<int> scatIsInterior_;
   DevBuf dGemm_, dPotrf_, dTrsm_, dEaR_, dEaSeg_, dEaS_, dQr_, dIdent_, dInts_, dScatSrc_, dScatDst_;

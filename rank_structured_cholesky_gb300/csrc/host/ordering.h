@@ -37,6 +37,7 @@ struct Params {
   int max_factor_attempts = 10;   // SparseSolver::_maxFactorAttempts
   double rank_alpha = 1.25;       // SparseSolver::_rankConstantAlpha
   uint32_t seed = 152;            // MathUtil::GENERATOR reseed in factorNumeric
+  int root_fp64 = 0;              // mixed precision: the root separator's dense Cholesky in FP64
 };
 
 struct CSC {

@@ -133,3 +133,27 @@ def test_c4_batched_slice():
         _, it, _, _ = O.pcg(prob.rhs[k], 1e-8, 500)
         assert abs(infos[k]["iterations"] - it) <= 1, (k, infos[k], it)
         assert np.linalg.norm(prob.rhs[k] - A @ X[k]) / np.linalg.norm(prob.rhs[k]) <= 1e-8
+
+
+@pytest.mark.parametrize("name", ["c2s", "c2"])
+def test_mixed_with_fp64_root_separator(name, cases):
+    """Mixed precision with the root separator's dense Cholesky in FP64
+    (root_fp64): the FP64 steps run (conversion time recorded in the step
+    timing's slot 6), the solve keeps the oracle's iteration count +-1 at
+    the 1e-8 residual, and one application is within MIXED_APPLY_TOL of the
+    FP64 oracle."""
+    prob, params, O, it_oracle = cases(name)
+    ctx = rs.Context(**params, precision=rs.MIXED, root_fp64=1)
+    G = rs.GpuFactor(ctx, prob.colptr, prob.rowind, prob.vals, prob.xyz)
+    assert G.describe()["root_fp64"] == 1
+    lib = rs.load_library()
+    out = np.zeros(24)
+    lib.rschol_step_timing(G.h, 1, None)
+    G.refactor(prob.vals)
+    lib.rschol_step_timing(G.h, 0, out.ctypes.data)
+    assert out[3 * 6 + 1] >= 2   # conversions in and out
+    b = prob.rhs[0]
+    assert rel(G.apply(b), O.apply(b)) < MIXED_APPLY_TOL
+    x, info = G.pcg(b, 1e-8, 2000)
+    assert abs(info["iterations"] - it_oracle) <= 1, (info, it_oracle)
+    assert info["true_residual"] <= 1e-8
