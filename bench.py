@@ -217,15 +217,18 @@ def run_reference(args):
 
 
 def traffic_from_profiles(kernel, workload="c2"):
-    """dram bytes per launch of `kernel` from the committed ncu summary, or None."""
+    """(dram bytes per launch, algorithmic bytes per launch) of `kernel` from
+    the committed ncu summary, either None when absent."""
     path = os.path.join(ROOT, "profiles", "%s_%s.md" % (kernel, workload))
+    got = {}
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1])
+            for key in ("traffic_bytes_per_launch", "algorithmic_bytes_per_launch"):
+                if line.startswith(key + ":"):
+                    got[key] = float(line.split(":", 1)[1])
     except OSError:
         pass
-    return None
+    return got.get("traffic_bytes_per_launch"), got.get("algorithmic_bytes_per_launch")
 
 
 def timed_solves(lib, rs, torch, prob, params, precision, device, local, steps, warmup, dist, step_timing):
@@ -327,7 +330,8 @@ def run_ours(args):
         torch.cuda.profiler.stop()
         if rank == 0:
             print(json.dumps({"profiled_steps": args.steps, "config": args.config, "precision": args.precision,
-                              "iterations": [infos[k].iterations for k in range(nrhs)]}), flush=True)
+                              "iterations": [infos[k].iterations for k in range(nrhs)],
+                              "fused_cholesky": F.describe().get("fused_cholesky")}), flush=True)
         return 0
 
     params = config_params(args.config)
@@ -439,11 +443,27 @@ def run_ours(args):
                     "peak_source": src, "flops_per_launch": flops / max(launches, 1),
                     "launch_ms": ms / max(launches, 1), "launches_per_step": launches / args.steps,
                     "share_of_step_time": ms / step_total_ms if step_total_ms else None}
+
+        # the fused Cholesky's algorithmic bytes: every job's lower front region
+        # (rows x first nUpd columns) read once and written once per launch
+        fc = desc.get("fused_cholesky", {})
+        chol_bytes = fc.get("algorithmic_bytes", 0.0) / max(fc.get("launches", 1), 1)
+        t_small, a_small = traffic_from_profiles("chol_fused_kernel", "c2s")
+        # the c2s capture's dram bytes per algorithmic byte, applied to this
+        # workload's algorithmic bytes per launch (traffic grows with the fronts)
+        chol_traffic = t_small / a_small * chol_bytes if (t_small and a_small) else None
         roof = roofline("chol_fused_kernel (blocked Cholesky and TRSM chains of a level, FP32 SIMT, ticketed tiles)",
-                        c[21], c[22], c[23], traffic_from_profiles("chol_fused_kernel", "c2s"),
-                        "dram bytes per launch, averaged over the c2s launches of profiles/chol_fused_kernel_c2s.md")
+                        c[21], c[22], c[23], chol_traffic,
+                        "profiles/chol_fused_kernel_c2s.md: dram bytes per algorithmic byte of the c2s launches, "
+                        "times this workload's algorithmic bytes per launch")
+        chol_launch_ms = roof["launch_ms"]
+        roof["algorithmic_bytes_per_launch"] = chol_bytes
+        roof["hbm_achieved_gbs"] = chol_bytes / (chol_launch_ms * 1e-3) / 1e9 if chol_launch_ms else None
+        roof["hbm_frac"] = roof["hbm_achieved_gbs"] / hbm if roof["hbm_achieved_gbs"] else None
+        roof["traffic_over_algorithmic"] = t_small / a_small if (t_small and a_small) else None
+        t_gemm, _ = traffic_from_profiles("gemm_tc_kernel", "c2s")
         roof_gemm = roofline("factor GEMMs (gemm_kernel SIMT and gemm_tc_kernel tcgen05)", c[0], c[1], c[2],
-                             traffic_from_profiles("gemm_kernel"), "profiles/gemm_kernel_c2.md")
+                             t_gemm, "profiles/gemm_tc_kernel_c2s.md (c2s launches)")
         apply_bytes = phase["apply_bytes"]
         its = main["iterations"][0]
         pcg_bytes = its * (apply_bytes + phase["spmv_bytes"] + 8.0 * 10 * n)

@@ -76,6 +76,8 @@ struct Impl {
   virtual long long launches() const = 0;
   virtual long long apply_launches() const = 0;
   virtual double flops() const = 0;
+  // fused Cholesky steps: algorithmic bytes of each launch (in launch order), total flops
+  virtual void chol_work(std::vector<double>* bytes, double* flops) const = 0;
   virtual double apply_bytes() const = 0;
   virtual size_t bytes() const = 0;
   virtual std::vector<std::array<double, 6>> batch_tuning() const = 0;
@@ -124,6 +126,15 @@ struct ImplT : Impl {
   long long launches() const override { return fe.launches; }
   long long apply_launches() const override { return se.launches_per_apply(); }
   double flops() const override { return fe.flops; }
+  void chol_work(std::vector<double>* bytes, double* flops) const override {
+    bytes->clear();
+    *flops = 0;
+    for (const Step& st : fe.steps_)
+      if (st.kind == ST_CHOL) {
+        bytes->push_back(st.bytes);
+        *flops += st.flops;
+      }
+  }
   double apply_bytes() const override { return se.bytes_per_apply(); }
   size_t bytes() const override { return fe.deviceBytes; }
   std::vector<std::array<double, 6>> batch_tuning() const override { return se.batch_tuning(); }
@@ -701,7 +712,20 @@ const char* rschol_factor_describe(rschol_factor* f) {
     << ", \"attempts\": " << f->attempts << ", \"schedule\": {\"tc_min_k\": "
     << (f->impl->tc_min_k() == INT_MAX ? -1 : f->impl->tc_min_k())
     << ", \"fused\": " << (f->impl->fused_chol() ? "true" : "false") << ", \"tuned_ms\": " << f->tunedMs
-    << "}, \"batch_tuning\": [";
+    << "}";
+  {
+    std::vector<double> cb;
+    double cf = 0, total = 0;
+    f->impl->chol_work(&cb, &cf);
+    o << ", \"fused_cholesky\": {\"launches\": " << cb.size() << ", \"flops\": " << cf
+      << ", \"algorithmic_bytes_per_launch\": [";
+    for (size_t k = 0; k < cb.size(); ++k) {
+      o << (k ? ", " : "") << cb[k];
+      total += cb[k];
+    }
+    o << "], \"algorithmic_bytes\": " << total << "}";
+  }
+  o << ", \"batch_tuning\": [";
   bool first = true;
   for (const auto& row : f->impl->batch_tuning()) {   // per width class: class, RA, RC, cwR, cwC, ms
     o << (first ? "" : ", ") << "[" << row[0] << ", " << row[1] << ", " << row[2] << ", " << row[3] << ", " << row[4]

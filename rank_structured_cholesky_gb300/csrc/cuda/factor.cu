@@ -208,6 +208,8 @@ void FactorEngine<T>::emit_fused(const std::vector<CholJob<U>>& jobs, int kind, 
     ws += (long long)c.P * NB * NB;
     maxP = std::max(maxP, c.P);
     cjobs.push_back(c);
+    // the lower part of rows x first nUpd columns of the front: read and written once
+    for (long long col = 0; col < jb.nUpd; ++col) st.bytes += 2.0 * sizeof(U) * std::max(0LL, (long long)jb.nRows - col);
     for (int p = 0; p < c.P; ++p) {   // algorithmic flops, counted as the per-panel steps count them
       const int c0 = p == 0 ? 0 : c.w0 + NB * (p - 1), w = p == 0 ? c.w0 : NB;
       const int rows = jb.nRows - c0 - w, upd = jb.nUpd - c0 - w;

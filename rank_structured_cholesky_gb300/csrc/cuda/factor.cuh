@@ -61,6 +61,7 @@ struct Step {
                     // ST_GEMM: the tile width bn on the tensor cores, 0 on the SIMT kernel
   long long elems = 0;   // ST_GEMM_REDUCE: elements of C summed; ST_CHOL: ints of its counters
   double flops = 0;      // ST_CHOL: algorithmic flops of the launch
+  double bytes = 0;      // ST_CHOL: algorithmic bytes (each job's lower region read once and written once)
 };
 
 template <class T>
