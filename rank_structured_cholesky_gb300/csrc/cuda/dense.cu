@@ -465,6 +465,74 @@ __device__ void trsm_chunk_mul(T* B, int ldb, int nr, int w, T (*X)[65], T (*Li)
   __syncthreads();
 }
 
+// One FP32 tile product of the fused Cholesky, 256 threads:
+//   C := C - A B^T (sub) or C := A B^T,
+// C (M x N), A (M x K), B (N x K) row-major, M, N, K <= 64.  Every global
+// load of a thread is issued before the first use (one latency round instead
+// of one per K slice); a warp's load instruction covers 4 rows x 8 columns
+// (four full 32-byte sectors).  A and B land k-major in shared memory with a
+// pitch of 68 floats -- conflict-free stores, and a thread's four rows (four
+// columns) are one 16-byte shared load -- so a K step is 2 shared loads for
+// 16 FMAs (the 64 x 65 layout took 8).  Each thread owns rows 4 ty + a and
+// columns 4 tx + b; the products are summed in ascending k and subtracted
+// from C at the end.  A and C may alias (the TRSM items overwrite their
+// input): all of A is read before the barrier that precedes the stores.
+__device__ void tile_abt_f32(const float* A, int lda, const float* B, int ldb, float* C, int ldc, int M, int N,
+                             int K, bool sub, float* smem) {
+  constexpr int PITCH = 68;
+  float (*As)[PITCH] = reinterpret_cast<float (*)[PITCH]>(smem);
+  float (*Bs)[PITCH] = reinterpret_cast<float (*)[PITCH]>(smem + 64 * PITCH);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tx = tid & 15, ty = tid >> 4;
+  float ra[16], rb[16], c[4][4];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int pr = q * 8 + warp, i = 4 * (pr & 15) + (lane & 3), k = 8 * (pr >> 4) + (lane >> 2);
+    ra[q] = (i < M && k < K) ? __ldcg(A + (size_t)i * lda + k) : 0.f;
+    rb[q] = (i < N && k < K) ? __ldcg(B + (size_t)i * ldb + k) : 0.f;
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int i = 4 * ty + a, j = 4 * tx + b;
+      c[a][b] = (sub && i < M && j < N) ? __ldcg(C + (size_t)i * ldc + j) : 0.f;
+    }
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int pr = q * 8 + warp, i = 4 * (pr & 15) + (lane & 3), k = 8 * (pr >> 4) + (lane >> 2);
+    As[k][i] = ra[q];
+    Bs[k][i] = rb[q];
+  }
+  __syncthreads();
+  float acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < K; ++k) {
+    const float4 av = *reinterpret_cast<const float4*>(&As[k][4 * ty]);
+    const float4 bv = *reinterpret_cast<const float4*>(&Bs[k][4 * tx]);
+    const float ar[4] = {av.x, av.y, av.z, av.w}, br[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(ar[a], br[b], acc[a][b]);
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int i = 4 * ty + a;
+    if (i >= M) continue;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int j = 4 * tx + b;
+      if (j < N) C[(size_t)i * ldc + j] = sub ? c[a][b] - acc[a][b] : acc[a][b];
+    }
+  }
+  __syncthreads();
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) trsm_inv_kernel(const TrsmTask<T>* __restrict__ tasks, int nTasks) {
   // B (64-row chunk x w) := B L^{-T}: the block inverts its w x w tile and
@@ -584,6 +652,14 @@ __global__ void __launch_bounds__(256) chol_fused_kernel(const CholFusedJob<T>* 
     }
     done = pdone + p;
     doneVal = 1;
+  } else if (it.kind == CHOL_TRSM && std::is_same<T, float>::value) {
+    // X(a) := X(a) Li(p)^T with the panel's inverse tile straight from the workspace
+    const int r0 = rbnd(a), nr = min(rbnd(a + 1), j.nRows) - r0;
+    float* X = reinterpret_cast<float*>(F) + (size_t)r0 * ld + c0;
+    const float* Li = reinterpret_cast<const float*>(ws) + j.inv + (size_t)p * 4096;
+    tile_abt_f32(X, ld, Li, 64, X, ld, nr, wp, wp, false, reinterpret_cast<float*>(cf_smem));
+    done = tdone + a;
+    doneVal = p + 1;
   } else if (it.kind == CHOL_TRSM) {
     T (*X)[65] = reinterpret_cast<T (*)[65]>(cf_smem);
     T (*Li)[65] = reinterpret_cast<T (*)[65]>(cf_smem + sizeof(T) * 64 * 65);
@@ -594,6 +670,15 @@ __global__ void __launch_bounds__(256) chol_fused_kernel(const CholFusedJob<T>* 
     const int r0 = rbnd(a);
     trsm_chunk_mul<T>(F + (size_t)r0 * ld + c0, ld, min(rbnd(a + 1), j.nRows) - r0, wp, X, Li);
     done = tdone + a;
+    doneVal = p + 1;
+  } else if (std::is_same<T, float>::value) {   // update of tile (a, b) by panel p
+    const int r0 = rbnd(a), q0 = bnd(b);
+    float* Ff = reinterpret_cast<float*>(F);
+    const float* Bp = j.L ? reinterpret_cast<const float*>(j.L) + (size_t)q0 * j.ldl + c0 : Ff + (size_t)q0 * ld + c0;
+    const int m = min(rbnd(a + 1), j.nRows) - r0, n = min(bnd(b + 1), j.nUpd) - q0, ldb = j.L ? j.ldl : ld;
+    tile_abt_f32(Ff + (size_t)r0 * ld + c0, ld, Bp, ldb, Ff + (size_t)r0 * ld + q0, ld, m, n, wp, true,
+                 reinterpret_cast<float*>(cf_smem));
+    done = cnt + a * j.TU + b;
     doneVal = p + 1;
   } else {
     const int r0 = rbnd(a), q0 = bnd(b);

@@ -384,6 +384,8 @@ void FactorEngine<T>::emit_trsm(const std::vector<TrsmJob<T>>& jobs) {
       ws += (long long)c.P * NB * NB;
       maxP = std::max(maxP, c.P);
       cholJobs_.push_back(c);
+      // B read and written once, the lower triangle of L read once
+      st.bytes += sizeof(T) * (2.0 * jb.rows * jb.w + 0.5 * (double)jb.w * (jb.w + 1));
       for (int p = 0; p < c.P; ++p) {   // algorithmic flops, as the per-panel steps count them
         const int c0 = p == 0 ? 0 : c.w0 + NB * (p - 1), w = p == 0 ? c.w0 : NB;
         flops += (double)jb.rows * w * w + 2.0 * jb.rows * (double)(jb.w - c0 - w) * w;
