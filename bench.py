@@ -408,7 +408,19 @@ def run_ours(args):
             "true_residual": rf["true_residual"],
             "apply_rel_error_vs_fp64": float(np.linalg.norm(z_root - z_fp64) / np.linalg.norm(z_fp64)),
             "solution_rel_error_vs_fp64": float(np.linalg.norm(x_root - x_fp64) / np.linalg.norm(x_fp64))}
-        del pf, rf
+        # mixed precision with the split products as BF16 hi/lo pairs: its cost and its error
+        bf = timed_solves(lib, rs, torch, prob, dict(params, schur_bf16=1), "mixed", device, local, args.steps,
+                          args.warmup, dist, False)
+        z_bf = bf["F"].apply(b0)
+        x_bf, _ = bf["F"].pcg(b0, eps=1e-8)
+        plain["mixed_schur_bf16"] = {
+            "value": world * args.steps / bf["total_s"], "unit": "solves/s",
+            "factor_ms": statistics.median(bf["factor_ms"]), "pcg_ms": statistics.median(bf["pcg_ms"]),
+            "iterations": bf["iterations"] if nrhs > 1 else bf["iterations"][0],
+            "true_residual": bf["true_residual"],
+            "apply_rel_error_vs_fp64": float(np.linalg.norm(z_bf - z_fp64) / np.linalg.norm(z_fp64)),
+            "solution_rel_error_vs_fp64": float(np.linalg.norm(x_bf - x_fp64) / np.linalg.norm(x_fp64))}
+        del pf, rf, bf
 
     hbm, bf16, src = peaks()
     if rank == 0:

@@ -56,6 +56,10 @@ typedef struct rschol_params {
   int device;                /* CUDA device ordinal (0) */
   int root_fp64;             /* RSCHOL_MIXED only: the dense Cholesky of the root separator's
                                 blocks in FP64, the rest of the factor FP32 (0) */
+  int schur_bf16;            /* RSCHOL_MIXED only: the split-precision tensor-core products (the
+                                Schur-complement updates, projections, U^T U, X doubling) as
+                                BF16 hi/lo splits, three BF16 MMAs with FP32 accumulation, instead
+                                of split TF32 (0) */
 } rschol_params;
 
 typedef struct rschol_ctx rschol_ctx;
@@ -217,8 +221,9 @@ int rschol_step_timing(rschol_factor* f, int enable, double* out);
 
 /* Diagnostics (no reference counterpart): one tensor-core GEMM
  * C = -1.25 op(A) op(B) + 0.5 C on random M x N x K operands (tA / tB:
- * transposed storage, split: split-precision TF32, lower: lower-triangle
- * tiles only) against a host FP64 product.  out[0]: largest error relative to
+ * transposed storage, split: 0 plain TF32, 1 split TF32, 2 split BF16 (the
+ * schur_bf16 products); lower: lower-triangle tiles only) against a host
+ * FP64 product.  out[0]: largest error relative to
  * sum_k |a_ik b_kj| (+ |beta c_ij|), out[1]: largest absolute error. */
 int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int split, int lower, double* out);
 

@@ -57,7 +57,7 @@ class Params(ctypes.Structure):
         ("power_iters", ctypes.c_int), ("reorder_separators", ctypes.c_int), ("rank_constant", ctypes.c_double),
         ("diag_rank_constant", ctypes.c_double), ("max_factor_attempts", ctypes.c_int),
         ("rank_alpha", ctypes.c_double), ("seed", ctypes.c_uint), ("precision", ctypes.c_int),
-        ("device", ctypes.c_int), ("root_fp64", ctypes.c_int),
+        ("device", ctypes.c_int), ("root_fp64", ctypes.c_int), ("schur_bf16", ctypes.c_int),
     ]
 
 

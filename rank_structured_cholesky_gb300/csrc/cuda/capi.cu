@@ -57,6 +57,7 @@ Params to_params(const rschol_params& p) {
   q.rank_alpha = p.rank_alpha;
   q.seed = p.seed;
   q.root_fp64 = p.root_fp64;
+  q.schur_bf16 = p.schur_bf16;
   return q;
 }
 
@@ -240,6 +241,7 @@ void rschol_default_params(rschol_params* p) {
   p->precision = RSCHOL_FP64;
   p->device = 0;
   p->root_fp64 = 0;
+  p->schur_bf16 = 0;
 }
 
 rschol_ctx* rschol_create(const rschol_params* p) {
@@ -705,6 +707,7 @@ const char* rschol_factor_describe(rschol_factor* f) {
   s.pop_back();
   o << s << ", \"precision\": \"" << (f->precision == RSCHOL_MIXED ? "mixed" : "fp64") << "\""
     << ", \"root_fp64\": " << ((f->precision == RSCHOL_MIXED && f->prm.root_fp64) ? 1 : 0)
+    << ", \"schur_bf16\": " << ((f->precision == RSCHOL_MIXED && f->prm.schur_bf16) ? 1 : 0)
     << ", \"factor_launches\": " << f->impl->launches() << ", \"apply_launches\": " << f->impl->apply_launches()
     << ", \"factor_flops\": " << f->impl->flops() << ", \"apply_bytes\": " << f->impl->apply_bytes()
     << ", \"spmv_bytes\": " << f->pcg->spmvBytes << ", \"device_bytes\": " << f->impl->bytes()
@@ -806,20 +809,22 @@ extern "C" int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int spl
     t.bn = bn;
     t.tilesN = (N + bn - 1) / bn;
     t.tileBase = 0;
-    t.split = split;
+    t.split = split ? 1 : 0;
+    const int bf16 = split == 2;
     // K >= 1024 (and not lower): four K slices through the partial workspace
     const int tilesPer = ((M + 127) / 128) * t.tilesN;
     t.kSplit = 1;
     t.kLen = K;
     DevBuf dW, dIds, dBase;
     if (K >= 1024 && !lower) {
-      t.kLen = ((K + 3) / 4 + 31) / 32 * 32;
+      const int al = bf16 ? 64 : 32;
+      t.kLen = ((K + 3) / 4 + al - 1) / al * al;
       t.kSplit = (K + t.kLen - 1) / t.kLen;
       dW.alloc(sizeof(float) * (size_t)t.kSplit * tilesPer * 128 * bn);
       t.ws = dW.as<float>();
     }
     RSCHOL_CUDA(cudaMemcpy(dT.p, &t, sizeof(t), cudaMemcpyHostToDevice));
-    launch_gemm_tc(dT.as<GemmTask<float>>(), 1, tilesPer * t.kSplit, dE.as<int>(), 0, bn);
+    launch_gemm_tc(dT.as<GemmTask<float>>(), 1, tilesPer * t.kSplit, dE.as<int>(), 0, bn, bf16);
     if (t.kSplit > 1) {
       const int id = 0;
       const long long base[2] = {0, (long long)M * N};

@@ -127,9 +127,10 @@ void launch_block_convert(const CvtTask* dTasks, int nTasks, int maxN, int toDou
 // FP32 tasks on the tensor cores (tcgen05, TF32 or split TF32), 128 x bn
 // output tiles, bn = 64 or 128 for the whole launch (tileBase / tilesN counted
 // for that width; every task's bn equal to it); *dErr is set if an mbarrier
-// wait gives up.
+// wait gives up.  bf16: the launch's operands as BF16 (split tasks: hi/lo,
+// three kind::f16 MMAs; K slices of split tasks a multiple of 64).
 void launch_gemm_tc(const GemmTask<float>* dTasks, int nTasks, int totalTiles, int* dErr, cudaStream_t s,
-                    int bn = 64);
+                    int bn = 64, int bf16 = 0);
 // The tile width of a tensor-core launch whose widest task has N columns.
 inline int tc_tile_n(int maxN) { return maxN > 64 ? 128 : 64; }
 // C = alpha * sum of the K-slice partials + beta * C for the split tasks

@@ -58,7 +58,8 @@ void FactorEngine<float>::gemm_launch(const Step& st) {
     launch_gemm_splitk_reduce(dGemm_.as<GemmTask<float>>(), dSplitIds_.as<int>() + st.off, st.count,
                               dSplitBase_.as<long long>() + st.aux, st.elems, stream);
   else if (st.aux)
-    launch_gemm_tc(dGemm_.as<GemmTask<float>>() + st.off, st.count, st.grid, dFlag.as<int>() + 1, stream, st.aux);
+    launch_gemm_tc(dGemm_.as<GemmTask<float>>() + st.off, st.count, st.grid, dFlag.as<int>() + 1, stream,
+                   st.aux & 0xffff, st.aux >> 16);
   else
     launch_gemm<float>(dGemm_.as<GemmTask<float>>() + st.off, st.count, st.grid, stream);
 }
@@ -86,6 +87,11 @@ void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
     maxN = std::max(maxN, t.N);
   }
   const bool tc = useTc_ && maxK >= tcMinK_;
+  // BF16 hi/lo splits for the launch when asked for and it holds split tasks
+  bool bf = false;
+  if (tc && prm.schur_bf16)
+    for (auto& t : batch) bf = bf || t.split != 0;
+  const int kAlign = bf ? 64 : 32;   // K per pipeline stage: split-K slices start on one
   const int rowsPerTile = tc ? 128 : 64;
   const int bn = tc ? tc_tile_n(maxN) : 64;   // tile width: 128 x bn on the tensor cores
   long long baseTiles = 0;
@@ -106,7 +112,7 @@ void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
     if (tc && !t.lower && t.K >= 256 && baseTiles < want) {
       int ks = (int)std::min<long long>(16, std::min<long long>(t.K / 128, (want + baseTiles - 1) / baseTiles));
       if (ks > 1) {
-        const int kl = ((t.K + ks - 1) / ks + 31) / 32 * 32;
+        const int kl = ((t.K + ks - 1) / ks + kAlign - 1) / kAlign * kAlign;
         t.kSplit = (t.K + kl - 1) / kl;
         t.kLen = kl;
         wsOff = wsCur_;
@@ -120,7 +126,7 @@ void FactorEngine<T>::flush_gemm(std::vector<GemmTask<T>>& batch, int) {
     gemmWsOff_.push_back(wsOff);
   }
   Step st{ST_GEMM, first, (int)batch.size(), tiles};
-  st.aux = tc ? bn : 0;
+  st.aux = tc ? bn | (bf ? 1 << 16 : 0) : 0;   // the tile width, and BF16 splits in bit 16
   gemm_.insert(gemm_.end(), batch.begin(), batch.end());
   steps_.push_back(st);
   if (!ids.empty()) {

@@ -61,11 +61,14 @@ constexpr int WS_THREADS = 256;
 // buffers (hi at dst, lo at dst + loOff when split).  Element (r, k) of the
 // tile is src[(row0 + r) * ld + k0 + k] (kContig) or src[(k0 + k) * ld + row0
 // + r]; rows >= nRows and k >= kEnd read as zero.  vec: the 16-byte loads
-// along the contiguous dimension are aligned (checked per task).
-template <int ROWS>
+// along the contiguous dimension are aligned (checked per task).  BF: the
+// tile is stored as BF16 (hi = bf16(a), lo = bf16(a - hi)) at element
+// positions kPos .. kPos + 31 of the 64-element (128-byte) rows; otherwise as
+// TF32 filling the 32-element rows.
+template <int ROWS, bool BF>
 __device__ __forceinline__ void ws_load_tile(const float* __restrict__ src, int ld, bool kContig, bool vec, int row0,
                                              int nRows, int k0, int kEnd, uint32_t dst, uint32_t loOff, bool split,
-                                             int tid) {
+                                             int tid, int kPos = 0) {
   constexpr int PER = ROWS * 32 / 4 / 128;   // float4 groups per producer thread
   float4 v[PER];
   if (kContig) {
@@ -87,12 +90,21 @@ __device__ __forceinline__ void ws_load_tile(const float* __restrict__ src, int 
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
       const int g = tid + 128 * q, r = g >> 3, kk = (g & 7) * 4;
-      const uint32_t off = tc_off(r, kk);
-      const uint32_t h0 = to_tf32(v[q].x), h1 = to_tf32(v[q].y), h2 = to_tf32(v[q].z), h3 = to_tf32(v[q].w);
-      st_shared_v4(dst + off, h0, h1, h2, h3);
-      if (split)
-        st_shared_v4(dst + loOff + off, to_tf32(v[q].x - __uint_as_float(h0)), to_tf32(v[q].y - __uint_as_float(h1)),
-                     to_tf32(v[q].z - __uint_as_float(h2)), to_tf32(v[q].w - __uint_as_float(h3)));
+      if constexpr (BF) {
+        const uint32_t off = tc_off16(r, kPos + kk);
+        float l[4];
+        const uint32_t h01 = split_bf16x2(v[q].x, v[q].y, l[0], l[1]), h23 = split_bf16x2(v[q].z, v[q].w, l[2], l[3]);
+        st_shared_v2(dst + off, h01, h23);
+        if (split) st_shared_v2(dst + loOff + off, pack_bf16x2(l[0], l[1]), pack_bf16x2(l[2], l[3]));
+      } else {
+        const uint32_t off = tc_off(r, kk);
+        const uint32_t h0 = to_tf32(v[q].x), h1 = to_tf32(v[q].y), h2 = to_tf32(v[q].z), h3 = to_tf32(v[q].w);
+        st_shared_v4(dst + off, h0, h1, h2, h3);
+        if (split)
+          st_shared_v4(dst + loOff + off, to_tf32(v[q].x - __uint_as_float(h0)),
+                       to_tf32(v[q].y - __uint_as_float(h1)), to_tf32(v[q].z - __uint_as_float(h2)),
+                       to_tf32(v[q].w - __uint_as_float(h3)));
+      }
     }
   } else {
     // group g: k g / (ROWS / 4), rows 4 (g mod ROWS / 4) .. +3
@@ -117,18 +129,28 @@ __device__ __forceinline__ void ws_load_tile(const float* __restrict__ src, int 
       const float e[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const uint32_t off = tc_off(r + u, kk), h = to_tf32(e[u]);
-        st_shared_b32(dst + off, h);
-        if (split) st_shared_b32(dst + loOff + off, to_tf32(e[u] - __uint_as_float(h)));
+        if constexpr (BF) {
+          const uint32_t off = tc_off16(r + u, kPos + kk);
+          const __nv_bfloat16 h = __float2bfloat16_rn(e[u]);
+          st_shared_b16(dst + off, __bfloat16_as_ushort(h));
+          if (split)
+            st_shared_b16(dst + loOff + off, __bfloat16_as_ushort(__float2bfloat16_rn(e[u] - __bfloat162float(h))));
+        } else {
+          const uint32_t off = tc_off(r + u, kk), h = to_tf32(e[u]);
+          st_shared_b32(dst + off, h);
+          if (split) st_shared_b32(dst + loOff + off, to_tf32(e[u] - __uint_as_float(h)));
+        }
       }
     }
   }
 }
 
-template <int BN, int NS>
+template <int BN, int NS, bool BF>
 __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<float>* __restrict__ tasks,
                                                                   int nTasks, int* __restrict__ err) {
-  constexpr int A_BYTES = TC_BM * TC_BK * 4, B_BYTES = BN * TC_BK * 4;
+  // a stage holds 128-byte rows: 32 K as TF32, or 64 K as BF16
+  constexpr int SK = BF ? 2 * TC_BK : TC_BK;
+  constexpr int A_BYTES = TC_BM * 128, B_BYTES = BN * 128;
   constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;   // hi and lo of both operands
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   __shared__ __align__(8) uint64_t fullB[NS], emptyB[NS], doneB;
@@ -150,7 +172,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
   if (t.lower && row0 + TC_BM - 1 < col0) return;   // uniform over the block, before any allocation
   const int kl = t.kLen > 0 ? t.kLen : t.K;
   const int kBeg = slice * kl, kEnd = min(t.K, kBeg + kl);
-  const int nk = kEnd > kBeg ? (kEnd - kBeg + TC_BK - 1) / TC_BK : 0;
+  const int nk = kEnd > kBeg ? (kEnd - kBeg + SK - 1) / SK : 0;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool split = t.split != 0;
   const uint32_t sraw = (uint32_t)__cvta_generic_to_shared(tc_smem);
@@ -190,9 +212,14 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
       }
       if (sAbort) break;
       const uint32_t a = sbase + (uint32_t)(st * STAGE), b = a + 2 * A_BYTES;
-      const int k0 = kBeg + kt * TC_BK;
-      ws_load_tile<TC_BM>(t.A, t.lda, aK, aVec, row0, t.M, k0, kEnd, a, A_BYTES, split, tid);
-      ws_load_tile<BN>(t.B, t.ldb, bK, bVec, col0, t.N, k0, kEnd, b, B_BYTES, split, tid);
+      const int k0 = kBeg + kt * SK;
+#pragma unroll
+      for (int h = 0; h < SK / TC_BK; ++h) {
+        ws_load_tile<TC_BM, BF>(t.A, t.lda, aK, aVec, row0, t.M, k0 + TC_BK * h, kEnd, a, A_BYTES, split, tid,
+                                TC_BK * h);
+        ws_load_tile<BN, BF>(t.B, t.ldb, bK, bVec, col0, t.N, k0 + TC_BK * h, kEnd, b, B_BYTES, split, tid,
+                             TC_BK * h);
+      }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(full0 + 8u * st);
     }
@@ -210,13 +237,13 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t a = sbase + (uint32_t)(st * STAGE), b = a + 2 * A_BYTES;
 #pragma unroll
-        for (int kk = 0; kk < TC_BK / 8; ++kk) {
-          const uint32_t step = (uint32_t)kk * 32u;   // 8 TF32 = 32 bytes along the swizzled row
+        for (int kk = 0; kk < 4; ++kk) {
+          const uint32_t step = (uint32_t)kk * 32u;   // 8 TF32 or 16 BF16 = 32 bytes along the swizzled row
           const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
-          ws_mma<BN>(tmem, tc_smem_desc(a + step), tc_smem_desc(b + step), acc);
+          ws_mma<BN, BF>(tmem, tc_smem_desc(a + step), tc_smem_desc(b + step), acc);
           if (split) {
-            ws_mma<BN>(tmem, tc_smem_desc(a + step), tc_smem_desc(b + B_BYTES + step), 1u);
-            ws_mma<BN>(tmem, tc_smem_desc(a + A_BYTES + step), tc_smem_desc(b + step), 1u);
+            ws_mma<BN, BF>(tmem, tc_smem_desc(a + step), tc_smem_desc(b + B_BYTES + step), 1u);
+            ws_mma<BN, BF>(tmem, tc_smem_desc(a + A_BYTES + step), tc_smem_desc(b + step), 1u);
           }
         }
         tc_commit(empty0 + 8u * st);
@@ -315,22 +342,27 @@ __global__ void gemm_splitk_reduce(const GemmTask<float>* __restrict__ tasks, co
 
 }  // namespace
 
-template <int BN, int NS>
+template <int BN, int NS, bool BF>
 void launch_ws(const GemmTask<float>* d, int nTasks, int tiles, int* dErr, cudaStream_t s) {
-  constexpr int smem = NS * (2 * TC_BM * TC_BK * 4 + 2 * BN * TC_BK * 4) + 1024;
+  constexpr int smem = NS * (2 * TC_BM * 128 + 2 * BN * 128) + 1024;
   static_assert(smem <= 227 * 1024, "stages exceed shared memory");
   static std::once_flag once;
   std::call_once(once, [] {
-    RSCHOL_CUDA(cudaFuncSetAttribute(gemm_tc_kernel<BN, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    RSCHOL_CUDA(cudaFuncSetAttribute(gemm_tc_kernel<BN, NS, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   });
-  gemm_tc_kernel<BN, NS><<<tiles, WS_THREADS, smem, s>>>(d, nTasks, dErr);
+  gemm_tc_kernel<BN, NS, BF><<<tiles, WS_THREADS, smem, s>>>(d, nTasks, dErr);
   RSCHOL_LAUNCH_CHECK();
 }
 
-void launch_gemm_tc(const GemmTask<float>* d, int nTasks, int tiles, int* dErr, cudaStream_t s, int bn) {
+void launch_gemm_tc(const GemmTask<float>* d, int nTasks, int tiles, int* dErr, cudaStream_t s, int bn, int bf16) {
   if (nTasks <= 0 || tiles <= 0) return;
-  if (bn > 64) launch_ws<128, 3>(d, nTasks, tiles, dErr, s);
-  else launch_ws<64, 4>(d, nTasks, tiles, dErr, s);
+  if (bf16) {
+    if (bn > 64) launch_ws<128, 3, true>(d, nTasks, tiles, dErr, s);
+    else launch_ws<64, 4, true>(d, nTasks, tiles, dErr, s);
+  } else {
+    if (bn > 64) launch_ws<128, 3, false>(d, nTasks, tiles, dErr, s);
+    else launch_ws<64, 4, false>(d, nTasks, tiles, dErr, s);
+  }
 }
 
 void launch_gemm_splitk_reduce(const GemmTask<float>* d, const int* ids, int nIds, const long long* elemBase,

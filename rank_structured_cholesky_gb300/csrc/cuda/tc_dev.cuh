@@ -3,6 +3,8 @@
 // TF32 conversion, mbarriers, and the kind::tf32 MMA with M = 128 (one
 // accumulator row per TMEM lane), TMEM allocation and loads.
 #pragma once
+#include <cuda_bf16.h>
+
 #include <cstdint>
 
 namespace rschol {
@@ -15,6 +17,11 @@ constexpr int TC_SPIN_LIMIT = 1 << 22;   // polls before an mbarrier wait gives 
 // atom; its 16-byte chunk c is stored at chunk c ^ (r & 7).
 __device__ __forceinline__ uint32_t tc_off(int r, int k) {
   return (uint32_t)(((r >> 3) << 10) + ((r & 7) << 7) + ((((k >> 2) ^ (r & 7)) & 7) << 4) + ((k & 3) << 2));
+}
+
+// The same layout for 16-bit elements: a row is 64 BF16, a 16-byte chunk 8.
+__device__ __forceinline__ uint32_t tc_off16(int r, int k) {
+  return (uint32_t)(((r >> 3) << 10) + ((r & 7) << 7) + ((((k >> 3) ^ (r & 7)) & 7) << 4) + ((k & 7) << 1));
 }
 
 __device__ __forceinline__ uint64_t tc_smem_desc(uint32_t saddr) {
@@ -71,21 +78,52 @@ __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t
 __device__ __forceinline__ void st_shared_b32(uint32_t addr, uint32_t a) {
   asm volatile("st.shared.b32 [%0], %1;" ::"r"(addr), "r"(a) : "memory");
 }
-
-// Instruction descriptor: D f32, A and B tf32, both K-major, M = 128, N = BN.
-template <int BN>
-__host__ __device__ constexpr uint32_t ws_idesc() {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+__device__ __forceinline__ void st_shared_v2(uint32_t addr, uint32_t a, uint32_t b) {
+  asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(addr), "r"(a), "r"(b) : "memory");
+}
+__device__ __forceinline__ void st_shared_b16(uint32_t addr, unsigned short a) {
+  asm volatile("st.shared.b16 [%0], %1;" ::"r"(addr), "h"(a) : "memory");
 }
 
-template <int BN>
+// Two FP32 values as BF16 (round to nearest even), the first in the low half.
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+// The same, and the remainders a - bf16(a), b - bf16(b) (exact in FP32) for
+// the low part of a split product.
+__device__ __forceinline__ uint32_t split_bf16x2(float a, float b, float& ra, float& rb) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  ra = a - __low2float(v);
+  rb = b - __high2float(v);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// Instruction descriptor: D f32, A and B both tf32 (kind::tf32) or both
+// bf16 (kind::f16), both K-major, M = 128, N = BN.
+template <int BN, bool BF = false>
+__host__ __device__ constexpr uint32_t ws_idesc() {
+  return (1u << 4) | ((BF ? 1u : 2u) << 7) | ((BF ? 1u : 2u) << 10) | ((uint32_t)(BN >> 3) << 17) |
+         ((uint32_t)(128 >> 4) << 24);
+}
+
+// One MMA step of 32 bytes along K (8 TF32 or 16 BF16) into the accumulator.
+template <int BN, bool BF = false>
 __device__ __forceinline__ void ws_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(ws_idesc<BN>()), "r"(accumulate)
-      : "memory");
+  if constexpr (BF)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(ws_idesc<BN, true>()), "r"(accumulate)
+        : "memory");
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(ws_idesc<BN>()), "r"(accumulate)
+        : "memory");
 }
 
 // TMEM columns for the CTA (one warp, all lanes); the base address lands in

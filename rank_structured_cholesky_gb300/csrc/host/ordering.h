@@ -38,6 +38,7 @@ struct Params {
   double rank_alpha = 1.25;       // SparseSolver::_rankConstantAlpha
   uint32_t seed = 152;            // MathUtil::GENERATOR reseed in factorNumeric
   int root_fp64 = 0;              // mixed precision: the root separator's dense Cholesky in FP64
+  int schur_bf16 = 0;             // mixed precision: split products as BF16 hi/lo instead of TF32
 };
 
 struct CSC {

@@ -157,3 +157,23 @@ def test_mixed_with_fp64_root_separator(name, cases):
     x, info = G.pcg(b, 1e-8, 2000)
     assert abs(info["iterations"] - it_oracle) <= 1, (info, it_oracle)
     assert info["true_residual"] <= 1e-8
+
+
+@pytest.mark.parametrize("name", ["c2s", "c2", "c1"])
+def test_mixed_with_bf16_split_products(name, cases):
+    """Mixed precision with the split tensor-core products as BF16 hi/lo
+    pairs (schur_bf16): the BF16 kernels run (the launches are marked in the
+    factor description), and the solve reaches the 1e-8 residual within the
+    oracle's iteration count +-1 with one application within
+    MIXED_APPLY_TOL of the FP64 oracle."""
+    prob, params, O, it_oracle = cases(name)
+    ctx = rs.Context(**params, precision=rs.MIXED, schur_bf16=1)
+    G = rs.GpuFactor(ctx, prob.colptr, prob.rowind, prob.vals, prob.xyz)
+    assert G.describe()["schur_bf16"] == 1
+    b = prob.rhs[0]
+    err = rel(G.apply(b), O.apply(b))
+    x, info = G.pcg(b, 1e-8, 2000)
+    print("schur_bf16", name, "apply", err, "iterations", info["iterations"], "oracle", it_oracle)
+    assert err < MIXED_APPLY_TOL
+    assert abs(info["iterations"] - it_oracle) <= 1, (info, it_oracle)
+    assert info["true_residual"] <= 1e-8
