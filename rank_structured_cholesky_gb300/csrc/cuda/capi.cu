@@ -72,6 +72,7 @@ struct Impl {
   virtual void apply_batch(double* W, int k, cudaStream_t s) = 0;   // W: n x k row-major, permuted
   virtual int batch_capacity() const = 0;
   virtual int apply_batch_error(cudaStream_t s) = 0;
+  virtual long long batch_generation() const = 0;
   virtual void set_values(const double* lower) = 0;
   virtual double* device_values() = 0;
   virtual long long launches() const = 0;
@@ -111,6 +112,7 @@ struct ImplT : Impl {
   void apply_batch(double* W, int k, cudaStream_t s) override { se.apply_batch(W, k, s); }
   int batch_capacity() const override { return se.batch_capacity(); }
   int apply_batch_error(cudaStream_t s) override { return se.take_error_batch(s); }
+  long long batch_generation() const override { return se.batch_generation(); }
   void step_timing(bool on, double* out) override {
     if (out)
       for (int k = 0; k < 8; ++k) {
@@ -1008,7 +1010,8 @@ extern "C" rschol_session* rschol_session_create(rschol_factor* f, int max_colum
     out->f = f;
     out->ses.reset(new PcgSession(
         *f->pcg, k, f->dPerm.as<int>(), [impl, s](double* w, int kk) { impl->apply_batch(w, kk, s); },
-        [impl, s]() { return impl->apply_batch_error(s); }));
+        [impl, s]() { return impl->apply_batch_error(s); },
+        [impl]() { return (long long)(impl->planGen << 32) + impl->batch_generation(); }));
     return out.release();
   } catch (const std::exception& e) {
     fail(f->ctx, RSCHOL_E_CUDA, e.what());

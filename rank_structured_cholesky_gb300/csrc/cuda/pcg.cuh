@@ -114,9 +114,14 @@ class PcgSession {
     bool breakdown = false, finished = false;
   };
   // apply(W, k): in-place M^{-1} of an n x k permuted block;
-  // applyError(): 0, or non-zero when a wait of the last applies gave up.
+  // applyError(): 0, or non-zero when a wait of the last applies gave up;
+  // applyGen(): changes whenever the buffers apply() uses move.
+  // The iteration part of a step (apply, dots, SpMV, updates) is captured as
+  // a CUDA graph once two consecutive steps have the same width, column block
+  // and buffers, and replayed while they stay so (RSCHOL_SESSION_GRAPH=0: every
+  // step launches its kernels directly); both run the same kernels.
   PcgSession(PcgEngine& pcg, int kmax, const int* dPerm, std::function<void(double*, int)> apply,
-             std::function<int()> applyError);
+             std::function<int()> applyError, std::function<long long()> applyGen = {});
   ~PcgSession();
   void add(long long tag, int col, const double* b, double* x, double eps, int maxit);
   std::vector<Column> step();
@@ -135,6 +140,16 @@ class PcgSession {
   const int* perm_;
   std::function<void(double*, int)> apply_;
   std::function<int()> applyError_;
+  std::function<long long()> applyGen_;
+  struct GraphKey {
+    int k = -1, set = -1;
+    long long gen = -1, apply = -1;
+    bool operator==(const GraphKey& o) const { return k == o.k && set == o.set && gen == o.gen && apply == o.apply; }
+  };
+  bool useGraph_ = true;
+  long long gen_ = 0;                 // bumped when the session's own blocks are reallocated
+  GraphKey gKey_, lastKey_;
+  cudaGraphExec_t gExec_ = nullptr;   // the captured iteration for gKey_
   std::vector<Column> cols_;
   std::deque<Column> queue_;
   DevBuf x_[2], r_[2], d_[2], b_[2], s_, q_, part_, sc_;

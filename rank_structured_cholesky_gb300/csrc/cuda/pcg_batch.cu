@@ -6,6 +6,7 @@
 // then on (x and r frozen), as if its own loop had stopped.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "pcg.cuh"
 
@@ -445,8 +446,12 @@ std::vector<PcgResult> PcgEngine::solve_batch(const double* B, double* X, int k,
 // other columns in the block.
 
 PcgSession::PcgSession(PcgEngine& pcg, int kmax, const int* dPerm,
-                       std::function<void(double*, int)> apply, std::function<int()> applyError)
-    : pcg_(pcg), kmax_(kmax), perm_(dPerm), apply_(std::move(apply)), applyError_(std::move(applyError)) {
+                       std::function<void(double*, int)> apply, std::function<int()> applyError,
+                       std::function<long long()> applyGen)
+    : pcg_(pcg), kmax_(kmax), perm_(dPerm), apply_(std::move(apply)), applyError_(std::move(applyError)),
+      applyGen_(std::move(applyGen)) {
+  const char* g = std::getenv("RSCHOL_SESSION_GRAPH");
+  useGraph_ = !(g && g[0] == '0');
   if (kmax < 1 || kmax > KMAX) throw std::runtime_error("PcgSession: 1..64 columns");
   part_.alloc(sizeof(double) * BBLOCKS * kmax);
   sc_.alloc(sizeof(double) * S_COUNT * kmax);
@@ -455,6 +460,7 @@ PcgSession::PcgSession(PcgEngine& pcg, int kmax, const int* dPerm,
 }
 
 PcgSession::~PcgSession() {
+  if (gExec_) cudaGraphExecDestroy(gExec_);
   if (hsc_) cudaFreeHost(hsc_);
 }
 
@@ -465,6 +471,7 @@ void PcgSession::reserve_set(int set, int k) {
   const size_t nk = sizeof(double) * std::max<size_t>(1, (size_t)pcg_.n * k);
   for (auto* v : {&x_[set], &r_[set], &d_[set], &b_[set]}) v->alloc(nk);
   cap_[set] = k;
+  ++gen_;
 }
 
 void PcgSession::add(long long tag, int col, const double* b, double* x, double eps, int maxit) {
@@ -498,6 +505,7 @@ std::vector<PcgSession::Column> PcgSession::step() {
     s_.alloc(nk);
     q_.alloc(nk);
     capS_ = c;
+    ++gen_;
   }
   int m = 0;
   while (!queue_.empty() && (int)next.size() < kmax_) {
@@ -554,18 +562,49 @@ std::vector<PcgSession::Column> PcgSession::step() {
   const int* ci = pcg_.colind_.as<int>();
   const double* v = pcg_.vals_.as<double>();
   const size_t nkBytes = sizeof(double) * (size_t)n * k;
-  // 2. s = M^{-1} r; t = r.s; d = s + beta d
-  RSCHOL_CUDA(cudaMemcpyAsync(S, R, nkBytes, cudaMemcpyDeviceToDevice, st));
-  apply_(S, k);
-  dot_k(st, R, S, n, k, part);
-  finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_SLOT);
-  update_d_k(st, D, S, sc, n, k);
-  // 3. q = A d; alpha; x += alpha d; r -= alpha q; ||r|| / ||b||
-  spmv_k(st, n, k, rp, ci, v, D, Q, part);
-  finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_ALPHA);
-  update_xr_k(st, X, R, D, Q, sc, n, k, part);
-  finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_RNORM);
-  RSCHOL_LAUNCH_CHECK();
+  auto iteration = [&]() {
+    // 2. s = M^{-1} r; t = r.s; d = s + beta d
+    RSCHOL_CUDA(cudaMemcpyAsync(S, R, nkBytes, cudaMemcpyDeviceToDevice, st));
+    apply_(S, k);
+    dot_k(st, R, S, n, k, part);
+    finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_SLOT);
+    update_d_k(st, D, S, sc, n, k);
+    // 3. q = A d; alpha; x += alpha d; r -= alpha q; ||r|| / ||b||
+    spmv_k(st, n, k, rp, ci, v, D, Q, part);
+    finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_ALPHA);
+    update_xr_k(st, X, R, D, Q, sc, n, k, part);
+    finish_k_kernel<<<(k + 7) / 8, 256, 0, st>>>(part, BBLOCKS, k, sc, F_RNORM);
+    RSCHOL_LAUNCH_CHECK();
+  };
+  const GraphKey key{k, cur_, gen_, applyGen_ ? applyGen_() : 0};
+  if (useGraph_ && gExec_ && key == gKey_) {
+    RSCHOL_CUDA(cudaGraphLaunch(gExec_, st));
+  } else if (useGraph_ && key == lastKey_) {
+    // the previous step ran this iteration directly (so the apply's plan and
+    // tile shapes for k exist): capture it once and replay it from now on
+    if (gExec_) {
+      RSCHOL_CUDA(cudaGraphExecDestroy(gExec_));
+      gExec_ = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    RSCHOL_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      iteration();
+    } catch (...) {
+      cudaStreamEndCapture(st, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    RSCHOL_CUDA(cudaStreamEndCapture(st, &g));
+    const cudaError_t ie = cudaGraphInstantiate(&gExec_, g, 0);
+    cudaGraphDestroy(g);
+    RSCHOL_CUDA(ie);
+    gKey_ = key;
+    RSCHOL_CUDA(cudaGraphLaunch(gExec_, st));
+  } else {
+    iteration();
+  }
+  lastKey_ = key;
   launches += 8;
   RSCHOL_CUDA(cudaMemcpyAsync(hsc_, sc, sizeof(double) * S_COUNT * k, cudaMemcpyDeviceToHost, st));
   RSCHOL_CUDA(cudaStreamSynchronize(st));

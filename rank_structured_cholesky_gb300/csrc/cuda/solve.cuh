@@ -118,6 +118,9 @@ class SolveEngine {
   // the tile shapes chosen for each width class so far: (class, RA, RC, cwR, cwC, ms) rows
   std::vector<std::array<double, 6>> batch_tuning() const;
   int batch_capacity() const;
+  // bumped whenever the batched apply's buffers are reallocated or its tile
+  // shapes retuned (a graph that captured an apply must then be captured again)
+  long long batch_generation() const { return batchGen_; }
   int take_error_batch(cudaStream_t s);
   long long launches_per_apply() const { return launchesPerApply_; }
   double bytes_per_apply() const { return bytesPerApply_; }
@@ -174,7 +177,8 @@ class SolveEngine {
   long long wuTotal_ = 0, ipTotal_ = 0;
   int maxNI_ = 0;                      // largest interior supernode width
   std::vector<int> cMRowGrid_;         // per compressed level: 8-row blocks of the largest m
-  int kB_ = 0, kAllocB_ = 0, epochB_ = 0;
+  int kB_ = 0, kAllocB_ = 0;
+  long long batchGen_ = 0;
   DevBuf dWuB_, dYB_, dIpB_, dSyncB_, dWB_;
   struct BatchPlan {
     DevBuf tasks, sums, ws;   // GEMM tasks, K-slice sums and their slice products

@@ -471,9 +471,13 @@ __global__ void __launch_bounds__(256) slice_sum_kernel(const SliceSum<T>* __res
 }
 
 template <class A, class B>
-__global__ void convert_k_kernel(const A* __restrict__ src, B* __restrict__ dst, long long count) {
+__global__ void convert_k_kernel(const A* __restrict__ src, B* __restrict__ dst, long long count,
+                                 int* __restrict__ clr = nullptr, int nClr = 0) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
     dst[i] = (B)src[i];
+  // the last kernel of a batched apply also zeroes the interior completion
+  // counters (their last reader, the backward launch, has finished)
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nClr; i += gridDim.x * blockDim.x) clr[i] = 0;
 }
 
 int skinny_width(int k) {
@@ -508,10 +512,10 @@ void SolveEngine<T>::plan_batch(int k, int cwR, int cwC) {
     if (!dSyncB_.p) {
       dSyncB_.alloc(sizeof(int) * syncInts_);
       RSCHOL_CUDA(cudaMemsetAsync(dSyncB_.p, 0, sizeof(int) * syncInts_, st));
-      epochB_ = 0;
     }
     dWB_.alloc(sizeof(T) * std::max<long long>(1, (long long)S.n * k));   // the working copy of W
     kAllocB_ = k;
+    ++batchGen_;
     bPlans_.clear();   // the task lists point into the old buffers
   }
   auto found = bPlans_.find(key);
@@ -723,6 +727,7 @@ const typename SolveEngine<T>::BatchCfg& SolveEngine<T>::config_for(int k, cudaS
     RSCHOL_CUDA(cudaEventDestroy(e0));
     RSCHOL_CUDA(cudaEventDestroy(e1));
   }
+  ++batchGen_;   // new tile shapes: a captured apply would use the old ones
   return tuned_[kp] = best;
 }
 
@@ -756,10 +761,10 @@ void SolveEngine<T>::apply_batch_cfg(double* W64, int k, cudaStream_t st, const 
   T* w = dWB_.as<T>();
   convert_k_kernel<double, T><<<(unsigned)std::min<long long>((nk + 255) / 256, 4096), 256, 0, st>>>(W64, w, nk);
   RSCHOL_LAUNCH_CHECK();
-  if (++epochB_ >= (1 << 24)) {
-    RSCHOL_CUDA(cudaMemsetAsync(dSyncB_.p, 0, sizeof(int) * syncInts_, st));
-    epochB_ = 1;
-  }
+  // completion targets: every apply starts its counters at zero (they are
+  // cleared by its last kernel), so the apply keeps no host state and replays
+  // inside CUDA graphs
+  const int epoch = 1;
   int* sync = dSyncB_.as<int>();
   const size_t smem = sizeof(T) * (size_t)(maxNI_ + 64) * k;
   static std::once_flag once;
@@ -791,7 +796,7 @@ void SolveEngine<T>::apply_batch_cfg(double* W64, int k, cudaStream_t st, const 
   }
   if (nIWork_ > 0) {
     fwd<<<nIWork_, 256, smem, st>>>(dNodes_.as<SNode<T>>(), dIWork_.as<RowBlock>(), dRel_.as<int>(), dChild_.as<int>(),
-                                    sync, epochB_, k, w, dYB_.as<T>(), dWuB_.as<T>());
+                                    sync, epoch, k, w, dYB_.as<T>(), dWuB_.as<T>());
     RSCHOL_LAUNCH_CHECK();
   }
   const int* lvl = dLevelNodes_.as<int>();
@@ -839,11 +844,12 @@ void SolveEngine<T>::apply_batch_cfg(double* W64, int k, cudaStream_t st, const 
     gemm(6 * l + 5);
   }
   if (nIWork_ > 0) {
-    bwd<<<nIWork_, 256, smem, st>>>(dNodes_.as<SNode<T>>(), dIWorkB_.as<RowBlock>(), dRows_.as<int>(), sync, epochB_,
+    bwd<<<nIWork_, 256, smem, st>>>(dNodes_.as<SNode<T>>(), dIWorkB_.as<RowBlock>(), dRows_.as<int>(), sync, epoch,
                                     k, dIpB_.as<T>(), dYB_.as<T>(), w);
     RSCHOL_LAUNCH_CHECK();
   }
-  convert_k_kernel<T, double><<<(unsigned)std::min<long long>((nk + 255) / 256, 4096), 256, 0, st>>>(w, W64, nk);
+  convert_k_kernel<T, double><<<(unsigned)std::min<long long>((nk + 255) / 256, 4096), 256, 0, st>>>(
+      w, W64, nk, nIWork_ > 0 ? sync + SYNC_GLOBAL : nullptr, nIWork_ > 0 ? syncInts_ - SYNC_GLOBAL : 0);
   RSCHOL_LAUNCH_CHECK();
 }
 
@@ -856,7 +862,6 @@ int SolveEngine<T>::take_error_batch(cudaStream_t st) {
   if (e) {
     RSCHOL_CUDA(cudaMemsetAsync(dSyncB_.p, 0, sizeof(int) * syncInts_, st));
     RSCHOL_CUDA(cudaStreamSynchronize(st));
-    epochB_ = 0;
   }
   return e;
 }

@@ -87,3 +87,26 @@ def test_zero_right_hand_side_is_a_breakdown():
     assert st == 5   # RSCHOL_E_BREAKDOWN, as rschol_pcg reports a zero column
     assert np.all(x[0] == 0)
     assert info[1]["true_residual"] <= 10 * EPS
+
+
+@pytest.mark.parametrize("precision", [rs.FP64, rs.MIXED])
+def test_graph_replayed_steps_match_direct_launches(precision, monkeypatch):
+    """A session replays the iteration part of a step from a CUDA graph once
+    two consecutive steps have the same width and buffers; with
+    RSCHOL_SESSION_GRAPH=0 every step launches the same kernels directly.
+    Staggered joins change the width (a new capture) and a long run of
+    unchanged steps replays: bitwise the same x and iteration counts."""
+    prob = rs.diffusion(3, 12, sigma=1.0, seed=4)
+    rng = np.random.default_rng(11)
+    reqs = {t: rng.standard_normal((int(rng.integers(1, 4)), prob.n)) for t in range(1, 6)}
+    schedule = {0: [(1, reqs[1])], 1: [(2, reqs[2])], 5: [(3, reqs[3])], 6: [(4, reqs[4])], 20: [(5, reqs[5])]}
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("RSCHOL_SESSION_GRAPH", mode)
+        G = rs.GpuFactor(rs.Context(precision=precision, **PARAMS), prob.colptr, prob.rowind, prob.vals, prob.xyz)
+        out[mode] = _run(rs.Session(G, max_columns=8), schedule)
+        del G
+    for t in reqs:
+        assert out["0"][t][0] == 0 and out["1"][t][0] == 0
+        assert np.array_equal(out["0"][t][1], out["1"][t][1]), t
+        assert [i["iterations"] for i in out["0"][t][2]] == [i["iterations"] for i in out["1"][t][2]]
