@@ -475,7 +475,8 @@ def run_ours(args):
         roof["traffic_over_algorithmic"] = t_small / a_small if (t_small and a_small) else None
         t_gemm, _ = traffic_from_profiles("gemm_tc_kernel", "c2s")
         roof_gemm = roofline("factor GEMMs (gemm_kernel SIMT and gemm_tc_kernel tcgen05)", c[0], c[1], c[2],
-                             t_gemm, "profiles/gemm_tc_kernel_c2s.md (c2s launches)")
+                             t_gemm, "profiles/gemm_tc_kernel_c2s.md: average DRAM bytes of the c2s GEMM launches, "
+                             "not scaled")
         apply_bytes = phase["apply_bytes"]
         its = main["iterations"][0]
         pcg_bytes = its * (apply_bytes + phase["spmv_bytes"] + 8.0 * 10 * n)
