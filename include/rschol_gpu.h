@@ -227,6 +227,12 @@ int rschol_step_timing(rschol_factor* f, int enable, double* out);
  * sum_k |a_ik b_kj| (+ |beta c_ij|), out[1]: largest absolute error. */
 int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int split, int lower, double* out);
 
+/* Diagnostics (no reference counterpart): *ms = average device time of one
+ * tensor-core launch C (M x N) -= A (M x K) B^T (A, B row-major, the
+ * factor's update shape; split as in rschol_selftest_gemm; no K slices),
+ * over reps launches after one warm-up, on zero operands. */
+int rschol_bench_gemm(int M, int N, int K, int split, int reps, double* ms);
+
 /* Preconditioned CG from x0 = 0 with the factor as M, stopping at
  * ||r|| / ||b|| <= eps or maxit iterations; nrhs right-hand sides are solved
  * together, sharing the factor.

@@ -31,7 +31,7 @@ FP64, MIXED = 0, 1
 EXPORTED = [
     "rschol_default_params", "rschol_create", "rschol_destroy", "rschol_last_error", "rschol_factor_create",
     "rschol_refactor", "rschol_refactor_device", "rschol_stream", "rschol_profile", "rschol_factor_free", "rschol_precond_apply", "rschol_precond_apply_device",
-    "rschol_precond_apply_device_noalloc", "rschol_selftest_gemm", "rschol_step_timing", "rschol_pcg",
+    "rschol_precond_apply_device_noalloc", "rschol_selftest_gemm", "rschol_bench_gemm", "rschol_step_timing", "rschol_pcg",
     "rschol_pcg_device", "rschol_pcg_pysolve", "rschol_factor_n", "rschol_factor_device_bytes", "rschol_factor_num_nodes",
     "rschol_factor_node_info", "rschol_factor_node_l11", "rschol_factor_node_l21", "rschol_factor_perm",
     "rschol_factor_describe", "rschol_factor_stats", "rschol_problem_diffusion", "rschol_problem_elasticity",
@@ -94,6 +94,7 @@ def load_library():
         "rschol_precond_apply_device": (I, [P, P, P, I]),
         "rschol_precond_apply_device_noalloc": (I, [P, P, P, I]),
         "rschol_selftest_gemm": (I, [I, I, I, I, I, I, I, pD]),
+        "rschol_bench_gemm": (I, [I, I, I, I, I, pD]),
         "rschol_step_timing": (I, [P, I, P]),
         "rschol_pcg": (I, [P, pD, pD, I, D, I, ctypes.POINTER(PcgInfo)]),
         "rschol_pcg_device": (I, [P, P, P, I, D, I, ctypes.POINTER(PcgInfo)]),

@@ -866,6 +866,67 @@ extern "C" int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int spl
   return RSCHOL_OK;
 }
 
+// ---- diagnostics: device time of one tensor-core GEMM launch -----------------
+extern "C" int rschol_bench_gemm(int M, int N, int K, int split, int reps, double* ms) {
+  if (M <= 0 || N <= 0 || K <= 0 || reps <= 0 || !ms || split < 0 || split > 2) return RSCHOL_E_BAD_INPUT;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return RSCHOL_E_NO_DEVICE;
+  try {
+    // C (M x N) = A (M x K) B^T (B: N x K), both row-major: the factor's update shape
+    DevBuf dA, dB, dC, dT, dE;
+    dA.alloc(sizeof(float) * (size_t)M * K);
+    dB.alloc(sizeof(float) * (size_t)N * K);
+    dC.alloc(sizeof(float) * (size_t)M * N);
+    dT.alloc(sizeof(GemmTask<float>));
+    dE.alloc(sizeof(int));
+    RSCHOL_CUDA(cudaMemset(dA.p, 0, sizeof(float) * (size_t)M * K));
+    RSCHOL_CUDA(cudaMemset(dB.p, 0, sizeof(float) * (size_t)N * K));
+    RSCHOL_CUDA(cudaMemset(dC.p, 0, sizeof(float) * (size_t)M * N));
+    RSCHOL_CUDA(cudaMemset(dE.p, 0, sizeof(int)));
+    GemmTask<float> t{};
+    t.A = dA.as<float>();
+    t.B = dB.as<float>();
+    t.C = dC.as<float>();
+    t.M = M;
+    t.N = N;
+    t.K = K;
+    t.lda = K;
+    t.ldb = K;
+    t.ldc = N;
+    t.tA = 0;
+    t.tB = 1;
+    t.alpha = -1.f;
+    t.beta = 1.f;
+    const int bn = tc_tile_n(N);
+    t.bn = bn;
+    t.tilesN = (N + bn - 1) / bn;
+    t.split = split ? 1 : 0;
+    t.kSplit = 1;
+    t.kLen = K;
+    const int tiles = ((M + 127) / 128) * t.tilesN;
+    RSCHOL_CUDA(cudaMemcpy(dT.p, &t, sizeof(t), cudaMemcpyHostToDevice));
+    cudaEvent_t e0, e1;
+    RSCHOL_CUDA(cudaEventCreate(&e0));
+    RSCHOL_CUDA(cudaEventCreate(&e1));
+    launch_gemm_tc(dT.as<GemmTask<float>>(), 1, tiles, dE.as<int>(), 0, bn, split == 2);   // warm-up
+    RSCHOL_CUDA(cudaEventRecord(e0, 0));
+    for (int r = 0; r < reps; ++r) launch_gemm_tc(dT.as<GemmTask<float>>(), 1, tiles, dE.as<int>(), 0, bn, split == 2);
+    RSCHOL_CUDA(cudaEventRecord(e1, 0));
+    RSCHOL_CUDA(cudaEventSynchronize(e1));
+    float t_ms = 0;
+    RSCHOL_CUDA(cudaEventElapsedTime(&t_ms, e0, e1));
+    RSCHOL_CUDA(cudaEventDestroy(e0));
+    RSCHOL_CUDA(cudaEventDestroy(e1));
+    int err = 0;
+    RSCHOL_CUDA(cudaMemcpy(&err, dE.p, sizeof(int), cudaMemcpyDeviceToHost));
+    *ms = t_ms / reps;
+    if (err) return RSCHOL_E_TIMEOUT;
+  } catch (const std::exception&) {
+    return RSCHOL_E_CUDA;
+  }
+  return RSCHOL_OK;
+}
+
 // ---- allocation-free preconditioner apply ----------------------------------
 // The permuted work vector lives in a file-scope device array instead of a
 // buffer allocated on first use, so the call itself never allocates.  Its

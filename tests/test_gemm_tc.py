@@ -50,3 +50,10 @@ def test_tensor_core_gemm_lower_tiles(n, split):
     out = (ctypes.c_double * 2)()
     st = rs.load_library().rschol_selftest_gemm(n, n, 64, 0, 1, split, 1, out)
     assert st == 0 and out[0] < TOL[split], (st, out[0])
+
+
+@pytest.mark.parametrize("split", [0, 1, 2])
+def test_bench_gemm_times_a_launch(split):
+    ms = ctypes.c_double()
+    st = rs.load_library().rschol_bench_gemm(1024, 256, 512, split, 3, ctypes.byref(ms))
+    assert st == 0 and 0 < ms.value < 1e3, (st, ms.value)
