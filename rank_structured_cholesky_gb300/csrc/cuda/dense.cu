@@ -1039,9 +1039,10 @@ __global__ void __launch_bounds__(QRP_THREADS, 1) qr_panel_reg_kernel(const QrTa
 // over (row block of QA_RB rows, group of QA_CW columns):
 //   mode 0 (factor): W[j0:n, c] := (I - V T^T V^T) W[j0:n, c], c >= j0 + pw
 //   mode 1 (form Q): Y[j0:n, c] := (I - V T V^T) Y[j0:n, c],   c >= j0
-// in three launches: Zpart = V^T A per row block; Z = the row-block partials
-// added in order, M = T^T Z (or T Z); A -= V M per row block.  ws holds
-// Zpart (tasks x cgMax x rbMax x 16 x 16) and then M (tasks x cgMax x 16 x 16).
+// in two launches: Zpart = V^T A per row block; then per row block Z = the
+// row-block partials added in order, M = T^T Z (or T Z), A -= V M (every block
+// of a column group forms the same small M instead of a launch of its own).
+// ws holds Zpart (tasks x cgMax x rbMax x 16 x 16).
 constexpr int QA_RB = 256;   // rows per block of the apply
 
 template <class T>
@@ -1111,40 +1112,13 @@ __global__ void __launch_bounds__(256) qr_zpart_kernel(const QrTask<T>* __restri
 }
 
 template <class T>
-__global__ void __launch_bounds__(256) qr_zreduce_kernel(const QrTask<T>* __restrict__ tasks, int j0, int mode,
-                                                         T* __restrict__ ws, int cgMax, int rbMax, long long mOff) {
-  __shared__ T Z[QR_PB][QA_CW + 1];
-  __shared__ T Ts[QR_PB][QR_PB + 1];
-  const QrTask<T> t = tasks[blockIdx.y];
-  const int cg = blockIdx.x;
-  QrApplyView<T> w;
-  if (!qr_view(t, j0, mode, cg, w)) return;
-  const int tid = threadIdx.x, zp = tid % QR_PB, zc = tid / QR_PB;
-  {
-    const int a = tid / QR_PB, b = tid - a * QR_PB;   // T over the upper triangle of the diagonal block
-    Ts[a][b] = (a <= b && b < w.pw) ? w.V[(size_t)b * w.n + a] : T(0);
-  }
-  const int nrb = (w.nr + QA_RB - 1) / QA_RB;
-  const T* zpart = ws + ((size_t)blockIdx.y * cgMax + cg) * rbMax * (QR_PB * QA_CW) + zp * QA_CW + zc;
-  T z = T(0);
-  for (int rb = 0; rb < nrb; ++rb) z += zpart[(size_t)rb * (QR_PB * QA_CW)];
-  Z[zp][zc] = z;
-  __syncthreads();
-  T m = T(0);
-  if (mode == 0) {
-    for (int q = 0; q <= zp; ++q) m += Ts[q][zp] * Z[q][zc];   // T^T Z
-  } else {
-    for (int q = zp; q < QR_PB; ++q) m += Ts[zp][q] * Z[q][zc];   // T Z
-  }
-  ws[mOff + ((size_t)blockIdx.y * cgMax + cg) * (QR_PB * QA_CW) + zp * QA_CW + zc] = m;
-}
-
-template <class T>
 __global__ void __launch_bounds__(256) qr_update_kernel(const QrTask<T>* __restrict__ tasks, int j0, int mode,
-                                                        const T* __restrict__ ws, int cgMax, long long mOff) {
+                                                        const T* __restrict__ ws, int cgMax, int rbMax) {
   __shared__ T Vs[QA_ROWS][QR_PB + 1];
   __shared__ T As[QA_ROWS][QA_CW + 1];
   __shared__ T M[QR_PB][QA_CW + 1];
+  __shared__ T Z[QR_PB][QA_CW + 1];
+  __shared__ T Ts[QR_PB][QR_PB + 1];
   const QrTask<T> t = tasks[blockIdx.y];
   const int cg = blockIdx.x % cgMax, rb = blockIdx.x / cgMax;
   QrApplyView<T> w;
@@ -1154,8 +1128,25 @@ __global__ void __launch_bounds__(256) qr_update_kernel(const QrTask<T>* __restr
   const int r1 = min(w.nr, r0 + QA_RB);
   const int tid = threadIdx.x;
   {
+    // M = T^T Z (mode 0) or T Z (mode 1), Z = V^T A summed over the row blocks'
+    // partials in row-block order: every block of the column group forms the
+    // same M (a 16 x 16 reduction, cheaper than a launch of its own)
     const int zp = tid % QR_PB, zc = tid / QR_PB;
-    M[zp][zc] = ws[mOff + ((size_t)blockIdx.y * cgMax + cg) * (QR_PB * QA_CW) + zp * QA_CW + zc];
+    const int a = tid / QR_PB, b = tid - a * QR_PB;   // T over the upper triangle of the diagonal block
+    Ts[a][b] = (a <= b && b < w.pw) ? w.V[(size_t)b * w.n + a] : T(0);
+    const int nrb = (w.nr + QA_RB - 1) / QA_RB;
+    const T* zpart = ws + ((size_t)blockIdx.y * cgMax + cg) * rbMax * (QR_PB * QA_CW) + zp * QA_CW + zc;
+    T z = T(0);
+    for (int q = 0; q < nrb; ++q) z += zpart[(size_t)q * (QR_PB * QA_CW)];
+    Z[zp][zc] = z;
+    __syncthreads();
+    T m = T(0);
+    if (mode == 0) {
+      for (int q = 0; q <= zp; ++q) m += Ts[q][zp] * Z[q][zc];   // T^T Z
+    } else {
+      for (int q = zp; q < QR_PB; ++q) m += Ts[zp][q] * Z[q][zc];   // T Z
+    }
+    M[zp][zc] = m;
   }
   const int ai = tid % QA_ROWS, aq = (tid / QA_ROWS) * 4;
   for (int i0 = r0; i0 < r1; i0 += QA_ROWS) {
@@ -1310,21 +1301,19 @@ void launch_scatter(const double* A, const long long* si, const long long* di, l
 }
 long long householder_qr_workspace(int nTasks, int maxRows, int maxR) {
   const long long cgMax = (maxR + QA_CW - 1) / QA_CW, rbMax = (maxRows + QA_RB - 1) / QA_RB;
-  return (long long)nTasks * cgMax * (rbMax + 1) * (QR_PB * QA_CW);
+  return (long long)nTasks * cgMax * rbMax * (QR_PB * QA_CW);
 }
 
 template <class T>
 int launch_householder_qr(const QrTask<T>* d, int n, int maxRows, int maxR, T* ws, cudaStream_t s) {
   if (n <= 0 || maxR <= 0) return 0;
   const int cgMax = (maxR + QA_CW - 1) / QA_CW, rbMax = (maxRows + QA_RB - 1) / QA_RB;
-  const long long mOff = (long long)n * cgMax * rbMax * (QR_PB * QA_CW);
   int launches = 0;
   auto apply = [&](int j0, int mode) {
     qr_zpart_kernel<T><<<dim3(cgMax * rbMax, n), 256, 0, s>>>(d, j0, mode, ws, cgMax, rbMax);
-    qr_zreduce_kernel<T><<<dim3(cgMax, n), 256, 0, s>>>(d, j0, mode, ws, cgMax, rbMax, mOff);
-    qr_update_kernel<T><<<dim3(cgMax * rbMax, n), 256, 0, s>>>(d, j0, mode, ws, cgMax, mOff);
+    qr_update_kernel<T><<<dim3(cgMax * rbMax, n), 256, 0, s>>>(d, j0, mode, ws, cgMax, rbMax);
     RSCHOL_LAUNCH_CHECK();
-    launches += 3;
+    launches += 2;
   };
   static std::once_flag once;
   std::call_once(once, [] {
