@@ -32,30 +32,34 @@ using namespace tcdev;
 
 
 // ---------------------------------------------------------------------------
-// The kernel.  One 128 x BN output tile (and K slice) per CTA of 256 threads,
+// The kernel.  One 128 x BN output tile (and K slice) per CTA of 384 threads,
 // warp-specialised:
-//   warps 0-3  producers: each K tile of 32 goes global -> registers (16-byte
+//   warps 0-7  producers: each K tile of 32 goes global -> registers (16-byte
 //              vector loads along the operand's contiguous dimension) ->
 //              TF32 hi (and lo for the split products; transposed when the
 //              operand's contiguous dimension is M or N) -> one of NS stages
 //              in the K-major 128-byte-swizzled layout; then one arrival per
 //              thread on the stage's "full" barrier;
-//   warp 4     lane 0 issues the stage's tcgen05.mma (M 128, N BN, K 8; three
+//   warp 8     lane 0 issues the stage's tcgen05.mma (M 128, N BN, K 8; three
 //              per K step for split products) into the TMEM accumulator as soon
 //              as the stage is full, and commits to the stage's "empty"
 //              barrier, which frees it for the producers;
-//   warps 4-7  epilogue: after the final commit, TMEM -> registers
+//   warps 8-11 epilogue: after the final commit, TMEM -> registers
 //              (tcgen05.ld, 32 lanes each) -> shared rows -> C (or the
-//              K-slice partials) in coalesced rows, by all 256 threads.
+//              K-slice partials) in coalesced rows, by all threads.
 // NS stages keep NS K tiles in flight, so loads, conversion and MMAs of
-// different stages overlap.  (Measured against it on the c2 factor's GEMM
-// steps: both operands' loads issued before either is stored, with L2
-// prefetches of the tiles ahead, 4.33 vs 4.15 ms; asynchronous 16-byte
-// copies into three raw stages converted into two MMA stages, 5.15 ms.)  Every wait is bounded; a wait that gives up sets
+// different stages overlap.  The producers' global-load latency bounds a
+// stage, so eight producer warps (half the loads each) beat four.  (Measured
+// against it on the c2 factor's GEMM steps: both operands' loads issued
+// before either is stored, with L2 prefetches of the tiles ahead, 4.33 vs
+// 4.15 ms; asynchronous 16-byte copies into three raw stages converted into
+// two MMA stages, 5.15 ms.)  Every wait is bounded; a wait that gives up sets
 // *err, stops the loops, waits (bounded) for the CTA's issued MMAs and frees
 // the TMEM before returning.
 // ---------------------------------------------------------------------------
-constexpr int WS_THREADS = 256;
+constexpr int WS_PW = 8;                          // producer warps
+constexpr int WS_PT = 32 * WS_PW;                 // producer threads
+constexpr int WS_THREADS = WS_PT + 128;           // + the MMA / epilogue warpgroup
 
 // One ROWS x 32 K tile of an operand into the stage's swizzled K-major
 // buffers (hi at dst, lo at dst + loOff when split).  Element (r, k) of the
@@ -69,13 +73,13 @@ template <int ROWS, bool BF>
 __device__ __forceinline__ void ws_load_tile(const float* __restrict__ src, int ld, bool kContig, bool vec, int row0,
                                              int nRows, int k0, int kEnd, uint32_t dst, uint32_t loOff, bool split,
                                              int tid, int kPos = 0) {
-  constexpr int PER = ROWS * 32 / 4 / 128;   // float4 groups per producer thread
+  constexpr int PER = ROWS * 32 / 4 / WS_PT;   // float4 groups per producer thread
   float4 v[PER];
   if (kContig) {
     // group g: row g >> 3, k 4 (g & 7) .. +3
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
-      const int g = tid + 128 * q, r = g >> 3, kk = (g & 7) * 4;
+      const int g = tid + WS_PT * q, r = g >> 3, kk = (g & 7) * 4;
       const int gr = row0 + r, gk = k0 + kk;
       const float* p = src + (size_t)gr * ld + gk;
       if (gr < nRows && vec && gk + 3 < kEnd) {
@@ -89,7 +93,7 @@ __device__ __forceinline__ void ws_load_tile(const float* __restrict__ src, int 
     }
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
-      const int g = tid + 128 * q, r = g >> 3, kk = (g & 7) * 4;
+      const int g = tid + WS_PT * q, r = g >> 3, kk = (g & 7) * 4;
       if constexpr (BF) {
         const uint32_t off = tc_off16(r, kPos + kk);
         float l[4];
@@ -111,7 +115,7 @@ __device__ __forceinline__ void ws_load_tile(const float* __restrict__ src, int 
     constexpr int GR = ROWS / 4;
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
-      const int g = tid + 128 * q, kk = g / GR, r = (g % GR) * 4;
+      const int g = tid + WS_PT * q, kk = g / GR, r = (g % GR) * 4;
       const int gr = row0 + r, gk = k0 + kk;
       const float* p = src + (size_t)gk * ld + gr;
       if (gk < kEnd && vec && gr + 3 < nRows) {
@@ -125,7 +129,7 @@ __device__ __forceinline__ void ws_load_tile(const float* __restrict__ src, int 
     }
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
-      const int g = tid + 128 * q, kk = g / GR, r = (g % GR) * 4;
+      const int g = tid + WS_PT * q, kk = g / GR, r = (g % GR) * 4;
       const float e[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
@@ -181,12 +185,12 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
   const uint32_t empty0 = (uint32_t)__cvta_generic_to_shared(&emptyB[0]);
   const uint32_t done = (uint32_t)__cvta_generic_to_shared(&doneB);
 
-  if (warp == 4) {
+  if (warp == WS_PW) {
     tmem_alloc((uint32_t)__cvta_generic_to_shared(&tmemBase), BN);
   }
   if (tid == 0) {
     for (int st = 0; st < NS; ++st) {
-      mbar_init(full0 + 8u * st, 128);
+      mbar_init(full0 + 8u * st, WS_PT);
       mbar_init(empty0 + 8u * st, 1);
     }
     mbar_init(done, 1);
@@ -198,7 +202,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmemBase;
 
-  if (warp < 4) {
+  if (warp < WS_PW) {
     // ---- producers
     // 16-byte loads need the operand and its leading dimension aligned
     const bool aK = !t.tA, bK = t.tB != 0;   // K contiguous in memory
@@ -223,7 +227,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(full0 + 8u * st);
     }
-  } else if (warp == 4) {
+  } else if (warp == WS_PW) {
     // ---- MMA issue (one thread); the whole warp then joins the epilogue
     if (lane == 0) {
       int issued = 0;
@@ -254,10 +258,11 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
     }
     __syncwarp();
   }
-  // ---- epilogue: warps 4-7 take the accumulator rows 32 (warp - 4) + lane
+  // ---- epilogue: the last four warps take the accumulator rows 32 (warp - WS_PW) + lane (their TMEM lane
+  // quarters: warp % 4 == warp - WS_PW)
   float* buf = reinterpret_cast<float*>(tc_smem + (sbase - sraw));   // 128 x (BN + 1), stages are free now
   bool ok = true;
-  if (warp >= 4) {
+  if (warp >= WS_PW) {
     ok = mbar_wait(done, 0u);
     if (!ok) {
       atomicExch(err, 1);
@@ -267,9 +272,9 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
   __syncthreads();   // producers done too: the stage buffers may be reused
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const bool abort = sAbort != 0;
-  if (!abort && warp >= 4) {
-    const int row = 32 * (warp - 4) + lane;
-    const uint32_t taddr = tmem + ((uint32_t)(32 * (warp - 4)) << 16);
+  if (!abort && warp >= WS_PW) {
+    const int row = 32 * (warp - WS_PW) + lane;
+    const uint32_t taddr = tmem + ((uint32_t)(32 * (warp - WS_PW)) << 16);
 #pragma unroll
     for (int c0 = 0; c0 < BN; c0 += 32) {
       uint32_t r[32];
@@ -309,7 +314,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 4)
+  if (warp == WS_PW)
     tmem_dealloc(tmem, BN);
 }
 
