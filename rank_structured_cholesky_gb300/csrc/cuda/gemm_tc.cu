@@ -32,24 +32,25 @@ using namespace tcdev;
 
 
 // ---------------------------------------------------------------------------
-// The kernel.  One 128 x BN output tile (and K slice) per CTA of 384 threads,
+// The kernel.  One 128 x BN output tile (and K slice) per CTA of 640 threads,
 // warp-specialised:
-//   warps 0-7  producers: each K tile of 32 goes global -> registers (16-byte
+//   warps 0-15 producers: each K tile of 32 goes global -> registers (16-byte
 //              vector loads along the operand's contiguous dimension) ->
 //              TF32 hi (and lo for the split products; transposed when the
 //              operand's contiguous dimension is M or N) -> one of NS stages
 //              in the K-major 128-byte-swizzled layout; then one arrival per
 //              thread on the stage's "full" barrier;
-//   warp 8     lane 0 issues the stage's tcgen05.mma (M 128, N BN, K 8; three
+//   warp 16    lane 0 issues the stage's tcgen05.mma (M 128, N BN, K 8; three
 //              per K step for split products) into the TMEM accumulator as soon
 //              as the stage is full, and commits to the stage's "empty"
 //              barrier, which frees it for the producers;
-//   warps 8-11 epilogue: after the final commit, TMEM -> registers
+//   warps 16-19 epilogue: after the final commit, TMEM -> registers
 //              (tcgen05.ld, 32 lanes each) -> shared rows -> C (or the
 //              K-slice partials) in coalesced rows, by all threads.
 // NS stages keep NS K tiles in flight, so loads, conversion and MMAs of
 // different stages overlap.  The producers' global-load latency bounds a
-// stage, so eight producer warps (half the loads each) beat four.  (Measured
+// stage: sixteen producer warps beat eight (c2 factor 24.47 vs 24.27 ms), and
+// eight beat four (25.49 vs 24.39 ms).  (Measured
 // against it on the c2 factor's GEMM steps: both operands' loads issued
 // before either is stored, with L2 prefetches of the tiles ahead, 4.33 vs
 // 4.15 ms; asynchronous 16-byte copies into three raw stages converted into
@@ -57,7 +58,7 @@ using namespace tcdev;
 // *err, stops the loops, waits (bounded) for the CTA's issued MMAs and frees
 // the TMEM before returning.
 // ---------------------------------------------------------------------------
-constexpr int WS_PW = 8;                          // producer warps
+constexpr int WS_PW = 16;                         // producer warps
 constexpr int WS_PT = 32 * WS_PW;                 // producer threads
 constexpr int WS_THREADS = WS_PT + 128;           // + the MMA / epilogue warpgroup
 
