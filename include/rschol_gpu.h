@@ -224,13 +224,16 @@ int rschol_step_timing(rschol_factor* f, int enable, double* out);
  * transposed storage, split: 0 plain TF32, 1 split TF32, 2 split BF16 (the
  * schur_bf16 products); lower: lower-triangle tiles only) against a host
  * FP64 product.  out[0]: largest error relative to
- * sum_k |a_ik b_kj| (+ |beta c_ij|), out[1]: largest absolute error. */
+ * sum_k |a_ik b_kj| (+ |beta c_ij|), out[1]: largest absolute error, out[2]:
+ * 1 when the operands were staged by TMA (A M x K and B N x K row-major,
+ * aligned, TF32), 0 when through registers.  out holds 3 values. */
 int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int split, int lower, double* out);
 
 /* Diagnostics (no reference counterpart): *ms = average device time of one
  * tensor-core launch C (M x N) -= A (M x K) B^T (A, B row-major, the
- * factor's update shape; split as in rschol_selftest_gemm; no K slices),
- * over reps launches after one warm-up, on zero operands. */
+ * factor's update shape; split as in rschol_selftest_gemm; no K slices;
+ * TF32 operands staged by TMA when K is a multiple of 4), over reps launches
+ * after one warm-up, on zero operands. */
 int rschol_bench_gemm(int M, int N, int K, int split, int reps, double* ms);
 
 /* Preconditioned CG from x0 = 0 with the factor as M, stopping at

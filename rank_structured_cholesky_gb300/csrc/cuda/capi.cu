@@ -825,6 +825,17 @@ extern "C" int rschol_selftest_gemm(int M, int N, int K, int tA, int tB, int spl
       dW.alloc(sizeof(float) * (size_t)t.kSplit * tilesPer * 128 * bn);
       t.ws = dW.as<float>();
     }
+    DevBuf dMaps;   // K-major aligned operands of a TF32 launch: TMA staging
+    if (!bf16) {
+      std::vector<TensorMapBytes> maps;
+      if (encode_gemm_tmaps(&t, 1, bn, maps)) {
+        dMaps.alloc(maps.size() * sizeof(TensorMapBytes));
+        RSCHOL_CUDA(cudaMemcpy(dMaps.p, maps.data(), maps.size() * sizeof(TensorMapBytes), cudaMemcpyHostToDevice));
+        t.tmA = dMaps.as<TensorMapBytes>() + 0;
+        t.tmB = dMaps.as<TensorMapBytes>() + 1;
+      }
+    }
+    out[2] = t.tmA ? 1.0 : 0.0;
     RSCHOL_CUDA(cudaMemcpy(dT.p, &t, sizeof(t), cudaMemcpyHostToDevice));
     launch_gemm_tc(dT.as<GemmTask<float>>(), 1, tilesPer * t.kSplit, dE.as<int>(), 0, bn, bf16);
     if (t.kSplit > 1) {
@@ -904,6 +915,16 @@ extern "C" int rschol_bench_gemm(int M, int N, int K, int split, int reps, doubl
     t.kSplit = 1;
     t.kLen = K;
     const int tiles = ((M + 127) / 128) * t.tilesN;
+    DevBuf dMaps;
+    if (split != 2) {
+      std::vector<TensorMapBytes> maps;
+      if (encode_gemm_tmaps(&t, 1, bn, maps)) {
+        dMaps.alloc(maps.size() * sizeof(TensorMapBytes));
+        RSCHOL_CUDA(cudaMemcpy(dMaps.p, maps.data(), maps.size() * sizeof(TensorMapBytes), cudaMemcpyHostToDevice));
+        t.tmA = dMaps.as<TensorMapBytes>() + 0;
+        t.tmB = dMaps.as<TensorMapBytes>() + 1;
+      }
+    }
     RSCHOL_CUDA(cudaMemcpy(dT.p, &t, sizeof(t), cudaMemcpyHostToDevice));
     cudaEvent_t e0, e1;
     RSCHOL_CUDA(cudaEventCreate(&e0));

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 namespace rschol {
 
@@ -33,6 +34,15 @@ struct GemmTask {
   int kLen;       // K per slice (a multiple of 32)
   float* ws;      // kSplit x tiles x 128 x bn partials (kSplit > 1)
   int bn;         // tensor-core path: output tile width of the launch (64 or 128; 0: 64)
+  // tensor-core path: device addresses of the TMA tensor maps of A and B
+  // (K-major operands, 16-byte aligned), or null for register staging
+  const void* tmA;
+  const void* tmB;
+};
+
+// One TMA tensor map (the driver's 128-byte CUtensorMap, opaque here).
+struct alignas(64) TensorMapBytes {
+  unsigned char b[128];
 };
 
 // In-place lower Cholesky of one diagonal tile (n <= 64).  On a
@@ -131,6 +141,14 @@ void launch_block_convert(const CvtTask* dTasks, int nTasks, int maxN, int toDou
 // three kind::f16 MMAs; K slices of split tasks a multiple of 64).
 void launch_gemm_tc(const GemmTask<float>* dTasks, int nTasks, int totalTiles, int* dErr, cudaStream_t s,
                     int bn = 64, int bf16 = 0);
+// Host: TMA tensor maps for the tasks of one TF32 tensor-core launch of tile
+// width bn whose operands allow it (A M x K and B N x K row-major, both
+// 16-byte aligned with leading dimensions a multiple of 4 floats).  The maps
+// are appended to `maps`; such a task's tmA / tmB are set to 1 + the map's
+// index, for the caller to rebase to the maps' device addresses.  Returns how
+// many tasks got maps (0 when the driver entry point is missing or
+// RSCHOL_TMA=0).
+int encode_gemm_tmaps(GemmTask<float>* tasks, int count, int bn, std::vector<TensorMapBytes>& maps);
 // The tile width of a tensor-core launch whose widest task has N columns.
 inline int tc_tile_n(int maxN) { return maxN > 64 ? 128 : 64; }
 // C = alpha * sum of the K-slice partials + beta * C for the split tasks

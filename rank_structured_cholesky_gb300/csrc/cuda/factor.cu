@@ -1087,6 +1087,16 @@ void FactorEngine<T>::plan() {
   up(dCvt_, cvt_.data(), cvt_.size() * sizeof(CvtTask));
   up(dCholJobs_, cholJobs_.data(), cholJobs_.size() * sizeof(CholFusedJob<T>));
   up(dCholItems_, cholItems_.data(), cholItems_.size() * sizeof(CholItem));
+  if constexpr (std::is_same<T, float>::value) {   // TMA tensor maps of the TF32 tensor-core launches' operands
+    std::vector<TensorMapBytes> maps;
+    for (const Step& st : steps_)
+      if (st.kind == ST_GEMM && st.aux && !(st.aux >> 16)) encode_gemm_tmaps(&gemm_[st.off], st.count, st.aux & 0xffff, maps);
+    up(dTmaps_, maps.data(), maps.size() * sizeof(TensorMapBytes));
+    for (auto& g : gemm_) {   // 1 + map index -> the map's device address
+      if (g.tmA) g.tmA = dTmaps_.as<TensorMapBytes>() + ((uintptr_t)g.tmA - 1);
+      if (g.tmB) g.tmB = dTmaps_.as<TensorMapBytes>() + ((uintptr_t)g.tmB - 1);
+    }
+  }
   up(dGemm_, gemm_.data(), gemm_.size() * sizeof(GemmTask<T>));
   up(dPotrf_, potrf_.data(), potrf_.size() * sizeof(PotrfTask<T>));
   up(dTrsm_, trsm_.data(), trsm_.size() * sizeof(TrsmTask<T>));

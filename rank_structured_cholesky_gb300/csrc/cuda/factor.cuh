@@ -211,6 +211,7 @@ class FactorEngine {
   DevBuf dCholJobs64_, dCholItems64_, dCholSync64_, dCholWs64_;
   std::vector<long long> scatSrc_, scatDst_;
   std::vector<int> scatIsInterior_;
+  DevBuf dTmaps_;   // TMA tensor maps of the tensor-core GEMM tasks
   DevBuf dGemm_, dPotrf_, dTrsm_, dEaR_, dEaSeg_, dEaS_, dQr_, dIdent_, dInts_, dScatSrc_, dScatDst_;
   DevBuf dScatSrcC_, dScatDstC_;
   long long nScatI_ = 0, nScatC_ = 0;

@@ -16,7 +16,12 @@
 // a_lo = tf32(a - a_hi), and A B ~ A_hi B_hi + A_hi B_lo + A_lo B_hi (three
 // MMAs per K step, FP32 accuracy up to the dropped A_lo B_lo term), for the
 // Schur-complement updates whose errors the factor cannot absorb.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 
 #include "common.cuh"
@@ -150,6 +155,20 @@ __device__ __forceinline__ void ws_load_tile(const float* __restrict__ src, int 
   }
 }
 
+// A stage buffer of raw FP32 (bytes at base) rounded to TF32 in place; split:
+// the remainders tf32(a - hi) to the lo buffer that follows it.  The layout is
+// elementwise, so the swizzle needs no decoding.  All producer threads.
+__device__ __forceinline__ void tf32_in_place(uint32_t base, int bytes, bool split, int tid) {
+  for (int off = tid * 16; off < bytes; off += WS_PT * 16) {
+    const float4 v = ld_shared_v4(base + off);
+    const uint32_t h0 = to_tf32(v.x), h1 = to_tf32(v.y), h2 = to_tf32(v.z), h3 = to_tf32(v.w);
+    st_shared_v4(base + off, h0, h1, h2, h3);
+    if (split)
+      st_shared_v4(base + bytes + off, to_tf32(v.x - __uint_as_float(h0)), to_tf32(v.y - __uint_as_float(h1)),
+                   to_tf32(v.z - __uint_as_float(h2)), to_tf32(v.w - __uint_as_float(h3)));
+  }
+}
+
 template <int BN, int NS, bool BF>
 __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<float>* __restrict__ tasks,
                                                                   int nTasks, int* __restrict__ err) {
@@ -158,7 +177,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
   constexpr int A_BYTES = TC_BM * 128, B_BYTES = BN * 128;
   constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;   // hi and lo of both operands
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  __shared__ __align__(8) uint64_t fullB[NS], emptyB[NS], doneB;
+  __shared__ __align__(8) uint64_t fullB[NS], emptyB[NS], tmaB[NS], doneB;
   __shared__ uint32_t tmemBase;
   __shared__ volatile int sAbort;
   int lo = 0, hi = nTasks - 1;
@@ -185,6 +204,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
   const uint32_t full0 = (uint32_t)__cvta_generic_to_shared(&fullB[0]);
   const uint32_t empty0 = (uint32_t)__cvta_generic_to_shared(&emptyB[0]);
   const uint32_t done = (uint32_t)__cvta_generic_to_shared(&doneB);
+  const uint32_t tma0 = (uint32_t)__cvta_generic_to_shared(&tmaB[0]);
 
   if (warp == WS_PW) {
     tmem_alloc((uint32_t)__cvta_generic_to_shared(&tmemBase), BN);
@@ -193,6 +213,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
     for (int st = 0; st < NS; ++st) {
       mbar_init(full0 + 8u * st, WS_PT);
       mbar_init(empty0 + 8u * st, 1);
+      mbar_init(tma0 + 8u * st, 1);
     }
     mbar_init(done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -203,8 +224,44 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmemBase;
 
-  if (warp < WS_PW) {
-    // ---- producers
+  bool viaTma = false;
+  if constexpr (!BF) viaTma = t.tmA != nullptr && t.tmB != nullptr;
+  if (warp < WS_PW && viaTma) {
+    // ---- producers, TMA staging: thread 0 issues the two boxes of a stage
+    // (raw FP32 in the swizzled layout, zeros beyond the operands' extents);
+    // all producers then round the stage to TF32 in place and, for split
+    // products, write the remainders to the stage's lo buffers
+    const uint64_t mA = reinterpret_cast<uint64_t>(t.tmA), mB = reinterpret_cast<uint64_t>(t.tmB);
+    if (tid == 0) {
+      tmap_acquire(mA);
+      tmap_acquire(mB);
+    }
+    for (int kt = 0; kt < nk; ++kt) {
+      const int st = kt % NS, use = kt / NS;
+      if (use > 0 && !mbar_wait(empty0 + 8u * st, (uint32_t)((use - 1) & 1))) {
+        atomicExch(err, 1);
+        sAbort = 1;
+      }
+      if (sAbort) break;
+      const uint32_t a = sbase + (uint32_t)(st * STAGE), b = a + 2 * A_BYTES;
+      const int k0 = kBeg + kt * TC_BK;   // slices start on a K tile: a box never crosses into the next slice
+      if (tid == 0) {
+        mbar_arrive_expect_tx(tma0 + 8u * st, (uint32_t)(A_BYTES + B_BYTES));
+        tma_load_2d(a, mA, k0, row0, tma0 + 8u * st);
+        tma_load_2d(b, mB, k0, col0, tma0 + 8u * st);
+      }
+      if (!mbar_wait(tma0 + 8u * st, (uint32_t)(use & 1))) {
+        atomicExch(err, 1);
+        sAbort = 1;
+      }
+      if (sAbort) break;
+      tf32_in_place(a, A_BYTES, split, tid);
+      tf32_in_place(b, B_BYTES, split, tid);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(full0 + 8u * st);
+    }
+  } else if (warp < WS_PW) {
+    // ---- producers, register staging
     // 16-byte loads need the operand and its leading dimension aligned
     const bool aK = !t.tA, bK = t.tB != 0;   // K contiguous in memory
     const bool aVec = ((reinterpret_cast<uintptr_t>(t.A) & 15u) == 0) && (t.lda & 3) == 0;
@@ -369,6 +426,65 @@ void launch_gemm_tc(const GemmTask<float>* d, int nTasks, int tiles, int* dErr, 
     if (bn > 64) launch_ws<128, 3, false>(d, nTasks, tiles, dErr, s);
     else launch_ws<64, 4, false>(d, nTasks, tiles, dErr, s);
   }
+}
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    const char* e = std::getenv("RSCHOL_TMA");
+    if (e && e[0] == '0') return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+// The map of a K-major operand: `rows` rows of K floats, row stride ld
+// floats; boxes of 32 K x boxRows rows in the 128-byte swizzle (the layout the
+// MMA's shared-memory descriptors read); zeros beyond K and rows.
+bool encode_operand(PFN_cuTensorMapEncodeTiled_v12000 enc, TensorMapBytes& out, const float* base, int rows, int K,
+                    int ld, int boxRows) {
+  static_assert(sizeof(TensorMapBytes) == sizeof(CUtensorMap), "tensor map size");
+  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
+  const cuuint32_t box[2] = {32u, (cuuint32_t)boxRows};
+  const cuuint32_t estr[2] = {1u, 1u};
+  CUtensorMap m;
+  const CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return false;
+  std::memcpy(out.b, &m, sizeof(m));
+  return true;
+}
+
+}  // namespace
+
+int encode_gemm_tmaps(GemmTask<float>* tasks, int count, int bn, std::vector<TensorMapBytes>& maps) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return 0;
+  int got = 0;
+  for (int q = 0; q < count; ++q) {
+    GemmTask<float>& t = tasks[q];
+    t.tmA = t.tmB = nullptr;
+    const bool aligned = ((reinterpret_cast<uintptr_t>(t.A) | reinterpret_cast<uintptr_t>(t.B)) & 15u) == 0 &&
+                         (t.lda & 3) == 0 && (t.ldb & 3) == 0;
+    if (t.tA || !t.tB || !aligned || t.M <= 0 || t.N <= 0 || t.K <= 0) continue;
+    TensorMapBytes a, b;
+    if (!encode_operand(enc, a, t.A, t.M, t.K, t.lda, TC_BM) || !encode_operand(enc, b, t.B, t.N, t.K, t.ldb, bn))
+      continue;
+    maps.push_back(a);
+    t.tmA = reinterpret_cast<const void*>((uintptr_t)maps.size());
+    maps.push_back(b);
+    t.tmB = reinterpret_cast<const void*>((uintptr_t)maps.size());
+    ++got;
+  }
+  return got;
 }
 
 void launch_gemm_splitk_reduce(const GemmTask<float>* d, const int* ids, int nIds, const long long* elemBase,

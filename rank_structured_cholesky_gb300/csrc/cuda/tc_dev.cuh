@@ -68,6 +68,37 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
                : "memory");
 }
 
+// One arrival that also expects `bytes` of asynchronous (TMA) transactions.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t addr, uint32_t bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(addr),
+               "r"(bytes)
+               : "memory");
+}
+
+// The tensor map at tmap (global memory, 64-byte aligned, written before the
+// launch) made visible to the tensor-map proxy before its first use.
+__device__ __forceinline__ void tmap_acquire(uint64_t tmap) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tmap) : "memory");
+}
+
+// TMA: the box of the 2D tensor map at element coordinates (x, y) -> shared
+// memory at dst, completing `bytes` on the mbarrier at mbar.  x times the
+// element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, uint64_t tmap, int x, int y, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(dst),
+      "l"(tmap), "r"(x), "r"(y), "r"(mbar)
+      : "memory");
+}
+
+__device__ __forceinline__ float4 ld_shared_v4(uint32_t addr) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr)
+               : "memory");
+  return v;
+}
+
 __device__ __forceinline__ void mbar_arrive(uint32_t addr) {
   asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(addr) : "memory");
 }

@@ -37,17 +37,19 @@ TOL = {0: 2e-3, 1: 1e-5, 2: 1e-4}
 @pytest.mark.parametrize("shape", SHAPES)
 def test_tensor_core_gemm(shape, split):
     M, N, K, tA, tB = shape
-    out = (ctypes.c_double * 2)()
+    out = (ctypes.c_double * 3)()
     st = rs.load_library().rschol_selftest_gemm(M, N, K, tA, tB, split, 0, out)
     assert st == 0, st
     assert out[0] < TOL[split], (shape, split, out[0], out[1])
+    # A and B K-major with 16-byte rows (K a multiple of 4) in a TF32 launch: TMA staging
+    assert out[2] == (1.0 if (tA == 0 and tB == 1 and K % 4 == 0 and split != 2) else 0.0), out[2]
 
 
 @pytest.mark.parametrize("split", [1, 2])
 @pytest.mark.parametrize("n", [60, 400])
 def test_tensor_core_gemm_lower_tiles(n, split):
     # n = 400: 128-wide tiles, those strictly above the diagonal skipped
-    out = (ctypes.c_double * 2)()
+    out = (ctypes.c_double * 3)()
     st = rs.load_library().rschol_selftest_gemm(n, n, 64, 0, 1, split, 1, out)
     assert st == 0 and out[0] < TOL[split], (st, out[0])
 
