@@ -157,9 +157,9 @@ __device__ __forceinline__ void ws_load_tile(const float* __restrict__ src, int 
 
 // A stage buffer of raw FP32 (bytes at base) rounded to TF32 in place; split:
 // the remainders tf32(a - hi) to the lo buffer that follows it.  The layout is
-// elementwise, so the swizzle needs no decoding.  All producer threads.
-__device__ __forceinline__ void tf32_in_place(uint32_t base, int bytes, bool split, int tid) {
-  for (int off = tid * 16; off < bytes; off += WS_PT * 16) {
+// elementwise, so the swizzle needs no decoding.  Thread ctid of nThreads.
+__device__ __forceinline__ void tf32_in_place(uint32_t base, int bytes, bool split, int ctid, int nThreads) {
+  for (int off = ctid * 16; off < bytes; off += nThreads * 16) {
     const float4 v = ld_shared_v4(base + off);
     const uint32_t h0 = to_tf32(v.x), h1 = to_tf32(v.y), h2 = to_tf32(v.z), h3 = to_tf32(v.w);
     st_shared_v4(base + off, h0, h1, h2, h3);
@@ -209,9 +209,11 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
   if (warp == WS_PW) {
     tmem_alloc((uint32_t)__cvta_generic_to_shared(&tmemBase), BN);
   }
+  bool viaTma = false;
+  if constexpr (!BF) viaTma = t.tmA != nullptr && t.tmB != nullptr;
   if (tid == 0) {
     for (int st = 0; st < NS; ++st) {
-      mbar_init(full0 + 8u * st, WS_PT);
+      mbar_init(full0 + 8u * st, viaTma ? WS_PT - 32 : WS_PT);   // TMA staging: warp 0 issues, the rest convert
       mbar_init(empty0 + 8u * st, 1);
       mbar_init(tma0 + 8u * st, 1);
     }
@@ -224,39 +226,44 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmemBase;
 
-  bool viaTma = false;
-  if constexpr (!BF) viaTma = t.tmA != nullptr && t.tmB != nullptr;
-  if (warp < WS_PW && viaTma) {
-    // ---- producers, TMA staging: thread 0 issues the two boxes of a stage
-    // (raw FP32 in the swizzled layout, zeros beyond the operands' extents);
-    // all producers then round the stage to TF32 in place and, for split
-    // products, write the remainders to the stage's lo buffers
-    const uint64_t mA = reinterpret_cast<uint64_t>(t.tmA), mB = reinterpret_cast<uint64_t>(t.tmB);
-    if (tid == 0) {
+  if (warp == 0 && viaTma) {
+    // ---- TMA staging, issuer: lane 0 refills each stage as soon as the MMAs
+    // have released it (up to NS stages ahead of the conversion); the boxes
+    // are raw FP32 in the swizzled layout, zeros beyond the operands' extents
+    if (lane == 0) {
+      const uint64_t mA = reinterpret_cast<uint64_t>(t.tmA), mB = reinterpret_cast<uint64_t>(t.tmB);
       tmap_acquire(mA);
       tmap_acquire(mB);
-    }
-    for (int kt = 0; kt < nk; ++kt) {
-      const int st = kt % NS, use = kt / NS;
-      if (use > 0 && !mbar_wait(empty0 + 8u * st, (uint32_t)((use - 1) & 1))) {
-        atomicExch(err, 1);
-        sAbort = 1;
-      }
-      if (sAbort) break;
-      const uint32_t a = sbase + (uint32_t)(st * STAGE), b = a + 2 * A_BYTES;
-      const int k0 = kBeg + kt * TC_BK;   // slices start on a K tile: a box never crosses into the next slice
-      if (tid == 0) {
+      for (int kt = 0; kt < nk; ++kt) {
+        const int st = kt % NS, use = kt / NS;
+        if (use > 0 && !mbar_wait(empty0 + 8u * st, (uint32_t)((use - 1) & 1))) {
+          atomicExch(err, 1);
+          sAbort = 1;
+        }
+        if (sAbort) break;
+        const uint32_t a = sbase + (uint32_t)(st * STAGE), b = a + 2 * A_BYTES;
+        const int k0 = kBeg + kt * TC_BK;   // slices start on a K tile: a box never crosses into the next slice
         mbar_arrive_expect_tx(tma0 + 8u * st, (uint32_t)(A_BYTES + B_BYTES));
         tma_load_2d(a, mA, k0, row0, tma0 + 8u * st);
         tma_load_2d(b, mB, k0, col0, tma0 + 8u * st);
       }
+    }
+    __syncwarp();
+  } else if (warp < WS_PW && viaTma) {
+    // ---- TMA staging, converters (warps 1..): round each landed stage to
+    // TF32 in place and, for split products, write the remainders to its lo
+    // buffers; then one arrival per thread on the stage's "full" barrier
+    const int ctid = tid - 32, nct = WS_PT - 32;
+    for (int kt = 0; kt < nk; ++kt) {
+      const int st = kt % NS, use = kt / NS;
       if (!mbar_wait(tma0 + 8u * st, (uint32_t)(use & 1))) {
         atomicExch(err, 1);
         sAbort = 1;
       }
       if (sAbort) break;
-      tf32_in_place(a, A_BYTES, split, tid);
-      tf32_in_place(b, B_BYTES, split, tid);
+      const uint32_t a = sbase + (uint32_t)(st * STAGE), b = a + 2 * A_BYTES;
+      tf32_in_place(a, A_BYTES, split, ctid, nct);
+      tf32_in_place(b, B_BYTES, split, ctid, nct);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(full0 + 8u * st);
     }
