@@ -39,11 +39,17 @@ using namespace tcdev;
 // ---------------------------------------------------------------------------
 // The kernel.  One 128 x BN output tile (and K slice) per CTA of 640 threads,
 // warp-specialised:
-//   warps 0-15 producers: each K tile of 32 goes global -> registers (16-byte
-//              vector loads along the operand's contiguous dimension) ->
-//              TF32 hi (and lo for the split products; transposed when the
-//              operand's contiguous dimension is M or N) -> one of NS stages
-//              in the K-major 128-byte-swizzled layout; then one arrival per
+//   warps 0-15 producers, in one of two ways per task:
+//              TMA (the task carries tensor maps: K-major, 16-byte-aligned
+//              operands of a TF32 launch): warp 0 issues each K tile's two
+//              boxes (raw FP32, already in the swizzled layout) as soon as the
+//              stage is free; warps 1-15 round the landed tile to TF32 in
+//              place, write the split remainders, and arrive on "full";
+//              registers (the rest): each K tile of 32 goes global ->
+//              registers (16-byte vector loads along the operand's contiguous
+//              dimension) -> TF32 (or BF16) hi and lo, transposed when the
+//              operand's contiguous dimension is M or N -> one of NS stages in
+//              the K-major 128-byte-swizzled layout; then one arrival per
 //              thread on the stage's "full" barrier;
 //   warp 16    lane 0 issues the stage's tcgen05.mma (M 128, N BN, K 8; three
 //              per K step for split products) into the TMEM accumulator as soon
