@@ -148,8 +148,8 @@ int rschol_factor_autotune(rschol_factor* f, int max_columns);
 /* Autotuner of the factor's schedule (no reference counterpart): times
  * `repeats` numeric factorisations of the factor's current values under each
  * candidate -- FP32 GEMM steps on the tensor cores (128 x 64 or 128 x 128
- * tiles) from K >= 32, from K >= 128, from K >= 256, or none (64 x 64 SIMT
- * tiles); the blocked Cholesky
+ * tiles) from K >= 32, 64, 96, 128 or 256, or none (64 x 64 SIMT tiles);
+ * the blocked Cholesky
  * and TRSM chains of a level as one fused launch of 64 x 64 tile items or as
  * one launch per 64-column panel -- keeps the fastest and leaves the factor
  * refactored with it.  The candidates differ only in rounding.  Run it while

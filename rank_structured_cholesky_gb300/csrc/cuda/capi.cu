@@ -1039,7 +1039,7 @@ extern "C" int rschol_factor_tune_schedule(rschol_factor* f, int repeats) {
     RSCHOL_CUDA(cudaEventCreate(&e0));
     RSCHOL_CUDA(cudaEventCreate(&e1));
     std::vector<int> ks = {INT_MAX};
-    if (f->precision == RSCHOL_MIXED) ks = {32, 128, 256, INT_MAX};
+    if (f->precision == RSCHOL_MIXED) ks = {32, 64, 96, 128, 256, INT_MAX};
     int bestK = f->impl->tc_min_k();
     bool bestFused = f->impl->fused_chol();
     double best = 1e300;
