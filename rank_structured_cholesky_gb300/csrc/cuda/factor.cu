@@ -361,6 +361,39 @@ void FactorEngine<T>::emit_chol_t(const std::vector<CholJob<T>>& jobs) {
   }
 }
 
+// Columns per block of emit_l21: the TRSM chain inside a block is 8 panels
+// long, and the trailing GEMMs get K = 512 (the tensor cores' efficiency
+// grows with K; the fused chain's does not).
+constexpr int L21_BLOCK = 512;
+
+template <class T>
+void FactorEngine<T>::emit_l21(const std::vector<TrsmJob<T>>& jobs) {
+  int maxW = 0;
+  for (const auto& jb : jobs) maxW = std::max(maxW, jb.w);
+  if (!useTc_ || maxW <= L21_BLOCK) {
+    emit_trsm(jobs);
+    return;
+  }
+  for (int c0 = 0; c0 < maxW; c0 += L21_BLOCK) {
+    std::vector<TrsmJob<T>> tb;
+    for (const auto& jb : jobs)
+      if (c0 < jb.w && jb.rows > 0)
+        tb.push_back(TrsmJob<T>{jb.L + (size_t)c0 * jb.ldl + c0, jb.B + c0, jb.ldl, jb.ldb, jb.rows,
+                                std::min(L21_BLOCK, jb.w - c0)});
+    emit_trsm(tb);
+    // B[:, c1:] -= B[:, c0:c1] L[c1:, c0:c1]^T
+    std::vector<GemmTask<T>> gb;
+    int tiles = 0;
+    const int c1 = c0 + L21_BLOCK;
+    for (const auto& jb : jobs)
+      if (c1 < jb.w && jb.rows > 0)
+        push_gemm(mk_gemm<T>(jb.B + c0, jb.ldb, false, jb.L + (size_t)c1 * jb.ldl + c0, jb.ldl, true, jb.B + c1,
+                             jb.ldb, jb.rows, jb.w - c1, L21_BLOCK, T(-1), T(1)),
+                  tiles, gb);
+    flush_gemm(gb, tiles);
+  }
+}
+
 template <class T>
 void FactorEngine<T>::emit_trsm(const std::vector<TrsmJob<T>>& jobs) {
   if (fusedChol_) {   // one ticketed launch (TRSM jobs of the fused Cholesky kernel)
@@ -926,7 +959,7 @@ void FactorEngine<T>::plan() {
     }
     emit_chol(cj);
     emit_rf(hj);
-    emit_trsm(tj);
+    emit_l21(tj);
     for (int j : rec) {   // HODLR diagonals with recursive blocks, in block-list order
       const Node& nd = S.nodes[j];
       T* F = C0 + frontOff[j];
@@ -998,7 +1031,7 @@ void FactorEngine<T>::plan() {
         }
         emit_chol({CholJob<T>{Lb, L, sz, sz, sz, j + 1}});
       }
-      if (nd.m() > 0) emit_trsm({TrsmJob<T>{F, F + (size_t)nd.n * L, L, L, nd.m(), nd.n}});
+      if (nd.m() > 0) emit_l21({TrsmJob<T>{F, F + (size_t)nd.n * L, L, L, nd.m(), nd.n}});
     }
 
     // (d) off-diagonal range finder on L21 = F[n:n+m, 0:n]

@@ -141,6 +141,11 @@ class FactorEngine {
   void emit_fused(const std::vector<CholJob<U>>& jobs, int kind, std::vector<CholFusedJob<U>>& cjobs,
                   std::vector<CholItem>& items, long long& syncMax, long long& wsMax);
   void emit_trsm(const std::vector<TrsmJob<T>>& jobs);
+  // L21 = S21 L11^{-T} of large compressed supernodes: column blocks of
+  // L21_BLOCK, each a fused TRSM chain against its diagonal block followed by
+  // one tensor-core GEMM step for the columns right of it (FP32 with tensor
+  // cores; otherwise emit_trsm)
+  void emit_l21(const std::vector<TrsmJob<T>>& jobs);
   void emit_rf(const std::vector<RFJob<T>>& jobs);
   struct EaSrc {            // plan-time source of an extend-add
     ExtAddSource<T> s;      // rowRel filled from relOff
