@@ -329,6 +329,22 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
     }
     __syncwarp();
   }
+  // C of this tile into registers while the MMAs finish (all warps; rows warp + NW r, columns lane + 32 c):
+  // the write-out then needs no dependent global load per row
+  constexpr int NW = WS_THREADS / 32, RPW = (TC_BM + NW - 1) / NW, CPL = BN / 32;
+  float cpre[RPW][CPL];
+  const bool prefetchC = t.kSplit <= 1 && t.beta != 0.f;
+  if (prefetchC) {
+#pragma unroll
+    for (int q = 0; q < RPW; ++q) {
+      const int i = warp + NW * q, gm = row0 + i;
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        const int gn = col0 + lane + 32 * c;
+        cpre[q][c] = (i < TC_BM && gm < t.M && gn < t.N) ? __ldg(t.C + (size_t)gm * t.ldc + gn) : 0.f;
+      }
+    }
+  }
   // ---- epilogue: the last four warps take the accumulator rows 32 (warp - WS_PW) + lane (their TMEM lane
   // quarters: warp % 4 == warp - WS_PW)
   float* buf = reinterpret_cast<float*>(tc_smem + (sbase - sraw));   // 128 x (BN + 1), stages are free now
@@ -368,15 +384,17 @@ __global__ void __launch_bounds__(WS_THREADS, 1) gemm_tc_kernel(const GemmTask<f
       for (int i = warp; i < TC_BM; i += WS_THREADS / 32)
         for (int c = lane; c < BN; c += 32) part[i * BN + c] = buf[i * (BN + 1) + c];
     } else {
-      for (int i = warp; i < TC_BM; i += WS_THREADS / 32) {
-        const int gm = row0 + i;
-        if (gm >= t.M) break;
+#pragma unroll
+      for (int q = 0; q < RPW; ++q) {
+        const int i = warp + NW * q, gm = row0 + i;
+        if (i >= TC_BM || gm >= t.M) continue;
         float* crow = t.C + (size_t)gm * t.ldc;
-        for (int c = lane; c < BN; c += 32) {
-          const int gn = col0 + c;
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+          const int cc = lane + 32 * c, gn = col0 + cc;
           if (gn < t.N) {
-            float v = t.alpha * buf[i * (BN + 1) + c];
-            if (t.beta != 0.f) v = fmaf(t.beta, crow[gn], v);
+            float v = t.alpha * buf[i * (BN + 1) + cc];
+            if (prefetchC) v = fmaf(t.beta, cpre[q][c], v);
             crow[gn] = v;
           }
         }
