@@ -189,7 +189,14 @@ PcgEngine::PcgEngine(int n_, const std::vector<int>& rowptr, const std::vector<i
   RSCHOL_CUDA(cudaMemcpyAsync(colind_.p, colind.data(), sizeof(int) * colind.size(), cudaMemcpyHostToDevice, s));
   RSCHOL_CUDA(cudaMemcpyAsync(vals_.p, vals.data(), sizeof(double) * vals.size(), cudaMemcpyHostToDevice, s));
   const double avg = n > 0 ? (double)colind.size() / n : 1.0;
-  tpr_ = avg <= 6 ? 4 : avg <= 12 ? 8 : avg <= 40 ? 16 : 32;
+  // threads per row: one (each thread's loads all in flight at once) up to 12
+  // entries per row -- the c2 PCG took 20.84 ms at one, 20.99 at two, 21.14
+  // at four, 21.64 at eight -- then more for longer rows
+  tpr_ = avg <= 12 ? 1 : avg <= 40 ? 16 : 32;
+  if (const char* e = std::getenv("RSCHOL_SPMV_TPR")) {   // threads per row of the SpMV (1 ... 32)
+    const int t = std::atoi(e);
+    if (t == 1 || t == 2 || t == 4 || t == 8 || t == 16 || t == 32) tpr_ = t;
+  }
   nblk_ = (int)(((long long)n * tpr_ + VEC_THREADS - 1) / VEC_THREADS);
   for (auto* b : {&r_, &d_, &q_, &s_}) b->alloc(sizeof(double) * std::max(1, n));
   part_.alloc(sizeof(double) * std::max(nblk_, VEC_BLOCKS));
@@ -223,6 +230,8 @@ void PcgEngine::set_values(const std::vector<double>& vals) {
 
 void PcgEngine::spmv(const double* x, double* y) {
   switch (tpr_) {
+    case 1: launch_k(spmv_kernel<1>, dim3(nblk_), dim3(VEC_THREADS), 0, stream_, n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
+    case 2: launch_k(spmv_kernel<2>, dim3(nblk_), dim3(VEC_THREADS), 0, stream_, n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
     case 4: launch_k(spmv_kernel<4>, dim3(nblk_), dim3(VEC_THREADS), 0, stream_, n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
     case 8: launch_k(spmv_kernel<8>, dim3(nblk_), dim3(VEC_THREADS), 0, stream_, n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
     case 16: launch_k(spmv_kernel<16>, dim3(nblk_), dim3(VEC_THREADS), 0, stream_, n, rowptr_.as<int>(), colind_.as<int>(), vals_.as<double>(), x, y, part_.as<double>(), 1); break;
