@@ -53,7 +53,7 @@ CASES = {
 #  c2s  -- 3D variable-coefficient diffusion 32^3 (sigma 1, seed 1), the
 #          reference's default parameters;
 #  c2   -- the same at 64^3 (N = 262,144), the benchmark workload itself.
-BASELINE_CASES = {
+WORKLOAD_CASES = {
     "c1": dict(problem=("diffusion", 2, 128, 0.0, 0),
                params=dict(nd_leaf=64, max_dense_block=16, max_diag_block=32, rank_cap=32, oversampling=10)),
     "c3r": dict(problem=("elasticity", 20, 0.0, 0.0, 2), params=dict(nd_leaf=64, rank_cap=64)),
@@ -163,7 +163,7 @@ def ref_fixtures():
         json.dump({"source": "reference SeparatorTree.h/.cpp via oracle/_ref/ref_septree_kat", "cases": trees}, f,
                   indent=1)
     runs = {}
-    for name, case in list(CASES.items()) + list(BASELINE_CASES.items()):
+    for name, case in list(CASES.items()) + list(WORKLOAD_CASES.items()):
         prob = make_problem(case["problem"])
         F = po.OracleFactor(prob.colptr, prob.rowind, prob.vals, prob.xyz, case["params"])
         assert F.factor() == 0

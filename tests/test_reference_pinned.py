@@ -60,7 +60,7 @@ SMALL = ["2d48", "3d16", "3d20h", "el5", "c1", "c3r", "c2s"]
 
 
 def case_spec(name):
-    spec = mg.CASES.get(name) or mg.BASELINE_CASES[name]
+    spec = mg.CASES.get(name) or mg.WORKLOAD_CASES[name]
     return mg.make_problem(spec["problem"]), spec["params"]
 
 

@@ -58,7 +58,7 @@ def cases():
 
     def get(name):
         if name not in cache:
-            spec = mg.BASELINE_CASES[name]
+            spec = mg.WORKLOAD_CASES[name]
             prob = mg.make_problem(spec["problem"])
             O = po.OracleFactor(prob.colptr, prob.rowind, prob.vals, prob.xyz, spec["params"])
             assert O.factor() == 0
