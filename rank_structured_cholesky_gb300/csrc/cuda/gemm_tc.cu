@@ -60,8 +60,8 @@ using namespace tcdev;
 //              K-slice partials) in coalesced rows, by all threads.
 // NS stages keep NS K tiles in flight, so loads, conversion and MMAs of
 // different stages overlap.  The producers' global-load latency bounds a
-// stage: sixteen producer warps beat eight (c2 factor 24.47 vs 24.27 ms), and
-// eight beat four (25.49 vs 24.39 ms).  (Measured
+// stage: the c2 factor took 25.49 ms with four producer warps, 24.39 with
+// eight, 24.27 with sixteen.  (Measured
 // against it on the c2 factor's GEMM steps: both operands' loads issued
 // before either is stored, with L2 prefetches of the tiles ahead, 4.33 vs
 // 4.15 ms; asynchronous 16-byte copies into three raw stages converted into
