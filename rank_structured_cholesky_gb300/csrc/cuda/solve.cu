@@ -1,4 +1,5 @@
 #include <algorithm>
+#include <mutex>
 #include <cstdlib>
 #include <type_traits>
 
@@ -638,27 +639,35 @@ __global__ void __launch_bounds__(256) compressed_g_kernel(const SNode<T>* __res
 
 // Inverse of each lower-triangular diagonal block (column c by thread c,
 // forward substitution), written as pad x pad (row-major, row stride ldD)
-// with zeros outside the h x h lower triangle.
+// with zeros outside the h x h lower triangle.  The columns are formed in
+// shared memory (Xs[i][c], conflict-free across threads) and stored once, in
+// rows: the substitution's reads of earlier entries never go to global memory
+// (writing and re-reading D instead: c2 factorisation 21.64 vs 21.52 ms).
+// Dynamic shared memory: two SOLVE_RB x (SOLVE_RB + 1) tiles of T.
 template <class T>
 __global__ void __launch_bounds__(64) invert_diag_blocks(const DinvTask<T>* __restrict__ tasks) {
-  __shared__ T Ls[SOLVE_RB][SOLVE_RB + 1];
+  extern __shared__ __align__(16) unsigned char idb_smem[];
+  T (*Ls)[SOLVE_RB + 1] = reinterpret_cast<T (*)[SOLVE_RB + 1]>(idb_smem);
+  T (*Xs)[SOLVE_RB + 1] = reinterpret_cast<T (*)[SOLVE_RB + 1]>(idb_smem + sizeof(T) * SOLVE_RB * (SOLVE_RB + 1));
   const DinvTask<T> t = tasks[blockIdx.x];
   const int h = t.h, pad = t.pad, ldD = t.ldD, c = threadIdx.x;
   for (int idx = threadIdx.x; idx < h * h; idx += blockDim.x) {
     const int i = idx / h, j = idx - i * h;
     Ls[i][j] = (j <= i) ? t.L[(size_t)i * t.ld + j] : T(0);
   }
-  T* D = t.D;
-  if (c < pad)
-    for (int i = 0; i < pad; ++i) D[(size_t)i * ldD + c] = T(0);
+  for (int i = 0; i < SOLVE_RB; ++i) Xs[i][c] = T(0);
   __syncthreads();
   if (c < h) {
     for (int i = c; i < h; ++i) {
       T s = (i == c) ? T(1) : T(0);
-      for (int k = c; k < i; ++k) s -= Ls[i][k] * D[(size_t)k * ldD + c];
-      D[(size_t)i * ldD + c] = s / Ls[i][i];
+      for (int k = c; k < i; ++k) s -= Ls[i][k] * Xs[k][c];
+      Xs[i][c] = s / Ls[i][i];
     }
   }
+  __syncthreads();
+  T* D = t.D;
+  if (c < pad)
+    for (int i = 0; i < pad; ++i) D[(size_t)i * ldD + c] = (i < h && c < h) ? Xs[i][c] : T(0);
 }
 
 template <class A, class B>
@@ -1091,7 +1100,12 @@ template <class T>
 int SolveEngine<T>::prepare(cudaStream_t st) {
   int launches = 0;
   if (nDinv_ > 0) {
-    invert_diag_blocks<T><<<nDinv_, SOLVE_RB, 0, st>>>(dDinvTasks_.as<DinvTask<T>>());
+    constexpr int smem = 2 * (int)sizeof(T) * SOLVE_RB * (SOLVE_RB + 1);
+    static std::once_flag once;
+    std::call_once(once, [] {
+      RSCHOL_CUDA(cudaFuncSetAttribute(invert_diag_blocks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    });
+    invert_diag_blocks<T><<<nDinv_, SOLVE_RB, smem, st>>>(dDinvTasks_.as<DinvTask<T>>());
     RSCHOL_LAUNCH_CHECK();
     ++launches;
   }
