@@ -36,3 +36,16 @@ def test_reference_arm_does_not_load_the_gpu_library():
     out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert out.returncode == 0, out.stderr[-2000:]
     assert "GPU_LIB_ABSENT" in out.stdout
+
+
+def test_roofline_traffic_sources_parse():
+    """The bench line's roofline traffic comes from the committed ncu
+    summaries: the fused Cholesky's DRAM bytes and algorithmic bytes per c2s
+    launch (their ratio scales the traffic to c2), the GEMM launches' bytes."""
+    sys.path.insert(0, ROOT)
+    import bench
+    t, a = bench.traffic_from_profiles("chol_fused_kernel", "c2s")
+    assert t and a and 0.1 < t / a < 2.0, (t, a)
+    tg, _ = bench.traffic_from_profiles("gemm_tc_kernel", "c2s")
+    assert tg and tg > 0
+    assert bench.traffic_from_profiles("no_such_kernel", "c2s") == (None, None)
