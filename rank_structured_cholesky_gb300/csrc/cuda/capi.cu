@@ -16,6 +16,7 @@
 
 #include "../../../include/rschol_gpu.h"
 #include "../host/ordering.h"
+#include "../host/parallel.h"
 #include "../host/symbolic.h"
 #include "factor.cuh"
 #include "pcg.cuh"
@@ -364,18 +365,20 @@ int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* r
     f->permCsrSrc.resize(nnz);
     for (int j = 0; j < n; ++j) rp[f->ord.iperm[j] + 1] = colptr[j + 1] - colptr[j];
     for (int i = 0; i < n; ++i) rp[i + 1] += rp[i];
-    std::vector<std::pair<int, int>> tmp;
-    for (int i = 0; i < n; ++i) {
-      const int j = f->ord.perm[i];
-      tmp.clear();
-      for (int p = colptr[j]; p < colptr[j + 1]; ++p) tmp.push_back({f->ord.iperm[rowind[p]], p});
-      std::sort(tmp.begin(), tmp.end());
-      for (size_t k = 0; k < tmp.size(); ++k) {
-        ci[rp[i] + k] = tmp[k].first;
-        f->permCsrSrc[rp[i] + k] = tmp[k].second;
-        cv[rp[i] + k] = vals[tmp[k].second];
+    parallel_chunks(n, 16384, [&](long long b, long long e) {
+      std::vector<std::pair<int, int>> tmp;
+      for (long long i = b; i < e; ++i) {
+        const int j = f->ord.perm[i];
+        tmp.clear();
+        for (int p = colptr[j]; p < colptr[j + 1]; ++p) tmp.push_back({f->ord.iperm[rowind[p]], p});
+        std::sort(tmp.begin(), tmp.end());
+        for (size_t k = 0; k < tmp.size(); ++k) {
+          ci[rp[i] + k] = tmp[k].first;
+          f->permCsrSrc[rp[i] + k] = tmp[k].second;
+          cv[rp[i] + k] = vals[tmp[k].second];
+        }
       }
-    }
+    });
     f->tSymbolic = now_s() - t0;
     if (f->precision == RSCHOL_MIXED) f->impl.reset(new ImplT<float>(f->S, f->A, f->prm, ctx->stream));
     else f->impl.reset(new ImplT<double>(f->S, f->A, f->prm, ctx->stream));

@@ -11,6 +11,8 @@
 #include <string>
 #include <cstdlib>
 
+#include "parallel.h"
+
 namespace rschol {
 
 // ---------------------------------------------------------------------------
@@ -608,9 +610,12 @@ void nested_dissection(const CSC& A, const double* xyz, int ndLeaf, std::vector<
   S.level.assign(A.n, 0);
   std::vector<int> all(A.n);
   std::iota(all.begin(), all.end(), 0);
-  // Disconnected pieces are handled by the bisection itself.  The top four
-  // levels run their two halves concurrently (up to 16 threads).
-  if (A.n > 0) dissect_parallel(S, std::move(all), 4);
+  // Disconnected pieces are handled by the bisection itself.  The top levels
+  // run their two halves concurrently: log2 of the host threads, at most four
+  // levels (16 threads).
+  int depth = 0;
+  while (depth < 4 && (2 << depth) <= host_threads()) ++depth;
+  if (A.n > 0) dissect_parallel(S, std::move(all), depth);
   perm.clear();
   perm.reserve(A.n);
   comps.assign(S.compMembers.size(), Component());
@@ -917,7 +922,9 @@ OrderingResult build_ordering(const CSC& A, const double* xyz, const Params& prm
         int a = R.iperm[A.i[p]], b = R.iperm[j];
         if (a < b) C.i[fill[b]++] = a;
       }
-    for (int j = 0; j < n; ++j) std::sort(C.i.begin() + C.p[j], C.i.begin() + C.p[j + 1]);
+    parallel_chunks(n, 16384, [&](long long b, long long e) {
+      for (long long j = b; j < e; ++j) std::sort(C.i.begin() + C.p[j], C.i.begin() + C.p[j + 1]);
+    });
   }
   R.etree = etree_upper(C);
   std::vector<int> post(n);
@@ -973,14 +980,16 @@ CSC permute_lower(const CSC& A, const std::vector<int>& perm, const std::vector<
         fill[c]++;
       }
     }
-  std::vector<std::pair<int, double>> tmp;
-  for (int j = 0; j < n; ++j) {
-    tmp.clear();
-    for (int p = L.p[j]; p < L.p[j + 1]; ++p) tmp.push_back({L.i[p], L.x[p]});
-    std::sort(tmp.begin(), tmp.end(),
-              [](const std::pair<int, double>& a, const std::pair<int, double>& b) { return a.first < b.first; });
-    for (int p = L.p[j], k = 0; p < L.p[j + 1]; ++p, ++k) { L.i[p] = tmp[k].first; L.x[p] = tmp[k].second; }
-  }
+  parallel_chunks(n, 16384, [&](long long b, long long e) {
+    std::vector<std::pair<int, double>> tmp;
+    for (long long j = b; j < e; ++j) {
+      tmp.clear();
+      for (int p = L.p[j]; p < L.p[j + 1]; ++p) tmp.push_back({L.i[p], L.x[p]});
+      std::sort(tmp.begin(), tmp.end(),
+                [](const std::pair<int, double>& a, const std::pair<int, double>& b) { return a.first < b.first; });
+      for (int p = L.p[j], k = 0; p < L.p[j + 1]; ++p, ++k) { L.i[p] = tmp[k].first; L.x[p] = tmp[k].second; }
+    }
+  });
   (void)perm;
   return L;
 }

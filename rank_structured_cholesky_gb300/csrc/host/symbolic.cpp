@@ -1,11 +1,14 @@
 #include "symbolic.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <functional>
 #include <sstream>
 #include <stdexcept>
+
+#include "parallel.h"
 
 namespace rschol {
 
@@ -22,6 +25,131 @@ int block_rank(int nRows, int nCols, double c, int oversampling, int cap) {
 }
 
 namespace {
+
+// The row structure of supernode s: the rows of its columns below its
+// diagonal block and the rows of its children there, ascending; then its
+// interactions (runs of rows owned by one ancestor) and its parent, the owner
+// of its first row.  mark[] holds the calling thread's stamps.
+void fill_node(Symbolic& S, const CSC& A, int s, const std::vector<int>& kids, std::vector<int>& mark) {
+  Node& nd = S.nodes[s];
+  std::vector<int> rows;
+  for (int c = nd.c0; c <= nd.c1; ++c)
+    for (int p = A.p[c]; p < A.p[c + 1]; ++p) {
+      int r = A.i[p];
+      if (r > nd.c1 && mark[r] != s) { mark[r] = s; rows.push_back(r); }
+    }
+  for (int ch : kids)
+    for (int r : S.nodes[ch].rows)
+      if (r > nd.c1 && mark[r] != s) { mark[r] = s; rows.push_back(r); }
+  std::sort(rows.begin(), rows.end());
+  nd.rows.swap(rows);
+  nd.interNode.clear();
+  nd.interStart.clear();
+  for (int k = 0; k < (int)nd.rows.size(); ++k) {
+    int owner = S.colNode[nd.rows[k]];
+    if (nd.interNode.empty() || nd.interNode.back() != owner) {
+      nd.interNode.push_back(owner);
+      nd.interStart.push_back(k);
+    }
+  }
+  nd.interStart.push_back((int)nd.rows.size());
+  nd.parent = nd.interNode.empty() ? -1 : nd.interNode[0];
+}
+
+// Supernodes in ascending order: the children of s are complete before s.
+void fill_rows_serial(Symbolic& S, const CSC& A) {
+  const int nn = (int)S.nodes.size();
+  S.children.assign(nn, {});
+  std::vector<int> mark(A.n, -1);
+  for (int s = 0; s < nn; ++s) {
+    fill_node(S, A, s, S.children[s], mark);
+    if (S.nodes[s].parent >= 0) S.children[S.nodes[s].parent].push_back(s);
+  }
+}
+
+// The same sets with disjoint subtrees filled concurrently.  The supernodal
+// tree is predicted before any row is known: the first row below supernode s
+// is the smallest elimination-tree parent of its columns that lies beyond its
+// last column (a column's rows below its etree parent are rows of that
+// parent), so the parent of s is that row's owner.  Subtrees of the predicted
+// tree no larger than 1/(4T) of the columns are filled by T workers, the
+// supernodes above them afterwards in ascending order.  Every supernode's
+// parent is then checked against the owner of its computed first row: if
+// all agree, each supernode received exactly the children the serial
+// recursion gives it (by induction in ascending order), so the sets are
+// identical to the serial ones; otherwise returns false and the caller fills
+// them serially.  Columns permuted within a supernode after the etree was
+// computed do not change which supernode owns a column.
+bool fill_rows_parallel(Symbolic& S, const CSC& A, const std::vector<int>& etree) {
+  const int nn = (int)S.nodes.size();
+  const int T = host_threads();
+  if (T <= 1 || nn < 64 || A.n < 4096 || (int)etree.size() != A.n) return false;
+  std::vector<int> pred(nn, -1);
+  for (int s = 0; s < nn; ++s) {
+    const Node& nd = S.nodes[s];
+    int first = A.n;
+    for (int c = nd.c0; c <= nd.c1; ++c)
+      if (etree[c] > nd.c1 && etree[c] < first) first = etree[c];
+    if (first < A.n) pred[s] = S.colNode[first];
+    if (pred[s] >= 0 && pred[s] <= s) return false;
+  }
+  std::vector<std::vector<int>> kids(nn);
+  std::vector<long long> size(nn, 0);
+  for (int s = 0; s < nn; ++s) {
+    size[s] += S.nodes[s].n;
+    if (pred[s] >= 0) {
+      kids[pred[s]].push_back(s);
+      size[pred[s]] += size[s];
+    }
+  }
+  long long total = 0;
+  std::vector<int> stack;
+  for (int s = 0; s < nn; ++s)
+    if (pred[s] < 0) {
+      total += size[s];
+      stack.push_back(s);
+    }
+  const long long target = std::max(1LL, total / (4LL * T));
+  std::vector<char> top(nn, 0), isRoot(nn, 0);
+  std::vector<int> roots;
+  while (!stack.empty()) {
+    const int s = stack.back();
+    stack.pop_back();
+    if (size[s] > target && !kids[s].empty()) {
+      top[s] = 1;
+      for (int ch : kids[s]) stack.push_back(ch);
+    } else {
+      isRoot[s] = 1;
+      roots.push_back(s);
+    }
+  }
+  // members of each chosen subtree, ascending
+  std::vector<int> owner(nn, -1), slot(nn, -1);
+  for (int k = 0; k < (int)roots.size(); ++k) slot[roots[k]] = k;
+  std::vector<std::vector<int>> members(roots.size());
+  for (int s = nn - 1; s >= 0; --s)
+    if (isRoot[s]) owner[s] = s;
+    else if (!top[s]) owner[s] = owner[pred[s]];
+  for (int s = 0; s < nn; ++s)
+    if (owner[s] >= 0) members[slot[owner[s]]].push_back(s);
+  std::vector<int> queue(roots.size());
+  for (size_t k = 0; k < roots.size(); ++k) queue[k] = (int)k;
+  std::stable_sort(queue.begin(), queue.end(),
+                   [&](int a, int b) { return size[roots[a]] > size[roots[b]]; });
+  std::atomic<size_t> next(0);
+  run_workers(T, [&](int) {
+    std::vector<int> mark(A.n, -1);
+    for (size_t q; (q = next.fetch_add(1)) < queue.size();)
+      for (int s : members[queue[q]]) fill_node(S, A, s, kids[s], mark);
+  });
+  std::vector<int> mark(A.n, -1);
+  for (int s = 0; s < nn; ++s)
+    if (top[s]) fill_node(S, A, s, kids[s], mark);
+  for (int s = 0; s < nn; ++s)
+    if (S.nodes[s].parent != pred[s]) return false;
+  S.children.swap(kids);
+  return true;
+}
 
 // DiagonalBlock::init + buildTraversal + buildBlockList for one supernode.
 void build_hodlr(Node& nd, const std::vector<std::pair<int, int>>& leaves, int explicitThreshold) {
@@ -97,34 +225,7 @@ Symbolic build_symbolic(const CSC& A, const OrderingResult& ord, const Params& p
   // rows propagated from every supernode below it (findSystemRows +
   // propagateFillIn; propagating to the first ancestor only yields the same
   // sets).  IN_PLACE keeps fill from compressed supernodes.
-  S.children.assign(nn, {});
-  std::vector<int> mark(A.n, -1);
-  for (int s = 0; s < nn; ++s) {
-    Node& nd = S.nodes[s];
-    std::vector<int> rows;
-    for (int c = nd.c0; c <= nd.c1; ++c)
-      for (int p = A.p[c]; p < A.p[c + 1]; ++p) {
-        int r = A.i[p];
-        if (r > nd.c1 && mark[r] != s) { mark[r] = s; rows.push_back(r); }
-      }
-    for (int ch : S.children[s])
-      for (int r : S.nodes[ch].rows)
-        if (r > nd.c1 && mark[r] != s) { mark[r] = s; rows.push_back(r); }
-    std::sort(rows.begin(), rows.end());
-    nd.rows.swap(rows);
-    nd.interNode.clear();
-    nd.interStart.clear();
-    for (int k = 0; k < (int)nd.rows.size(); ++k) {
-      int owner = S.colNode[nd.rows[k]];
-      if (nd.interNode.empty() || nd.interNode.back() != owner) {
-        nd.interNode.push_back(owner);
-        nd.interStart.push_back(k);
-      }
-    }
-    nd.interStart.push_back((int)nd.rows.size());
-    nd.parent = nd.interNode.empty() ? -1 : nd.interNode[0];
-    if (nd.parent >= 0) S.children[nd.parent].push_back(s);
-  }
+  if (!fill_rows_parallel(S, A, ord.etree)) fill_rows_serial(S, A);
   // Diagonal blocks.
   for (int s = 0; s < nn; ++s) build_hodlr(S.nodes[s], ord.diagBlocks[s], prm.explicit_threshold);
   // Interior blocks: maximal runs of uncompressed supernodes.
