@@ -211,6 +211,7 @@ struct rschol_factor {
   int kCap = 0;
   int nrhsCap = 0;
   double tSymbolic = 0, tNumeric = 0;
+  double tPlan = 0;     // device plan: schedule, arenas, Gaussian stream, PCG engine
   int attempts = 0;
   double diagRankConstant = 0.5;
   double tunedMs = 0;   // rschol_factor_tune_schedule: the chosen schedule's factorisation time
@@ -380,10 +381,18 @@ int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* r
       }
     });
     f->tSymbolic = now_s() - t0;
-    if (f->precision == RSCHOL_MIXED) f->impl.reset(new ImplT<float>(f->S, f->A, f->prm, ctx->stream));
-    else f->impl.reset(new ImplT<double>(f->S, f->A, f->prm, ctx->stream));
-    f->impl->plan();
-    f->pcg.reset(new PcgEngine(n, rp, ci, cv, ctx->stream));
+    const double t1 = now_s();
+    {
+      PlanClock clk("create");
+      if (f->precision == RSCHOL_MIXED) f->impl.reset(new ImplT<float>(f->S, f->A, f->prm, ctx->stream));
+      else f->impl.reset(new ImplT<double>(f->S, f->A, f->prm, ctx->stream));
+      clk.mark("engines");
+      f->impl->plan();
+      clk.mark("plan");
+      f->pcg.reset(new PcgEngine(n, rp, ci, cv, ctx->stream));
+      clk.mark("pcg");
+    }
+    f->tPlan = now_s() - t1;
     f->dPerm.alloc(sizeof(int) * n);
     RSCHOL_CUDA(cudaMemcpy(f->dPerm.p, f->ord.perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     f->dLowerSrc.alloc(sizeof(int) * std::max<size_t>(1, f->lowerSrc.size()));
@@ -716,7 +725,7 @@ const char* rschol_factor_describe(rschol_factor* f) {
     << ", \"factor_launches\": " << f->impl->launches() << ", \"apply_launches\": " << f->impl->apply_launches()
     << ", \"factor_flops\": " << f->impl->flops() << ", \"apply_bytes\": " << f->impl->apply_bytes()
     << ", \"spmv_bytes\": " << f->pcg->spmvBytes << ", \"device_bytes\": " << f->impl->bytes()
-    << ", \"symbolic_s\": " << f->tSymbolic << ", \"numeric_s\": " << f->tNumeric
+    << ", \"symbolic_s\": " << f->tSymbolic << ", \"plan_s\": " << f->tPlan << ", \"numeric_s\": " << f->tNumeric
     << ", \"attempts\": " << f->attempts << ", \"schedule\": {\"tc_min_k\": "
     << (f->impl->tc_min_k() == INT_MAX ? -1 : f->impl->tc_min_k())
     << ", \"fused\": " << (f->impl->fused_chol() ? "true" : "false") << ", \"tuned_ms\": " << f->tunedMs

@@ -3,12 +3,40 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
 #include <utility>
 
 namespace rschol {
+
+// RSCHOL_PLAN_TRACE=1: the host seconds of each planning phase, one line on
+// stderr per plan (the phases between successive mark() calls).
+struct PlanClock {
+  bool on = false;
+  std::chrono::steady_clock::time_point t;
+  std::string line;
+  explicit PlanClock(const char* what) {
+    const char* e = std::getenv("RSCHOL_PLAN_TRACE");
+    on = e && e[0] == '1';
+    if (on) {
+      line = what;
+      t = std::chrono::steady_clock::now();
+    }
+  }
+  void mark(const char* phase) {
+    if (!on) return;
+    const auto u = std::chrono::steady_clock::now();
+    line += std::string(" ") + phase + " " + std::to_string(std::chrono::duration<double>(u - t).count());
+    t = u;
+  }
+  ~PlanClock() {
+    if (on) std::fprintf(stderr, "%s\n", line.c_str());
+  }
+};
 
 struct CudaError : std::runtime_error {
   explicit CudaError(const std::string& s) : std::runtime_error(s) {}

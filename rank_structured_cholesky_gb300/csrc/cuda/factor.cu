@@ -215,7 +215,10 @@ void FactorEngine<T>::emit_fused(const std::vector<CholJob<U>>& jobs, int kind, 
     maxP = std::max(maxP, c.P);
     cjobs.push_back(c);
     // the lower part of rows x first nUpd columns of the front: read and written once
-    for (long long col = 0; col < jb.nUpd; ++col) st.bytes += 2.0 * sizeof(U) * std::max(0LL, (long long)jb.nRows - col);
+    {
+      const long long k = std::min(jb.nUpd, jb.nRows);   // sum of nRows - col over col < k
+      st.bytes += 2.0 * sizeof(U) * (double)(k * jb.nRows - k * (k - 1) / 2);
+    }
     for (int p = 0; p < c.P; ++p) {   // algorithmic flops, counted as the per-panel steps count them
       const int c0 = p == 0 ? 0 : c.w0 + NB * (p - 1), w = p == 0 ? c.w0 : NB;
       const int rows = jb.nRows - c0 - w, upd = jb.nUpd - c0 - w;
@@ -491,24 +494,43 @@ void FactorEngine<T>::emit_trsm(const std::vector<TrsmJob<T>>& jobs) {
 
 template <class T>
 void FactorEngine<T>::emit_extadd(const std::vector<EaTarget>& tgs) {
-  // bucket every source row by its target row; sources keep their order
+  // bucket every source row by its target row (a counting sort: target rows
+  // ascending, each row's segments in source order)
   const long long first = (long long)eaR_.size();
+  {   // room for this level's rows and segments, growing geometrically
+    size_t segs = 0, rows = 0;
+    for (const EaTarget& t : tgs) {
+      rows += (size_t)t.rows;
+      for (const EaSrc& es : t.src) segs += (size_t)std::max(0, es.aHi - es.aLo);
+    }
+    if (eaSeg_.size() + segs > eaSeg_.capacity()) eaSeg_.reserve(std::max(eaSeg_.size() + segs, 2 * eaSeg_.capacity()));
+    if (eaR_.size() + rows > eaR_.capacity()) eaR_.reserve(std::max(eaR_.size() + rows, 2 * eaR_.capacity()));
+  }
+  std::vector<int> cnt, fill;
   for (const EaTarget& t : tgs) {
-    std::vector<std::vector<ExtAddSeg>> bucket(t.rows);
+    cnt.assign(t.rows + 1, 0);
+    const int s0 = (int)eaS_.size();
     for (const EaSrc& es : t.src) {
-      const int sidx = (int)eaS_.size();
       ExtAddSource<T> src = es.s;
       src.rowRel = reinterpret_cast<const int*>(es.relOff);   // rebased at upload
       eaS_.push_back(src);
-      for (int a = es.aLo; a < es.aHi; ++a) bucket[ints_[es.relOff + a]].push_back(ExtAddSeg{sidx, a});
+      for (int a = es.aLo; a < es.aHi; ++a) cnt[ints_[es.relOff + a] + 1]++;
+    }
+    for (int row = 0; row < t.rows; ++row) cnt[row + 1] += cnt[row];
+    const int base = (int)eaSeg_.size();
+    eaSeg_.resize((size_t)base + cnt[t.rows]);
+    fill.assign(cnt.begin(), cnt.end() - 1);
+    int sidx = s0;
+    for (const EaSrc& es : t.src) {
+      for (int a = es.aLo; a < es.aHi; ++a) eaSeg_[(size_t)base + fill[ints_[es.relOff + a]]++] = ExtAddSeg{sidx, a};
+      ++sidx;
     }
     for (int row = 0; row < t.rows; ++row) {
-      if (bucket[row].empty()) continue;
+      if (cnt[row + 1] == cnt[row]) continue;
       ExtAddRow<T> R{};
       R.Frow = t.F + (size_t)row * t.ld;
-      R.segBegin = (int)eaSeg_.size();
-      eaSeg_.insert(eaSeg_.end(), bucket[row].begin(), bucket[row].end());
-      R.segEnd = (int)eaSeg_.size();
+      R.segBegin = base + cnt[row];
+      R.segEnd = base + cnt[row + 1];
       eaR_.push_back(R);
     }
   }
@@ -588,6 +610,7 @@ void FactorEngine<T>::emit_rf(const std::vector<RFJob<T>>& jobs) {
 
 template <class T>
 void FactorEngine<T>::plan() {
+  PlanClock clk("factor plan");
   drop_graphs();   // the captured schedule points into the buffers about to be replaced
   runsSincePlan_ = 0;
   droppedItem_ = false;
@@ -743,6 +766,7 @@ void FactorEngine<T>::plan() {
   } else {
     dRoot64_.alloc(0);
   }
+  clk.mark("arenas");
   T* const I0 = interior();
   T* const C0 = compressed();
   T* const V0 = vu();
@@ -751,20 +775,50 @@ void FactorEngine<T>::plan() {
   T* const G0 = dGauss.as<T>();
 
   // ---- Gaussian stream (reseeded generator; raw draws on the host, the
-  // Box-Muller transform on the device)
+  // Box-Muller transform on the device), in chunks of 2^21 Gaussians through
+  // two pinned host buffers: the host draws chunk c + 1 while chunk c is
+  // copied and transformed, and no host copy of the whole raw stream (8 bytes
+  // per Gaussian, 379 MB for 3D 96^3) is allocated and first-touched.  A host
+  // buffer is refilled only after the event recorded behind its last copy.
   {
     const long long total = S.totalDraws;
     if (total > 0) {
-      std::vector<uint32_t> raw((size_t)total * 2);
+      const long long chunk = std::min<long long>(total, 1LL << 21);
+      struct Staging {
+        cudaStream_t s = nullptr;
+        uint32_t* host[2] = {nullptr, nullptr};
+        cudaEvent_t copied[2] = {nullptr, nullptr};
+        ~Staging() {
+          if (s) cudaStreamSynchronize(s);   // nothing may still read a buffer freed here
+          for (int b = 0; b < 2; ++b) {
+            if (copied[b]) cudaEventDestroy(copied[b]);
+            if (host[b]) cudaFreeHost(host[b]);
+          }
+        }
+      } stg;
+      stg.s = stream;
+      DevBuf dRaw[2];
+      for (int b = 0; b < 2; ++b) {
+        RSCHOL_CUDA(cudaMallocHost(&stg.host[b], sizeof(uint32_t) * 2 * chunk));
+        RSCHOL_CUDA(cudaEventCreateWithFlags(&stg.copied[b], cudaEventDisableTiming));
+        dRaw[b].alloc(sizeof(uint32_t) * 2 * chunk);
+      }
       MT19937 g(prm.seed);
-      g.rawDraws(total * 2, raw.data());
-      DevBuf dRaw;
-      dRaw.alloc(raw.size() * sizeof(uint32_t));
-      RSCHOL_CUDA(cudaMemcpyAsync(dRaw.p, raw.data(), raw.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
-      launch_box_muller<T>(dRaw.as<uint32_t>(), total, G0, stream);
+      long long k0 = 0;
+      for (int c = 0; k0 < total; ++c, k0 += chunk) {
+        const int b = c & 1;
+        const long long k = std::min(chunk, total - k0);
+        if (c >= 2) RSCHOL_CUDA(cudaEventSynchronize(stg.copied[b]));
+        g.rawDraws(2 * k, stg.host[b]);
+        RSCHOL_CUDA(cudaMemcpyAsync(dRaw[b].p, stg.host[b], sizeof(uint32_t) * 2 * k, cudaMemcpyHostToDevice,
+                                    stream));
+        RSCHOL_CUDA(cudaEventRecord(stg.copied[b], stream));
+        launch_box_muller<T>(dRaw[b].as<uint32_t>(), k, G0 + k0, stream);
+      }
       RSCHOL_CUDA(cudaStreamSynchronize(stream));
     }
   }
+  clk.mark("gaussians");
   auto draw_of = [&](int node, int kind, int hnode) -> const T* {
     for (const SketchDraw& d : S.draws)
       if (d.node == node && d.kind == kind && (kind == 2 || d.h == hnode)) return G0 + d.offset;
@@ -794,6 +848,7 @@ void FactorEngine<T>::plan() {
   scatSrc_.insert(scatSrc_.end(), csrc.begin(), csrc.end());
   scatDst_.insert(scatDst_.end(), cdst.begin(), cdst.end());
 
+  clk.mark("scatter");
   // ---- interior levels: extend-add of the children's update blocks, then
   // the blocked partial Cholesky of every front (L panel + update block).
   for (auto& lv : interiorLevels) {
@@ -837,6 +892,7 @@ void FactorEngine<T>::plan() {
     emit_chol(jobs);
   }
 
+  clk.mark("interior");
   // ---- compressed levels
   for (auto& lv : compressedLevels) {
     // (a) compressed-descendant contributions V_c[s0:] (Q_c V_c[s0:s1]^T)
@@ -1058,6 +1114,7 @@ void FactorEngine<T>::plan() {
     emit_rf(oj);
   }
 
+  clk.mark("compressed");
   // RSCHOL_PLAN_LOG=1: one line per GEMM step on stderr (tasks, tiles, flops,
   // largest M / N / K) for tuning the batched kernels
   if (const char* e = std::getenv("RSCHOL_PLAN_LOG")) {
@@ -1141,6 +1198,7 @@ void FactorEngine<T>::plan() {
   up(dScatSrc_, scatSrc_.data(), scatSrc_.size() * sizeof(long long));
   up(dScatDst_, scatDst_.data(), scatDst_.size() * sizeof(long long));
   RSCHOL_CUDA(cudaStreamSynchronize(stream));
+  clk.mark("upload");
   deviceBytes += ints_.size() * 4 + gemm_.size() * sizeof(GemmTask<T>) + scatSrc_.size() * 16 +
                  cholItems_.size() * sizeof(CholItem) + cholJobs_.size() * sizeof(CholFusedJob<T>) +
                  sizeof(int) * cholSync_ + sizeof(T) * cholWs_;

@@ -708,6 +708,7 @@ SolveEngine<T>::SolveEngine(FactorEngine<T>& F) : F_(F) {
 
 template <class T>
 void SolveEngine<T>::plan() {
+  PlanClock clk("solve plan");
   const Symbolic& S = F_.S;
   const int nn = (int)S.nodes.size();
   nodes_.assign(nn, SNode<T>{});
@@ -912,6 +913,7 @@ void SolveEngine<T>::plan() {
     cMRowGrid_.push_back((maxM + 7) / 8);
     cColGrid_.push_back((maxN + 255) / 256);
   }
+  clk.mark("layout");
   cudaStream_t st = F_.stream;
   auto up = [&](DevBuf& b, const void* src, size_t bytes) {
     b.alloc(std::max<size_t>(bytes, 16));
@@ -933,7 +935,9 @@ void SolveEngine<T>::plan() {
     else nodes_[s].Dinv = dDinv_.as<T>() + dinvNodeOff[s];
   }
   nDinv_ = (int)dinvTasks.size();
+  clk.mark("arenas");
   plan_inverse(xOff);
+  clk.mark("inverse");
   // per-row contribution lists of the compressed supernodes (in source order)
   {
     std::vector<long long> cstart;
@@ -992,6 +996,7 @@ void SolveEngine<T>::plan() {
   RSCHOL_CUDA(cudaMemsetAsync(dSync_.p, 0, sizeof(int) * syncCur, st));
   if (!std::is_same<T, double>::value) dW_.alloc(sizeof(T) * std::max(1, S.n));
   RSCHOL_CUDA(cudaStreamSynchronize(st));
+  clk.mark("upload");
   const int maxSmem = 200 * 1024;
   RSCHOL_CUDA(cudaFuncSetAttribute(interior_forward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
   RSCHOL_CUDA(cudaFuncSetAttribute(interior_backward_chunks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));

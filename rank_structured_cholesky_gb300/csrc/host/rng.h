@@ -57,9 +57,26 @@ class MT19937 {
     for (long long i = 0; i < count; ++i) out[i] = randNorm(0.0, 1.0);
   }
 
-  // Raw 32-bit draws (two per Gaussian) for a device-side Box-Muller transform.
+  // Raw 32-bit draws (two per Gaussian) for a device-side Box-Muller transform:
+  // the same stream as count calls of randInt(), tempered a whole state
+  // block at a time.
   void rawDraws(long long count, uint32_t* out) {
-    for (long long i = 0; i < count; ++i) out[i] = randInt();
+    while (count > 0) {
+      if (left_ == 0) reload();
+      const int k = (int)(count < left_ ? count : left_);
+      const uint32_t* src = state_ + next_;
+      for (int i = 0; i < k; ++i) {
+        uint32_t y = src[i];
+        y ^= (y >> 11);
+        y ^= (y << 7) & 0x9d2c5680u;
+        y ^= (y << 15) & 0xefc60000u;
+        out[i] = y ^ (y >> 18);
+      }
+      next_ += k;
+      left_ -= k;
+      out += k;
+      count -= k;
+    }
   }
 
  private:
