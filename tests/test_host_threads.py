@@ -55,3 +55,52 @@ def test_setup_passes_independent_of_thread_count():
         assert n >= 4096 and nn >= 64, (name, n, nn)
     for t in (3, 8):
         assert digests(t) == one, t
+
+
+PARALLEL_CHECK = r"""
+#include <atomic>
+#include <cstdio>
+#include <stdexcept>
+#include <vector>
+#include "parallel.h"
+int main() {
+  using namespace rschol;
+  const long long n = 100003;
+  std::vector<int> hits(n, 0);
+  parallel_chunks(n, 1000, [&](long long b, long long e) {
+    for (long long i = b; i < e; ++i) hits[i]++;
+  });
+  for (long long i = 0; i < n; ++i)
+    if (hits[i] != 1) return 1;
+  std::atomic<int> calls(0), mask(0);
+  run_workers(5, [&](int t) { calls++; mask |= 1 << t; });
+  if (calls != 5 || mask != 31) return 2;
+  bool caught = false;
+  try {
+    parallel_chunks(n, 10, [&](long long b, long long e) {
+      if (b <= 77777 && 77777 < e) throw std::runtime_error("chunk failed");
+    });
+  } catch (const std::runtime_error&) {
+    caught = true;
+  }
+  if (!caught) return 3;
+  std::printf("%d\n", host_threads());
+  return 0;
+}
+"""
+
+
+def test_parallel_helpers(tmp_path):
+    """Every index visited once, every worker run once, a worker's exception
+    rethrown on the calling thread; RSCHOL_HOST_THREADS is honoured."""
+    src = tmp_path / "par.cpp"
+    src.write_text(PARALLEL_CHECK)
+    exe = tmp_path / "par"
+    host = os.path.join(ROOT, "rank_structured_cholesky_gb300", "csrc", "host")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-pthread", "-I", host, str(src), "-o", str(exe)], check=True,
+                   stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    for threads in ("1", "4", "16"):
+        env = dict(os.environ, RSCHOL_HOST_THREADS=threads)
+        r = subprocess.run([str(exe)], env=env, capture_output=True, text=True, timeout=60)
+        assert r.returncode == 0, (threads, r.returncode)
+        assert r.stdout.strip() == threads
