@@ -630,7 +630,7 @@ def run_serving(args):
     rank, world, dist = dist_setup(args.gpus)
     local = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(local)
-    count, rate = args.requests, 200.0
+    count, rate = args.requests, args.rate
     stream = serving_stream(count, rate, seed=5)
     probs, rhs = serving_pool(sorted(set(int(m) for m in stream[1])))
     budget = args.hbm_budget_gb * 1e9
@@ -697,6 +697,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--requests", type=int, default=2000, help="c5: requests in the stream")
+    ap.add_argument("--rate", type=float, default=200.0,
+                    help="c5: mean Poisson arrival rate, requests/s (200 saturates one GB300; a lower rate "
+                         "measures latency below saturation)")
     ap.add_argument("--workers", type=int, default=8, help="c5: server worker threads")
     ap.add_argument("--hbm-budget-gb", type=float, default=200.0, help="c5: device bytes for cached factors")
     ap.add_argument("--profile", action="store_true",
