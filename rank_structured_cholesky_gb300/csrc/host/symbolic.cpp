@@ -7,6 +7,7 @@
 #include <functional>
 #include <sstream>
 #include <stdexcept>
+#include <string>
 
 #include "parallel.h"
 
@@ -247,7 +248,11 @@ Symbolic build_symbolic(const CSC& A, const OrderingResult& ord, const Params& p
           else anc.push_back(nd.interNode[q]);
         }
         if (S.nodes[k].H.size() > 1)
-          throw std::runtime_error("uncompressed supernode with a hierarchical diagonal is not supported");
+          throw std::runtime_error("uncompressed supernode " + std::to_string(k) + " has " +
+                                   std::to_string(nd.n) + " columns, more than max_diag_block = " +
+                                   std::to_string(prm.max_diag_block) +
+                                   ": a hierarchical diagonal on an uncompressed supernode is not supported "
+                                   "(raise max_diag_block to at least " + std::to_string(nd.n) + ")");
       }
       std::sort(anc.begin(), anc.end());
       anc.erase(std::unique(anc.begin(), anc.end()), anc.end());

@@ -178,3 +178,16 @@ def test_supernode_rows_match_brute_force_fill():
         assert F.node_rows(k).tolist() == expect
         covered += c1 - c0 + 1
     assert covered == n
+
+
+def test_hierarchical_diagonal_on_uncompressed_supernode_is_rejected(capfd):
+    """A relaxed uncompressed supernode wider than max_diag_block would need a
+    HODLR diagonal outside the compressed levels: rejected with a message
+    that names the parameter and the width it needs (the library returns it
+    with RSCHOL_E_UNSUPPORTED; the oracle shares the host code)."""
+    from oracle import pyoracle as po
+    p = rs.diffusion(2, 9, 7, sigma=1.0, seed=3)
+    with pytest.raises(RuntimeError):
+        po.OracleFactor(p.colptr, p.rowind, p.vals, p.xyz, dict(max_dense_block=4, max_diag_block=8, nd_leaf=4))
+    err = capfd.readouterr().err
+    assert "more than max_diag_block = 8" in err and "raise max_diag_block to at least" in err, err
