@@ -88,6 +88,17 @@ const char* rschol_last_error(const rschol_ctx* ctx);
 int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* rowind,
                          const double* vals, const double* xyz, rschol_factor** out);
 
+/* Whether rschol_factor_create can take this structure with these parameters
+ * (NULL: the defaults): the host ordering and symbolic analysis alone, no
+ * device and no values needed.  RSCHOL_OK; RSCHOL_E_BAD_INPUT for an invalid
+ * pattern; RSCHOL_E_UNSUPPORTED when an uncompressed supernode would need a
+ * hierarchical diagonal (one wider than max_diag_block), which the device
+ * factorisation does not build.  The reason is written to msg (at most
+ * msg_len bytes, NUL-terminated; msg may be NULL).  No reference counterpart:
+ * the reference builds such a diagonal. */
+int rschol_check_structure(int n, const int* colptr, const int* rowind, const double* xyz,
+                           const rschol_params* params, char* msg, int msg_len);
+
 /* New values, same pattern: FactorPreconditioner::initialize with only the
  * numeric factor needed (FactorPreconditioner.cpp:115-129). */
 int rschol_refactor(rschol_factor* f, const double* vals);

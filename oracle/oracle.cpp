@@ -151,7 +151,7 @@ static void sub_forward(const Factor& F, const NodeList& L, const std::vector<in
     int d = L.nodes[q];
     const Node& nd = F.S.nodes[d];
     double* Xd = X + (size_t)L.start[q] * k;
-    trsm_left(nd.n, k, F.hd[d][nd.hroot].leaf.data(), nd.n, false, Xd, k);
+    hsolve(F, d, nd.hroot, Xd, k, false);   // a dense L11 is the HODLR root leaf
     if (nd.nStored == 0) continue;
     T.assign((size_t)nd.nStored * k, 0.0);
     gemm(nd.nStored, k, nd.n, 1.0, F.off[d].data(), nd.n, false, Xd, k, false, 0.0, T.data(), k);
@@ -180,9 +180,11 @@ static void sub_backward(const Factor& F, const NodeList& L, const std::vector<i
       }
       gemm(nd.n, k, nd.nStored, -1.0, F.off[d].data(), nd.n, true, G.data(), k, false, 1.0, Xd, k);
     }
-    trsm_left(nd.n, k, F.hd[d][nd.hroot].leaf.data(), nd.n, true, Xd, k);
+    hsolve(F, d, nd.hroot, Xd, k, true);
   }
 }
+
+static int factor_hodlr(Factor& F, int j, const std::vector<double>& S11);
 
 // ---------------------------------------------------------------------------
 // Interior-node numeric factorisation (left-looking within the block).
@@ -221,6 +223,25 @@ static int factor_interior(Factor& F, int j) {
     }
   }
   for (int r = 0; r < nd.m(); ++r) rowPos[nd.rows[r]] = -1;
+  if (nd.H.size() > 1) {
+    // A hierarchical diagonal (an uncompressed supernode wider than
+    // max_diag_block): the compressed supernodes' block-list walk over the
+    // explicit Schur complement D, then the stored rows solved with the
+    // expanded L11, L21 = S21 L11^-T (choleskyOffDiagonalSolve through
+    // diagonalSolve, Supernode.cpp:3700-3760).
+    const int info = factor_hodlr(F, j, D);
+    if (info != 0) return info;
+    if (ns > 0) {
+      std::vector<double> X((size_t)n * ns);
+      for (int r = 0; r < ns; ++r)
+        for (int c = 0; c < n; ++c) X[(size_t)c * ns + r] = O[(size_t)r * n + c];
+      hsolve(F, j, nd.hroot, X.data(), ns, false);
+      for (int r = 0; r < ns; ++r)
+        for (int c = 0; c < n; ++c) O[(size_t)r * n + c] = X[(size_t)c * ns + r];
+    }
+    F.off[j].swap(O);
+    return 0;
+  }
   int info = potrf(n, D.data(), n);
   if (info != 0) return info;
   trsm_right_lt(ns, n, D.data(), n, O.data(), n);
@@ -431,79 +452,15 @@ static void range_finder(int m, int n, int r, int powerIters, const double* G,
   rankOut = r;
 }
 
-static int factor_compressed(Factor& F, int j) {
-  Node& nd = F.S.nodes[j];
-  const int n = nd.n, m = nd.m();
-  OpMaps M;
-  M.cMap.assign(F.S.n, -1);
-  M.rMap.assign(F.S.n, -1);
-  for (int c = nd.c0; c <= nd.c1; ++c) M.cMap[c] = c - nd.c0;
-  for (int r = 0; r < m; ++r) M.rMap[nd.rows[r]] = r;
-
-  // Schur complement of the diagonal: A_CC - compressed descendants
-  // (compressedDiagonalUpdate, Supernode.cpp:1266-1414) - interior blocks
-  // (applyInteriorBlockDiagonalUpdate, FactorManager.cpp:3003-3090).
-  std::vector<double> S11((size_t)n * n, 0.0);
-  for (int c = nd.c0; c <= nd.c1; ++c)
-    for (int p = F.A.p[c]; p < F.A.p[c + 1]; ++p) {
-      int r = F.A.i[p];
-      if (r <= nd.c1) S11[(size_t)(r - nd.c0) * n + (c - nd.c0)] = F.A.x[p];
-    }
-  std::vector<double> T1, T2;
-  for (int d : F.compDesc[j]) {
-    const Node& dn = F.S.nodes[d];
-    int q = 0;
-    while (dn.interNode[q] != j) ++q;
-    const int s0 = dn.interStart[q], k1 = dn.interStart[q + 1] - s0, r = F.rank[d];
-    if (r == 0) continue;
-    const double* Vc = F.V[d].data() + (size_t)s0 * r;
-    T1.assign((size_t)r * k1, 0.0);
-    gemm(r, k1, r, 1.0, F.UtU[d].data(), r, false, Vc, r, true, 0.0, T1.data(), k1);
-    T2.assign((size_t)k1 * k1, 0.0);
-    gemm(k1, k1, r, 1.0, Vc, r, false, T1.data(), k1, false, 0.0, T2.data(), k1);
-    for (int a = 0; a < k1; ++a)
-      for (int b = 0; b < k1; ++b)
-        S11[(size_t)(dn.rows[s0 + a] - nd.c0) * n + (dn.rows[s0 + b] - nd.c0)] -= T2[(size_t)a * k1 + b];
-  }
-  {
-    std::vector<int> listPos(F.S.nodes.size(), -1);
-    for (int b : F.blockDesc[j]) {
-      NodeList L = make_list(F, block_nodes(F, b, j, false));
-      if (L.nodes.empty()) continue;
-      for (size_t q = 0; q < L.nodes.size(); ++q) listPos[L.nodes[q]] = (int)q;
-      // nonzero columns of A_{S,C}
-      std::vector<int> colSel, colOf(n, -1);
-      for (size_t q = 0; q < L.nodes.size(); ++q) {
-        const Node& dn = F.S.nodes[L.nodes[q]];
-        for (int c = dn.c0; c <= dn.c1; ++c)
-          for (int p = F.A.p[c]; p < F.A.p[c + 1]; ++p) {
-            int cc = M.cMap[F.A.i[p]];
-            if (cc >= 0 && colOf[cc] < 0) { colOf[cc] = 0; colSel.push_back(cc); }
-          }
-      }
-      std::sort(colSel.begin(), colSel.end());
-      const int kk = (int)colSel.size();
-      if (kk == 0) { for (int d : L.nodes) listPos[d] = -1; continue; }
-      for (int t = 0; t < kk; ++t) colOf[colSel[t]] = t;
-      std::vector<double> W((size_t)L.total * kk, 0.0);
-      for (size_t q = 0; q < L.nodes.size(); ++q) {
-        const Node& dn = F.S.nodes[L.nodes[q]];
-        for (int c = dn.c0; c <= dn.c1; ++c)
-          for (int p = F.A.p[c]; p < F.A.p[c + 1]; ++p) {
-            int cc = M.cMap[F.A.i[p]];
-            if (cc >= 0) W[(size_t)(L.start[q] + c - dn.c0) * kk + colOf[cc]] += F.A.x[p];
-          }
-      }
-      sub_forward(F, L, listPos, W.data(), kk);
-      std::vector<double> WtW((size_t)kk * kk, 0.0);
-      gemm(kk, kk, L.total, 1.0, W.data(), kk, true, W.data(), kk, false, 0.0, WtW.data(), kk);
-      for (int a = 0; a < kk; ++a)
-        for (int b = 0; b < kk; ++b) S11[(size_t)colSel[a] * n + colSel[b]] -= WtW[(size_t)a * kk + b];
-      for (int d : L.nodes) listPos[d] = -1;
-    }
-  }
-
-  // factorCompressedDiagonal: walk the HODLR block list.
+// factorCompressedDiagonal (FactorManager.cpp:8907-9036): walk node j's
+// HODLR block list over its n x n Schur complement S11 (row-major; only the
+// lower triangle and the blocks below the diagonal are read).  Used for
+// compressed supernodes and for uncompressed supernodes whose diagonal is
+// hierarchical (the reference factors every supernode's diagonal through its
+// DiagonalBlock, FactorManager.cpp:640-652).  Returns 0 or a POTRF info.
+static int factor_hodlr(Factor& F, int j, const std::vector<double>& S11) {
+  const Node& nd = F.S.nodes[j];
+  const int n = nd.n;
   std::vector<HData>& hd = F.hd[j];
   for (const rschol::BlockEntry& be : nd.blocks) {
     const HNode& x = nd.H[be.h];
@@ -618,6 +575,87 @@ static int factor_compressed(Factor& F, int j) {
                    hd[be.h].U, rk);
       hd[be.h].rank = rk;
     }
+  }
+
+  return 0;
+}
+
+static int factor_compressed(Factor& F, int j) {
+  Node& nd = F.S.nodes[j];
+  const int n = nd.n, m = nd.m();
+  OpMaps M;
+  M.cMap.assign(F.S.n, -1);
+  M.rMap.assign(F.S.n, -1);
+  for (int c = nd.c0; c <= nd.c1; ++c) M.cMap[c] = c - nd.c0;
+  for (int r = 0; r < m; ++r) M.rMap[nd.rows[r]] = r;
+
+  // Schur complement of the diagonal: A_CC - compressed descendants
+  // (compressedDiagonalUpdate, Supernode.cpp:1266-1414) - interior blocks
+  // (applyInteriorBlockDiagonalUpdate, FactorManager.cpp:3003-3090).
+  std::vector<double> S11((size_t)n * n, 0.0);
+  for (int c = nd.c0; c <= nd.c1; ++c)
+    for (int p = F.A.p[c]; p < F.A.p[c + 1]; ++p) {
+      int r = F.A.i[p];
+      if (r <= nd.c1) S11[(size_t)(r - nd.c0) * n + (c - nd.c0)] = F.A.x[p];
+    }
+  std::vector<double> T1, T2;
+  for (int d : F.compDesc[j]) {
+    const Node& dn = F.S.nodes[d];
+    int q = 0;
+    while (dn.interNode[q] != j) ++q;
+    const int s0 = dn.interStart[q], k1 = dn.interStart[q + 1] - s0, r = F.rank[d];
+    if (r == 0) continue;
+    const double* Vc = F.V[d].data() + (size_t)s0 * r;
+    T1.assign((size_t)r * k1, 0.0);
+    gemm(r, k1, r, 1.0, F.UtU[d].data(), r, false, Vc, r, true, 0.0, T1.data(), k1);
+    T2.assign((size_t)k1 * k1, 0.0);
+    gemm(k1, k1, r, 1.0, Vc, r, false, T1.data(), k1, false, 0.0, T2.data(), k1);
+    for (int a = 0; a < k1; ++a)
+      for (int b = 0; b < k1; ++b)
+        S11[(size_t)(dn.rows[s0 + a] - nd.c0) * n + (dn.rows[s0 + b] - nd.c0)] -= T2[(size_t)a * k1 + b];
+  }
+  {
+    std::vector<int> listPos(F.S.nodes.size(), -1);
+    for (int b : F.blockDesc[j]) {
+      NodeList L = make_list(F, block_nodes(F, b, j, false));
+      if (L.nodes.empty()) continue;
+      for (size_t q = 0; q < L.nodes.size(); ++q) listPos[L.nodes[q]] = (int)q;
+      // nonzero columns of A_{S,C}
+      std::vector<int> colSel, colOf(n, -1);
+      for (size_t q = 0; q < L.nodes.size(); ++q) {
+        const Node& dn = F.S.nodes[L.nodes[q]];
+        for (int c = dn.c0; c <= dn.c1; ++c)
+          for (int p = F.A.p[c]; p < F.A.p[c + 1]; ++p) {
+            int cc = M.cMap[F.A.i[p]];
+            if (cc >= 0 && colOf[cc] < 0) { colOf[cc] = 0; colSel.push_back(cc); }
+          }
+      }
+      std::sort(colSel.begin(), colSel.end());
+      const int kk = (int)colSel.size();
+      if (kk == 0) { for (int d : L.nodes) listPos[d] = -1; continue; }
+      for (int t = 0; t < kk; ++t) colOf[colSel[t]] = t;
+      std::vector<double> W((size_t)L.total * kk, 0.0);
+      for (size_t q = 0; q < L.nodes.size(); ++q) {
+        const Node& dn = F.S.nodes[L.nodes[q]];
+        for (int c = dn.c0; c <= dn.c1; ++c)
+          for (int p = F.A.p[c]; p < F.A.p[c + 1]; ++p) {
+            int cc = M.cMap[F.A.i[p]];
+            if (cc >= 0) W[(size_t)(L.start[q] + c - dn.c0) * kk + colOf[cc]] += F.A.x[p];
+          }
+      }
+      sub_forward(F, L, listPos, W.data(), kk);
+      std::vector<double> WtW((size_t)kk * kk, 0.0);
+      gemm(kk, kk, L.total, 1.0, W.data(), kk, true, W.data(), kk, false, 0.0, WtW.data(), kk);
+      for (int a = 0; a < kk; ++a)
+        for (int b = 0; b < kk; ++b) S11[(size_t)colSel[a] * n + colSel[b]] -= WtW[(size_t)a * kk + b];
+      for (int d : L.nodes) listPos[d] = -1;
+    }
+  }
+
+  // factorCompressedDiagonal: walk the HODLR block list.
+  {
+    const int info = factor_hodlr(F, j, S11);
+    if (info != 0) return info;
   }
 
   // Off-diagonal compression (offDiagonalDecomposition + fullBasisProject).
@@ -856,10 +894,11 @@ void* oracle_create(int n, const int* colptr, const int* rowind, const double* v
 void oracle_free(void* h) { delete (Factor*)h; }
 
 // Numeric factorisation with the reference's retry policy
-// (SparseSolver.cpp:174-214): an indefinite diagonal of a compressed node
-// (IndefiniteDiagonalError from its DiagonalBlock, DiagonalBlock.cpp:372-376,
-// 429-435) is retried with a larger diagonal rank constant; a non-positive
-// pivot of an uncompressed node is where the reference aborts
+// (SparseSolver.cpp:174-214): an indefinite diagonal factored through a
+// DiagonalBlock -- every compressed node's, and an uncompressed node's whose
+// diagonal is hierarchical (IndefiniteDiagonalError, DiagonalBlock.cpp:372-376,
+// 429-435) -- is retried with a larger diagonal rank constant; a non-positive
+// pivot of an uncompressed node's dense diagonal is where the reference aborts
 // (Supernode.cpp:3681-3689), so it is returned at once.  Returns 0 or the
 // 1-based index of the node whose diagonal was not positive definite.
 int oracle_factor(void* h) {
@@ -873,7 +912,8 @@ int oracle_factor(void* h) {
     F.attempts++;
     status = oracle::numeric(F);
     if (status == 0) break;
-    if (!F.S.nodes[status - 1].compressed) break;
+    const rschol::Node& bad = F.S.nodes[status - 1];
+    if (!bad.compressed && bad.H.size() <= 1) break;
     dc *= F.prm.rank_alpha;
   }
   F.diagRankConstant = dc;

@@ -30,6 +30,7 @@ FP64, MIXED = 0, 1
 # Every entry point declared in include/rschol_gpu.h.
 EXPORTED = [
     "rschol_default_params", "rschol_create", "rschol_destroy", "rschol_last_error", "rschol_factor_create",
+    "rschol_check_structure",
     "rschol_refactor", "rschol_refactor_device", "rschol_stream", "rschol_profile", "rschol_factor_free", "rschol_precond_apply", "rschol_precond_apply_device",
     "rschol_precond_apply_device_noalloc", "rschol_selftest_gemm", "rschol_bench_gemm", "rschol_step_timing", "rschol_pcg",
     "rschol_pcg_device", "rschol_pcg_pysolve", "rschol_factor_n", "rschol_factor_device_bytes", "rschol_factor_num_nodes",
@@ -85,6 +86,7 @@ def load_library():
         "rschol_destroy": (None, [P]),
         "rschol_last_error": (ctypes.c_char_p, [P]),
         "rschol_factor_create": (I, [P, I, pI, pI, pD, pD, ctypes.POINTER(P)]),
+        "rschol_check_structure": (I, [I, pI, pI, pD, ctypes.POINTER(Params), ctypes.c_char_p, I]),
         "rschol_refactor": (I, [P, pD]),
         "rschol_refactor_device": (I, [P, P]),
         "rschol_stream": (P, [P]),
@@ -220,6 +222,22 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+def check_structure(colptr, rowind, xyz=None, **params):
+    """(status, reason): whether GpuFactor can take this pattern with these
+    parameters, from the host ordering and symbolic analysis alone (no device)."""
+    colptr = np.ascontiguousarray(colptr, np.int32)
+    rowind = np.ascontiguousarray(rowind, np.int32)
+    xp = None
+    if xyz is not None:
+        xyz = np.ascontiguousarray(xyz, np.float64)
+        xp = _dp(xyz)
+    prm = default_params(**params)
+    msg = ctypes.create_string_buffer(512)
+    st = load_library().rschol_check_structure(len(colptr) - 1, _ip(colptr), _ip(rowind), xp, ctypes.byref(prm),
+                                               msg, len(msg))
+    return st, msg.value.decode()
 
 
 class GpuFactor:

@@ -324,18 +324,61 @@ static int numeric_with_retry(rschol_factor* f) {
   return RSCHOL_OK;
 }
 
+// The pattern checks of rschol_factor_create; "" when the CSC arrays are valid.
+static std::string csc_problem(int n, const int* colptr, const int* rowind) {
+  if (n <= 0 || !colptr || !rowind) return "empty or null matrix";
+  if (colptr[0] != 0) return "colptr[0] must be 0";
+  for (int j = 0; j < n; ++j)
+    if (colptr[j + 1] < colptr[j]) return "colptr must be non-decreasing";
+  const int nnz = colptr[n];
+  for (int k = 0; k < nnz; ++k)
+    if (rowind[k] < 0 || rowind[k] >= n) return "row index out of range";
+  return std::string();
+}
+
+// Host ordering and symbolic analysis only (no CUDA call): whether
+// rschol_factor_create can take this structure with these parameters.
+int rschol_check_structure(int n, const int* colptr, const int* rowind, const double* xyz,
+                           const rschol_params* params, char* msg, int msg_len) {
+  auto report = [&](int code, const std::string& why) {
+    if (msg && msg_len > 0) {
+      const size_t k = std::min(why.size(), (size_t)msg_len - 1);
+      std::memcpy(msg, why.data(), k);
+      msg[k] = 0;
+    }
+    return code;
+  };
+  const std::string bad = csc_problem(n, colptr, rowind);
+  if (!bad.empty()) return report(RSCHOL_E_BAD_INPUT, bad);
+  try {
+    rschol_params c;
+    if (params) c = *params;
+    else rschol_default_params(&c);
+    const Params prm = to_params(c);
+    CSC A;
+    A.n = n;
+    A.p.assign(colptr, colptr + n + 1);
+    A.i.assign(rowind, rowind + colptr[n]);
+    const OrderingResult ord = build_ordering(A, xyz, prm);
+    const Symbolic S = build_symbolic(permute_lower(A, ord.perm, ord.iperm), ord, prm);
+    const std::string why = unsupported_reason(S, prm);
+    return why.empty() ? report(RSCHOL_OK, "") : report(RSCHOL_E_UNSUPPORTED, why);
+  } catch (const std::exception& e) {
+    return report(RSCHOL_E_UNSUPPORTED, e.what());
+  }
+}
+
 int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* rowind, const double* vals,
                          const double* xyz, rschol_factor** out) {
   if (!ctx || !out) return RSCHOL_E_BAD_INPUT;
   *out = nullptr;
   if (!ctx->stream) return fail(ctx, RSCHOL_E_NO_DEVICE, ctx->err.empty() ? "no device" : ctx->err);
-  if (n <= 0 || !colptr || !rowind || !vals) return fail(ctx, RSCHOL_E_BAD_INPUT, "empty or null matrix");
-  if (colptr[0] != 0) return fail(ctx, RSCHOL_E_BAD_INPUT, "colptr[0] must be 0");
-  for (int j = 0; j < n; ++j)
-    if (colptr[j + 1] < colptr[j]) return fail(ctx, RSCHOL_E_BAD_INPUT, "colptr must be non-decreasing");
+  if (!vals) return fail(ctx, RSCHOL_E_BAD_INPUT, "empty or null matrix");
+  {
+    const std::string bad = csc_problem(n, colptr, rowind);
+    if (!bad.empty()) return fail(ctx, RSCHOL_E_BAD_INPUT, bad);
+  }
   const int nnz = colptr[n];
-  for (int k = 0; k < nnz; ++k)
-    if (rowind[k] < 0 || rowind[k] >= n) return fail(ctx, RSCHOL_E_BAD_INPUT, "row index out of range");
   std::unique_ptr<rschol_factor> f(new rschol_factor());
   AccountScope acct(&f->devBytes);
   f->ctx = ctx;
@@ -360,6 +403,10 @@ int rschol_factor_create(rschol_ctx* ctx, int n, const int* colptr, const int* r
       f->A = std::move(L);
     }
     f->S = build_symbolic(f->A, f->ord, f->prm);
+    {
+      const std::string why = unsupported_reason(f->S, f->prm);
+      if (!why.empty()) return fail(ctx, RSCHOL_E_UNSUPPORTED, why);
+    }
     // permuted full CSR for the PCG SpMV (symmetric: CSC columns = CSR rows)
     std::vector<int> rp(n + 1, 0), ci(nnz);
     std::vector<double> cv(nnz);

@@ -247,12 +247,6 @@ Symbolic build_symbolic(const CSC& A, const OrderingResult& ord, const Params& p
           if (nd.interNode[q] <= ib.n1) nd.nStored = nd.interStart[q + 1];
           else anc.push_back(nd.interNode[q]);
         }
-        if (S.nodes[k].H.size() > 1)
-          throw std::runtime_error("uncompressed supernode " + std::to_string(k) + " has " +
-                                   std::to_string(nd.n) + " columns, more than max_diag_block = " +
-                                   std::to_string(prm.max_diag_block) +
-                                   ": a hierarchical diagonal on an uncompressed supernode is not supported "
-                                   "(raise max_diag_block to at least " + std::to_string(nd.n) + ")");
       }
       std::sort(anc.begin(), anc.end());
       anc.erase(std::unique(anc.begin(), anc.end()), anc.end());
@@ -335,6 +329,18 @@ void assign_ranks(Symbolic& S, const Params& prm, double rankConstant, double di
     }
   }
   S.totalDraws = off;
+}
+
+std::string unsupported_reason(const Symbolic& S, const Params& prm) {
+  for (size_t k = 0; k < S.nodes.size(); ++k) {
+    const Node& nd = S.nodes[k];
+    if (!nd.compressed && nd.H.size() > 1)
+      return "uncompressed supernode " + std::to_string(k) + " has " + std::to_string(nd.n) +
+             " columns, more than max_diag_block = " + std::to_string(prm.max_diag_block) +
+             ": a hierarchical diagonal on an uncompressed supernode is not supported on the device (raise "
+             "max_diag_block to at least " + std::to_string(nd.n) + ")";
+  }
+  return std::string();
 }
 
 std::string describe(const Symbolic& S) {

@@ -96,6 +96,11 @@ Symbolic build_symbolic(const CSC& Alower, const OrderingResult& ord, const Para
 // constants (SparseSolver::factorNumeric's retry bumps the diagonal one).
 void assign_ranks(Symbolic& S, const Params& prm, double rankConstant, double diagRankConstant);
 
+// Why the device factorisation cannot take this structure ("" when it can):
+// an uncompressed supernode wider than max_diag_block has a hierarchical
+// diagonal, which only the compressed levels factor on the device.
+std::string unsupported_reason(const Symbolic& S, const Params& prm);
+
 std::string describe(const Symbolic& S);
 
 }  // namespace rschol

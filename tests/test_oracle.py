@@ -103,3 +103,30 @@ def test_oracle_retry_policy(compressed):
     assert t["attempts"] == (10 if compressed else 1)
     if compressed:
         assert abs(t["diag_rank_constant"] - 0.5 * 1.25 ** 10) < 1e-9
+
+
+@pytest.mark.parametrize("shape,prm", [
+    ((2, 40, 37, None), dict(max_dense_block=100, max_diag_block=12, nd_leaf=32)),
+    ((2, 40, 37, None), dict(max_dense_block=8, max_diag_block=12, nd_leaf=32)),
+    ((3, 12, 11, 10), dict(max_dense_block=400, max_diag_block=16, nd_leaf=48)),
+    ((3, 12, 11, 10), dict(max_dense_block=24, max_diag_block=16, nd_leaf=48)),
+])
+def test_hierarchical_diagonal_on_uncompressed_supernodes(shape, prm):
+    """Uncompressed supernodes wider than max_diag_block get a HODLR diagonal,
+    factored by the same block-list walk as a compressed supernode's over
+    their explicit Schur complement, with their stored rows solved by the
+    expanded L11 (the reference factors every diagonal through its
+    DiagonalBlock).  Every block explicit and every rank full: the factor is
+    exact (one PCG iteration); at the default ranks the PCG converges."""
+    d, nx, ny, nz = shape
+    p = rs.diffusion(d, nx, ny, nz, sigma=1.0, seed=3)
+    exact = po.OracleFactor(p.colptr, p.rowind, p.vals, p.xyz, dict(prm, rank_constant=1e3, diag_rank_constant=1e3))
+    assert exact.factor() == 0
+    infos = [exact.node_info(j) for j in range(exact.num_nodes())]
+    assert sum(1 for i in infos if not i["compressed"] and i["hodlr_nodes"] > 1) > 0
+    _, it, _, true = exact.pcg(p.rhs[0], 1e-8, 100)
+    assert it == 1 and true < 1e-12, (it, true)
+    F = po.OracleFactor(p.colptr, p.rowind, p.vals, p.xyz, prm)
+    assert F.factor() == 0
+    _, it, _, true = F.pcg(p.rhs[0], 1e-8, 100)
+    assert it <= 20 and true <= 1e-8, (it, true)

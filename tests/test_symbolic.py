@@ -180,14 +180,19 @@ def test_supernode_rows_match_brute_force_fill():
     assert covered == n
 
 
-def test_hierarchical_diagonal_on_uncompressed_supernode_is_rejected(capfd):
-    """A relaxed uncompressed supernode wider than max_diag_block would need a
-    HODLR diagonal outside the compressed levels: rejected with a message
-    that names the parameter and the width it needs (the library returns it
-    with RSCHOL_E_UNSUPPORTED; the oracle shares the host code)."""
-    from oracle import pyoracle as po
+
+def test_structure_check_names_unsupported_hierarchical_diagonal():
+    """rschol_check_structure (host ordering + symbolic, no device): a relaxed
+    uncompressed supernode wider than max_diag_block would need a HODLR
+    diagonal, which the device factorisation does not build -- reported as
+    RSCHOL_E_UNSUPPORTED with the width it needs; the default parameters take
+    the same matrix; an invalid pattern is RSCHOL_E_BAD_INPUT."""
     p = rs.diffusion(2, 9, 7, sigma=1.0, seed=3)
-    with pytest.raises(RuntimeError):
-        po.OracleFactor(p.colptr, p.rowind, p.vals, p.xyz, dict(max_dense_block=4, max_diag_block=8, nd_leaf=4))
-    err = capfd.readouterr().err
-    assert "more than max_diag_block = 8" in err and "raise max_diag_block to at least" in err, err
+    st, why = rs.check_structure(p.colptr, p.rowind, p.xyz, max_dense_block=4, max_diag_block=8, nd_leaf=4)
+    assert rs.STATUS_NAMES[st] == "RSCHOL_E_UNSUPPORTED"
+    assert "more than max_diag_block = 8" in why and "raise max_diag_block to at least" in why, why
+    assert rs.check_structure(p.colptr, p.rowind, p.xyz) == (rs.RSCHOL_OK, "")
+    bad = p.colptr.copy()
+    bad[0] = 1
+    st, why = rs.check_structure(bad, p.rowind, p.xyz)
+    assert rs.STATUS_NAMES[st] == "RSCHOL_E_BAD_INPUT" and "colptr" in why
